@@ -1,0 +1,504 @@
+"""TEST INFRASTRUCTURE ONLY -- the CPU oracle for the GIWAXS forward path.
+
+This module is the checker, not the product.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg may import it.  The
+product (giwaxsim_gb300) never calls into it and fails loudly when its CUDA
+library is missing.
+
+It restates, in float64/complex128 numpy, the reference's forward path:
+
+  tools/utilities.py:303-317   rotate_coords_z
+  tools/voxelgrids.py:238-309  rectangular_collapse_lengths
+  tools/voxelgrids.py:311-416  rotate_project_fft_coords  (deposit, fill_bkg,
+                                smoothing, fftn/fftshift/|.|^2, slice axes)
+  tools/voxelgrids.py:464-506  process_file2              (binning)
+  tools/comparison.py:673-788  voxelgridmaker_fitting     (driver, divide,
+                                crop, f0)
+  tools/voxelgrids.py:16-48    downselect_voxelgrid
+  tools/voxelgrids.py:828-857  add_f0_q_3d
+  tools/detector.py:5-29       make_detector
+  tools/detector.py:33-162     rotate_about_normal/horizontal/vertical
+  tools/detector.py:194-232    intersect_detector (the second definition,
+                                which shadows the first)
+  tools/detector.py:234-244    rotate_psi_phi_theta
+  tools/detector.py:246-275    mirror_vertical_horizontal
+  tools/detector.py:278-300    generate_detector_ints
+  tools/comparison.py:790-870  detectormaker_fitting
+  old_modules/voxelgridmaker.py:56-61  averaging of I(q) over input files
+
+Differences from the reference, all deliberate:
+  * BLAS products are evaluated by oracle_fma.c as the explicit fused chain
+    that OpenBLAS uses on x86_64 (pinned in tests/golden), so the oracle is
+    bit-reproducible on any host.
+  * phis may be passed explicitly (the reference always derives them).
+  * the count grid is returned alongside I(q); accumulation is serial.
+  * detectormaker copies the summed image before releasing it (the reference
+    reads a closed shared-memory buffer when mirror=False).
+  * smoothing accepts a non-integer sigma; mask edges are ceil(lo+sigma) and
+    ceil(hi-sigma), which are the reference's slice bounds for integer sigma.
+
+Parity status: pinned.  tests/golden holds outputs of the reference itself
+(imported in a shim with f'=f''=0), and tests/test_oracle_golden.py checks this
+module against them.  The xraydb f'/f'' lookup is not reproduced (xraydb is
+not installed); f values are an input to both the oracle and the product.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+from numpy.fft import fft2, fftshift
+from scipy.ndimage import gaussian_filter1d
+
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        from . import build_oracle
+        path = build_oracle.build()
+        lib = ctypes.CDLL(path)
+        p = ctypes.c_void_p
+        lib.oracle_rotate_rows.argtypes = [p, ctypes.c_int64, p, p]
+        lib.oracle_rotate_rows.restype = None
+        lib.oracle_rotate_xyz.argtypes = [p, p, p, ctypes.c_int64, p, p, p, p]
+        lib.oracle_rotate_xyz.restype = None
+        _LIB = lib
+    return _LIB
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def fma_rows(pts, R):
+    """np.dot(pts, R.T) with the BLAS fused evaluation order (n >= 2)."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    out = np.empty_like(pts)
+    _lib().oracle_rotate_rows(_ptr(pts), len(pts), _ptr(R), _ptr(out))
+    return out
+
+
+def fma_xyz(x, y, z, R):
+    """R @ vstack([x, y, z]) with the BLAS fused evaluation order."""
+    shape = np.shape(x)
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    y = np.ascontiguousarray(y, dtype=np.float64).ravel()
+    z = np.ascontiguousarray(z, dtype=np.float64).ravel()
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    ox, oy, oz = np.empty_like(x), np.empty_like(y), np.empty_like(z)
+    _lib().oracle_rotate_xyz(_ptr(x), _ptr(y), _ptr(z), len(x), _ptr(R),
+                             _ptr(ox), _ptr(oy), _ptr(oz))
+    return ox.reshape(shape), oy.reshape(shape), oz.reshape(shape)
+
+
+# --------------------------------------------------------------------------
+# tables: International Tables Vol. C, Table 6.1.1.4 (Cromer-Mann) for the
+# elements the tests use, and atomic numbers.
+Z_OF = {"H": 1, "C": 6, "N": 7, "O": 8, "F": 9, "Si": 14, "S": 16}
+CROMER_MANN = {
+    "C": (2.31, 20.8439, 1.02, 10.2075, 1.5886, 0.5687, 0.865, 51.6512, 0.2156),
+}
+
+
+# --------------------------------------------------------------------------
+# voxel path
+
+def rotate_coords_z(coords, phi):
+    """utilities.py:303-317: coords @ Rz(phi).T."""
+    pr = np.radians(phi)
+    R = np.array([[np.cos(pr), -np.sin(pr), 0],
+                  [np.sin(pr), np.cos(pr), 0],
+                  [0, 0, 1]])
+    return fma_rows(coords, R)
+
+
+def rectangular_collapse_lengths(x_vals, hor_length, ver_length, phi):
+    """voxelgrids.py:238-309, vectorised with the same branch order and the
+    same floating-point expression trees."""
+    x_vals = np.asarray(x_vals, dtype=np.float64)
+    if phi > 90:
+        phi = phi - 90
+        hor_length, ver_length = ver_length, hor_length
+    theta = 90 - phi
+    theta_rad = np.deg2rad(theta)
+    phi_rad = np.deg2rad(phi)
+    if phi == 0:
+        return np.where(x_vals < hor_length, ver_length, 0).astype(np.float64)
+    if phi == 90:
+        return np.where(x_vals < ver_length, hor_length, 0).astype(np.float64)
+    stop1 = ver_length * np.cos(theta_rad)
+    stop2 = hor_length * np.cos(phi_rad)
+    if stop1 < stop2:
+        mid_length = ver_length / np.sin(theta_rad)
+    else:
+        stop1, stop2 = stop2, stop1
+        mid_length = hor_length / np.sin(phi_rad)
+    out = np.zeros_like(x_vals)
+    vc = ver_length * np.cos(theta_rad)
+    base = np.sqrt(ver_length ** 2 - vc ** 2)
+    tphi = np.tan(phi_rad)
+    ttheta = np.tan(theta_rad)
+    cphi = np.cos(phi_rad)
+    ctheta = np.cos(theta_rad)
+    for i, x in enumerate(x_vals):
+        if x == 0:
+            v = 0.0
+        elif x < stop1:
+            v = (base + x * tphi) - ((vc - x) * ttheta)
+        elif x <= stop2:
+            v = mid_length
+        elif x < stop1 + stop2:
+            v = (hor_length - ((x - vc) / cphi)) / ctheta
+        else:
+            v = 0.0
+        out[i] = v
+    return out
+
+
+def mask_bounds(lo, hi, sigma, n):
+    """Start/stop of the smoothing plateau mask[lo+sigma : hi-sigma] with
+    Python slice normalisation (voxelgrids.py:369-370); ceil() extends the
+    bounds to non-integer sigma."""
+    start = int(math.ceil(lo + sigma))
+    stop = int(math.ceil(hi - sigma))
+    s, e, _ = slice(start, stop).indices(n)
+    return s, e
+
+
+def smooth_profile(n, lo, hi, sigma):
+    """gaussian_filter1d(mask, sigma, mode='wrap') of the plateau mask."""
+    m = np.zeros(n)
+    s, e = mask_bounds(lo, hi, sigma, n)
+    m[s:e] = 1
+    return gaussian_filter1d(m, sigma=sigma, mode="wrap")
+
+
+def project_slice(coords, f_values, phi, grid_size, r_voxel_size, avg_voxel_f,
+                  x_bound, y_bound, z_bound, fill_bkg, smooth):
+    """voxelgrids.py:318-379: rotate, shift, nearest-bin deposit, fill, smooth.
+    Returns (grid complex128 (g,g) [z,y], info dict)."""
+    g = grid_size
+    rot = rotate_coords_z(coords, phi)
+    rot[:, 0] -= np.min(rot[:, 0])
+    rot[:, 1] -= np.min(rot[:, 1])
+    rot[:, 2] -= np.min(rot[:, 2])
+    yi = (rot[:, 1] // r_voxel_size).astype(int)
+    zi = (rot[:, 2] // r_voxel_size).astype(int)
+    ok = (yi >= 0) & (yi < g) & (zi >= 0) & (zi < g)
+    yi, zi, fv = yi[ok], zi[ok], f_values[ok]
+    grid = np.zeros((g, g), dtype=complex)
+    np.add.at(grid, (zi, yi), fv)
+    max_voxels = np.sqrt(x_bound ** 2 + y_bound ** 2) // r_voxel_size
+    y_min, z_min = np.min(yi), np.min(zi)
+    y_max, z_max = np.max(yi), np.max(zi)
+    if fill_bkg:
+        xv = np.arange(g) * r_voxel_size
+        lengths = rectangular_collapse_lengths(xv, y_bound, x_bound, phi)
+        missing = (max_voxels - (lengths // r_voxel_size)).astype(int)
+        grid = grid + np.tile(missing * avg_voxel_f, (g, 1))
+        fillv = avg_voxel_f * max_voxels
+        grid[:z_min, :] = fillv
+        grid[z_max:, :] = fillv
+        grid[z_min:z_max + 1, :y_min + 1] = fillv
+        grid[z_min:z_max + 1, y_max:] = fillv
+    if smooth:
+        avg_val = avg_voxel_f * max_voxels
+        my = smooth_profile(g, y_min, y_max, smooth)
+        mz = smooth_profile(g, z_min, z_max, smooth)
+        M = np.outer(mz, my)
+        grid = grid * M + avg_val * (1 - M)
+    info = dict(y_idx=yi, z_idx=zi, valid=ok, y_min=y_min, y_max=y_max,
+                z_min=z_min, z_max=z_max, max_voxels=max_voxels)
+    return grid, info
+
+
+def slice_intensity(grid):
+    """voxelgrids.py:388-392: |fftshift(fftn(grid))|^2."""
+    return np.abs(fftshift(fft2(grid))) ** 2
+
+
+def slice_axes(grid_size, r_voxel_size, phi):
+    """voxelgrids.py:382-402: (det_h_qx, det_h_qy, det_v_qz)."""
+    q_h = fftshift(np.fft.fftfreq(grid_size, d=r_voxel_size) * 2 * np.pi)
+    q_v = fftshift(np.fft.fftfreq(grid_size, d=r_voxel_size) * 2 * np.pi)
+    right_qy = np.max(q_h) * np.cos(np.deg2rad(-phi))
+    right_qx = -np.max(q_h) * np.sin(np.deg2rad(-phi))
+    hy = np.linspace(-right_qy, right_qy, num=len(q_h))
+    hx = np.linspace(-right_qx, right_qx, num=len(q_h))
+    return hx, hy, q_v
+
+
+def bin_indices(det_h_qx, det_h_qy, det_v_qz, qx, qy, qz):
+    """voxelgrids.py:474-499: masks and flat voxel indices of one slice.
+    Returns (v_mask, h_mask, qy_idx[h], qx_idx[h], qz_idx[v])."""
+    hm = ((det_h_qx <= np.max(qx)) & (det_h_qx >= np.min(qx))
+          & (det_h_qy <= np.max(qy)) & (det_h_qy >= np.min(qy)))
+    vm = (det_v_qz <= np.max(qz)) & (det_v_qz >= np.min(qz))
+    dq = np.diff(qz)[0]
+    ix = ((det_h_qx[hm] - np.min(qx)) // dq).astype(int)
+    iy = ((det_h_qy[hm] - np.min(qy)) // dq).astype(int)
+    iz = ((det_v_qz[vm] - np.min(qz)) // dq).astype(int)
+    return vm, hm, iy, ix, iz
+
+
+def bin_slice(iq_2d, det_h_qx, det_h_qy, det_v_qz, qx, qy, qz, vsum, vcount):
+    """voxelgrids.py:464-506 (process_file2) into plain arrays."""
+    vm, hm, iy, ix, iz = bin_indices(det_h_qx, det_h_qy, det_v_qz, qx, qy, qz)
+    sub = iq_2d[vm, :][:, hm]
+    IY = np.broadcast_to(iy[None, :], sub.shape).ravel()
+    IX = np.broadcast_to(ix[None, :], sub.shape).ravel()
+    IZ = np.broadcast_to(iz[:, None], sub.shape).ravel()
+    np.add.at(vsum, (IY, IX, IZ), sub.ravel())
+    np.add.at(vcount, (IY, IX, IZ), 1.0)
+
+
+def voxel_geometry(r_voxel_size, q_voxel_size, max_q, coords=None):
+    """comparison.py:704-731: checks, grid size, q axis, automatic phis."""
+    max_q_diag = np.sqrt(2) * max_q
+    if max_q_diag > 2 * np.pi / r_voxel_size:
+        raise Exception("Max_q is non-physical for given voxel size")
+    grid_size = int(np.ceil(2 * np.pi / (q_voxel_size * r_voxel_size)))
+    if coords is not None:
+        b = [np.max(coords[:, i]) - np.min(coords[:, i]) for i in range(3)]
+        if grid_size * r_voxel_size < np.min(b):
+            raise Exception("Calculated real-space bounds smaller than "
+                            "simulation. Please lower delta_q value")
+    max_q_diag = max_q_diag + max_q_diag % q_voxel_size
+    q_num = ((2 * max_q_diag / q_voxel_size) + 1).astype(int)
+    if q_num % 2 == 0:
+        q_num += 1
+    q = np.linspace(-max_q_diag, max_q_diag, q_num)
+    dphi = np.arctan(q_voxel_size / max_q_diag)
+    phi_num = np.ceil(2 * np.pi / dphi).astype(int)
+    phis = np.linspace(0, 180 - (180 / phi_num), num=phi_num)
+    return grid_size, q, phis
+
+
+def downselect_voxelgrid(grid, x_axis, y_axis, z_axis, max_val):
+    """voxelgrids.py:16-48."""
+    vs = np.abs(x_axis[1] - x_axis[0])
+    max_val = max_val + vs
+    xi = np.where(np.abs(x_axis) < max_val)[0]
+    yi = np.where(np.abs(y_axis) < max_val)[0]
+    zi = np.where(np.abs(z_axis) < max_val)[0]
+    sub = grid[yi[0]:yi[-1] + 1, xi[0]:xi[-1] + 1, zi[0]:zi[-1] + 1]
+    return (sub, x_axis[xi[0]:xi[-1] + 1], y_axis[yi[0]:yi[-1] + 1],
+            z_axis[zi[0]:zi[-1] + 1])
+
+
+def f0_factor(qx_axis, qy_axis, qz_axis, element="C"):
+    """voxelgrids.py:838-854: ((sum_i a_i exp(-b_i q^2/16pi^2) + c)/Z)^2."""
+    Z = Z_OF[element]
+    a = CROMER_MANN[element]
+    qx, qy, qz = np.meshgrid(qx_axis, qy_axis, qz_axis)
+    q2 = qx ** 2 + qy ** 2 + qz ** 2
+    s = 16 * np.pi ** 2
+    return ((a[0] * np.exp(-a[1] * q2 / s) + a[2] * np.exp(-a[3] * q2 / s)
+             + a[4] * np.exp(-a[5] * q2 / s) + a[6] * np.exp(-a[7] * q2 / s)
+             + a[8]) / Z) ** 2
+
+
+def add_f0_q_3d(iq, qx_axis, qy_axis, qz_axis, element="C"):
+    """voxelgrids.py:828-857."""
+    return iq * f0_factor(qx_axis, qy_axis, qz_axis, element)
+
+
+def structure_constants(coords, f_values, r_voxel_size):
+    """comparison.py:712-744: bounds and the average voxel scattering factor."""
+    xb = np.max(coords[:, 0]) - np.min(coords[:, 0])
+    yb = np.max(coords[:, 1]) - np.min(coords[:, 1])
+    zb = np.max(coords[:, 2]) - np.min(coords[:, 2])
+    avg = (np.sum(f_values) / (xb * yb * zb)) * r_voxel_size ** 3
+    return xb, yb, zb, avg
+
+
+def voxelgrid(structures, r_voxel_size, q_voxel_size, max_q, phis=None,
+              fill_bkg=False, smooth=0, f0_element="C", keep_full=False):
+    """comparison.py:673-788 restated; `structures` is a list of
+    (coords (N,3) float64, f_values (N,) complex128).  With several
+    structures the cropped I(q) grids are averaged before the f0 factor, as
+    old_modules/voxelgridmaker.py:56-72 does.
+
+    Returns dict(iq, qx, qy, qz, count, sum) -- count/sum are the cropped
+    count and sum grids of the last structure's accumulation (counts are
+    structure independent)."""
+    grid_size, q, auto_phis = voxel_geometry(r_voxel_size, q_voxel_size, max_q,
+                                             structures[0][0])
+    if phis is None:
+        phis = auto_phis
+    qn = len(q)
+    iq_acc = None
+    for coords, fv in structures:
+        voxel_geometry(r_voxel_size, q_voxel_size, max_q, coords)
+        xb, yb, zb, avg = structure_constants(coords, fv, r_voxel_size)
+        vsum = np.zeros((qn, qn, qn))
+        vcnt = np.zeros((qn, qn, qn))
+        for phi in phis:
+            grid, _ = project_slice(coords, fv, phi, grid_size, r_voxel_size,
+                                    avg, xb, yb, zb, fill_bkg, smooth)
+            iq2 = slice_intensity(grid)
+            hx, hy, vz = slice_axes(grid_size, r_voxel_size, phi)
+            bin_slice(iq2, hx, hy, vz, q, q, q, vsum, vcnt)
+        iq = np.divide(vsum, vcnt, out=np.zeros_like(vsum), where=vcnt != 0)
+        iq_s, qxs, qys, qzs = downselect_voxelgrid(iq, q, q, q, max_q)
+        iq_acc = iq_s.copy() if iq_acc is None else iq_acc + iq_s
+    iq_acc = iq_acc / len(structures) if len(structures) > 1 else iq_acc
+    out = dict(iq=add_f0_q_3d(iq_acc, qxs, qys, qzs, f0_element),
+               qx=qxs, qy=qys, qz=qzs,
+               count=downselect_voxelgrid(vcnt, q, q, q, max_q)[0],
+               sum=downselect_voxelgrid(vsum, q, q, q, max_q)[0],
+               grid_size=grid_size, q=q, phis=np.asarray(phis))
+    if keep_full:
+        out["full_sum"], out["full_count"] = vsum, vcnt
+    return out
+
+
+# --------------------------------------------------------------------------
+# detector path
+
+def rotation_matrix(u, theta):
+    """utilities.py:222-245 (Rodrigues), same expression trees."""
+    ux, uy, uz = u[0], u[1], u[2]
+    R = np.zeros((3, 3))
+    c, s = np.cos(theta), np.sin(theta)
+    R[0, 0] = c + ux ** 2 * (1 - c)
+    R[0, 1] = ux * uy * (1 - c) - uz * s
+    R[0, 2] = ux * uz * (1 - c) + uy * s
+    R[1, 0] = uy * ux * (1 - c) + uz * s
+    R[1, 1] = c + uy ** 2 * (1 - c)
+    R[1, 2] = uy * uz * (1 - c) - ux * s
+    R[2, 0] = uz * ux * (1 - c) - uy * s
+    R[2, 1] = uz * uy * (1 - c) + ux * s
+    R[2, 2] = c + uz ** 2 * (1 - c)
+    return R
+
+
+def make_detector(h_max, nh, v_max, nv):
+    """detector.py:5-29."""
+    h = np.linspace(-h_max, h_max, nh)
+    v = np.linspace(-v_max, v_max, nv)
+    y, z = np.meshgrid(h, v)
+    return np.zeros_like(y), y, z, h, v
+
+
+def _corner(x, y, z, i, j):
+    return np.array([x[i, j], y[i, j], z[i, j]])
+
+
+def axis_matrix(x, y, z, kind, angle_deg):
+    """The rotation matrix each of detector.py:33-162 builds from the current
+    grid's corners."""
+    p1 = _corner(x, y, z, 0, 0)
+    if kind == "psi":
+        v1 = _corner(x, y, z, 0, -1) - p1
+        v2 = _corner(x, y, z, -1, 0) - p1
+        ax = np.cross(v1, v2)
+    elif kind == "theta":
+        ax = _corner(x, y, z, 0, -1) - p1
+    elif kind == "phi":
+        ax = _corner(x, y, z, -1, 0) - p1
+    else:
+        raise ValueError(kind)
+    ax = ax / np.linalg.norm(ax)
+    return rotation_matrix(ax, np.radians(angle_deg))
+
+
+def rotate_about(x, y, z, kind, angle_deg):
+    R = axis_matrix(x, y, z, kind, angle_deg)
+    return fma_xyz(x, y, z, R)
+
+
+def rotate_psi_phi_theta(x, y, z, psi, phi, theta):
+    """detector.py:234-244."""
+    x, y, z = rotate_about(x, y, z, "psi", psi)
+    x, y, z = rotate_about(x, y, z, "phi", phi)
+    x, y, z = rotate_about(x, y, z, "theta", theta)
+    return x, y, z
+
+
+def intersect_indices(iq_shape, qx, qy, qz, x, y, z):
+    """detector.py:213-224: clipped voxel indices of each pixel."""
+    dq = np.diff(qz)[0]
+    ix = ((x.ravel() - np.min(qx)) // dq).astype(int)
+    iy = ((y.ravel() - np.min(qy)) // dq).astype(int)
+    iz = ((z.ravel() - np.min(qz)) // dq).astype(int)
+    ix = np.clip(ix, 0, iq_shape[1] - 1)
+    iy = np.clip(iy, 0, iq_shape[0] - 1)
+    iz = np.clip(iz, 0, iq_shape[2] - 1)
+    return iy, ix, iz
+
+
+def intersect_detector(iq, qx, qy, qz, x, y, z):
+    """detector.py:194-232."""
+    iy, ix, iz = intersect_indices(iq.shape, qx, qy, qz, x, y, z)
+    return iq[iy, ix, iz].reshape(x.shape)
+
+
+def mirror_vertical_horizontal(qmap):
+    """detector.py:246-275."""
+    lr = np.fliplr(qmap)
+    ud = np.flipud(qmap)
+    udlr = np.fliplr(ud)
+    out = qmap + lr + ud + udlr
+    nr, nc = qmap.shape
+    if nr % 2:
+        row = qmap[nr // 2, :]
+        out[nr // 2, :] = (row + row[::-1]) * 2
+    if nc % 2:
+        col = qmap[:, nc // 2]
+        out[:, nc // 2] = (col + col[::-1]) * 2
+    if nr % 2 and nc % 2:
+        out[nr // 2, nc // 2] = qmap[nr // 2, nc // 2] * 4
+    return out
+
+
+def init_detector(num_pixels, max_q, angle_init_vals, angle_init_axs):
+    """comparison.py:792-818."""
+    x, y, z, h, v = make_detector(max_q, num_pixels, max_q, num_pixels)
+    for val, ax in zip(angle_init_vals, angle_init_axs):
+        if ax in ("psi", "phi", "theta"):
+            x, y, z = rotate_about(x, y, z, ax, val)
+    return x, y, z, h, v
+
+
+def orientation_list(psis, psi_w, phis, phi_w, thetas, theta_w):
+    """comparison.py:836-841 ordering: psi outer, phi, theta inner."""
+    out = []
+    for ps, pw in zip(psis, psi_w):
+        for ph, hw in zip(phis, phi_w):
+            for th, tw in zip(thetas, theta_w):
+                out.append((ps, pw, ph, hw, th, tw))
+    return out
+
+
+def detector(iq, qx, qy, qz, num_pixels, max_q, angle_init_vals,
+             angle_init_axs, psis, psi_weights, phis, phi_weights, thetas,
+             theta_weights, mirror=True):
+    """comparison.py:790-870 restated with weights passed as arrays (None ->
+    uniform) and a serial orientation loop."""
+    x0, y0, z0, h, v = init_detector(num_pixels, max_q, angle_init_vals,
+                                     angle_init_axs)
+    psis, phis, thetas = map(np.asarray, (psis, phis, thetas))
+    psi_weights = (np.ones_like(psis) / len(psis) if psi_weights is None
+                   else np.asarray(psi_weights))
+    phi_weights = (np.ones_like(phis) / len(phis) if phi_weights is None
+                   else np.asarray(phi_weights))
+    theta_weights = (np.ones_like(thetas) / len(thetas) if theta_weights is None
+                     else np.asarray(theta_weights))
+    acc = np.zeros((num_pixels, num_pixels))
+    for ps, pw, ph, hw, th, tw in orientation_list(
+            psis, psi_weights, phis, phi_weights, thetas, theta_weights):
+        x, y, z = rotate_psi_phi_theta(x0, y0, z0, ps, ph, th)
+        d = intersect_detector(iq, qx, qy, qz, x, y, z)
+        d = d * (pw * hw * tw)
+        acc += d
+    det = acc.copy()
+    if mirror:
+        det = mirror_vertical_horizontal(det)
+    det[det != det] = 1e-6
+    det[det <= 0] = 1e-6
+    det *= 1e-6
+    return det, h, v

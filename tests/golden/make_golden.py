@@ -1,0 +1,207 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference
+GIWAXSim code itself (a Python package, imported from its checkout).
+
+Run in a container that has the reference checkout:
+    python tests/golden/make_golden.py [/path/to/reference]
+
+The reference imports matplotlib, mpl_toolkits, fabio, lmfit and xraydb and
+scipy.signal.tukey at module level; none of these is on the computation path
+under test, so they are replaced with inert stubs and the tukey alias.  xraydb's
+f'/f'' lookup returns 0, i.e. f = Z for every atom (the product and the oracle
+take f values as an input, so this is the parity boundary).
+
+Every fixture is small (the whole set is a few MB) so the CPU test suite loads
+it in seconds.  Inputs are seeded and stored next to the outputs.
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+class _Stub(types.ModuleType):
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        return lambda *a, **k: None
+
+
+def _import_reference():
+    import scipy.signal
+    import scipy.signal.windows
+    for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.cm",
+                 "matplotlib.ticker", "matplotlib.colors", "mpl_toolkits",
+                 "mpl_toolkits.mplot3d", "xraydb", "fabio", "lmfit"]:
+        m = _Stub(name)
+        m.__path__ = []
+        sys.modules[name] = m
+    sys.modules["xraydb"].f1_chantler = lambda el, e: 0.0
+    sys.modules["xraydb"].f2_chantler = lambda el, e: 0.0
+    if not hasattr(scipy.signal, "tukey"):
+        scipy.signal.tukey = scipy.signal.windows.tukey
+    sys.path.insert(0, REF)
+    from tools import comparison, detector, utilities, voxelgrids
+    return comparison, detector, utilities, voxelgrids
+
+
+def small_graphite(seed=0, size=(12.0, 11.0, 13.0)):
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from giwaxsim_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    xyz, _ = workloads.graphite_slab(size, rng, disp_sigma=0.05)
+    return xyz
+
+
+def main():
+    comparison, detector, utilities, voxelgrids = _import_reference()
+    rng = np.random.default_rng(1234)
+
+    # 1. rotations: atoms (np.dot(coords, R.T)) and detector planes
+    #    (R @ vstack) -- pins the fused BLAS evaluation order.
+    coords = rng.uniform(-60, 60, (300, 3))
+    phis = np.concatenate([[0.0, 45.0, 90.0, 179.0],
+                           rng.uniform(0, 180, 6)])
+    rot = np.stack([utilities.rotate_coords_z(coords, p) for p in phis])
+    dx, dy, dz, dh, dv = detector.make_detector(2.5, 9, 2.5, 7)
+    det_rots = []
+    angles = [(90.0, 30.0, 10.0), (12.5, 0.0, 0.0), (0.0, 47.0, 0.0),
+              (0.0, 0.0, 33.0), (170.0, 95.0, 181.0)]
+    for a in angles:
+        x, y, z = detector.rotate_about_normal(dx, dy, dz, a[0])
+        x, y, z = detector.rotate_about_vertical(x, y, z, a[1])
+        x, y, z = detector.rotate_about_horizontal(x, y, z, a[2])
+        det_rots.append(np.stack([x, y, z]))
+    np.savez_compressed(os.path.join(HERE, "golden_rotation.npz"),
+                        coords=coords, phis=phis, rot=rot,
+                        det_angles=np.array(angles), det_rot=np.stack(det_rots))
+
+    # 2. numpy floor division on values adjacent to multiples of the divisor
+    bs = np.array([0.3, 0.25, 0.2, 0.03, 0.02, 0.015, 0.04095, 0.1])
+    a_list, b_list = [], []
+    for b in bs:
+        k = rng.integers(-2000, 2000, 400).astype(np.float64)
+        a = k * b
+        for arr in (a, np.nextafter(a, np.inf), np.nextafter(a, -np.inf)):
+            a_list.append(arr)
+            b_list.append(np.full(arr.shape, b))
+    fa, fb = np.concatenate(a_list), np.concatenate(b_list)
+    np.savez_compressed(os.path.join(HERE, "golden_floordiv.npz"),
+                        a=fa, b=fb, q=fa // fb)
+
+    # 3. rectangular_collapse_lengths
+    cases = []
+    for phi in [0.0, 30.0, 45.0, 60.0, 89.0, 90.0, 91.0, 120.0, 135.0, 179.0,
+                180.0] + list(rng.uniform(0, 180, 8)):
+        for hor, ver in [(50.0, 50.0), (30.0, 70.0), (97.3, 41.2)]:
+            xv = np.arange(350) * 0.3
+            cases.append((phi, hor, ver,
+                          voxelgrids.rectangular_collapse_lengths(
+                              xv, hor, ver, phi).astype(np.float64)))
+    np.savez_compressed(os.path.join(HERE, "golden_collapse.npz"),
+                        phi=np.array([c[0] for c in cases]),
+                        hor=np.array([c[1] for c in cases]),
+                        ver=np.array([c[2] for c in cases]),
+                        x=np.arange(350) * 0.3,
+                        lengths=np.stack([c[3] for c in cases]))
+
+    # 4. single slices through the reference's own per-slice worker
+    #    (rotate_project_fft_coords -> process_file2), all fill/smooth modes.
+    xyz = small_graphite(0)
+    elements = np.array(["C"] * len(xyz))
+    r, dq, max_q = 0.5, 0.15, 1.5
+    g = int(np.ceil(2 * np.pi / (dq * r)))
+    mqd = np.sqrt(2) * max_q
+    mqd = mqd + mqd % dq
+    qn = int((2 * mqd / dq) + 1)
+    qn += (qn % 2 == 0)
+    q = np.linspace(-mqd, mqd, qn)
+    f_values = np.full(len(xyz), 6.0 + 0j)
+    xb, yb, zb = [np.max(xyz[:, i]) - np.min(xyz[:, i]) for i in range(3)]
+    avg = (np.sum(f_values) / (xb * yb * zb)) * r ** 3
+    slice_phis = np.array([0.0, 17.0, 45.0, 90.0, 133.5])
+    out = dict(coords=xyz, r=r, dq=dq, max_q=max_q, g=g, q=q,
+               phis=slice_phis)
+    for mode, (fill, smooth) in {"plain": (False, 0), "fill": (True, 0),
+                                 "smooth": (False, 2),
+                                 "fillsmooth": (True, 1)}.items():
+        shm_s = utilities.create_shared_array((qn, qn, qn))
+        shm_c = utilities.create_shared_array((qn, qn, qn))
+        try:
+            vs = np.ndarray((qn, qn, qn), dtype=np.float64, buffer=shm_s.buf)
+            vc = np.ndarray((qn, qn, qn), dtype=np.float64, buffer=shm_c.buf)
+            vs[:] = 0
+            vc[:] = 0
+            for phi in slice_phis:
+                voxelgrids.rotate_project_fft_coords(
+                    (xyz, f_values, phi, g, r, avg, xb, yb, zb, fill, smooth,
+                     q, q, q, shm_s.name, shm_c.name))
+            out["sum_" + mode] = vs.copy()
+            out["count_" + mode] = vc.copy()
+        finally:
+            shm_s.close()
+            shm_s.unlink()
+            shm_c.close()
+            shm_c.unlink()
+    np.savez_compressed(os.path.join(HERE, "golden_slices.npz"), **out)
+
+    # 5. the full voxel driver (automatic phis, threaded as shipped)
+    xyz = small_graphite(1, size=(10.0, 10.0, 10.0))
+    elements = np.array(["C"] * len(xyz))
+    vox = {}
+    for mode, (fill, smooth) in {"plain": (False, 0),
+                                 "fillsmooth": (True, 1)}.items():
+        iq, qx, qy, qz = comparison.voxelgridmaker_fitting(
+            xyz, elements, 0.5, 0.2, 1.2, 10000, fill_bkg=fill, smooth=smooth)
+        vox["iq_" + mode] = iq
+    np.savez_compressed(os.path.join(HERE, "golden_voxel.npz"), coords=xyz,
+                        r=0.5, dq=0.2, max_q=1.2, qx=qx, qy=qy, qz=qz, **vox)
+
+    # 6. the detector driver on that grid (mirror=True: the shipped code
+    #    reads a released buffer when mirror=False)
+    iq = vox["iq_plain"]
+    psis = np.linspace(0, 180, 7)
+    dphis = np.array([0.0, 20.0])
+    thetas = np.array([0.0, 5.0])
+    det_sum, det_h, det_v = comparison.detectormaker_fitting(
+        iq, qx, qy, qz, 21, 1.2, (90.0, 30.0, 10.0), ("psi", "phi", "theta"),
+        psis, None, dphis, None, thetas, None, mirror=True)
+    det_sum2, _, _ = comparison.detectormaker_fitting(
+        iq, qx, qy, qz, 16, 1.2, (0.0, 0.0, 0.0), ("None", "None", "None"),
+        np.linspace(0, 90, 10), None, np.array([0.0]), None,
+        np.array([0.0]), None, mirror=True)
+    # single orientations through generate_detector_ints' pieces
+    x0, y0, z0, _, _ = detector.make_detector(1.2, 21, 1.2, 21)
+    singles = []
+    for a in [(0.0, 0.0, 0.0), (33.0, 12.0, 7.0), (90.0, 0.0, 0.0)]:
+        x, y, z = detector.rotate_psi_phi_theta(x0, y0, z0, *a)
+        singles.append(detector.intersect_detector(iq, qx, qy, qz, x, y, z))
+    np.savez_compressed(os.path.join(HERE, "golden_detector.npz"),
+                        det_sum=det_sum, det_h=det_h, det_v=det_v,
+                        det_sum2=det_sum2, single_angles=np.array(
+                            [(0.0, 0.0, 0.0), (33.0, 12.0, 7.0),
+                             (90.0, 0.0, 0.0)]),
+                        singles=np.stack(singles))
+    # mirror fold on odd and even shapes
+    mi = {}
+    for shp in [(7, 9), (8, 6), (7, 6), (8, 9)]:
+        a = rng.normal(size=shp)
+        mi["in_%dx%d" % shp] = a
+        mi["out_%dx%d" % shp] = detector.mirror_vertical_horizontal(a)
+    np.savez_compressed(os.path.join(HERE, "golden_mirror.npz"), **mi)
+
+    # 7. add_f0_q_3d and downselect_voxelgrid
+    qa = np.linspace(-2.0, 2.0, 21)
+    grid = rng.uniform(0, 1, (21, 21, 21))
+    f0 = voxelgrids.add_f0_q_3d(grid, qa, qa, qa, "C")
+    ds = voxelgrids.downselect_voxelgrid(grid, qa, qa, qa, 1.1)
+    np.savez_compressed(os.path.join(HERE, "golden_f0.npz"), q=qa, grid=grid,
+                        f0=f0, ds_grid=ds[0], ds_x=ds[1])
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

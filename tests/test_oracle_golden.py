@@ -1,0 +1,116 @@
+"""The oracle against outputs of the reference itself (tests/golden, made by
+tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import giwaxs_oracle as O
+from tests.conftest import golden
+
+
+def test_rotate_coords_z_bits():
+    d = golden("golden_rotation.npz")
+    for phi, ref in zip(d["phis"], d["rot"]):
+        got = O.rotate_coords_z(d["coords"], phi)
+        assert np.array_equal(got, ref), phi
+
+
+def test_detector_rotation_chain_bits():
+    d = golden("golden_rotation.npz")
+    x0, y0, z0, _, _ = O.make_detector(2.5, 9, 2.5, 7)
+    for ang, ref in zip(d["det_angles"], d["det_rot"]):
+        x, y, z = O.rotate_about(x0, y0, z0, "psi", ang[0])
+        x, y, z = O.rotate_about(x, y, z, "phi", ang[1])
+        x, y, z = O.rotate_about(x, y, z, "theta", ang[2])
+        assert np.array_equal(np.stack([x, y, z]), ref), ang
+
+
+def test_floor_division_is_exact_real_floor():
+    from fractions import Fraction
+    import math
+    d = golden("golden_floordiv.npz")
+    assert np.array_equal(d["a"] // d["b"], d["q"])
+    sub = slice(0, None, 7)
+    exact = [math.floor(Fraction(float(a)) / Fraction(float(b)))
+             for a, b in zip(d["a"][sub], d["b"][sub])]
+    assert np.array_equal(np.array(exact, dtype=np.float64), d["q"][sub])
+
+
+def test_collapse_lengths_bits():
+    d = golden("golden_collapse.npz")
+    for phi, hor, ver, ref in zip(d["phi"], d["hor"], d["ver"], d["lengths"]):
+        got = O.rectangular_collapse_lengths(d["x"], hor, ver, phi)
+        assert np.array_equal(got, ref), (phi, hor, ver)
+
+
+@pytest.mark.parametrize("mode,fill,smooth", [
+    ("plain", False, 0), ("fill", True, 0), ("smooth", False, 2),
+    ("fillsmooth", True, 1)])
+def test_slices_sum_count(mode, fill, smooth):
+    d = golden("golden_slices.npz")
+    xyz, q, g, r = d["coords"], d["q"], int(d["g"]), float(d["r"])
+    fv = np.full(len(xyz), 6.0 + 0j)
+    xb, yb, zb, avg = O.structure_constants(xyz, fv, r)
+    qn = len(q)
+    vs, vc = np.zeros((qn,) * 3), np.zeros((qn,) * 3)
+    for phi in d["phis"]:
+        grid, _ = O.project_slice(xyz, fv, phi, g, r, avg, xb, yb, zb, fill,
+                                  smooth)
+        hx, hy, vz = O.slice_axes(g, r, phi)
+        O.bin_slice(O.slice_intensity(grid), hx, hy, vz, q, q, q, vs, vc)
+    assert np.array_equal(vc, d["count_" + mode])
+    ref = d["sum_" + mode]
+    assert np.linalg.norm(vs - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("mode,fill,smooth", [("plain", False, 0),
+                                              ("fillsmooth", True, 1)])
+def test_voxel_driver(mode, fill, smooth):
+    d = golden("golden_voxel.npz")
+    xyz = d["coords"]
+    fv = np.full(len(xyz), 6.0 + 0j)
+    out = O.voxelgrid([(xyz, fv)], float(d["r"]), float(d["dq"]),
+                      float(d["max_q"]), None, fill, smooth)
+    for k in ("qx", "qy", "qz"):
+        assert np.array_equal(out[k], d[k])
+    ref = d["iq_" + mode]
+    assert out["iq"].shape == ref.shape
+    assert np.linalg.norm(out["iq"] - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+def test_detector_driver():
+    v = golden("golden_voxel.npz")
+    d = golden("golden_detector.npz")
+    iq, qx, qy, qz = v["iq_plain"], v["qx"], v["qy"], v["qz"]
+    det, h, vv = O.detector(iq, qx, qy, qz, 21, 1.2, (90.0, 30.0, 10.0),
+                            ("psi", "phi", "theta"), np.linspace(0, 180, 7),
+                            None, np.array([0.0, 20.0]), None,
+                            np.array([0.0, 5.0]), None, mirror=True)
+    assert np.array_equal(h, d["det_h"]) and np.array_equal(vv, d["det_v"])
+    assert np.linalg.norm(det - d["det_sum"]) <= 1e-13 * np.linalg.norm(
+        d["det_sum"])
+    det2, _, _ = O.detector(iq, qx, qy, qz, 16, 1.2, (0.0, 0.0, 0.0),
+                            ("None",) * 3, np.linspace(0, 90, 10), None,
+                            np.array([0.0]), None, np.array([0.0]), None, True)
+    assert np.linalg.norm(det2 - d["det_sum2"]) <= 1e-13 * np.linalg.norm(
+        d["det_sum2"])
+    x0, y0, z0, _, _ = O.make_detector(1.2, 21, 1.2, 21)
+    for ang, ref in zip(d["single_angles"], d["singles"]):
+        x, y, z = O.rotate_psi_phi_theta(x0, y0, z0, *ang)
+        assert np.array_equal(O.intersect_detector(iq, qx, qy, qz, x, y, z),
+                              ref)
+
+
+def test_mirror():
+    d = golden("golden_mirror.npz")
+    for shp in [(7, 9), (8, 6), (7, 6), (8, 9)]:
+        got = O.mirror_vertical_horizontal(d["in_%dx%d" % shp])
+        assert np.array_equal(got, d["out_%dx%d" % shp])
+
+
+def test_f0_and_downselect():
+    d = golden("golden_f0.npz")
+    q = d["q"]
+    got = O.add_f0_q_3d(d["grid"], q, q, q, "C")
+    assert np.allclose(got, d["f0"], rtol=1e-14, atol=0)
+    sub, x, _, _ = O.downselect_voxelgrid(d["grid"], q, q, q, 1.1)
+    assert np.array_equal(sub, d["ds_grid"]) and np.array_equal(x, d["ds_x"])
