@@ -1,0 +1,457 @@
+"""Benchmark of the GIWAXS forward path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload si-100A]
+
+A step is one full voxel stage over every phi slice of the workload (all
+slices -> cropped I(q) with counts, average and f0).  Headline metric:
+slices/s.  The same JSON line also carries the seconds per detector image
+(voxel stage + detector, batched and plain), the roofline of the dominant
+kernel, the CPU baseline (the float64 numpy oracle on the host cores), the
+SM clocks sampled during the timed region, and e2e (the public drop-in API
+voxelgridmaker_fitting on host numpy arrays, copies included).
+
+Multi-GPU: the path has no exchange step that this build performs; each rank
+runs an independent replica of the workload (weak scaling), rank 0 prints.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "slices/s & s/detector image: batched vs plain on 1 GB300 at <=1e-5 rel err vs FP64"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="si-100A")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx = float(s[1])
+            except (ValueError, IndexError):
+                continue
+            for k, n in enumerate(names):
+                if len(s) > 3 + k and s[3 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ workload
+def load_workload(name):
+    from giwaxsim_gb300 import forward as F
+    from giwaxsim_gb300 import workloads as W
+    w = W.WORKLOADS[name]
+    structs = W.structures(name)
+    geom = F.VoxelGeometry(w["r"], w["dq"], w["max_q"])
+    phis = W.phis_linspace(w["n_phi"])
+    items = [(xyz, F.element_f_values(el, w["energy"]), wt)
+             for xyz, el, wt in structs]
+    return w, structs, geom, phis, items
+
+
+def detector_args(w, geom):
+    init_vals, init_axs = w["init"]
+    a, b, n = w["psis"]
+    psis = np.linspace(a, b, n)
+    one = np.array([0.0])
+    return dict(num_pixels=w["num_pixels"], max_q=w["max_q"],
+                angle_init_vals=init_vals, angle_init_axs=init_axs, psis=psis,
+                psi_weights=np.ones_like(psis) / len(psis), phis=one,
+                phi_weights=one + 1.0, thetas=one, theta_weights=one + 1.0)
+
+
+# ------------------------------------------------------------------ gb300 arm
+def run_gb300(args, world, rank, local, pg):
+    from giwaxsim_gb300 import _native as N
+    from giwaxsim_gb300 import forward as F
+    from giwaxsim_gb300.tools import comparison
+
+    w, structs, geom, phis, items = load_workload(args.workload)
+    ctx = N.Context(local)
+    n_slices = len(items) * len(phis)
+    plan = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
+                       smooth=w["smooth"], ctx=ctx)
+    plan.set_atoms()
+    plan.execute()
+    ctx.synchronize()
+    plan.capture_graph()
+    info = plan.info()
+    # L2 flush buffer (written between timed iterations, outside the events)
+    flush = None
+    try:
+        import torch
+        flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32,
+                            device="cuda:%d" % local)
+    except Exception:
+        flush = None
+
+    stream = ctx.stream()
+    import torch
+    ts = torch.cuda.ExternalStream(stream, device="cuda:%d" % local)
+
+    def do_flush():
+        if flush is not None:
+            with torch.cuda.stream(ts):
+                flush.fill_(1.0)
+
+    for _ in range(args.warmup):
+        plan.execute()
+    ctx.synchronize()
+    barrier(pg)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launch_count()
+    evs = []
+    for _ in range(args.steps):
+        do_flush()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ts)
+        plan.execute()
+        e1.record(ts)
+        evs.append((e0, e1))
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    t_ms = sum(a.elapsed_time(b) for a, b in evs)
+    t_ms = max_over_ranks(pg, t_ms)
+    barrier(pg)
+    ms_per_step = t_ms / args.steps
+    value = world * n_slices * args.steps / (t_ms / 1e3)
+
+    # detector (batched) on the device-resident float32 I(q)
+    dargs = detector_args(w, geom)
+    q = geom.q_crop
+    det = F.DetectorPlan((plan.Qc,) * 3, q, q, q, dargs["num_pixels"],
+                         dargs["max_q"], dargs["angle_init_vals"],
+                         dargs["angle_init_axs"], dargs["psis"],
+                         dargs["psi_weights"], dargs["phis"],
+                         dargs["phi_weights"], dargs["thetas"],
+                         dargs["theta_weights"], mirror=True, ctx=ctx)
+    det.set_iq_device32(plan.device_iq32())
+    for _ in range(2):
+        det.execute()
+    ctx.synchronize()
+    d0 = torch.cuda.Event(enable_timing=True)
+    d1 = torch.cuda.Event(enable_timing=True)
+    d0.record(ts)
+    nd = max(1, args.steps)
+    for _ in range(nd):
+        det.execute()
+    d1.record(ts)
+    torch.cuda.synchronize()
+    det_ms = d0.elapsed_time(d1) / nd
+
+    # per-kernel device times (eager, instrumented replica of the same work)
+    eager = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
+                        smooth=w["smooth"], ctx=ctx)
+    eager.set_atoms()
+    eager.execute()
+    ctx.synchronize()
+    ctx.set_timing(True)
+    eager.execute()
+    det.execute()
+    kt = ctx.kernel_times()
+    ctx.set_timing(False)
+    eager.close()
+
+    # plain per-rotation path: one slice per launch sequence, full grid
+    plain = None
+    if not args.no_plain:
+        n_plain = min(len(phis), 24)
+        pp = F.VoxelPlan(geom, items[:1], phis=phis[:n_plain],
+                         fill_bkg=w["fill_bkg"], smooth=w["smooth"],
+                         mode="plain", ctx=ctx)
+        pp.set_atoms()
+        pp.execute()
+        ctx.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(ts)
+        pp.execute()
+        p1.record(ts)
+        torch.cuda.synchronize()
+        plain_ms = p0.elapsed_time(p1)
+        plain = n_plain / (plain_ms / 1e3)
+        pp.close()
+
+    # e2e through the public API with host arrays
+    e2e = None
+    if len(items) == 1:
+        xyz, el, wt = structs[0]
+        t_e = []
+        for k in range(1 + max(1, min(args.steps, 3))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            iq, qx, qy, qz = comparison.voxelgridmaker_fitting(
+                xyz, el, w["r"], w["dq"], w["max_q"], w["energy"],
+                fill_bkg=w["fill_bkg"], smooth=w["smooth"], phis=phis,
+                weights=wt, ctx=ctx)
+            t_e.append(time.perf_counter() - t0)
+        te = float(np.mean(t_e[1:]))
+        e2e = {"value": world * n_slices / te, "unit": "slices/s",
+               "h2d_bytes_per_step": int(xyz.size * 8 + len(xyz) * 8),
+               "d2h_bytes_per_step": int(iq.size * 8),
+               "s_per_step": te}
+
+    # roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    top = max(kt.items(), key=lambda kv: kv[1][0]) if kt else None
+    roof = None
+    if top:
+        name, (ms_tot, nl) = top
+        avg_ms = ms_tot / max(nl, 1)
+        algo = algorithmic_bytes(name, info, w, n_slices, dargs, plan.Qc)
+        achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
+        roof = {"kernel": name, "bound": "hbm", "achieved": achieved,
+                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": None, "avg_launch_ms": avg_ms,
+                "algorithmic_bytes_per_launch": algo}
+    kernel_share = {k: {"ms": round(v[0], 4), "launches": v[1]}
+                    for k, v in kt.items()}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, w, geom, phis, items)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "slices/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 accum)",
+        "data": "synthetic (seeded structure generator)",
+        "config": {"workload": args.workload, "atoms": int(len(plan.xyz)),
+                   "grid_size": geom.grid_size, "crop": plan.Qc,
+                   "slices_per_step": n_slices,
+                   "detector_px": w["num_pixels"],
+                   "orientations": int(det.n_orient),
+                   "l2": "flushed between timed iterations (2x L2 write)",
+                   "plan": info},
+        "s_per_detector_image": {
+            "batched": ms_per_step / 1e3 / len(items) + det_ms / 1e3,
+            "detector_only_s": det_ms / 1e3,
+            "plain": (n_slices / plain / len(items) + det_ms / 1e3) if plain else None},
+        "plain_slices_per_s": plain,
+        "batched_vs_plain": (value / world / plain) if plain else None,
+        "gpu_launches": int(launches),
+        "e2e": e2e, "roofline": roof, "kernel_ms": kernel_share,
+        "cpu_baseline": cpu, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    for p_ in (det, plan):
+        p_.close()
+
+
+def algorithmic_bytes(name, info, w, n_slices, dargs, Qc):
+    """Bytes a launch of `name` must move at minimum (its inputs read once,
+    outputs written once), per the plan's sizes."""
+    S = info["batch"]
+    if name == "row_czt":
+        return S * info["Lz"] * (info["Ly"] + info["Nc"]) * 8
+    if name == "col_czt_bin":
+        # F1 read + float64 read-modify-write of every binned pixel
+        return S * (info["Lz"] * info["Nc"] * 8 + info["Nr"] * info["Nc"] * 16)
+    if name == "detector":
+        npx = dargs["num_pixels"] ** 2
+        return len(dargs["psis"]) * npx * 4 + npx * 8
+    if name == "finalize":
+        return Qc ** 3 * (8 + 8 + 4)
+    return None
+
+
+# ------------------------------------------------------------------ CPU
+def _cpu_slices(payload):
+    from oracle import giwaxs_oracle as O
+    (xyz, fv, phis, g, r, fill, smooth, q, consts, vs, vc) = payload
+    xb, yb, zb, avg = consts
+    t0 = time.perf_counter()
+    for phi in phis:
+        grid, _ = O.project_slice(xyz, fv, phi, g, r, avg, xb, yb, zb, fill,
+                                  smooth)
+        hx, hy, vz = O.slice_axes(g, r, phi)
+        O.bin_slice(O.slice_intensity(grid), hx, hy, vz, q, q, q, vs, vc)
+    return time.perf_counter() - t0, len(phis)
+
+
+def cpu_baseline(args, w, geom, phis, items, budget=None):
+    """The float64 numpy oracle on a bounded sample of the workload's slices,
+    threaded over slices like the reference's ThreadPoolExecutor."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import giwaxs_oracle as O
+    budget = budget or args.cpu_seconds
+    xyz, fv, wt = items[0]
+    fvw = fv if wt is None else fv * wt
+    consts = O.structure_constants(xyz, fvw, w["r"])
+    cores = os.cpu_count() or 1
+    workers = min(32, cores + 4)
+    # one shared (sum, count) grid, as the reference's threads share one
+    qn = len(geom.q)
+    vs = np.zeros((qn, qn, qn))
+    vc = np.zeros((qn, qn, qn))
+    # one slice first to size the sample
+    t1, _ = _cpu_slices((xyz, fvw, phis[:1], geom.grid_size, w["r"],
+                         w["fill_bkg"], w["smooth"], geom.q, consts, vs, vc))
+    per_batch = workers
+    n_target = max(1, int(budget / max(t1, 1e-3) * min(workers, cores) * 0.5))
+    n_target = min(n_target, len(phis))
+    sample = phis[np.linspace(0, len(phis) - 1, n_target).astype(int)]
+    chunks = [sample[i::per_batch] for i in range(per_batch)]
+    chunks = [c for c in chunks if len(c)]
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        list(ex.map(_cpu_slices, [(xyz, fvw, c, geom.grid_size, w["r"],
+                                   w["fill_bkg"], w["smooth"], geom.q, consts,
+                                   vs, vc) for c in chunks]))
+    dt = time.perf_counter() - t0
+    return {"value": len(sample) / dt, "unit": "slices/s", "cores": cores,
+            "threads": workers, "kind": "port",
+            "sample": "%d of %d slices of %s (float64 numpy oracle, %d "
+                      "threads), %.1f s" % (len(sample), len(phis),
+                                             args.workload, workers, dt)}
+
+
+def run_reference(args, world, rank, local, pg):
+    if rank != 0:
+        return
+    w, structs, geom, phis, items = load_workload(args.workload)
+    vals = []
+    for _ in range(max(1, args.warmup > 0) + args.steps):
+        vals.append(cpu_baseline(args, w, geom, phis, items,
+                                 budget=max(2.0, args.cpu_seconds / max(1, args.steps))))
+    v = vals[-args.steps:]
+    value = float(np.mean([x["value"] for x in v]))
+    cb = dict(v[-1])
+    cb["value"] = value
+    out = {"metric": METRIC, "impl": "reference", "value": value,
+           "unit": "slices/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": None,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded structure generator)",
+           "config": {"workload": args.workload,
+                      "slices_per_step": len(phis) * len(items)},
+           "cpu_baseline": cb,
+           "e2e": {"value": value, "unit": "slices/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, local, pg)
+    else:
+        run_gb300(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

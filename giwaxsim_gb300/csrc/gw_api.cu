@@ -1,0 +1,253 @@
+// Context, error reporting, allocation and host helpers of the C ABI.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "gw_common.cuh"
+
+namespace gw {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int status, const std::string &msg) {
+  set_error(msg);
+  return status;
+}
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "%s failed: %s (%s) at %s:%d", what,
+           cudaGetErrorName(e), cudaGetErrorString(e), file, line);
+  set_error(buf);
+  return e == cudaErrorMemoryAllocation ? GW_ERR_OOM : GW_ERR_CUDA;
+}
+
+static std::atomic<long long> g_alloc_count{0};
+
+cudaError_t dev_malloc(void **p, size_t bytes) {
+  static const long long fail_after = [] {
+    const char *s = getenv("GW_FAIL_ALLOC_AFTER");
+    return s ? atoll(s) : -1LL;
+  }();
+  const long long n = g_alloc_count.fetch_add(1);
+  if (fail_after >= 0 && n >= fail_after) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+
+void dev_free(void *p) {
+  if (p) cudaFree(p);
+}
+
+int check_device_error(gw_ctx *ctx, const char *where) {
+  int h = 0;
+  GW_CUDA(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  GW_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (h == GW_DEVERR_NONE) return GW_OK;
+  GW_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+  const char *what = "unknown device check";
+  switch (h) {
+    case GW_DEVERR_BOX:
+      what = "an atom fell outside the slice window sized from the structure "
+             "bounds";
+      break;
+    case GW_DEVERR_MASK_WRAP:
+      what = "the smoothing mask wraps around the grid (structure extent "
+             "smaller than 2*smooth); unsupported";
+      break;
+    case GW_DEVERR_NO_ATOMS:
+      what = "zero-size array to reduction operation minimum which has no "
+             "identity (no atom inside the real-space grid)";
+      break;
+  }
+  return fail(GW_ERR_BOUNDS, std::string(where) + ": " + what);
+}
+
+static cudaEvent_t take_event(gw_ctx *c) {
+  if (!c->ev_free.empty()) {
+    cudaEvent_t e = c->ev_free.back();
+    c->ev_free.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+KTimer::KTimer(gw_ctx *ctx, int category) : c(ctx), cat(category) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!c->timing || cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone)
+    return;
+  a = take_event(c);
+  if (a) cudaEventRecord(a, c->stream);
+}
+
+KTimer::~KTimer() {
+  if (!a) return;
+  cudaEvent_t b = take_event(c);
+  if (!b) return;
+  cudaEventRecord(b, c->stream);
+  c->pending.push_back({a, b, cat});
+}
+
+static void collect(gw_ctx *c) {
+  for (auto &p : c->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      c->kms[p.cat] += ms;
+      c->kn[p.cat] += 1;
+    }
+    c->ev_free.push_back(p.a);
+    c->ev_free.push_back(p.b);
+  }
+  c->pending.clear();
+}
+
+}  // namespace gw
+
+extern "C" {
+
+int gw_ctx_set_timing(gw_ctx *c, int32_t on) {
+  if (!c) return gw::fail(GW_ERR_ARG, "gw_ctx_set_timing: null context");
+  if (on) {
+    GW_CUDA(cudaStreamSynchronize(c->stream));
+    gw::collect(c);
+    for (int i = 0; i < GW_K_COUNT; ++i) { c->kms[i] = 0; c->kn[i] = 0; }
+  }
+  c->timing = on != 0;
+  return GW_OK;
+}
+
+int gw_ctx_kernel_times(gw_ctx *c, double *ms, int64_t *launches, int32_t n) {
+  if (!c || !ms || !launches) return gw::fail(GW_ERR_ARG, "gw_ctx_kernel_times: null argument");
+  GW_CUDA(cudaStreamSynchronize(c->stream));
+  gw::collect(c);
+  const int k = n < GW_K_COUNT ? n : GW_K_COUNT;
+  for (int i = 0; i < k; ++i) { ms[i] = c->kms[i]; launches[i] = c->kn[i]; }
+  return k;
+}
+
+const char *gw_kernel_category_name(int32_t i) {
+  static const char *names[GW_K_COUNT] = {
+      "prep", "tables", "deposit", "profile", "row_czt", "col_czt_bin",
+      "finalize", "detector", "det_epilogue", "misc"};
+  return (i >= 0 && i < GW_K_COUNT) ? names[i] : "unknown";
+}
+
+int gw_version(void) { return 1; }
+
+const char *gw_status_string(int s) {
+  switch (s) {
+    case GW_OK: return "GW_OK";
+    case GW_ERR_ARG: return "GW_ERR_ARG";
+    case GW_ERR_OOM: return "GW_ERR_OOM";
+    case GW_ERR_CUDA: return "GW_ERR_CUDA";
+    case GW_ERR_TIMEOUT: return "GW_ERR_TIMEOUT";
+    case GW_ERR_BOUNDS: return "GW_ERR_BOUNDS";
+    case GW_ERR_STATE: return "GW_ERR_STATE";
+  }
+  return "GW_UNKNOWN";
+}
+
+size_t gw_last_error(char *buf, size_t len) {
+  const std::string &m = gw::g_last_error;
+  if (buf && len) {
+    size_t n = m.size() < len - 1 ? m.size() : len - 1;
+    memcpy(buf, m.data(), n);
+    buf[n] = 0;
+  }
+  return m.size();
+}
+
+int gw_ctx_create(int device, gw_ctx **out) {
+  if (!out) return gw::fail(GW_ERR_ARG, "gw_ctx_create: out is null");
+  int n = 0;
+  GW_CUDA(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n)
+    return gw::fail(GW_ERR_ARG, "gw_ctx_create: no such CUDA device");
+  GW_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  GW_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10)
+    return gw::fail(GW_ERR_ARG, "gw_ctx_create: this library is built for "
+                                "sm_103a (GB300); device is older");
+  auto *c = new gw_ctx();
+  c->device = device;
+  c->sm_count = prop.multiProcessorCount;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = gw::dev_malloc((void **)&c->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    gw_ctx_destroy(c);
+    return gw::cuda_fail(e, "gw_ctx_create", __FILE__, __LINE__);
+  }
+  *out = c;
+  return GW_OK;
+}
+
+int gw_ctx_destroy(gw_ctx *c) {
+  if (!c) return GW_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  gw::collect(c);
+  for (cudaEvent_t e : c->ev_free) cudaEventDestroy(e);
+  gw::dev_free(c->d_err);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return GW_OK;
+}
+
+int gw_ctx_synchronize(gw_ctx *c) {
+  if (!c) return gw::fail(GW_ERR_ARG, "gw_ctx_synchronize: null context");
+  GW_CUDA(cudaStreamSynchronize(c->stream));
+  return gw::check_device_error(c, "device checks");
+}
+
+int gw_ctx_stream(gw_ctx *c, void **stream) {
+  if (!c || !stream) return gw::fail(GW_ERR_ARG, "gw_ctx_stream: null argument");
+  *stream = (void *)c->stream;
+  return GW_OK;
+}
+
+int64_t gw_ctx_launch_count(gw_ctx *c) { return c ? c->launches : -1; }
+
+int gw_rotate_points(const double *R, const double *pts, int64_t n,
+                     double *out) {
+  if (!R || (!pts && n) || (!out && n) || n < 0)
+    return gw::fail(GW_ERR_ARG, "gw_rotate_points: invalid argument");
+  for (int64_t k = 0; k < n; ++k) {
+    const double x = pts[3 * k], y = pts[3 * k + 1], z = pts[3 * k + 2];
+    const double a = rot_chain(R, x, y, z);
+    const double b = rot_chain(R + 3, x, y, z);
+    const double c = rot_chain(R + 6, x, y, z);
+    out[3 * k] = a;
+    out[3 * k + 1] = b;
+    out[3 * k + 2] = c;
+  }
+  return GW_OK;
+}
+
+int gw_collapse_base(const double *ver, const double *cos_t, int64_t n,
+                     double *out) {
+  if (n < 0 || (n && (!ver || !cos_t || !out)))
+    return gw::fail(GW_ERR_ARG, "gw_collapse_base: invalid argument");
+  // numpy's scalar x**2 calls libm pow(), which is not always x*x; the
+  // volatile exponent keeps the compiler from folding pow(x, 2.0) to x*x.
+  volatile double two = 2.0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double vc = ver[i] * cos_t[i];
+    out[i] = std::sqrt(std::pow(ver[i], two) - std::pow(vc, two));
+  }
+  return GW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+// Shared device/host helpers of the GIWAXS GB300 library.
+//
+// Exactness rules used throughout:
+//  * numpy's float `a // b` is the exact floor of the real quotient
+//    (npy_divmod: fmod-based, then snapped).  floor_div_exact() reproduces
+//    it with a rounded quotient estimate and two sign tests of fused
+//    remainders, each of which is exact in sign.
+//  * BLAS 3-term dot products are the fused chain
+//    fma(p2,R2, fma(p1,R1, p0*R0)); rot_chain() states it with intrinsics.
+//  * np.linspace(start, stop, num)[i] = i*step + start (two roundings), or
+//    (i/div)*delta + start when step == 0, and the last element is stop.
+// All FP64 arithmetic that feeds an index uses __d*_rn intrinsics so that
+// nvcc cannot contract it into different fused operations.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "giwaxs_gb300.h"
+
+#define GW_HD __host__ __device__ __forceinline__
+
+// ---------------------------------------------------------------- exact ops
+#ifdef __CUDA_ARCH__
+#define GW_DMUL(a, b) __dmul_rn((a), (b))
+#define GW_DADD(a, b) __dadd_rn((a), (b))
+#define GW_DSUB(a, b) __dsub_rn((a), (b))
+#define GW_DDIV(a, b) __ddiv_rn((a), (b))
+#define GW_DFMA(a, b, c) __fma_rn((a), (b), (c))
+#define GW_DSQRT(a) __dsqrt_rn(a)
+#else
+#include <cmath>
+#define GW_DMUL(a, b) ((a) * (b))
+#define GW_DADD(a, b) ((a) + (b))
+#define GW_DSUB(a, b) ((a) - (b))
+#define GW_DDIV(a, b) ((a) / (b))
+#define GW_DFMA(a, b, c) std::fma((a), (b), (c))
+#define GW_DSQRT(a) std::sqrt(a)
+#endif
+
+// Exact floor(a / b) for b > 0 and |a/b| < 2^52, as numpy's float //.
+// inv_b is 1/b rounded (any estimate within a few ulps works).
+GW_HD double floor_div_exact(double a, double b, double inv_b) {
+  double k = floor(GW_DMUL(a, inv_b));
+  if (GW_DFMA(-k, b, a) < 0.0) {
+    k = GW_DSUB(k, 1.0);
+  } else if (GW_DFMA(-GW_DADD(k, 1.0), b, a) >= 0.0) {
+    k = GW_DADD(k, 1.0);
+  }
+  return k;
+}
+
+// Row i of R (row-major 3x3) applied to (x,y,z) in the BLAS fused order.
+GW_HD double rot_chain(const double *Ri, double x, double y, double z) {
+  return GW_DFMA(z, Ri[2], GW_DFMA(y, Ri[1], GW_DMUL(x, Ri[0])));
+}
+
+// np.linspace(start, stop, num)[i]
+GW_HD double linspace_at(double start, double stop, int num, int i) {
+  if (i == num - 1) return stop;
+  double div = (double)(num - 1);
+  double delta = GW_DSUB(stop, start);
+  double step = GW_DDIV(delta, div);
+  double y;
+  if (step == 0.0) {
+    y = GW_DMUL(GW_DDIV((double)i, div), delta);
+  } else {
+    y = GW_DMUL((double)i, step);
+  }
+  return GW_DADD(y, start);
+}
+
+// Order-preserving map double -> uint64 (for atomicMin/Max on doubles).
+GW_HD unsigned long long dbl_ord(double d) {
+#ifdef __CUDA_ARCH__
+  long long b = __double_as_longlong(d);
+#else
+  long long b;
+  memcpy(&b, &d, sizeof b);
+#endif
+  return b >= 0 ? ((unsigned long long)b | 0x8000000000000000ULL)
+                : ~(unsigned long long)b;
+}
+GW_HD double ord_dbl(unsigned long long u) {
+  long long b = (u & 0x8000000000000000ULL)
+                    ? (long long)(u & 0x7fffffffffffffffULL)
+                    : (long long)~u;
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+// ---------------------------------------------------------------- context
+#include <vector>
+
+enum gw_kcat {
+  GW_K_PREP = 0,     // per-structure z reduction and z indices
+  GW_K_TABLES,       // per-phi column tables and count factors
+  GW_K_DEPOSIT,      // per-slice y reduction + atom deposit
+  GW_K_PROFILE,      // fill_bkg / smoothing profiles
+  GW_K_ROW,          // row chirp-z transforms
+  GW_K_COLBIN,       // column chirp-z transforms + |F|^2 + binning
+  GW_K_FINALIZE,     // average, crop, f0
+  GW_K_DETECTOR,     // detector orientation sum
+  GW_K_DET_EPI,      // mirror / clamp / scale
+  GW_K_MISC,         // conversions, debug
+  GW_K_COUNT
+};
+
+struct gw_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  int sm_count = 0;
+  // device-side error word: first failing check writes its code.
+  int *d_err = nullptr;
+  // per-kernel timing
+  int timing = 0;
+  std::vector<cudaEvent_t> ev_free;
+  struct Pending { cudaEvent_t a, b; int cat; };
+  std::vector<Pending> pending;
+  double kms[GW_K_COUNT] = {};
+  int64_t kn[GW_K_COUNT] = {};
+};
+
+namespace gw {
+
+// thread-local last error message
+void set_error(const std::string &msg);
+int fail(int status, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+// fault injection for allocation failures: GW_FAIL_ALLOC_AFTER=<n> makes the
+// (n+1)-th device allocation of the process fail with GW_ERR_OOM.
+cudaError_t dev_malloc(void **p, size_t bytes);
+void dev_free(void *p);
+
+// checks the device error word of ctx (synchronizes the stream)
+int check_device_error(gw_ctx *ctx, const char *where);
+
+}  // namespace gw
+
+#define GW_CUDA(call)                                                    \
+  do {                                                                   \
+    cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess)                                               \
+      return gw::cuda_fail(_e, #call, __FILE__, __LINE__);               \
+  } while (0)
+
+#define GW_LAUNCHED(ctx)                                                 \
+  do {                                                                   \
+    (ctx)->launches++;                                                   \
+    cudaError_t _e = cudaGetLastError();                                 \
+    if (_e != cudaSuccess)                                               \
+      return gw::cuda_fail(_e, "kernel launch", __FILE__, __LINE__);     \
+  } while (0)
+
+namespace gw {
+// Brackets one launch with events when ctx->timing is on.
+struct KTimer {
+  gw_ctx *c;
+  int cat;
+  cudaEvent_t a = nullptr;
+  KTimer(gw_ctx *ctx, int category);
+  ~KTimer();
+};
+}  // namespace gw
+
+#define GW_TRY(expr)                                                     \
+  do {                                                                   \
+    int _s = (expr);                                                     \
+    if (_s != GW_OK) return _s;                                          \
+  } while (0)
+
+// device error codes written to ctx->d_err
+enum { GW_DEVERR_NONE = 0, GW_DEVERR_BOX = 1, GW_DEVERR_MASK_WRAP = 2,
+       GW_DEVERR_NO_ATOMS = 3 };
+
+__device__ __forceinline__ void dev_error(int *err, int code) {
+  atomicCAS(err, 0, code);
+}
+
+// float2 complex helpers
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  return make_float2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) {
+  return make_float2(a.x * s, a.y * s);
+}

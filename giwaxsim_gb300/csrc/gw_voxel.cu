@@ -1,0 +1,1192 @@
+// Voxel stage: atoms -> per-phi projected scattering-factor slices -> 2-D
+// DFT -> |F|^2 -> rotational binning -> I(q) average, crop and f0 factor.
+//
+// Reference: tools/comparison.py:673-788 (voxelgridmaker_fitting), the
+// per-slice worker tools/voxelgrids.py:311-416 and the binning
+// tools/voxelgrids.py:464-506.
+//
+// GB300 design (batched mode):
+//  * A slice's real-space grid is D + Cbg, with Cbg the constant background
+//    that fill_bkg/smoothing paint outside the slab and D compactly
+//    supported (slab footprint plus the Gaussian tail).  DFT(Cbg) is a
+//    single value at q = 0, added back before |.|^2.  Only D is transformed.
+//  * Only the output rows/columns whose pixels land in the cropped cube are
+//    produced: each 1-D DFT is a band-limited chirp-z transform
+//    X[k0+m] = B[m] * sum_n (D[n] A[n]) h[m-n], evaluated as a circular
+//    convolution with power-of-two shared-memory FFTs (gw_fft.cuh).
+//  * Row transforms (along y) write an intermediate F1[slice][z][col];
+//    column transforms (along z) finish the DFT and bin |F|^2 straight into
+//    the float64 sum grid of the cropped cube with atomics.
+//  * Counts depend only on geometry and factor as C2[qy,qx] * C1[qz]; the
+//    count grid is never materialised.
+// Plain mode keeps the reference's structure: the full g x g grid with its
+// background, the full transform, binning into the whole q_num^3 cube and a
+// crop afterwards, one slice per launch sequence.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "gw_common.cuh"
+#include "gw_fft.cuh"
+
+namespace {
+
+constexpr int kMinM = 64, kMaxM = 8192;
+
+struct SliceArgs {
+  // geometry
+  int g;
+  double r, inv_r;
+  int n_phi;
+  int y_lo, Ly, z_lo, Lz;
+  int fill, smooth_on;
+  float sigma;
+  int radius;
+  int plain;
+  // arrays
+  const double *xyz;
+  const float2 *f;
+  const int *zidx;
+  const gw_structure *st;
+  const gw_phi *ph;
+  const double *clbase;  // per slice
+  unsigned long long *ymin_ord;
+  int4 *ext;  // y_min, y_max, z_min, z_max (valid atoms)
+  float2 *box;
+  float2 *amo;
+  float *my, *mz;
+  const float *gw;  // gaussian weights, 2*radius+1
+  int *err;
+};
+
+// ------------------------------------------------------------ structure prep
+__global__ void k_zmin(const double *xyz, const gw_structure *st,
+                       unsigned long long *zmin_ord) {
+  const gw_structure s = st[blockIdx.y];
+  unsigned long long best = ~0ULL;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    double z = xyz[3 * (s.atom_begin + i) + 2];
+    best = min(best, dbl_ord(z));
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0 && best != ~0ULL)
+    atomicMin(zmin_ord + blockIdx.y, best);
+}
+
+// z index is phi independent: rotation about z leaves z unchanged
+// (fma(z,1,fma(y,0,x*0)) == z), utilities.py:303-317.
+__global__ void k_zidx(const double *xyz, const gw_structure *st,
+                       const unsigned long long *zmin_ord, double r,
+                       double inv_r, int *zidx) {
+  const gw_structure s = st[blockIdx.y];
+  const double zmin = ord_dbl(zmin_ord[blockIdx.y]);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = s.atom_begin + i;
+    double z = GW_DSUB(xyz[3 * a + 2], zmin);
+    zidx[a] = (int)floor_div_exact(z, r, inv_r);
+  }
+}
+
+// ------------------------------------------------------------ per slice
+__device__ __forceinline__ double rot_y(const double *p, double c, double s) {
+  // column 1 of np.dot(coords, Rz.T): fma(z,0,fma(y,c,x*s)) == fma(y,c,x*s)
+  return GW_DFMA(p[1], c, GW_DMUL(p[0], s));
+}
+
+__global__ void k_ymin(SliceArgs a, int slice0) {
+  const int sl = slice0 + blockIdx.y;
+  const int t = sl / a.n_phi, p = sl % a.n_phi;
+  const gw_structure s = a.st[t];
+  const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
+  unsigned long long best = ~0ULL;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    best = min(best, dbl_ord(rot_y(a.xyz + 3 * (s.atom_begin + i), c, sn)));
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0 && best != ~0ULL)
+    atomicMin(a.ymin_ord + sl, best);
+}
+
+// voxelgrids.py:321-341: shift, floor-divide, valid mask, np.add.at deposit.
+__global__ void k_deposit(SliceArgs a, int slice0) {
+  const int sl = slice0 + blockIdx.y;
+  const int t = sl / a.n_phi, p = sl % a.n_phi;
+  const gw_structure s = a.st[t];
+  const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
+  const double ymin = ord_dbl(a.ymin_ord[sl]);
+  float2 *box = a.box + (size_t)blockIdx.y * a.Lz * a.Ly;
+  int ymn = INT_MAX, ymx = -1, zmn = INT_MAX, zmx = -1;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t at = s.atom_begin + i;
+    const double y = GW_DSUB(rot_y(a.xyz + 3 * at, c, sn), ymin);
+    const int yi = (int)floor_div_exact(y, a.r, a.inv_r);
+    const int zi = a.zidx[at];
+    if (yi >= 0 && yi < a.g && zi >= 0 && zi < a.g) {
+      ymn = min(ymn, yi); ymx = max(ymx, yi);
+      zmn = min(zmn, zi); zmx = max(zmx, zi);
+      int yy = yi - a.y_lo; if (yy >= a.g) yy -= a.g;
+      int zz = zi - a.z_lo; if (zz >= a.g) zz -= a.g;
+      if (yy < a.Ly && zz < a.Lz) {
+        float2 *dst = box + (size_t)zz * a.Ly + yy;
+        const float2 fv = a.f[at];
+        atomicAdd(&dst->x, fv.x);
+        atomicAdd(&dst->y, fv.y);
+      } else {
+        dev_error(a.err, GW_DEVERR_BOX);
+      }
+    }
+  }
+  ymn = __reduce_min_sync(0xffffffffu, ymn);
+  ymx = __reduce_max_sync(0xffffffffu, ymx);
+  zmn = __reduce_min_sync(0xffffffffu, zmn);
+  zmx = __reduce_max_sync(0xffffffffu, zmx);
+  if ((threadIdx.x & 31) == 0 && ymx >= 0) {
+    int4 *e = a.ext + sl;
+    atomicMin(&e->x, ymn); atomicMax(&e->y, ymx);
+    atomicMin(&e->z, zmn); atomicMax(&e->w, zmx);
+  }
+}
+
+// rectangular_collapse_lengths (voxelgrids.py:238-309) at column x_val.
+__device__ double collapse_length(const gw_phi &ph, double hor, double ver,
+                                  double base, double x) {
+  if (ph.cl_swap) { double t = hor; hor = ver; ver = t; }
+  if (ph.cl_case == 0) return x < hor ? ver : 0.0;
+  if (ph.cl_case == 1) return x < ver ? hor : 0.0;
+  const double vc = GW_DMUL(ver, ph.cos_t);
+  double stop1 = vc, stop2 = GW_DMUL(hor, ph.cos_p), mid;
+  if (stop1 < stop2) {
+    mid = GW_DDIV(ver, ph.sin_t);
+  } else {
+    double t = stop1; stop1 = stop2; stop2 = t;
+    mid = GW_DDIV(hor, ph.sin_p);
+  }
+  if (x == 0.0) return 0.0;
+  if (x < stop1) {
+    const double tot = GW_DADD(base, GW_DMUL(x, ph.tan_p));
+    const double miss = GW_DMUL(GW_DSUB(vc, x), ph.tan_t);
+    return GW_DSUB(tot, miss);
+  }
+  if (x <= stop2) return mid;
+  if (x < GW_DADD(stop1, stop2)) {
+    const double rem = GW_DSUB(hor, GW_DDIV(GW_DSUB(x, vc), ph.cos_p));
+    return GW_DDIV(rem, ph.cos_t);
+  }
+  return 0.0;
+}
+
+// Python slice normalisation of [start:stop] on a length-n axis.
+__device__ __forceinline__ void py_slice(int start, int stop, int n, int &s,
+                                         int &e) {
+  if (start < 0) { start += n; if (start < 0) start = 0; }
+  else if (start > n) start = n;
+  if (stop < 0) { stop += n; if (stop < 0) stop = 0; }
+  else if (stop > n) stop = n;
+  s = start;
+  e = stop;
+}
+
+// gaussian_filter1d(mask, sigma, mode='wrap') of the plateau [ms, me).
+__device__ float smooth_at(int i, int ms, int me, int g, int radius,
+                           const float *w) {
+  float acc = 0.f;
+  for (int j = -radius; j <= radius; ++j) {
+    int k = i + j;
+    k %= g; if (k < 0) k += g;
+    if (k >= ms && k < me) acc += w[j + radius];
+  }
+  return acc;
+}
+
+// Per-slice profiles: fill_bkg column term (minus the background) and the
+// two separable smoothing masks (voxelgrids.py:344-379).
+__global__ void k_profile(SliceArgs a, int slice0) {
+  const int sl = slice0 + blockIdx.x;
+  const int t = sl / a.n_phi, p = sl % a.n_phi;
+  const gw_structure s = a.st[t];
+  const gw_phi ph = a.ph[p];
+  const int4 e = a.ext[sl];
+  if (e.y < 0) {  // no valid atom: np.min of an empty array raises
+    if (threadIdx.x == 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
+    return;
+  }
+  const double cre = GW_DMUL(s.avg_f_re, s.max_voxels);
+  const double cim = GW_DMUL(s.avg_f_im, s.max_voxels);
+  const bool bg = !a.plain && (a.fill || a.smooth_on);
+  if (a.fill) {
+    const double base = a.clbase[sl];
+    for (int yy = threadIdx.x; yy < a.Ly; yy += blockDim.x) {
+      int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
+      const double x = GW_DMUL((double)yi, a.r);
+      const double len = collapse_length(ph, s.y_bound, s.x_bound, base, x);
+      const double nm = GW_DSUB(s.max_voxels, floor_div_exact(len, a.r, a.inv_r));
+      const double n_missing = (double)(long long)nm;
+      double re = GW_DMUL(n_missing, s.avg_f_re);
+      double im = GW_DMUL(n_missing, s.avg_f_im);
+      if (bg) { re -= cre; im -= cim; }
+      a.amo[(size_t)blockIdx.x * a.Ly + yy] = make_float2((float)re, (float)im);
+    }
+  }
+  if (a.smooth_on) {
+    const float sg = a.sigma;
+    int ys, ye, zs, ze;
+    py_slice((int)ceilf((float)e.x + sg), (int)ceilf((float)e.y - sg), a.g, ys, ye);
+    py_slice((int)ceilf((float)e.z + sg), (int)ceilf((float)e.w - sg), a.g, zs, ze);
+    for (int yy = threadIdx.x; yy < a.Ly; yy += blockDim.x) {
+      int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
+      a.my[(size_t)blockIdx.x * a.Ly + yy] = smooth_at(yi, ys, ye, a.g, a.radius, a.gw);
+    }
+    for (int zz = threadIdx.x; zz < a.Lz; zz += blockDim.x) {
+      int zi = a.z_lo + zz; if (zi < 0) zi += a.g; if (zi >= a.g) zi -= a.g;
+      a.mz[(size_t)blockIdx.x * a.Lz + zz] = smooth_at(zi, zs, ze, a.g, a.radius, a.gw);
+    }
+    // the smoothing support must lie inside the transformed window
+    if (threadIdx.x == 0 && a.Ly < a.g) {
+      int l = a.y_lo - 1; if (l < 0) l += a.g;
+      int r = a.y_lo + a.Ly; r %= a.g; if (r < 0) r += a.g;
+      if (smooth_at(l, ys, ye, a.g, a.radius, a.gw) != 0.f ||
+          smooth_at(r, ys, ye, a.g, a.radius, a.gw) != 0.f)
+        dev_error(a.err, GW_DEVERR_MASK_WRAP);
+    }
+    if (threadIdx.x == 0 && a.Lz < a.g) {
+      int l = a.z_lo - 1; if (l < 0) l += a.g;
+      int r = a.z_lo + a.Lz; r %= a.g; if (r < 0) r += a.g;
+      if (smooth_at(l, zs, ze, a.g, a.radius, a.gw) != 0.f ||
+          smooth_at(r, zs, ze, a.g, a.radius, a.gw) != 0.f)
+        dev_error(a.err, GW_DEVERR_MASK_WRAP);
+    }
+  }
+}
+
+// --------------------------------------------------------------- CZT stages
+struct CztArgs {
+  int M;
+  int L, N;  // input length, output length
+  const float2 *A, *H, *B, *tw;
+};
+
+// D value of box element (zz, yy) of slice slot `slot`.
+__device__ __forceinline__ float2 d_value(const SliceArgs &a, int slot, int sl,
+                                          int zz, int yy, float2 dep, float2 cd,
+                                          float2 cbg, int4 e) {
+  float2 v;
+  if (a.fill) {
+    int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
+    int zi = a.z_lo + zz; if (zi < 0) zi += a.g; if (zi >= a.g) zi -= a.g;
+    const bool inside = zi >= e.z && zi < e.w && yi > e.x && yi < e.y;
+    v = inside ? cadd(dep, a.amo[(size_t)slot * a.Ly + yy]) : cd;
+  } else {
+    v = csub(dep, cbg);
+  }
+  if (a.smooth_on) {
+    const float m = a.mz[(size_t)slot * a.Lz + zz] * a.my[(size_t)slot * a.Ly + yy];
+    v = make_float2(v.x * m + cd.x * (1.f - m), v.y * m + cd.y * (1.f - m));
+  }
+  return v;
+}
+
+struct SliceConst {
+  float2 cbg, cd;
+};
+
+__device__ __forceinline__ SliceConst slice_const(const SliceArgs &a, int sl) {
+  const gw_structure s = a.st[sl / a.n_phi];
+  const float2 c = make_float2((float)GW_DMUL(s.avg_f_re, s.max_voxels),
+                               (float)GW_DMUL(s.avg_f_im, s.max_voxels));
+  SliceConst k;
+  const bool bg = !a.plain && (a.fill || a.smooth_on);
+  k.cbg = bg ? c : make_float2(0.f, 0.f);
+  k.cd = bg ? make_float2(0.f, 0.f) : c;
+  return k;
+}
+
+// Row stage: for NB rows (slice, z) transform along y, keep Nc outputs.
+template <int M>
+__global__ void __launch_bounds__(FftShape<M>::NT)
+k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
+          float2 *F1) {
+  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  extern __shared__ float2 smem[];
+  float2 *buf = smem;
+  float2 *tw = smem + NB * M;
+  for (int t = threadIdx.x; t < M; t += NT) tw[t] = cz.tw[t];
+  const int row0 = blockIdx.x * NB;
+  for (int idx = threadIdx.x; idx < NB * M; idx += NT) {
+    const int f = idx / M, n = idx % M;
+    const int row = row0 + f;
+    float2 v = make_float2(0.f, 0.f);
+    if (row < n_rows && n < cz.L) {
+      const int slot = row / a.Lz, zz = row % a.Lz;
+      const int sl = slice0 + slot;
+      const SliceConst k = slice_const(a, sl);
+      const float2 dep = a.box[((size_t)slot * a.Lz + zz) * a.Ly + n];
+      v = cmul(d_value(a, slot, sl, zz, n, dep, k.cd, k.cbg, a.ext[sl]), cz.A[n]);
+    }
+    buf[idx] = v;
+  }
+  __syncthreads();
+  fft_block<M, NB, NT, false>(buf, tw);
+  for (int idx = threadIdx.x; idx < NB * M; idx += NT)
+    buf[idx] = cmul(buf[idx], cz.H[idx % M]);
+  __syncthreads();
+  fft_block<M, NB, NT, true>(buf, tw);
+  for (int idx = threadIdx.x; idx < NB * nc_out; idx += NT) {
+    const int f = idx / nc_out, m = idx % nc_out;
+    const int row = row0 + f;
+    if (row < n_rows)
+      F1[(size_t)row * nc_out + m] = cmul(buf[f * M + m], cz.B[m]);
+  }
+}
+
+struct BinArgs {
+  const int *colofs;  // [n_phi][Nc], -1 = not binned
+  const int *rowofs;  // [Nr], -1 = not binned
+  double *sum;        // window^3 float64
+  float2 *sumk;       // window^3 (sum, compensation) for Kahan float32
+  int kahan;
+  int k0, kz0;        // frequency of output column 0 / row 0
+  float dc_scale;     // g*g
+};
+
+__device__ __forceinline__ void kahan_add(float2 *addr, float x) {
+  unsigned long long *p = reinterpret_cast<unsigned long long *>(addr);
+  unsigned long long old = *p, assumed;
+  do {
+    assumed = old;
+    float2 sc;
+    memcpy(&sc, &assumed, 8);
+    const float y = x - sc.y;
+    const float t = sc.x + y;
+    const float c = (t - sc.x) - y;
+    float2 nw = make_float2(t, c);
+    unsigned long long nv;
+    memcpy(&nv, &nw, 8);
+    old = atomicCAS(p, assumed, nv);
+  } while (old != assumed);
+}
+
+// Column stage: NB columns of one slice; transform along z, |.|^2, bin.
+template <int M>
+__global__ void __launch_bounds__(FftShape<M>::NT)
+k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
+              const float2 *F1) {
+  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  extern __shared__ float2 smem[];
+  float2 *buf = smem;
+  float2 *tw = smem + NB * M;
+  const int slot = blockIdx.y, sl = slice0 + slot;
+  const int p = sl % a.n_phi;
+  const int m0 = blockIdx.x * NB;
+  const int *cofs = bn.colofs + (size_t)p * nc;
+  // skip column groups none of whose pixels lands in the binned window
+  bool any = false;
+  for (int f = 0; f < NB; ++f)
+    if (m0 + f < nc && cofs[m0 + f] >= 0) any = true;
+  if (!any) return;
+  for (int t = threadIdx.x; t < M; t += NT) tw[t] = cz.tw[t];
+  const float2 *src = F1 + (size_t)slot * a.Lz * nc;
+  for (int idx = threadIdx.x; idx < NB * M; idx += NT) {
+    const int f = idx % NB, n = idx / NB;
+    float2 v = make_float2(0.f, 0.f);
+    if (n < cz.L && m0 + f < nc) v = cmul(src[(size_t)n * nc + m0 + f], cz.A[n]);
+    buf[f * M + n] = v;
+  }
+  __syncthreads();
+  fft_block<M, NB, NT, false>(buf, tw);
+  for (int idx = threadIdx.x; idx < NB * M; idx += NT)
+    buf[idx] = cmul(buf[idx], cz.H[idx % M]);
+  __syncthreads();
+  fft_block<M, NB, NT, true>(buf, tw);
+  const SliceConst k = slice_const(a, sl);
+  const int nr = cz.N;
+  for (int idx = threadIdx.x; idx < NB * nr; idx += NT) {
+    const int f = idx / nr, mr = idx % nr;
+    const int m = m0 + f;
+    if (m >= nc) continue;
+    const int co = cofs[m], ro = bn.rowofs[mr];
+    if (co < 0 || ro < 0) continue;
+    float2 X = cmul(buf[f * M + mr], cz.B[mr]);
+    if (bn.k0 + m == 0 && bn.kz0 + mr == 0) {
+      X.x += k.cbg.x * bn.dc_scale;
+      X.y += k.cbg.y * bn.dc_scale;
+    }
+    const float I = X.x * X.x + X.y * X.y;
+    if (bn.kahan)
+      kahan_add(bn.sumk + co + ro, I);
+    else
+      atomicAdd(bn.sum + co + ro, (double)I);
+  }
+}
+
+// ---------------------------------------------------------- geometry tables
+// Column tables per phi (voxelgrids.py:396-401 slice axes, :475-498 mask and
+// indices): window offset ((iy-wlo)*W + (ix-wlo))*W, or -1.
+__global__ void k_col_tables(const gw_phi *ph, int g, int k0, int nc,
+                             double qmin, double qmax, double dq, double inv_dq,
+                             int wlo, int whi, int W, int *colofs,
+                             unsigned int *C2) {
+  const int p = blockIdx.x;
+  const double rqy = ph[p].right_qy, rqx = ph[p].right_qx;
+  for (int m = threadIdx.x; m < nc; m += blockDim.x) {
+    const int c = k0 + m + g / 2;  // column index of the shifted slice
+    int out = -1;
+    if (c >= 0 && c < g) {
+      const double hy = linspace_at(-rqy, rqy, g, c);
+      const double hx = linspace_at(-rqx, rqx, g, c);
+      if (hx <= qmax && hx >= qmin && hy <= qmax && hy >= qmin) {
+        const int ix = (int)floor_div_exact(GW_DSUB(hx, qmin), dq, inv_dq);
+        const int iy = (int)floor_div_exact(GW_DSUB(hy, qmin), dq, inv_dq);
+        if (ix >= wlo && ix <= whi && iy >= wlo && iy <= whi) {
+          out = ((iy - wlo) * W + (ix - wlo)) * W;
+          atomicAdd(C2 + (iy - wlo) * W + (ix - wlo), 1u);
+        }
+      }
+    }
+    colofs[(size_t)p * nc + m] = out;
+  }
+}
+
+// I = sum / count (0 where count == 0), crop, f0 factor (comparison.py:765-786,
+// voxelgrids.py:16-48, :828-857).  Output in crop coordinates (qy,qx,qz).
+__global__ void k_finalize(const double *sum, const float2 *sumk, int kahan,
+                           const unsigned int *C2, const int *C1, int W,
+                           int off, int Qc, double n_struct_div,
+                           const float *f0tab, int use_f0, float f0_c,
+                           float f0_invz, double *out64, float *out32) {
+  const int64_t total = (int64_t)Qc * Qc * Qc;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < total;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(v % Qc);
+    const int ix = (int)((v / Qc) % Qc);
+    const int iy = (int)(v / ((int64_t)Qc * Qc));
+    const int wy = iy + off, wx = ix + off, wz = iz + off;
+    const size_t w = ((size_t)wy * W + wx) * W + wz;
+    const double cnt = (double)C2[(size_t)wy * W + wx] * (double)C1[wz];
+    double s;
+    if (kahan) {
+      const float2 sc = sumk[w];
+      s = (double)sc.x - (double)sc.y;
+    } else {
+      s = sum[w];
+    }
+    double I = cnt != 0.0 ? s / (cnt * n_struct_div) : 0.0;
+    if (use_f0) {
+      float acc = f0_c;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float *t = f0tab + i * 3 * Qc;
+        acc += t[ix] * t[Qc + iy] * t[2 * Qc + iz];
+      }
+      const float fq = acc * f0_invz;
+      I *= (double)(fq * fq);
+    }
+    out64[v] = I;
+    out32[v] = (float)I;
+  }
+}
+
+// per-slice extents start empty: min fields INT_MAX, max fields -1
+__global__ void k_ext_init(int4 *ext, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) ext[i] = make_int4(INT_MAX, -1, INT_MAX, -1);
+}
+
+__global__ void k_debug_deposit(SliceArgs a, int sl, int *yo, int *zo) {
+  const int t = sl / a.n_phi, p = sl % a.n_phi;
+  const gw_structure s = a.st[t];
+  const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
+  const double ymin = ord_dbl(a.ymin_ord[sl]);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t at = s.atom_begin + i;
+    const double y = GW_DSUB(rot_y(a.xyz + 3 * at, c, sn), ymin);
+    const int yi = (int)floor_div_exact(y, a.r, a.inv_r);
+    const int zi = a.zidx[at];
+    const bool ok = yi >= 0 && yi < a.g && zi >= 0 && zi < a.g;
+    yo[i] = ok ? yi : -1;
+    zo[i] = ok ? zi : -1;
+  }
+}
+
+// ------------------------------------------------------------ host tables
+using cd = std::complex<double>;
+
+void fft_inplace_host(std::vector<cd> &a) {
+  const size_t n = a.size();
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(a[i], a[j]);
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    for (size_t i = 0; i < n; i += len) {
+      for (size_t k = 0; k < len / 2; ++k) {
+        const double ang = -2.0 * M_PI * (double)k / (double)len;
+        const cd w(std::cos(ang), std::sin(ang));
+        const cd u = a[i + k], v = a[i + k + len / 2] * w;
+        a[i + k] = u + v;
+        a[i + k + len / 2] = u - v;
+      }
+    }
+  }
+}
+
+// exp(-i*pi*e/g) with e reduced mod 2g exactly
+cd chirp(long long e, long long g) {
+  long long m = e % (2 * g);
+  if (m < 0) m += 2 * g;
+  const double ang = -M_PI * (double)m / (double)g;
+  return cd(std::cos(ang), std::sin(ang));
+}
+
+struct CztTables {
+  std::vector<float2> A, H, B, tw;
+};
+
+// X[k0+m] = sum_{n<L} x[lo+n] W^{(lo+n)(k0+m)}, W = exp(-2 pi i/g), via
+// B[m] * conv(x*A, h)[m], h[j] = W^{-j^2/2}, j in [-(L-1), N-1].
+CztTables make_czt(int g, int lo, int L, int k0, int N, int M) {
+  CztTables t;
+  t.A.resize(L); t.B.resize(N); t.H.resize(M); t.tw.resize(M);
+  for (int n = 0; n < L; ++n) {
+    const cd w = chirp(2LL * n * k0 + 1LL * n * n, g);  // W^{n k0 + n^2/2}
+    t.A[n] = make_float2((float)w.real(), (float)w.imag());
+  }
+  for (int m = 0; m < N; ++m) {  // W^{lo (k0+m) + m^2/2}
+    const cd w = chirp(2LL * lo * (k0 + m) + 1LL * m * m, g);
+    t.B[m] = make_float2((float)w.real(), (float)w.imag());
+  }
+  std::vector<cd> h(M, cd(0, 0));
+  for (int j = -(L - 1); j <= N - 1; ++j) {  // W^{-j^2/2}
+    const cd w = chirp(-1LL * j * j, g);
+    h[(j % M + M) % M] = w;
+  }
+  fft_inplace_host(h);
+  for (int i = 0; i < M; ++i) {
+    const cd v = h[i] / (double)M;
+    t.H[i] = make_float2((float)v.real(), (float)v.imag());
+  }
+  for (int i = 0; i < M; ++i) {
+    const double ang = -2.0 * M_PI * (double)i / (double)M;
+    t.tw[i] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+  }
+  return t;
+}
+
+int next_pow2(int n) {
+  int m = kMinM;
+  while (m < n) m <<= 1;
+  return m;
+}
+
+template <typename T>
+int upload(T **dst, const std::vector<T> &v, size_t *bytes) {
+  if (v.empty()) { *dst = nullptr; return GW_OK; }
+  GW_CUDA(gw::dev_malloc((void **)dst, v.size() * sizeof(T)));
+  *bytes += v.size() * sizeof(T);
+  GW_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T),
+                     cudaMemcpyHostToDevice));
+  return GW_OK;
+}
+
+template <typename T>
+int alloc(T **dst, size_t n, size_t *bytes) {
+  if (n == 0) { *dst = nullptr; return GW_OK; }
+  GW_CUDA(gw::dev_malloc((void **)dst, n * sizeof(T)));
+  *bytes += n * sizeof(T);
+  return GW_OK;
+}
+
+}  // namespace
+
+// ================================================================== plan
+struct gw_voxel_plan {
+  gw_ctx *ctx = nullptr;
+  gw_voxel_params p{};
+  int n_struct = 0, n_phi = 0, n_slices = 0;
+  std::vector<gw_structure> structs;
+  std::vector<gw_phi> phis;
+  int g = 0, plain = 0, Qc = 0, lo = 0, hi = 0, wlo = 0, whi = 0, W = 0;
+  double r = 0, inv_r = 0, dq = 0, inv_dq = 0;
+  int radius = 0;
+  int y_lo = 0, Ly = 0, z_lo = 0, Lz = 0, k0 = 0, Nc = 0, kz0 = 0, Nr = 0;
+  int My = 0, Mz = 0, S = 1;
+  int64_t n_atoms = -1;
+  size_t bytes = 0;
+  std::vector<int> C1host;
+  // device
+  double *d_xyz = nullptr;
+  float2 *d_f = nullptr;
+  int *d_zidx = nullptr;
+  gw_structure *d_structs = nullptr;
+  gw_phi *d_phis = nullptr;
+  double *d_clbase = nullptr;
+  unsigned long long *d_zmin = nullptr, *d_ymin = nullptr;
+  int4 *d_ext = nullptr;
+  float2 *d_Ay = nullptr, *d_Hy = nullptr, *d_By = nullptr, *d_twy = nullptr;
+  float2 *d_Az = nullptr, *d_Hz = nullptr, *d_Bz = nullptr, *d_twz = nullptr;
+  float *d_gw = nullptr;
+  int *d_colofs = nullptr, *d_rowofs = nullptr, *d_C1 = nullptr;
+  unsigned int *d_C2 = nullptr;
+  double *d_sum = nullptr;
+  float2 *d_sumk = nullptr;
+  float *d_f0 = nullptr;
+  double *d_iq64 = nullptr;
+  float *d_iq32 = nullptr;
+  float2 *d_box = nullptr, *d_F1 = nullptr, *d_amo = nullptr;
+  float *d_my = nullptr, *d_mz = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_kernels = 0;
+  bool executed = false;
+};
+
+namespace {
+
+SliceArgs slice_args(gw_voxel_plan *P) {
+  SliceArgs a{};
+  a.g = P->g; a.r = P->r; a.inv_r = P->inv_r; a.n_phi = P->n_phi;
+  a.y_lo = P->y_lo; a.Ly = P->Ly; a.z_lo = P->z_lo; a.Lz = P->Lz;
+  a.fill = P->p.fill_bkg != 0; a.smooth_on = P->p.smooth != 0.0;
+  a.sigma = (float)P->p.smooth; a.radius = P->radius; a.plain = P->plain;
+  a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
+  a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
+  a.ext = P->d_ext; a.box = P->d_box; a.amo = P->d_amo; a.my = P->d_my;
+  a.mz = P->d_mz; a.gw = P->d_gw; a.err = P->ctx->d_err;
+  return a;
+}
+
+template <int M>
+int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+               int slice0, int n_rows) {
+  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  const size_t smem = (size_t)(NB * M + M) * sizeof(float2);
+  static bool attr = false;
+  if (!attr) {
+    GW_CUDA(cudaFuncSetAttribute(k_row_czt<M>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = true;
+  }
+  const int blocks = (n_rows + NB - 1) / NB;
+  gw::KTimer tm(P->ctx, GW_K_ROW);
+  k_row_czt<M><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_rows,
+                                                     P->Nc, P->d_F1);
+  GW_LAUNCHED(P->ctx);
+  return GW_OK;
+}
+
+template <int M>
+int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+               const BinArgs &bn, int slice0, int n_sl) {
+  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  const size_t smem = (size_t)(NB * M + M) * sizeof(float2);
+  static bool attr = false;
+  if (!attr) {
+    GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = true;
+  }
+  dim3 grid((P->Nc + NB - 1) / NB, n_sl);
+  gw::KTimer tm(P->ctx, GW_K_COLBIN);
+  k_col_czt_bin<M><<<grid, NT, smem, P->ctx->stream>>>(a, cz, bn, slice0,
+                                                       P->Nc, P->d_F1);
+  GW_LAUNCHED(P->ctx);
+  return GW_OK;
+}
+
+#define GW_DISPATCH_M(M_, fn, ...)                                        \
+  switch (M_) {                                                         \
+    case 64: return fn<64>(__VA_ARGS__);                                \
+    case 128: return fn<128>(__VA_ARGS__);                              \
+    case 256: return fn<256>(__VA_ARGS__);                              \
+    case 512: return fn<512>(__VA_ARGS__);                              \
+    case 1024: return fn<1024>(__VA_ARGS__);                            \
+    case 2048: return fn<2048>(__VA_ARGS__);                            \
+    case 4096: return fn<4096>(__VA_ARGS__);                            \
+    case 8192: return fn<8192>(__VA_ARGS__);                            \
+    default: return gw::fail(GW_ERR_ARG, "unsupported FFT size");       \
+  }
+
+int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                 int s0, int n) {
+  GW_DISPATCH_M(P->My, launch_row, P, a, cz, s0, n)
+}
+int col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                 const BinArgs &bn, int s0, int n) {
+  GW_DISPATCH_M(P->Mz, launch_col, P, a, cz, bn, s0, n)
+}
+
+// Enqueue the whole chain (no synchronisation).
+int enqueue(gw_voxel_plan *P) {
+  gw_ctx *ctx = P->ctx;
+  cudaStream_t st = ctx->stream;
+  const size_t W3 = (size_t)P->W * P->W * P->W;
+  if (P->p.accum == GW_ACCUM_KAHAN32)
+    GW_CUDA(cudaMemsetAsync(P->d_sumk, 0, W3 * sizeof(float2), st));
+  else
+    GW_CUDA(cudaMemsetAsync(P->d_sum, 0, W3 * sizeof(double), st));
+  GW_CUDA(cudaMemsetAsync(P->d_C2, 0, (size_t)P->W * P->W * sizeof(unsigned), st));
+  GW_CUDA(cudaMemsetAsync(P->d_zmin, 0xff, P->n_struct * sizeof(unsigned long long), st));
+  GW_CUDA(cudaMemsetAsync(P->d_ymin, 0xff, P->n_slices * sizeof(unsigned long long), st));
+  int64_t max_atoms = 0;
+  for (auto &s : P->structs) max_atoms = std::max(max_atoms, s.atom_count);
+  const int nblk_at = (int)std::min<int64_t>(
+      std::max<int64_t>(1, (max_atoms + 255) / 256), 4 * ctx->sm_count);
+  {
+    gw::KTimer tm(ctx, GW_K_PREP);
+    k_zmin<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(P->d_xyz, P->d_structs, P->d_zmin);
+    GW_LAUNCHED(ctx);
+  }
+  {
+    gw::KTimer tm(ctx, GW_K_PREP);
+    k_zidx<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(P->d_xyz, P->d_structs, P->d_zmin,
+                                                     P->r, P->inv_r, P->d_zidx);
+    GW_LAUNCHED(ctx);
+  }
+  {
+    gw::KTimer tm(ctx, GW_K_TABLES);
+    k_col_tables<<<P->n_phi, 256, 0, st>>>(P->d_phis, P->g, P->k0, P->Nc,
+                                           P->p.q_min, P->p.q_max, P->dq,
+                                           P->inv_dq, P->wlo, P->whi, P->W,
+                                           P->d_colofs, P->d_C2);
+    GW_LAUNCHED(ctx);
+  }
+
+  SliceArgs a = slice_args(P);
+  CztArgs cy{P->My, P->Ly, P->Nc, P->d_Ay, P->d_Hy, P->d_By, P->d_twy};
+  CztArgs cz{P->Mz, P->Lz, P->Nr, P->d_Az, P->d_Hz, P->d_Bz, P->d_twz};
+  BinArgs bn{P->d_colofs, P->d_rowofs, P->d_sum, P->d_sumk,
+             P->p.accum == GW_ACCUM_KAHAN32, P->k0, P->kz0,
+             (float)((double)P->g * (double)P->g)};
+  for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
+    const int n = std::min(P->S, P->n_slices - s0);
+    GW_CUDA(cudaMemsetAsync(P->d_box, 0,
+                            (size_t)n * P->Lz * P->Ly * sizeof(float2), st));
+    {
+      gw::KTimer tm(ctx, GW_K_DEPOSIT);
+      k_ymin<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+      GW_LAUNCHED(ctx);
+    }
+    {
+      gw::KTimer tm(ctx, GW_K_DEPOSIT);
+      k_deposit<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+      GW_LAUNCHED(ctx);
+    }
+    if (a.fill || a.smooth_on) {
+      gw::KTimer tm(ctx, GW_K_PROFILE);
+      k_profile<<<n, 256, 0, st>>>(a, s0);
+      GW_LAUNCHED(ctx);
+    }
+    GW_TRY(row_dispatch(P, a, cy, s0, n * P->Lz));
+    GW_TRY(col_dispatch(P, a, cz, bn, s0, n));
+  }
+  const int fin_blocks = std::max(1, std::min(
+      (int)(((int64_t)P->Qc * P->Qc * P->Qc + 255) / 256), 8 * ctx->sm_count));
+  const float f0c = (float)P->p.f0_coef[8];
+  const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
+  {
+    gw::KTimer tm(ctx, GW_K_FINALIZE);
+    k_finalize<<<fin_blocks, 256, 0, st>>>(
+        P->d_sum, P->d_sumk, P->p.accum == GW_ACCUM_KAHAN32, P->d_C2, P->d_C1,
+        P->W, P->lo - P->wlo, P->Qc,
+        P->p.average ? (double)P->n_struct : 1.0, P->d_f0, P->p.f0_z > 0, f0c,
+        f0iz, P->d_iq64, P->d_iq32);
+    GW_LAUNCHED(ctx);
+  }
+  return GW_OK;
+}
+
+}  // namespace
+
+
+extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
+                                    const gw_structure *structs,
+                                    int32_t n_struct, const gw_phi *phis,
+                                    int32_t n_phi, gw_voxel_plan **out) {
+  if (!ctx || !p || !structs || !phis || !out)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: null argument");
+  if (n_struct < 1 || n_phi < 1)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: need >= 1 structure and >= 1 phi");
+  if (p->grid_size < 2 || p->r_voxel_size <= 0 || p->dq <= 0 || p->q_num < 3 ||
+      p->crop_lo < 0 || p->crop_hi >= p->q_num || p->crop_lo > p->crop_hi)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: invalid geometry");
+  if (p->smooth < 0)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: smooth must be >= 0");
+  GW_CUDA(cudaSetDevice(ctx->device));
+  auto *P = new gw_voxel_plan();
+  P->ctx = ctx;
+  P->p = *p;
+  P->n_struct = n_struct;
+  P->n_phi = n_phi;
+  P->n_slices = n_struct * n_phi;
+  P->structs.assign(structs, structs + n_struct);
+  P->phis.assign(phis, phis + n_phi);
+  P->g = p->grid_size;
+  P->plain = p->mode == GW_VOXEL_PLAIN;
+  P->r = p->r_voxel_size;
+  P->inv_r = 1.0 / P->r;
+  P->dq = p->dq;
+  P->inv_dq = 1.0 / P->dq;
+  P->lo = p->crop_lo;
+  P->hi = p->crop_hi;
+  P->Qc = P->hi - P->lo + 1;
+  if (P->plain) { P->wlo = 0; P->whi = p->q_num - 1; }
+  else { P->wlo = P->lo; P->whi = P->hi; }
+  P->W = P->whi - P->wlo + 1;
+  const int g = P->g;
+  const double sigma = p->smooth;
+  P->radius = sigma > 0 ? (int)(4.0 * sigma + 0.5) : 0;
+
+  // row table (phi independent): fftshift(fftfreq(g, r)) * 2pi
+  std::vector<int> rowofs_all(g, -1);
+  P->C1host.assign(P->W, 0);
+  {
+    const double val = 1.0 / ((double)g * P->r);
+    for (int i = 0; i < g; ++i) {
+      const long long k = (long long)i - g / 2;
+      const double q = (((double)k * val) * 2.0) * M_PI;
+      if (q <= p->q_max && q >= p->q_min) {
+        const int iz = (int)floor_div_exact(q - p->q_min, P->dq, P->inv_dq);
+        if (iz >= P->wlo && iz <= P->whi) rowofs_all[i] = iz - P->wlo;
+      }
+    }
+  }
+  int r0 = -1, r1 = -1;
+  if (P->plain) {
+    r0 = 0; r1 = g - 1;
+  } else {
+    for (int i = 0; i < g; ++i)
+      if (rowofs_all[i] >= 0) { if (r0 < 0) r0 = i; r1 = i; }
+    if (r0 < 0) { delete P; return gw::fail(GW_ERR_ARG, "no slice row lands in the cropped cube"); }
+  }
+  P->kz0 = r0 - g / 2;
+  P->Nr = r1 - r0 + 1;
+  std::vector<int> rowofs(P->Nr);
+  for (int i = 0; i < P->Nr; ++i) {
+    rowofs[i] = rowofs_all[r0 + i];
+    if (rowofs[i] >= 0) P->C1host[rowofs[i]]++;
+  }
+  // column band
+  if (P->plain) {
+    P->k0 = -(g / 2);
+    P->Nc = g;
+  } else {
+    // |q| reached by the binned window, then the widest column band over
+    // phi (45 degrees), plus a margin; exact per-column validity comes from
+    // k_col_tables.
+    const double qa = std::max(std::fabs(p->q_min + P->lo * P->dq),
+                               std::fabs(p->q_min + (P->hi + 1) * P->dq));
+    const double hcap = (qa + 2 * P->dq) * std::sqrt(2.0);
+    const double dh = 2.0 * p->h_max / (g - 1);
+    const int K = (int)std::ceil(hcap / dh) + 2;
+    int c_lo = std::max(0, (g - 1) / 2 - K);
+    int c_hi = std::min(g - 1, g / 2 + K);
+    P->k0 = c_lo - g / 2;
+    P->Nc = c_hi - c_lo + 1;
+  }
+  // real-space windows
+  if (P->plain) {
+    P->y_lo = 0; P->Ly = g; P->z_lo = 0; P->Lz = g;
+  } else {
+    int ybound = 0, zbound = 0;
+    for (int t = 0; t < n_struct; ++t) {
+      const gw_structure &s = structs[t];
+      zbound = std::max(zbound, (int)std::floor(s.z_bound * P->inv_r + 1e-6) + 1);
+      for (int q = 0; q < n_phi; ++q) {
+        const double ext = s.x_bound * std::fabs(phis[q].sin_phi) +
+                           s.y_bound * std::fabs(phis[q].cos_phi);
+        ybound = std::max(ybound, (int)std::floor(ext * P->inv_r + 1e-6) + 1);
+      }
+    }
+    const int tail = P->radius;
+    const int lo_off = sigma > 0 ? std::min(0, (int)std::ceil(sigma) - P->radius) : 0;
+    P->y_lo = lo_off;
+    P->Ly = ybound + tail - lo_off + 1;
+    if (P->Ly >= g) { P->Ly = g; P->y_lo = 0; }
+    P->z_lo = lo_off;
+    P->Lz = zbound + tail - lo_off + 1;
+    if (P->Lz >= g) { P->Lz = g; P->z_lo = 0; }
+  }
+  P->My = next_pow2(P->Ly + P->Nc - 1);
+  P->Mz = next_pow2(P->Lz + P->Nr - 1);
+  if (P->My > kMaxM || P->Mz > kMaxM) {
+    delete P;
+    return gw::fail(GW_ERR_ARG, "slice transform larger than 8192 points");
+  }
+  // batch size: keep the per-batch intermediates near L2 size
+  {
+    const size_t per = (size_t)P->Lz * (P->Ly + P->Nc) * sizeof(float2) +
+                       (P->Ly + P->Lz) * 12;
+    int S = p->batch_slices > 0 ? p->batch_slices
+                                : (int)std::max<size_t>(1, (96u << 20) / per);
+    if (P->plain) S = 1;
+    P->S = std::min(S, P->n_slices);
+  }
+
+  int st = GW_OK;
+  size_t &B = P->bytes;
+  // per-slice collapse base (pow on the host, as numpy's scalar ** does)
+  std::vector<double> clbase(P->n_slices, 0.0);
+  if (p->fill_bkg) {
+    std::vector<double> ver(P->n_slices), cost(P->n_slices);
+    for (int t = 0; t < n_struct; ++t)
+      for (int q = 0; q < n_phi; ++q) {
+        const gw_phi &ph = phis[q];
+        ver[(size_t)t * n_phi + q] = ph.cl_swap ? structs[t].y_bound : structs[t].x_bound;
+        cost[(size_t)t * n_phi + q] = ph.cos_t;
+      }
+    GW_TRY(gw_collapse_base(ver.data(), cost.data(), P->n_slices, clbase.data()));
+  }
+  // Gaussian weights (scipy.ndimage._gaussian_kernel1d, order 0)
+  std::vector<float> gwv;
+  if (sigma > 0) {
+    std::vector<double> w(2 * P->radius + 1);
+    double sum = 0;
+    for (int j = -P->radius; j <= P->radius; ++j) {
+      w[j + P->radius] = std::exp(-0.5 / (sigma * sigma) * (double)j * j);
+      sum += w[j + P->radius];
+    }
+    for (double v : w) gwv.push_back((float)(v / sum));
+  }
+  // f0 tables (separable exp factors) on the cropped axis
+  std::vector<float> f0tab;
+  if (p->f0_z > 0) {
+    f0tab.resize(4 * 3 * P->Qc);
+    const double s16 = 16.0 * M_PI * M_PI;
+    for (int i = 0; i < 4; ++i)
+      for (int ax = 0; ax < 3; ++ax)
+        for (int k = 0; k < P->Qc; ++k) {
+          const double q = linspace_at(p->q_min, p->q_max, p->q_num, P->lo + k);
+          double e = std::exp(-p->f0_coef[2 * i + 1] * q * q / s16);
+          if (ax == 0) e *= p->f0_coef[2 * i];  // a_i folded into the x factor
+          f0tab[(i * 3 + ax) * P->Qc + k] = (float)e;
+        }
+  }
+  CztTables ty = make_czt(g, P->y_lo, P->Ly, P->k0, P->Nc, P->My);
+  CztTables tz = make_czt(g, P->z_lo, P->Lz, P->kz0, P->Nr, P->Mz);
+  const size_t W3 = (size_t)P->W * P->W * P->W;
+  const size_t Qc3 = (size_t)P->Qc * P->Qc * P->Qc;
+  if ((st = upload(&P->d_structs, P->structs, &B)) ||
+      (st = upload(&P->d_phis, P->phis, &B)) ||
+      (st = upload(&P->d_clbase, clbase, &B)) ||
+      (st = upload(&P->d_gw, gwv, &B)) || (st = upload(&P->d_f0, f0tab, &B)) ||
+      (st = upload(&P->d_rowofs, rowofs, &B)) ||
+      (st = upload(&P->d_C1, P->C1host, &B)) ||
+      (st = upload(&P->d_Ay, ty.A, &B)) || (st = upload(&P->d_Hy, ty.H, &B)) ||
+      (st = upload(&P->d_By, ty.B, &B)) || (st = upload(&P->d_twy, ty.tw, &B)) ||
+      (st = upload(&P->d_Az, tz.A, &B)) || (st = upload(&P->d_Hz, tz.H, &B)) ||
+      (st = upload(&P->d_Bz, tz.B, &B)) || (st = upload(&P->d_twz, tz.tw, &B)) ||
+      (st = alloc(&P->d_zmin, n_struct, &B)) ||
+      (st = alloc(&P->d_ymin, P->n_slices, &B)) ||
+      (st = alloc(&P->d_ext, P->n_slices, &B)) ||
+      (st = alloc(&P->d_colofs, (size_t)n_phi * P->Nc, &B)) ||
+      (st = alloc(&P->d_C2, (size_t)P->W * P->W, &B)) ||
+      (st = (p->accum == GW_ACCUM_KAHAN32 ? alloc(&P->d_sumk, W3, &B)
+                                          : alloc(&P->d_sum, W3, &B))) ||
+      (st = alloc(&P->d_iq64, Qc3, &B)) || (st = alloc(&P->d_iq32, Qc3, &B)) ||
+      (st = alloc(&P->d_box, (size_t)P->S * P->Lz * P->Ly, &B)) ||
+      (st = alloc(&P->d_F1, (size_t)P->S * P->Lz * P->Nc, &B)) ||
+      (st = alloc(&P->d_amo, (size_t)P->S * P->Ly, &B)) ||
+      (st = alloc(&P->d_my, (size_t)P->S * P->Ly, &B)) ||
+      (st = alloc(&P->d_mz, (size_t)P->S * P->Lz, &B))) {
+    gw_voxel_plan_destroy(P);
+    return st;
+  }
+  *out = P;
+  return GW_OK;
+}
+
+extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
+  if (!P) return GW_OK;
+  if (P->gexec) cudaGraphExecDestroy(P->gexec);
+  if (P->graph) cudaGraphDestroy(P->graph);
+  void *ptrs[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_structs, P->d_phis,
+                  P->d_clbase, P->d_zmin, P->d_ymin, P->d_ext, P->d_Ay,
+                  P->d_Hy, P->d_By, P->d_twy, P->d_Az, P->d_Hz, P->d_Bz,
+                  P->d_twz, P->d_gw, P->d_colofs, P->d_rowofs, P->d_C1,
+                  P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
+                  P->d_iq32, P->d_box, P->d_F1, P->d_amo, P->d_my, P->d_mz};
+  for (void *q : ptrs) gw::dev_free(q);
+  delete P;
+  return GW_OK;
+}
+
+extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
+                                  const float *f, int64_t n, int32_t on_device) {
+  if (!P || !xyz || !f || n < 1)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: null argument or no atoms");
+  for (auto &s : P->structs)
+    if (s.atom_begin < 0 || s.atom_count < 1 || s.atom_begin + s.atom_count > n)
+      return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: structure atom range outside the atom arrays");
+  if (n != P->n_atoms) {
+    gw::dev_free(P->d_xyz); gw::dev_free(P->d_f); gw::dev_free(P->d_zidx);
+    P->d_xyz = nullptr; P->d_f = nullptr; P->d_zidx = nullptr;
+    GW_CUDA(gw::dev_malloc((void **)&P->d_xyz, (size_t)n * 3 * sizeof(double)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_f, (size_t)n * sizeof(float2)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_zidx, (size_t)n * sizeof(int)));
+    P->n_atoms = n;
+    if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    if (P->graph) { cudaGraphDestroy(P->graph); P->graph = nullptr; }
+  }
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  GW_CUDA(cudaMemcpyAsync(P->d_xyz, xyz, (size_t)n * 3 * sizeof(double), kind, P->ctx->stream));
+  GW_CUDA(cudaMemcpyAsync(P->d_f, f, (size_t)n * sizeof(float2), kind, P->ctx->stream));
+  return GW_OK;
+}
+
+static int voxel_enqueue_all(gw_voxel_plan *P) {
+  k_ext_init<<<(P->n_slices + 255) / 256, 256, 0, P->ctx->stream>>>(P->d_ext, P->n_slices);
+  GW_LAUNCHED(P->ctx);
+  return enqueue(P);
+}
+
+extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
+  if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_execute: null plan");
+  if (P->n_atoms < 0) return gw::fail(GW_ERR_STATE, "gw_voxel_execute: atoms not set");
+  GW_CUDA(cudaSetDevice(P->ctx->device));
+  if (P->gexec) {
+    GW_CUDA(cudaGraphLaunch(P->gexec, P->ctx->stream));
+    P->ctx->launches += P->graph_kernels;
+  } else {
+    GW_TRY(voxel_enqueue_all(P));
+  }
+  P->executed = true;
+  return GW_OK;
+}
+
+extern "C" int gw_voxel_capture_graph(gw_voxel_plan *P) {
+  if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_capture_graph: null plan");
+  if (P->n_atoms < 0) return gw::fail(GW_ERR_STATE, "gw_voxel_capture_graph: atoms not set");
+  if (P->gexec) return GW_OK;
+  GW_CUDA(cudaSetDevice(P->ctx->device));
+  // first-launch attributes must be set outside capture
+  GW_TRY(voxel_enqueue_all(P));
+  GW_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  const int64_t before = P->ctx->launches;
+  GW_CUDA(cudaStreamBeginCapture(P->ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int st = voxel_enqueue_all(P);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(P->ctx->stream, &graph);
+  if (st != GW_OK) { if (graph) cudaGraphDestroy(graph); return st; }
+  if (e != cudaSuccess) return gw::cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+  P->graph_kernels = P->ctx->launches - before;
+  P->ctx->launches = before;
+  P->graph = graph;
+  GW_CUDA(cudaGraphInstantiate(&P->gexec, graph, 0));
+  return GW_OK;
+}
+
+extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) {
+  if (!P || !iq) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq: null argument");
+  if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq: plan not executed");
+  const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
+  GW_CUDA(cudaMemcpyAsync(iq, P->d_iq64, n * sizeof(double),
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          P->ctx->stream));
+  return gw::check_device_error(P->ctx, "voxel stage");
+}
+
+extern "C" int gw_voxel_device_iq32(gw_voxel_plan *P, const float **iq32) {
+  if (!P || !iq32) return gw::fail(GW_ERR_ARG, "gw_voxel_device_iq32: null argument");
+  *iq32 = P->d_iq32;
+  return GW_OK;
+}
+
+extern "C" int gw_voxel_get_counts(gw_voxel_plan *P, double *counts) {
+  if (!P || !counts) return gw::fail(GW_ERR_ARG, "gw_voxel_get_counts: null argument");
+  if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_counts: plan not executed");
+  std::vector<unsigned> C2((size_t)P->W * P->W);
+  GW_CUDA(cudaMemcpyAsync(C2.data(), P->d_C2, C2.size() * sizeof(unsigned),
+                          cudaMemcpyDeviceToHost, P->ctx->stream));
+  GW_TRY(gw::check_device_error(P->ctx, "voxel stage"));
+  const int off = P->lo - P->wlo, Q = P->Qc;
+  for (int y = 0; y < Q; ++y)
+    for (int x = 0; x < Q; ++x)
+      for (int z = 0; z < Q; ++z)
+        counts[((size_t)y * Q + x) * Q + z] =
+            (double)C2[(size_t)(y + off) * P->W + x + off] *
+            (double)P->C1host[z + off] * (double)P->n_struct;
+  return GW_OK;
+}
+
+extern "C" int gw_voxel_get_sums(gw_voxel_plan *P, double *sums) {
+  if (!P || !sums) return gw::fail(GW_ERR_ARG, "gw_voxel_get_sums: null argument");
+  if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_sums: plan not executed");
+  const size_t W3 = (size_t)P->W * P->W * P->W;
+  std::vector<double> s(W3);
+  if (P->p.accum == GW_ACCUM_KAHAN32) {
+    std::vector<float2> k(W3);
+    GW_CUDA(cudaMemcpyAsync(k.data(), P->d_sumk, W3 * sizeof(float2),
+                            cudaMemcpyDeviceToHost, P->ctx->stream));
+    GW_TRY(gw::check_device_error(P->ctx, "voxel stage"));
+    for (size_t i = 0; i < W3; ++i) s[i] = (double)k[i].x - (double)k[i].y;
+  } else {
+    GW_CUDA(cudaMemcpyAsync(s.data(), P->d_sum, W3 * sizeof(double),
+                            cudaMemcpyDeviceToHost, P->ctx->stream));
+    GW_TRY(gw::check_device_error(P->ctx, "voxel stage"));
+  }
+  const int off = P->lo - P->wlo, Q = P->Qc;
+  for (int y = 0; y < Q; ++y)
+    for (int x = 0; x < Q; ++x)
+      for (int z = 0; z < Q; ++z)
+        sums[((size_t)y * Q + x) * Q + z] =
+            s[((size_t)(y + off) * P->W + x + off) * P->W + z + off];
+  return GW_OK;
+}
+
+extern "C" int gw_voxel_info(gw_voxel_plan *P, int64_t *info, int32_t n) {
+  if (!P || !info) return gw::fail(GW_ERR_ARG, "gw_voxel_info: null argument");
+  const int64_t v[] = {P->Qc, P->S, P->Ly, P->Lz, P->Nc, P->Nr, P->My, P->Mz,
+                       P->y_lo, P->z_lo, P->k0, P->kz0, P->n_slices,
+                       (int64_t)P->bytes, P->graph_kernels};
+  const int k = std::min<int>(n, (int)(sizeof v / sizeof v[0]));
+  for (int i = 0; i < k; ++i) info[i] = v[i];
+  return k;
+}
+
+extern "C" int gw_voxel_debug_deposit(gw_voxel_plan *P, int32_t slice,
+                                      int32_t *y_idx, int32_t *z_idx) {
+  if (!P || !y_idx || !z_idx) return gw::fail(GW_ERR_ARG, "gw_voxel_debug_deposit: null argument");
+  if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_debug_deposit: plan not executed");
+  if (slice < 0 || slice >= P->n_slices) return gw::fail(GW_ERR_ARG, "gw_voxel_debug_deposit: slice out of range");
+  const gw_structure &s = P->structs[slice / P->n_phi];
+  int *dy = nullptr, *dz = nullptr;
+  GW_CUDA(gw::dev_malloc((void **)&dy, s.atom_count * sizeof(int)));
+  cudaError_t e = gw::dev_malloc((void **)&dz, s.atom_count * sizeof(int));
+  if (e != cudaSuccess) { gw::dev_free(dy); return gw::cuda_fail(e, "dev_malloc", __FILE__, __LINE__); }
+  SliceArgs a = slice_args(P);
+  k_debug_deposit<<<256, 256, 0, P->ctx->stream>>>(a, slice, dy, dz);
+  P->ctx->launches++;
+  e = cudaMemcpyAsync(y_idx, dy, s.atom_count * sizeof(int), cudaMemcpyDeviceToHost, P->ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(z_idx, dz, s.atom_count * sizeof(int), cudaMemcpyDeviceToHost, P->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->ctx->stream);
+  gw::dev_free(dy);
+  gw::dev_free(dz);
+  if (e != cudaSuccess) return gw::cuda_fail(e, "debug deposit", __FILE__, __LINE__);
+  return GW_OK;
+}
+
+extern "C" int gw_voxelgrid(gw_ctx *ctx, const gw_voxel_params *p,
+                            const gw_structure *structs, int32_t n_struct,
+                            const gw_phi *phis, int32_t n_phi,
+                            const double *xyz, const float *f, int64_t n_atoms,
+                            double *iq_out) {
+  gw_voxel_plan *P = nullptr;
+  GW_TRY(gw_voxel_plan_create(ctx, p, structs, n_struct, phis, n_phi, &P));
+  int st = gw_voxel_set_atoms(P, xyz, f, n_atoms, 0);
+  if (st == GW_OK) st = gw_voxel_execute(P);
+  if (st == GW_OK) st = gw_voxel_get_iq(P, iq_out, 0);
+  gw_voxel_plan_destroy(P);
+  return st;
+}

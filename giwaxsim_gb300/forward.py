@@ -1,0 +1,387 @@
+"""Host side of the forward path: reference-exact geometry and per-slice
+scalars, and thin owners of the native voxel and detector plans.
+
+Everything here is O(number of slices + orientations) host work on small
+arrays; per-atom and per-pixel work is on the GPU (libgiwaxs_gb300.so).
+The host computes, with numpy, exactly the scalars the reference computes
+with numpy (its trig, pow and reductions), so that the device replays the
+same float64 arithmetic per atom and per pixel:
+
+  tools/comparison.py:704-744   grid size, q axis, automatic phis, checks,
+                                bounds, f values, avg_voxel_f
+  tools/voxelgrids.py:16-48     crop range (downselect_voxelgrid)
+  tools/voxelgrids.py:253-285   rectangular_collapse_lengths branch scalars
+  tools/voxelgrids.py:382-399   slice h-axis end points
+  tools/comparison.py:790-841   detector set-up, weights, orientation order
+  tools/detector.py:33-162      axis of each plane rotation from the
+                                current plane's corners
+"""
+import ctypes
+import warnings
+
+import numpy as np
+from numpy.fft import fftfreq, fftshift
+
+from . import _native as N
+from .tools.ptable_dict import aff_dict, ptable
+
+
+# ------------------------------------------------------------------ voxel
+class VoxelGeometry:
+    """Grid, q axis, automatic phis and crop of voxelgridmaker_fitting
+    (comparison.py:704-731) and downselect_voxelgrid (voxelgrids.py:35-46)."""
+
+    def __init__(self, r_voxel_size, q_voxel_size, max_q):
+        max_q_diag = np.sqrt(2) * max_q
+        if max_q_diag > 2 * np.pi / r_voxel_size:
+            raise Exception("Max_q is non-physical for given voxel size")
+        self.r_voxel_size = r_voxel_size
+        self.q_voxel_size = q_voxel_size
+        self.max_q = max_q
+        self.grid_size = int(np.ceil(2 * np.pi / (q_voxel_size * r_voxel_size)))
+        max_q_diag = max_q_diag + max_q_diag % q_voxel_size
+        q_num = ((2 * max_q_diag / q_voxel_size) + 1).astype(int)
+        if q_num % 2 == 0:
+            q_num += 1
+        self.q = np.linspace(-max_q_diag, max_q_diag, q_num)
+        self.q_num = int(q_num)
+        dphi = np.arctan(q_voxel_size / max_q_diag)
+        phi_num = np.ceil(2 * np.pi / dphi).astype(int)
+        self.auto_phis = np.linspace(0, 180 - (180 / phi_num), num=phi_num)
+        # downselect_voxelgrid on the (identical) x, y and z axes
+        voxel = np.abs(self.q[1] - self.q[0])
+        keep = np.where(np.abs(self.q) < max_q + voxel)[0]
+        self.crop_lo, self.crop_hi = int(keep[0]), int(keep[-1])
+        self.q_crop = self.q[self.crop_lo:self.crop_hi + 1]
+        self.dq = np.diff(self.q)[0]
+        q_h = fftshift(fftfreq(self.grid_size, d=r_voxel_size) * 2 * np.pi)
+        self.h_max = np.max(q_h)
+
+    def check_bounds(self, coords):
+        b = [np.max(coords[:, i]) - np.min(coords[:, i]) for i in range(3)]
+        if self.grid_size * self.r_voxel_size < np.min(b):
+            raise Exception("Calculated real-space bounds smaller than "
+                            "simulation. Please lower delta_q value")
+
+    def phi_table(self, phis):
+        """Per-slice scalars as numpy computes them in the reference."""
+        phis = np.asarray(phis, dtype=np.float64)
+        t = np.zeros(len(phis), dtype=np.dtype(N.Phi))
+        pr = np.radians(phis)
+        t["cos_phi"] = np.cos(pr)
+        t["sin_phi"] = np.sin(pr)
+        t["right_qy"] = self.h_max * np.cos(np.deg2rad(-phis))
+        t["right_qx"] = -self.h_max * np.sin(np.deg2rad(-phis))
+        swap = phis > 90
+        padj = np.where(swap, phis - 90, phis)
+        theta = 90 - padj
+        tr, pa = np.deg2rad(theta), np.deg2rad(padj)
+        t["cl_case"] = np.where(padj == 0, 0, np.where(padj == 90, 1, 2))
+        t["cl_swap"] = swap.astype(np.int32)
+        t["cos_t"], t["sin_t"], t["tan_t"] = np.cos(tr), np.sin(tr), np.tan(tr)
+        t["cos_p"], t["sin_p"], t["tan_p"] = np.cos(pa), np.sin(pa), np.tan(pa)
+        return t
+
+
+def element_f_values(elements, energy, f1f2=None):
+    """f = Z + f' + i f'' per atom (comparison.py:735-739)."""
+    from .tools.utilities import get_element_f1_f2_dict
+    elements = np.asarray(elements)
+    uniq, inv = np.unique(elements, return_inverse=True)
+    d = f1f2 if f1f2 is not None else get_element_f1_f2_dict(energy, uniq)
+    vals = np.array([complex(d[e]) for e in uniq], dtype=complex)
+    vals += np.array([ptable[e] for e in uniq])
+    return vals[inv]
+
+
+def structure_constants(coords, f_values, r_voxel_size):
+    """x/y/z bounds, avg_voxel_f (comparison.py:712-744) and max_voxels
+    (voxelgrids.py:344)."""
+    xb = np.max(coords[:, 0]) - np.min(coords[:, 0])
+    yb = np.max(coords[:, 1]) - np.min(coords[:, 1])
+    zb = np.max(coords[:, 2]) - np.min(coords[:, 2])
+    avg = (np.sum(f_values) / (xb * yb * zb)) * r_voxel_size ** 3
+    max_voxels = np.sqrt(xb ** 2 + yb ** 2) // r_voxel_size
+    return xb, yb, zb, complex(avg), float(max_voxels)
+
+
+def f0_params(element):
+    if element is None:
+        return [0.0] * 9, 0.0
+    return list(aff_dict[element]), float(ptable[element])
+
+
+class VoxelPlan:
+    """Owner of a gw_voxel_plan for one geometry, a list of structures and
+    a list of phis.  structures: list of (coords (N,3), f_values (N,)
+    complex, weights (N,) or None)."""
+
+    def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
+                 mode="batched", accum="fp64", average=True, f0_element="C",
+                 batch_slices=0, ctx=None):
+        self.geom = geom
+        self.ctx = ctx or N.default_context()
+        self.phis = geom.auto_phis if phis is None else np.asarray(phis, np.float64)
+        if len(self.phis) < 1:
+            raise ValueError("at least one phi is required")
+        r = geom.r_voxel_size
+        st = np.zeros(len(structures), dtype=np.dtype(N.Structure))
+        xyz, fs = [], []
+        begin = 0
+        for i, (coords, fv, w) in enumerate(structures):
+            coords = np.ascontiguousarray(coords, dtype=np.float64)
+            if coords.ndim != 2 or coords.shape[1] != 3 or len(coords) == 0:
+                raise ValueError("coords must be a non-empty (N, 3) array")
+            geom.check_bounds(coords)
+            fv = np.asarray(fv, dtype=complex)
+            if w is not None:
+                fv = fv * np.asarray(w, dtype=np.float64)
+            xb, yb, zb, avg, mv = structure_constants(coords, fv, r)
+            st[i] = (begin, len(coords), xb, yb, zb, avg.real, avg.imag, mv)
+            begin += len(coords)
+            xyz.append(coords)
+            fs.append(fv.astype(np.complex64))
+        self.structs = st
+        self.xyz = np.ascontiguousarray(np.concatenate(xyz))
+        self.f = np.ascontiguousarray(np.concatenate(fs)).view(np.float32)
+        self.phi_tab = geom.phi_table(self.phis)
+        p = N.VoxelParams()
+        p.grid_size = geom.grid_size
+        p.r_voxel_size = r
+        p.q_num = geom.q_num
+        p.q_min, p.q_max = geom.q[0], geom.q[-1]
+        p.dq = geom.dq
+        p.crop_lo, p.crop_hi = geom.crop_lo, geom.crop_hi
+        p.h_max = geom.h_max
+        p.fill_bkg = int(bool(fill_bkg))
+        p.smooth = float(smooth) if smooth else 0.0
+        p.mode = {"batched": N.GW_VOXEL_BATCHED, "plain": N.GW_VOXEL_PLAIN}[mode]
+        p.accum = {"fp64": N.GW_ACCUM_FP64, "kahan32": N.GW_ACCUM_KAHAN32}[accum]
+        p.average = int(bool(average))
+        coef, z = f0_params(f0_element)
+        for i in range(9):
+            p.f0_coef[i] = coef[i]
+        p.f0_z = z
+        p.batch_slices = int(batch_slices)
+        self.params = p
+        h = ctypes.c_void_p()
+        N.check(N.lib().gw_voxel_plan_create(
+            self.ctx.handle, ctypes.byref(p), N.ptr(self.structs),
+            len(self.structs), N.ptr(self.phi_tab), len(self.phi_tab),
+            ctypes.byref(h)))
+        self.handle = h
+        self.Qc = geom.crop_hi - geom.crop_lo + 1
+
+    def set_atoms(self, xyz=None, f=None, on_device=False):
+        if xyz is None:
+            xyz, f = self.xyz, self.f
+        if on_device:
+            N.check(N.lib().gw_voxel_set_atoms(self.handle, ctypes.c_void_p(xyz),
+                                               ctypes.c_void_p(f),
+                                               len(self.xyz), 1))
+        else:
+            N.check(N.lib().gw_voxel_set_atoms(self.handle, N.ptr(xyz), N.ptr(f),
+                                               len(xyz), 0))
+
+    def execute(self):
+        N.check(N.lib().gw_voxel_execute(self.handle))
+
+    def capture_graph(self):
+        N.check(N.lib().gw_voxel_capture_graph(self.handle))
+
+    def iq(self, out=None):
+        out = np.empty((self.Qc,) * 3) if out is None else out
+        N.check(N.lib().gw_voxel_get_iq(self.handle, N.ptr(out), 0))
+        return out
+
+    def iq_to_device(self, dev_ptr):
+        N.check(N.lib().gw_voxel_get_iq(self.handle, ctypes.c_void_p(dev_ptr), 1))
+
+    def device_iq32(self):
+        p = ctypes.c_void_p()
+        N.check(N.lib().gw_voxel_device_iq32(self.handle, ctypes.byref(p)))
+        return p.value
+
+    def counts(self):
+        out = np.empty((self.Qc,) * 3)
+        N.check(N.lib().gw_voxel_get_counts(self.handle, N.ptr(out)))
+        return out
+
+    def sums(self):
+        out = np.empty((self.Qc,) * 3)
+        N.check(N.lib().gw_voxel_get_sums(self.handle, N.ptr(out)))
+        return out
+
+    def info(self):
+        v = np.zeros(16, dtype=np.int64)
+        n = N.lib().gw_voxel_info(self.handle, N.ptr(v), 16)
+        keys = ["crop", "batch", "Ly", "Lz", "Nc", "Nr", "My", "Mz", "y_lo",
+                "z_lo", "k0", "kz0", "n_slices", "device_bytes",
+                "graph_kernels"]
+        return dict(zip(keys, (int(x) for x in v[:n])))
+
+    def debug_deposit(self, slice_index):
+        t = int(slice_index) // len(self.phis)
+        n = int(self.structs[t]["atom_count"])
+        y = np.empty(n, np.int32)
+        z = np.empty(n, np.int32)
+        N.check(N.lib().gw_voxel_debug_deposit(self.handle, int(slice_index),
+                                               N.ptr(y), N.ptr(z)))
+        return y, z
+
+    def close(self):
+        if getattr(self, "handle", None):
+            N.lib().gw_voxel_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ detector
+def rotation_matrix(u, theta):
+    """Rodrigues rotation (utilities.py:222-245), same expression trees."""
+    ux, uy, uz = u[0], u[1], u[2]
+    R = np.zeros((3, 3))
+    R[0, 0] = np.cos(theta) + ux ** 2 * (1 - np.cos(theta))
+    R[0, 1] = ux * uy * (1 - np.cos(theta)) - uz * np.sin(theta)
+    R[0, 2] = ux * uz * (1 - np.cos(theta)) + uy * np.sin(theta)
+    R[1, 0] = uy * ux * (1 - np.cos(theta)) + uz * np.sin(theta)
+    R[1, 1] = np.cos(theta) + uy ** 2 * (1 - np.cos(theta))
+    R[1, 2] = uy * uz * (1 - np.cos(theta)) - ux * np.sin(theta)
+    R[2, 0] = uz * ux * (1 - np.cos(theta)) - uy * np.sin(theta)
+    R[2, 1] = uz * uy * (1 - np.cos(theta)) + ux * np.sin(theta)
+    R[2, 2] = np.cos(theta) + uz ** 2 * (1 - np.cos(theta))
+    return R
+
+
+class PlaneCorners:
+    """The three plane corners [0,0], [0,-1], [-1,0] the reference derives
+    rotation axes from (detector.py:58-60, 104-105, 146-147), carried through
+    the same fused-chain rotations as the full plane."""
+
+    def __init__(self, h, v):
+        self.pts = np.array([[0.0, h[0], v[0]], [0.0, h[-1], v[0]],
+                             [0.0, h[0], v[-1]]])
+
+    def matrix(self, kind, angle):
+        p1, p2, p3 = self.pts
+        if kind == "psi":
+            axis = np.cross(p2 - p1, p3 - p1)
+        elif kind == "theta":
+            axis = p2 - p1
+        elif kind == "phi":
+            axis = p3 - p1
+        else:
+            raise ValueError(kind)
+        axis /= np.linalg.norm(axis)
+        return rotation_matrix(axis, np.radians(angle))
+
+    def rotate(self, R):
+        out = PlaneCorners.__new__(PlaneCorners)
+        out.pts = N.rotate_points(R, self.pts)
+        return out
+
+
+_IDENTITY = np.eye(3)
+
+
+class DetectorPlan:
+    """Owner of a gw_detector_plan (comparison.py:790-870)."""
+
+    def __init__(self, iq_shape, qx, qy, qz, num_pixels, max_q,
+                 angle_init_vals, angle_init_axs, psis, psi_weights, phis,
+                 phi_weights, thetas, theta_weights, mirror=True,
+                 accum="fp64", ctx=None):
+        self.ctx = ctx or N.default_context()
+        nh = nv = int(num_pixels)
+        h = np.linspace(-max_q, max_q, nh)
+        v = np.linspace(-max_q, max_q, nv)
+        self.det_h, self.det_v = h, v
+        corners = PlaneCorners(h, v)
+        init = []
+        for val, ax in zip(angle_init_vals, angle_init_axs):
+            if ax in ("psi", "phi", "theta"):
+                R = corners.matrix(ax, val)
+                corners = corners.rotate(R)
+                init.append(R)
+        psis, phis, thetas = (np.atleast_1d(np.asarray(a)) for a in
+                              (psis, phis, thetas))
+        n_rot, mats, weights = [], [], []
+        for ps, pw in zip(psis, psi_weights):
+            for ph, hw in zip(phis, phi_weights):
+                for th, tw in zip(thetas, theta_weights):
+                    c = corners
+                    k = 0
+                    for kind, ang in (("psi", ps), ("phi", ph), ("theta", th)):
+                        R = c.matrix(kind, ang)
+                        c = c.rotate(R)
+                        if not np.array_equal(R, _IDENTITY):
+                            mats.append(R)
+                            k += 1
+                    n_rot.append(k)
+                    weights.append(pw * hw * tw)
+        if not weights:
+            raise ValueError("no detector orientation")
+        self.n_orient = len(weights)
+        self.iq_shape = tuple(int(s) for s in iq_shape)
+        p = N.DetectorParams()
+        p.n_h, p.n_v = nh, nv
+        for i in range(3):
+            p.iq_shape[i] = self.iq_shape[i]
+        p.qmin_x, p.qmin_y, p.qmin_z = np.min(qx), np.min(qy), np.min(qz)
+        p.dq = np.diff(qz)[0]
+        p.mirror = int(bool(mirror))
+        p.accum = {"fp64": N.GW_ACCUM_FP64, "kahan32": N.GW_ACCUM_KAHAN32}[accum]
+        self.params = p
+        self._h = np.ascontiguousarray(h)
+        self._v = np.ascontiguousarray(v)
+        self._init = np.ascontiguousarray(np.array(init).reshape(-1, 9)) if init else None
+        self._nrot = np.ascontiguousarray(np.array(n_rot, dtype=np.int32))
+        self._mats = (np.ascontiguousarray(np.array(mats).reshape(-1, 9))
+                      if mats else None)
+        self._w = np.ascontiguousarray(np.array(weights, dtype=np.float64))
+        hdl = ctypes.c_void_p()
+        N.check(N.lib().gw_detector_plan_create(
+            self.ctx.handle, ctypes.byref(p), N.ptr(self._h), N.ptr(self._v),
+            N.ptr(self._init), len(init), N.ptr(self._nrot), N.ptr(self._mats),
+            N.ptr(self._w), self.n_orient, ctypes.byref(hdl)))
+        self.handle = hdl
+
+    def set_iq(self, iq):
+        iq = np.ascontiguousarray(iq, dtype=np.float64)
+        if iq.shape != self.iq_shape:
+            raise ValueError("iq shape %s != plan shape %s" % (iq.shape, self.iq_shape))
+        N.check(N.lib().gw_detector_set_iq(self.handle, N.ptr(iq), 0))
+
+    def set_iq_device32(self, dev_ptr):
+        N.check(N.lib().gw_detector_set_iq32_device(self.handle,
+                                                    ctypes.c_void_p(dev_ptr)))
+
+    def execute(self):
+        N.check(N.lib().gw_detector_execute(self.handle))
+
+    def result(self):
+        out = np.empty((self.params.n_v, self.params.n_h))
+        N.check(N.lib().gw_detector_get(self.handle, N.ptr(out), 0))
+        return out
+
+    def debug_indices(self, orient):
+        out = np.empty(self.params.n_v * self.params.n_h, dtype=np.int64)
+        N.check(N.lib().gw_detector_debug_indices(self.handle, int(orient),
+                                                  N.ptr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None):
+            N.lib().gw_detector_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

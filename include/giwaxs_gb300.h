@@ -1,0 +1,214 @@
+/*
+ * giwaxs_gb300.h -- C ABI of the GB300 (sm_103a) GIWAXS forward path.
+ *
+ * The reference (tchaney97/giwaxsim) is pure Python/numpy; its hot path is
+ * reached through these Python entry points, which this library replaces:
+ *
+ *   tools/comparison.py:673  voxelgridmaker_fitting(...)  -> gw_voxel_*
+ *   tools/voxelgrids.py:311  rotate_project_fft_coords(args)  (per slice)
+ *   tools/voxelgrids.py:464  process_file2(...)               (binning)
+ *   tools/comparison.py:790  detectormaker_fitting(...)   -> gw_detector_*
+ *   tools/detector.py:278    generate_detector_ints(args)     (per orientation)
+ *   tools/detector.py:194    intersect_detector(...)
+ *
+ * A reference-side binding is plain ctypes; the
+ * package giwaxsim_gb300.tools.* is that binding, with the reference's
+ * signatures.  All entry points return a gw_status; gw_last_error() gives
+ * the message of the last failure on the calling thread.  Pointers are plain
+ * host or device addresses; a flag says which.  No call allocates pinned
+ * host memory or keeps host pointers after it returns.
+ *
+ * Threading: a gw_ctx owns one CUDA stream; calls on one context must not
+ * overlap.  Different contexts may be used from different threads.
+ */
+#ifndef GIWAXS_GB300_H
+#define GIWAXS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ------------------------------------------------------------ */
+enum gw_status {
+  GW_OK = 0,
+  GW_ERR_ARG = 1,     /* invalid argument; message names it                */
+  GW_ERR_OOM = 2,     /* device allocation failed (or GW_FAIL_ALLOC_AFTER)  */
+  GW_ERR_CUDA = 3,    /* a CUDA runtime call failed                         */
+  GW_ERR_TIMEOUT = 4, /* a bounded device wait ran out                      */
+  GW_ERR_BOUNDS = 5,  /* a device-side range check failed                   */
+  GW_ERR_STATE = 6    /* call out of order (e.g. execute before set_atoms)  */
+};
+
+int gw_version(void);
+const char *gw_status_string(int status);
+/* Copies the calling thread's last error message (NUL-terminated, truncated
+ * to len-1).  Returns the full message length. */
+size_t gw_last_error(char *buf, size_t len);
+
+/* ---- context ----------------------------------------------------------- */
+typedef struct gw_ctx gw_ctx;
+int gw_ctx_create(int device, gw_ctx **out);
+int gw_ctx_destroy(gw_ctx *ctx);
+int gw_ctx_synchronize(gw_ctx *ctx);
+/* The context's cudaStream_t, for callers that order their own work. */
+int gw_ctx_stream(gw_ctx *ctx, void **stream);
+/* Number of kernels this library launched on the context so far (graph
+ * replays count the kernels inside the graph). */
+int64_t gw_ctx_launch_count(gw_ctx *ctx);
+
+/* Per-kernel device timing.  When on, every kernel launch of the library on
+ * this context is bracketed by CUDA events on the context stream (eager
+ * execution only; graph replays are not instrumented).  gw_ctx_kernel_times
+ * synchronises, then fills total milliseconds and launch counts per kernel
+ * category (names from gw_kernel_category_name) and returns the number of
+ * categories; the totals accumulate until timing is switched on again. */
+int gw_ctx_set_timing(gw_ctx *ctx, int32_t on);
+int gw_ctx_kernel_times(gw_ctx *ctx, double *ms, int64_t *launches,
+                        int32_t n);
+const char *gw_kernel_category_name(int32_t category);
+
+/* ---- host helpers ------------------------------------------------------ */
+/* out[k*3+i] = fma(p2,R[i][2], fma(p1,R[i][1], p0*R[i][0])): the fused
+ * order OpenBLAS uses for np.dot(coords, R.T) (tools/utilities.py:315) and
+ * R @ vstack (tools/detector.py:71).  R row-major 3x3, pts (n,3). */
+int gw_rotate_points(const double *R, const double *pts, int64_t n,
+                     double *out);
+/* rectangular_collapse_lengths' per-slice constant
+ * sqrt(ver**2 - (ver*cos_t)**2) (tools/voxelgrids.py:292) with the host
+ * libm pow(), which is what numpy's scalar ** calls. */
+int gw_collapse_base(const double *ver, const double *cos_t, int64_t n,
+                     double *out);
+
+/* ---- voxel stage: I(qx,qy,qz) from atoms ----------------------------- */
+enum { GW_VOXEL_BATCHED = 0, GW_VOXEL_PLAIN = 1 };
+enum { GW_ACCUM_FP64 = 0, GW_ACCUM_KAHAN32 = 1 };
+
+typedef struct gw_voxel_params {
+  int32_t grid_size;    /* g = ceil(2pi/(dq*r))          comparison.py:710 */
+  double r_voxel_size;  /* r                                               */
+  int32_t q_num;        /* length of the full q axis     comparison.py:721 */
+  double q_min, q_max;  /* first / last value of the full axis             */
+  double dq;            /* np.diff(qz)[0]                voxelgrids.py:496 */
+  int32_t crop_lo, crop_hi; /* inclusive index range kept by
+                               downselect_voxelgrid      voxelgrids.py:16  */
+  double h_max;         /* max(fftshift(fftfreq(g,r))*2pi) voxelgrids.py:396 */
+  int32_t fill_bkg;     /*                               voxelgrids.py:350 */
+  double smooth;        /* sigma in r-voxels, 0 = off    voxelgrids.py:364 */
+  int32_t mode;         /* GW_VOXEL_BATCHED | GW_VOXEL_PLAIN               */
+  int32_t accum;        /* GW_ACCUM_FP64 | GW_ACCUM_KAHAN32                */
+  int32_t average;      /* 1: divide by the number of structures
+                           (old_modules/voxelgridmaker.py:56-61)           */
+  double f0_coef[9];    /* Cromer-Mann a1,b1,..,a4,b4,c  voxelgrids.py:849 */
+  double f0_z;          /* Z of the f0 element; <= 0 skips the f0 factor   */
+  int32_t batch_slices; /* slices per batch, 0 = automatic                 */
+  int32_t reserved[7];
+} gw_voxel_params;
+
+typedef struct gw_structure {
+  int64_t atom_begin, atom_count; /* slice of the atom arrays            */
+  double x_bound, y_bound, z_bound; /* max-min per axis comparison.py:712 */
+  double avg_f_re, avg_f_im;      /* avg_voxel_f      comparison.py:744   */
+  double max_voxels;              /* sqrt(xb**2+yb**2)//r voxelgrids.py:344 */
+} gw_structure;
+
+typedef struct gw_phi {
+  double cos_phi, sin_phi;   /* np.cos/np.sin(np.radians(phi))  utilities.py:305-312 */
+  double right_qy, right_qx; /* slice h-axis end points       voxelgrids.py:396-399 */
+  /* rectangular_collapse_lengths (voxelgrids.py:253-285) after the phi>90
+   * fold: case 0 (phi'==0), 1 (phi'==90), 2 (general); swap = phi>90. */
+  int32_t cl_case, cl_swap;
+  double cos_t, sin_t, tan_t; /* of theta' = 90 - phi' (radians) */
+  double cos_p, sin_p, tan_p; /* of phi' (radians)               */
+} gw_phi;
+
+typedef struct gw_voxel_plan gw_voxel_plan;
+
+/* Build a plan for n_struct structures x n_phi rotations.  All tables that
+ * depend only on sizes (CZT chirps, twiddles) are made here. */
+int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
+                         const gw_structure *structs, int32_t n_struct,
+                         const gw_phi *phis, int32_t n_phi,
+                         gw_voxel_plan **out);
+int gw_voxel_plan_destroy(gw_voxel_plan *plan);
+/* Atoms: xyz (n,3) float64, f (n,2) float32 complex scattering factor
+ * (Z + f' + i f'', times any per-atom weight).  on_device: 0 host, 1 device
+ * (device pointers are copied into the plan). */
+int gw_voxel_set_atoms(gw_voxel_plan *plan, const double *xyz, const float *f,
+                       int64_t n_atoms, int32_t on_device);
+/* Enqueue the whole forward chain on the context stream (a CUDA graph
+ * replay when gw_voxel_capture_graph succeeded). */
+int gw_voxel_execute(gw_voxel_plan *plan);
+int gw_voxel_capture_graph(gw_voxel_plan *plan);
+/* Results (synchronous).  iq: crop^3 float64, C order (qy,qx,qz).
+ * on_device: write to a device pointer instead of host memory. */
+int gw_voxel_get_iq(gw_voxel_plan *plan, double *iq, int32_t on_device);
+/* Device pointer to the float32 copy of I(q) the detector gathers from. */
+int gw_voxel_device_iq32(gw_voxel_plan *plan, const float **iq32);
+/* Parity hooks: the cropped count and sum grids (float64, crop^3). */
+int gw_voxel_get_counts(gw_voxel_plan *plan, double *counts);
+int gw_voxel_get_sums(gw_voxel_plan *plan, double *sums);
+/* Plan sizes: see GW_INFO_* in the implementation's order:
+ * [crop, batch, Ly, Lz, Nc, Nr, My, Mz, y_lo, z_lo, k0, kz0, n_slices,
+ *  device_bytes]. Returns the number written. */
+int gw_voxel_info(gw_voxel_plan *plan, int64_t *info, int32_t n);
+/* Deposit indices of one slice (after execute): y,z voxel index per atom of
+ * that slice's structure, -1 where the reference's valid_mask drops it
+ * (voxelgrids.py:328-335). */
+int gw_voxel_debug_deposit(gw_voxel_plan *plan, int32_t slice, int32_t *y_idx,
+                           int32_t *z_idx);
+/* One-shot: plan, upload, execute, download, destroy (host buffers). */
+int gw_voxelgrid(gw_ctx *ctx, const gw_voxel_params *p,
+                 const gw_structure *structs, int32_t n_struct,
+                 const gw_phi *phis, int32_t n_phi, const double *xyz,
+                 const float *f, int64_t n_atoms, double *iq_out);
+
+/* ---- detector stage ---------------------------------------------------- */
+typedef struct gw_detector_params {
+  int32_t n_h, n_v;         /* pixels (horizontal, vertical)             */
+  int32_t iq_shape[3];      /* (ny, nx, nz) of the I(q) grid              */
+  double qmin_x, qmin_y, qmin_z; /* np.min(qx), np.min(qy), np.min(qz)   */
+  double dq;                /* np.diff(qz)[0]           detector.py:213   */
+  int32_t mirror;           /* mirror_vertical_horizontal  comparison.py:857 */
+  int32_t accum;            /* GW_ACCUM_FP64 | GW_ACCUM_KAHAN32           */
+  int32_t reserved[6];
+} gw_detector_params;
+
+typedef struct gw_detector_plan gw_detector_plan;
+
+/* h_axis (n_h) and v_axis (n_v): make_detector's linspaces
+ * (detector.py:24-25).  init_R: n_init 3x3 row-major matrices applied in
+ * order to the plane (comparison.py:799-818).  Per orientation o,
+ * n_rot[o] matrices (0..3, identity ones omitted) follow one another in
+ * rot_R, and weights[o] = psi_w*phi_w*theta_w (detector.py:292). */
+int gw_detector_plan_create(gw_ctx *ctx, const gw_detector_params *p,
+                            const double *h_axis, const double *v_axis,
+                            const double *init_R, int32_t n_init,
+                            const int32_t *n_rot, const double *rot_R,
+                            const double *weights, int32_t n_orient,
+                            gw_detector_plan **out);
+int gw_detector_plan_destroy(gw_detector_plan *plan);
+/* I(q) to sample: float64 host or device array (converted to float32 on
+ * the device), or a float32 device array used in place (gw_voxel_device_iq32). */
+int gw_detector_set_iq(gw_detector_plan *plan, const double *iq,
+                       int32_t on_device);
+int gw_detector_set_iq32_device(gw_detector_plan *plan, const float *iq32);
+int gw_detector_execute(gw_detector_plan *plan);
+/* (n_v, n_h) float64 image after the epilogue (comparison.py:857-868). */
+int gw_detector_get(gw_detector_plan *plan, double *out, int32_t on_device);
+/* Flat (y*nx+x)*nz+z voxel index each pixel gathers for orientation o. */
+int gw_detector_debug_indices(gw_detector_plan *plan, int32_t orient,
+                              int64_t *flat_idx);
+/* One-shot with host buffers. */
+int gw_detector(gw_ctx *ctx, const gw_detector_params *p, const double *iq,
+                const double *h_axis, const double *v_axis,
+                const double *init_R, int32_t n_init, const int32_t *n_rot,
+                const double *rot_R, const double *weights, int32_t n_orient,
+                double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GIWAXS_GB300_H */

@@ -1,0 +1,96 @@
+"""Host-side geometry of the product (giwaxsim_gb300.forward) against the
+oracle and the reference-derived fixtures.  CPU only."""
+import numpy as np
+import pytest
+
+from giwaxsim_gb300 import forward as F
+from giwaxsim_gb300 import workloads as W
+from giwaxsim_gb300.tools import comparison, utilities
+from oracle import giwaxs_oracle as O
+from tests.conftest import golden
+
+GEOMS = [(0.3, 0.03, 3.0), (0.25, 0.02, 4.0), (0.3, 0.04095, 3.0),
+         (0.2, 0.015, 2.5), (0.5, 0.15, 1.5), (0.3, 0.02, 2.0)]
+
+
+@pytest.mark.parametrize("r,dq,mq", GEOMS)
+def test_geometry_matches_oracle(r, dq, mq):
+    g = F.VoxelGeometry(r, dq, mq)
+    gs, q, phis = O.voxel_geometry(r, dq, mq)
+    assert g.grid_size == gs
+    assert np.array_equal(g.q, q)
+    assert np.array_equal(g.auto_phis, phis)
+    sub, qs, _, _ = O.downselect_voxelgrid(np.zeros((len(q),) * 3, np.int8),
+                                           q, q, q, mq)
+    assert np.array_equal(g.q_crop, qs)
+    assert g.dq == np.diff(q)[0]
+
+
+def test_geometry_errors():
+    with pytest.raises(Exception, match="Max_q is non-physical"):
+        F.VoxelGeometry(1.0, 0.1, 10.0)
+    g = F.VoxelGeometry(0.5, 0.15, 1.5)
+    with pytest.raises(Exception, match="real-space bounds smaller"):
+        g.check_bounds(np.array([[0, 0, 0], [100.0, 100.0, 100.0]]))
+
+
+def test_phi_table_matches_reference_scalars():
+    g = F.VoxelGeometry(0.3, 0.03, 3.0)
+    phis = np.concatenate([g.auto_phis[:50], [0.0, 45.0, 90.0, 91.0, 135.0,
+                                              179.5]])
+    t = g.phi_table(phis)
+    for i, phi in enumerate(phis):
+        pr = np.radians(phi)
+        assert t["cos_phi"][i] == np.cos(pr) and t["sin_phi"][i] == np.sin(pr)
+        hx, hy, _ = O.slice_axes(g.grid_size, 0.3, phi)
+        assert t["right_qy"][i] == hy[-1] and t["right_qx"][i] == hx[-1]
+        p = phi - 90 if phi > 90 else phi
+        tr, pa = np.deg2rad(90 - p), np.deg2rad(p)
+        assert t["tan_t"][i] == np.tan(tr) and t["tan_p"][i] == np.tan(pa)
+        assert t["cos_t"][i] == np.cos(tr) and t["sin_p"][i] == np.sin(pa)
+        assert t["cl_swap"][i] == (phi > 90)
+
+
+def test_structure_constants_match_oracle():
+    for name in ("graphite-50A", "si-100A"):
+        xyz, el, _ = W.structures(name)[0]
+        fv = F.element_f_values(el, 10000.0)
+        xb, yb, zb, avg, mv = F.structure_constants(xyz, fv, 0.3)
+        oxb, oyb, ozb, oavg = O.structure_constants(xyz, fv, 0.3)
+        assert (xb, yb, zb, avg) == (oxb, oyb, ozb, oavg)
+        assert mv == np.sqrt(xb ** 2 + yb ** 2) // 0.3
+
+
+def test_detector_corner_matrices_match_full_plane():
+    """Rotation matrices from the tracked corners equal the ones the
+    reference builds from the full rotated plane."""
+    x, y, z, h, v = O.make_detector(2.0, 33, 2.0, 33)
+    c = F.PlaneCorners(h, v)
+    for kind, ang in [("psi", 90.0), ("phi", 30.0), ("theta", 10.0),
+                      ("psi", 17.0), ("theta", 0.0), ("phi", 123.0)]:
+        Rf = O.axis_matrix(x, y, z, kind, ang)
+        Rc = c.matrix(kind, ang)
+        assert np.array_equal(Rf, Rc), (kind, ang)
+        x, y, z = O.fma_xyz(x, y, z, Rf)
+        c = c.rotate(Rc)
+
+
+def test_slabmaker_and_lstsq():
+    rng = np.random.default_rng(0)
+    sim = rng.uniform(0, 1, (20, 20))
+    mask = (rng.uniform(0, 1, (20, 20)) > 0.8).astype(int)
+    reb = 3.0 * sim + 0.25
+    s, o = comparison.optimize_scale_offset(sim, reb, mask)
+    assert abs(s - 3.0) < 1e-12 and abs(o - 0.25) < 1e-12
+
+
+def test_config_parsing(tmp_path):
+    p = tmp_path / "cfg.txt"
+    p.write_text("# comment\nr_voxel_size=0.3\nfill_bkg=True\nkey=a=b\n\n")
+    cfg = utilities.parse_config_file(str(p))
+    assert cfg == {"r_voxel_size": "0.3", "fill_bkg": "True", "key": "a=b"}
+    assert utilities.str_to_bool("Yes") is True
+    assert utilities.str_to_bool("off") is False
+    assert utilities.str_to_bool("maybe") is False
+    with pytest.raises(ValueError):
+        utilities.str_to_bool("maybe", default=None)
