@@ -31,7 +31,7 @@ EXPORTS = [
     "gw_detector_plan_create", "gw_detector_plan_destroy",
     "gw_detector_set_iq", "gw_detector_set_iq32_device",
     "gw_detector_execute", "gw_detector_get", "gw_detector_debug_indices",
-    "gw_detector",
+    "gw_detector_noalloc", "gw_detector",
 ]
 
 
@@ -128,6 +128,8 @@ def _declare(lib):
         "gw_detector_execute": ([P], ctypes.c_int),
         "gw_detector_get": ([P, P, i32], ctypes.c_int),
         "gw_detector_debug_indices": ([P, i32, P], ctypes.c_int),
+        "gw_detector_noalloc": ([P, P, P, P, P, i32, P, P, P, i32, P, P],
+                                ctypes.c_int),
         "gw_detector": ([P, P, P, P, P, P, i32, P, P, P, i32, P], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():

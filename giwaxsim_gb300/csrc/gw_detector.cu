@@ -14,6 +14,8 @@
 // unchanged.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "gw_common.cuh"
@@ -324,4 +326,130 @@ extern "C" int gw_detector(gw_ctx *ctx, const gw_detector_params *p,
   if (st == GW_OK) st = gw_detector_get(P, out, 0);
   gw_detector_plan_destroy(P);
   return st;
+}
+
+// ======================================================================
+// Allocation-free detector entry point (no counterpart in the reference).
+//
+// Some callers cannot allocate device memory at the moment they need a
+// detector image: an acquisition or fitting loop that reserved its whole
+// GPU memory budget up front (a framework's caching allocator owns it, or a
+// real-time pipeline must not pay cudaMalloc/cudaFree, which can block on
+// other streams' work or fail under memory pressure mid-run).
+// gw_detector_noalloc takes every input and the output as caller-owned
+// device pointers and keeps its only scratch -- the float64 per-pixel sum
+// over orientations -- in the fixed array below, so it calls no cudaMalloc,
+// cudaFree or allocating library routine.
+//
+// The array is a module-level __device__ variable: every GPU that loads this
+// library holds its 8 MiB until the process exits.  It is shared by all
+// calls on that GPU and keeps the previous call's contents; the kernel writes
+// every pixel it later reads, so nothing has to be cleared.  Calls whose work
+// overlaps on the GPU (different streams, or threads issuing concurrently)
+// race on it and must be serialised by the caller.
+constexpr int kNoAllocMaxPixels = 1 << 20;  // 1024 x 1024 pixels
+static __device__ __align__(256) double g_noalloc_sum[kNoAllocMaxPixels];
+
+namespace {
+
+// k_detector with the per-orientation rotation offsets accumulated on the
+// fly from n_rot (the caller passes only counts), writing into `sum`.
+__global__ void k_detector_noalloc(DetArgs a, const int *n_rot, double *sum) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= a.nh * a.nv) return;
+  const int i = pix / a.nh, j = pix % a.nh;
+  double x0, y0, z0;
+  base_point(a, i, j, x0, y0, z0);
+  double acc = 0.0;
+  float s = 0.f, c = 0.f;
+  int start = 0;
+  for (int o = 0; o < a.n_orient; ++o) {
+    const int n = n_rot[o];
+    double x = x0, y = y0, z = z0;
+    for (int k = 0; k < n; ++k) rotate(a.rot_R + 9 * (start + k), x, y, z);
+    start += n;
+    const int ix = clip_idx(x, a.qmin_x, a.dq, a.inv_dq, a.nx);
+    const int iy = clip_idx(y, a.qmin_y, a.dq, a.inv_dq, a.ny);
+    const int iz = clip_idx(z, a.qmin_z, a.dq, a.inv_dq, a.nz);
+    const float v = __ldg(a.iq + ((int64_t)iy * a.nx + ix) * a.nz + iz);
+    if (!a.kahan) {
+      acc = fma((double)v, a.w[o], acc);
+    } else {
+      const float yv = v * (float)a.w[o] - c;
+      const float t = s + yv;
+      c = (t - s) - yv;
+      s = t;
+    }
+  }
+  sum[pix] = a.kahan ? (double)s - (double)c : acc;
+}
+
+// Device address of g_noalloc_sum, looked up once per device.  In host code
+// the symbol names a host-side shadow, not device memory, so it must never
+// be passed to a kernel directly.
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[128] = {};
+
+int noalloc_scratch(int device, double **out) {
+  if (device < 0 || device >= 128)
+    return gw::fail(GW_ERR_ARG, "gw_detector_noalloc: device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sum);
+    if (e != cudaSuccess)
+      return gw::cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_sum)", __FILE__,
+                           __LINE__);
+    g_noalloc_ptr[device] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return GW_OK;
+}
+
+}  // namespace
+
+extern "C" int gw_detector_noalloc(const gw_detector_params *p,
+                                   const float *iq32, const double *h_axis,
+                                   const double *v_axis, const double *init_R,
+                                   int32_t n_init, const int32_t *n_rot,
+                                   const double *rot_R, const double *weights,
+                                   int32_t n_orient, double *out,
+                                   void *stream) {
+  if (!p || !iq32 || !h_axis || !v_axis || !n_rot || !weights || !out)
+    return gw::fail(GW_ERR_ARG, "gw_detector_noalloc: null argument");
+  if (n_init < 0 || n_init > 3 || (n_init > 0 && !init_R))
+    return gw::fail(GW_ERR_ARG, "gw_detector_noalloc: n_init must be 0..3 with init_R given");
+  if (p->n_h < 1 || p->n_v < 1 || n_orient < 1 || p->iq_shape[0] < 1 ||
+      p->iq_shape[1] < 1 || p->iq_shape[2] < 1 || !(p->dq > 0))
+    return gw::fail(GW_ERR_ARG, "gw_detector_noalloc: invalid sizes");
+  if ((int64_t)p->n_h * p->n_v > kNoAllocMaxPixels)
+    return gw::fail(GW_ERR_ARG,
+                    "gw_detector_noalloc: detector has " +
+                        std::to_string((int64_t)p->n_h * p->n_v) +
+                        " pixels; the allocation-free entry point is limited "
+                        "to 1048576 (1024 x 1024). Use gw_detector_plan_create "
+                        "for larger images.");
+  int device = 0;
+  GW_CUDA(cudaGetDevice(&device));
+  double *sum = nullptr;
+  GW_TRY(noalloc_scratch(device, &sum));
+  DetArgs a{};
+  a.nh = p->n_h; a.nv = p->n_v;
+  a.ny = p->iq_shape[0]; a.nx = p->iq_shape[1]; a.nz = p->iq_shape[2];
+  a.qmin_x = p->qmin_x; a.qmin_y = p->qmin_y; a.qmin_z = p->qmin_z;
+  a.dq = p->dq; a.inv_dq = 1.0 / p->dq;
+  a.h = h_axis; a.v = v_axis; a.init_R = init_R; a.n_init = n_init;
+  a.rot_start = nullptr; a.rot_n = nullptr; a.rot_R = rot_R; a.w = weights;
+  a.n_orient = n_orient; a.iq = iq32;
+  a.kahan = p->accum == GW_ACCUM_KAHAN32;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int npx = p->n_h * p->n_v;
+  k_detector_noalloc<<<(npx + 127) / 128, 128, 0, st>>>(a, n_rot, sum);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return gw::cuda_fail(e, "k_detector_noalloc launch", __FILE__, __LINE__);
+  k_det_epilogue<<<(npx + 255) / 256, 256, 0, st>>>(sum, p->n_v, p->n_h,
+                                                    p->mirror, out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return gw::cuda_fail(e, "k_det_epilogue launch", __FILE__, __LINE__);
+  return GW_OK;
 }

@@ -201,6 +201,26 @@ int gw_detector_get(gw_detector_plan *plan, double *out, int32_t on_device);
 /* Flat (y*nx+x)*nz+z voxel index each pixel gathers for orientation o. */
 int gw_detector_debug_indices(gw_detector_plan *plan, int32_t orient,
                               int64_t *flat_idx);
+/* Allocation-free detector image; no counterpart in the reference.  For
+ * callers that cannot allocate device memory when they need an image (their
+ * memory budget is reserved up front, or a cudaMalloc/cudaFree stall or
+ * failure mid-loop is not acceptable).  Every pointer is caller-owned device
+ * memory: iq32 float32 (ny*nx*nz), h_axis/v_axis float64, init_R n_init
+ * 3x3 matrices, n_rot int32 per orientation (0..3) with rot_R holding the
+ * sum of n_rot matrices, weights float64 per orientation, out float64
+ * (n_v, n_h).  Work is enqueued on `stream` (a cudaStream_t of the current
+ * device) and not waited for.  The only scratch is a fixed 8 MiB float64
+ * image inside the library, so images are limited to 1024 x 1024 pixels
+ * (GW_ERR_ARG beyond).  The scratch is shared by all calls on a device:
+ * calls that overlap on the GPU race, so serialise them.  The first call on
+ * a device looks up the scratch address (cudaGetSymbolAddress); make that
+ * first call before any stream capture. */
+int gw_detector_noalloc(const gw_detector_params *p, const float *iq32,
+                        const double *h_axis, const double *v_axis,
+                        const double *init_R, int32_t n_init,
+                        const int32_t *n_rot, const double *rot_R,
+                        const double *weights, int32_t n_orient, double *out,
+                        void *stream);
 /* One-shot with host buffers. */
 int gw_detector(gw_ctx *ctx, const gw_detector_params *p, const double *iq,
                 const double *h_axis, const double *v_axis,
