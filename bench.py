@@ -41,6 +41,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--phis", type=int, default=0,
+                    help="use this many slices instead of the workload's")
+    ap.add_argument("--profile", action="store_true",
+                    help="one eager voxel pass and one detector pass, no "
+                         "timing (for ncu)")
     return ap.parse_args()
 
 
@@ -141,13 +146,13 @@ def max_over_ranks(pg, x):
 
 
 # ------------------------------------------------------------------ workload
-def load_workload(name):
+def load_workload(name, n_phi=0):
     from giwaxsim_gb300 import forward as F
     from giwaxsim_gb300 import workloads as W
     w = W.WORKLOADS[name]
     structs = W.structures(name)
     geom = F.VoxelGeometry(w["r"], w["dq"], w["max_q"])
-    phis = W.phis_linspace(w["n_phi"])
+    phis = W.phis_linspace(n_phi or w["n_phi"])
     items = [(xyz, F.element_f_values(el, w["energy"]), wt)
              for xyz, el, wt in structs]
     return w, structs, geom, phis, items
@@ -170,9 +175,12 @@ def run_gb300(args, world, rank, local, pg):
     from giwaxsim_gb300 import forward as F
     from giwaxsim_gb300.tools import comparison
 
-    w, structs, geom, phis, items = load_workload(args.workload)
+    w, structs, geom, phis, items = load_workload(args.workload, args.phis)
     ctx = N.Context(local)
     n_slices = len(items) * len(phis)
+    if args.profile:
+        run_profile(args, w, geom, phis, items, ctx)
+        return
     plan = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
                        smooth=w["smooth"], ctx=ctx)
     plan.set_atoms()
@@ -349,6 +357,31 @@ def run_gb300(args, world, rank, local, pg):
         p_.close()
 
 
+def run_profile(args, w, geom, phis, items, ctx):
+    """One eager pass of the voxel stage and one detector image."""
+    from giwaxsim_gb300 import forward as F
+    plan = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
+                       smooth=w["smooth"], ctx=ctx)
+    plan.set_atoms()
+    plan.execute()
+    ctx.synchronize()
+    dargs = detector_args(w, geom)
+    q = geom.q_crop
+    det = F.DetectorPlan((plan.Qc,) * 3, q, q, q, dargs["num_pixels"],
+                         dargs["max_q"], dargs["angle_init_vals"],
+                         dargs["angle_init_axs"], dargs["psis"],
+                         dargs["psi_weights"], dargs["phis"],
+                         dargs["phi_weights"], dargs["thetas"],
+                         dargs["theta_weights"], mirror=True, ctx=ctx)
+    det.set_iq_device32(plan.device_iq32())
+    det.execute()
+    ctx.synchronize()
+    print(json.dumps({"profile": args.workload, "slices": len(phis) * len(items),
+                      "plan": plan.info(), "orientations": det.n_orient}))
+    det.close()
+    plan.close()
+
+
 def algorithmic_bytes(name, info, w, n_slices, dargs, Qc):
     """Bytes a launch of `name` must move at minimum (its inputs read once,
     outputs written once), per the plan's sizes."""
@@ -420,7 +453,7 @@ def cpu_baseline(args, w, geom, phis, items, budget=None):
 def run_reference(args, world, rank, local, pg):
     if rank != 0:
         return
-    w, structs, geom, phis, items = load_workload(args.workload)
+    w, structs, geom, phis, items = load_workload(args.workload, args.phis)
     vals = []
     for _ in range(max(1, args.warmup > 0) + args.steps):
         vals.append(cpu_baseline(args, w, geom, phis, items,

@@ -83,7 +83,8 @@ class DetectorParams(ctypes.Structure):
                 ("iq_shape", ctypes.c_int32 * 3), ("qmin_x", ctypes.c_double),
                 ("qmin_y", ctypes.c_double), ("qmin_z", ctypes.c_double),
                 ("dq", ctypes.c_double), ("mirror", ctypes.c_int32),
-                ("accum", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("accum", ctypes.c_int32), ("exact", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 _lib = None

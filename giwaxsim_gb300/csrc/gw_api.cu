@@ -139,7 +139,7 @@ int gw_ctx_kernel_times(gw_ctx *c, double *ms, int64_t *launches, int32_t n) {
 const char *gw_kernel_category_name(int32_t i) {
   static const char *names[GW_K_COUNT] = {
       "prep", "tables", "deposit", "profile", "row_czt", "col_czt_bin",
-      "finalize", "detector", "det_epilogue", "misc"};
+      "finalize", "detector", "det_fix", "det_epilogue", "misc"};
   return (i >= 0 && i < GW_K_COUNT) ? names[i] : "unknown";
 }
 

@@ -108,6 +108,7 @@ enum gw_kcat {
   GW_K_COLBIN,       // column chirp-z transforms + |F|^2 + binning
   GW_K_FINALIZE,     // average, crop, f0
   GW_K_DETECTOR,     // detector orientation sum
+  GW_K_DET_FIX,      // exact replay of the detector's undecided samples
   GW_K_DET_EPI,      // mirror / clamp / scale
   GW_K_MISC,         // conversions, debug
   GW_K_COUNT

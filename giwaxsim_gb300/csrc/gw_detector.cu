@@ -14,6 +14,7 @@
 // unchanged.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -131,6 +132,158 @@ __global__ void k_det_debug(DetArgs a, int o, int64_t *idx) {
   idx[pix] = gather_index(a, o, x, y, z);
 }
 
+// ---------------------------------------------------------------- fast path
+// Per orientation, the composed rotation M = R_n...R_1 maps the base plane
+// point p0 to index space: t = (M p0 - qmin) / dq = A p0 + b.  Evaluated in
+// float32, t differs from the exact float64 replay by at most d (a bound the
+// host derives from |A|, |p0| and |b|: 10 u S + 1e-5 with u = 2^-24 and S the
+// sum of the magnitudes of the terms).  When floor(t-d) and floor(t+d) agree
+// after clipping on all three axes the gathered voxel is the exact one;
+// otherwise the (pixel, orientation) pair goes to a worklist that
+// k_detector_fix replays with the exact float64 chain.
+struct OrientFast {
+  float A[9];
+  float b[3];
+  float d[3];
+  float w;
+  int fix[3];  // >= 0: the axis' coordinate is exactly +-0 for every pixel
+  int pad;     //       and its (clipped) index is this constant
+};
+constexpr int kOrientFloats = sizeof(OrientFast) / 4;
+
+constexpr int kDetThreads = 256, kDetPix = 2, kDetChunk = 128, kDetFlush = 16;
+
+__device__ __forceinline__ bool fast_axis(float t, float d, int n, int &k) {
+  const float lo = fminf(fmaxf(floorf(t - d), 0.f), (float)(n - 1));
+  const float hi = fminf(fmaxf(floorf(t + d), 0.f), (float)(n - 1));
+  k = (int)lo;
+  return lo == hi;
+}
+
+__device__ __forceinline__ bool fast_index(const OrientFast &T, const DetArgs &a,
+                                           float x, float y, float z,
+                                           int64_t &idx) {
+  const float tx = fmaf(T.A[0], x, fmaf(T.A[1], y, fmaf(T.A[2], z, T.b[0])));
+  const float ty = fmaf(T.A[3], x, fmaf(T.A[4], y, fmaf(T.A[5], z, T.b[1])));
+  const float tz = fmaf(T.A[6], x, fmaf(T.A[7], y, fmaf(T.A[8], z, T.b[2])));
+  int ix, iy, iz;
+  bool ok = fast_axis(tx, T.d[0], a.nx, ix) & fast_axis(ty, T.d[1], a.ny, iy) &
+            fast_axis(tz, T.d[2], a.nz, iz);
+  if (T.fix[0] >= 0 || T.fix[1] >= 0 || T.fix[2] >= 0) {
+    ok = (T.fix[0] >= 0 || fast_axis(tx, T.d[0], a.nx, ix)) &
+         (T.fix[1] >= 0 || fast_axis(ty, T.d[1], a.ny, iy)) &
+         (T.fix[2] >= 0 || fast_axis(tz, T.d[2], a.nz, iz));
+    if (T.fix[0] >= 0) ix = T.fix[0];
+    if (T.fix[1] >= 0) iy = T.fix[1];
+    if (T.fix[2] >= 0) iz = T.fix[2];
+  }
+  idx = ((int64_t)iy * a.nx + ix) * a.nz + iz;
+  return ok;
+}
+
+__global__ void __launch_bounds__(kDetThreads)
+k_detector_fast(DetArgs a, const OrientFast *ot, double *acc_out, int2 *wl,
+                int *wl_count, int wl_cap) {
+  __shared__ OrientFast s_ot[kDetChunk];
+  const int npx = a.nh * a.nv;
+  const int lane = threadIdx.x & 31;
+  int pix[kDetPix];
+  bool valid[kDetPix];
+  float xf[kDetPix], yf[kDetPix], zf[kDetPix];
+  double x0[kDetPix], y0[kDetPix], z0[kDetPix];
+  double acc[kDetPix];
+  float part[kDetPix], kc[kDetPix];
+#pragma unroll
+  for (int k = 0; k < kDetPix; ++k) {
+    pix[k] = blockIdx.x * (kDetThreads * kDetPix) + k * kDetThreads + threadIdx.x;
+    valid[k] = pix[k] < npx;
+    x0[k] = y0[k] = z0[k] = 0.0;
+    if (valid[k]) base_point(a, pix[k] / a.nh, pix[k] % a.nh, x0[k], y0[k], z0[k]);
+    xf[k] = (float)x0[k]; yf[k] = (float)y0[k]; zf[k] = (float)z0[k];
+    acc[k] = 0.0; part[k] = 0.f; kc[k] = 0.f;
+  }
+  for (int c0 = 0; c0 < a.n_orient; c0 += kDetChunk) {
+    const int nc = min(kDetChunk, a.n_orient - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * kOrientFloats; t += kDetThreads)
+      reinterpret_cast<float *>(s_ot)[t] = reinterpret_cast<const float *>(ot + c0)[t];
+    __syncthreads();
+    for (int oo = 0; oo < nc; ++oo) {
+      const OrientFast &T = s_ot[oo];
+      const int o = c0 + oo;
+#pragma unroll
+      for (int k = 0; k < kDetPix; ++k) {
+        int64_t idx;
+        const bool ok = fast_index(T, a, xf[k], yf[k], zf[k], idx);
+        const bool need = valid[k] && !ok;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        bool inline_exact = false;
+        if (m) {
+          int base = 0;
+          const int leader = __ffs(m) - 1;
+          if (lane == leader) base = atomicAdd(wl_count, __popc(m));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (need) {
+            const int slot = base + __popc(m & ((1u << lane) - 1u));
+            if (slot < wl_cap) wl[slot] = make_int2(pix[k], o);
+            else inline_exact = true;
+          }
+        }
+        float v = 0.f;
+        if (valid[k] && ok) v = __ldg(a.iq + idx);
+        if (inline_exact) v = __ldg(a.iq + gather_index(a, o, x0[k], y0[k], z0[k]));
+        if (valid[k] && (ok || inline_exact)) {
+          if (!a.kahan) {
+            part[k] = fmaf(v, T.w, part[k]);
+          } else {
+            const float yv = v * T.w - kc[k];
+            const float t = part[k] + yv;
+            kc[k] = (t - part[k]) - yv;
+            part[k] = t;
+          }
+        }
+      }
+      // float32 partial sums of kDetFlush orientations, float64 across them
+      if (!a.kahan && ((o + 1) % kDetFlush == 0)) {
+#pragma unroll
+        for (int k = 0; k < kDetPix; ++k) { acc[k] += (double)part[k]; part[k] = 0.f; }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kDetPix; ++k) {
+    if (!valid[k]) continue;
+    acc_out[pix[k]] = a.kahan ? (double)part[k] - (double)kc[k]
+                              : acc[k] + (double)part[k];
+  }
+}
+
+// Exact float64 replay of the worklist's (pixel, orientation) pairs.
+__global__ void k_detector_fix(DetArgs a, const int2 *wl, const int *wl_count,
+                               int wl_cap, double *acc) {
+  const int n = min(*wl_count, wl_cap);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += gridDim.x * blockDim.x) {
+    const int2 it = wl[e];
+    double x, y, z;
+    base_point(a, it.x / a.nh, it.x % a.nh, x, y, z);
+    const float v = __ldg(a.iq + gather_index(a, it.y, x, y, z));
+    atomicAdd(acc + it.x, (double)v * a.w[it.y]);
+  }
+}
+
+__global__ void k_det_debug_fast(DetArgs a, const OrientFast *ot, int o,
+                                 int64_t *idx) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= a.nh * a.nv) return;
+  double x, y, z;
+  base_point(a, pix / a.nh, pix % a.nh, x, y, z);
+  int64_t k;
+  if (!fast_index(ot[o], a, (float)x, (float)y, (float)z, k))
+    k = gather_index(a, o, x, y, z);
+  idx[pix] = k;
+}
+
 }  // namespace
 
 struct gw_detector_plan {
@@ -143,6 +296,10 @@ struct gw_detector_plan {
   float *d_iq_own = nullptr;
   const float *iq = nullptr;
   double *d_acc = nullptr, *d_out = nullptr;
+  OrientFast *d_ot = nullptr;   // fast-path orientation table
+  int2 *d_wl = nullptr;         // exact-replay worklist
+  int *d_wl_count = nullptr;
+  int wl_cap = 0;
   bool executed = false;
 };
 
@@ -216,6 +373,98 @@ extern "C" int gw_detector_plan_create(gw_ctx *ctx, const gw_detector_params *p,
     gw_detector_plan_destroy(P);
     return gw::cuda_fail(e, "detector buffers", __FILE__, __LINE__);
   }
+  if (!p->exact) {
+    // corners of the base plane after the initial rotations bound |p0|
+    double pmax[3] = {0, 0, 0};
+    const double hs[2] = {h_axis[0], h_axis[p->n_h - 1]};
+    const double vs[2] = {v_axis[0], v_axis[p->n_v - 1]};
+    for (double hh : hs)
+      for (double vv : vs) {
+        double c[3] = {0.0, hh, vv};
+        for (int k = 0; k < n_init; ++k) {
+          const double *R = init_R + 9 * k;
+          const double a0 = rot_chain(R, c[0], c[1], c[2]);
+          const double a1 = rot_chain(R + 3, c[0], c[1], c[2]);
+          const double a2 = rot_chain(R + 6, c[0], c[1], c[2]);
+          c[0] = a0; c[1] = a1; c[2] = a2;
+        }
+        for (int k = 0; k < 3; ++k) pmax[k] = std::max(pmax[k], std::fabs(c[k]) * (1 + 1e-12));
+      }
+    const double inv_dq = 1.0 / p->dq;
+    const double qmin[3] = {p->qmin_x, p->qmin_y, p->qmin_z};
+    const int dims[3] = {p->iq_shape[1], p->iq_shape[0], p->iq_shape[2]};  // x, y, z
+    // Axes whose coordinate is exactly +-0 for every pixel: the plane starts
+    // at x = 0 (detector.py:27); a rotation keeps output c at +-0 when each
+    // of its row-c entries is 0 or multiplies a coordinate that is +-0
+    // (fma of exact zeros).  Such an axis gathers index floor((0-qmin)/dq),
+    // a constant; deciding it in float32 would be ambiguous whenever q=0
+    // lies on a voxel boundary.
+    auto propagate = [](const double *R, const bool in[3], bool out[3]) {
+      for (int c = 0; c < 3; ++c) {
+        bool z = true;
+        for (int k = 0; k < 3; ++k) z = z && (R[3 * c + k] == 0.0 || in[k]);
+        out[c] = z;
+      }
+    };
+    bool zero0[3] = {true, false, false};
+    for (int k = 0; k < n_init; ++k) {
+      bool nz[3];
+      propagate(init_R + 9 * k, zero0, nz);
+      std::copy(nz, nz + 3, zero0);
+    }
+    std::vector<OrientFast> ot(n_orient);
+    for (int o = 0; o < n_orient; ++o) {
+      bool zero[3] = {zero0[0], zero0[1], zero0[2]};
+      for (int r = 0; r < rn[o]; ++r) {
+        bool nz[3];
+        propagate(rot_R + 9 * (rs[o] + r), zero, nz);
+        std::copy(nz, nz + 3, zero);
+      }
+      for (int c = 0; c < 3; ++c) {
+        ot[o].fix[c] = -1;
+        if (zero[c]) {
+          double k = floor_div_exact(0.0 - qmin[c], p->dq, inv_dq);
+          k = std::min(std::max(k, 0.0), (double)(dims[c] - 1));
+          ot[o].fix[c] = (int)k;
+        }
+      }
+      ot[o].pad = 0;
+      double M[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+      for (int r = 0; r < rn[o]; ++r) {
+        const double *R = rot_R + 9 * (rs[o] + r);
+        double T[9];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j)
+            T[3 * i + j] = R[3 * i] * M[j] + R[3 * i + 1] * M[3 + j] + R[3 * i + 2] * M[6 + j];
+        std::copy(T, T + 9, M);
+      }
+      for (int c = 0; c < 3; ++c) {
+        double S = std::fabs(qmin[c] * inv_dq);
+        for (int k = 0; k < 3; ++k) {
+          ot[o].A[3 * c + k] = (float)(M[3 * c + k] * inv_dq);
+          S += std::fabs(M[3 * c + k] * inv_dq) * pmax[k];
+        }
+        ot[o].b[c] = (float)(-qmin[c] * inv_dq);
+        ot[o].d[c] = (float)(10.0 * std::ldexp(1.0, -24) * S + 1e-5);
+      }
+      ot[o].w = (float)weights[o];
+    }
+    const int64_t pairs = (int64_t)npx * n_orient;
+    P->wl_cap = (int)std::max<int64_t>(1 << 16, std::min<int64_t>(pairs / 8, 1 << 26));
+    // GW_DET_WORKLIST_CAP shrinks the worklist (tests use it to exercise the
+    // in-kernel exact path taken when the list is full)
+    if (const char *cap = getenv("GW_DET_WORKLIST_CAP")) P->wl_cap = std::max(1, atoi(cap));
+    if ((st = up(&P->d_ot, ot.data(), ot.size()))) {
+      gw_detector_plan_destroy(P);
+      return st;
+    }
+    e = gw::dev_malloc((void **)&P->d_wl, (size_t)P->wl_cap * sizeof(int2));
+    if (e == cudaSuccess) e = gw::dev_malloc((void **)&P->d_wl_count, sizeof(int));
+    if (e != cudaSuccess) {
+      gw_detector_plan_destroy(P);
+      return gw::cuda_fail(e, "detector worklist", __FILE__, __LINE__);
+    }
+  }
   *out = P;
   return GW_OK;
 }
@@ -223,7 +472,8 @@ extern "C" int gw_detector_plan_create(gw_ctx *ctx, const gw_detector_params *p,
 extern "C" int gw_detector_plan_destroy(gw_detector_plan *P) {
   if (!P) return GW_OK;
   void *ptrs[] = {P->d_h, P->d_v, P->d_init, P->d_rot, P->d_w, P->d_rs,
-                  P->d_rn, P->d_iq_own, P->d_acc, P->d_out};
+                  P->d_rn, P->d_iq_own, P->d_acc, P->d_out, P->d_ot, P->d_wl,
+                  P->d_wl_count};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -270,9 +520,22 @@ extern "C" int gw_detector_execute(gw_detector_plan *P) {
   GW_CUDA(cudaSetDevice(P->ctx->device));
   const int npx = P->p.n_h * P->p.n_v;
   DetArgs a = det_args(P);
-  {
+  if (P->p.exact) {
     gw::KTimer tm(P->ctx, GW_K_DETECTOR);
     k_detector<<<(npx + 127) / 128, 128, 0, P->ctx->stream>>>(a, P->d_acc);
+    GW_LAUNCHED(P->ctx);
+  } else {
+    GW_CUDA(cudaMemsetAsync(P->d_wl_count, 0, sizeof(int), P->ctx->stream));
+    {
+      gw::KTimer tm(P->ctx, GW_K_DETECTOR);
+      const int per = kDetThreads * kDetPix;
+      k_detector_fast<<<(npx + per - 1) / per, kDetThreads, 0, P->ctx->stream>>>(
+          a, P->d_ot, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);
+      GW_LAUNCHED(P->ctx);
+    }
+    gw::KTimer tm(P->ctx, GW_K_DET_FIX);
+    k_detector_fix<<<2 * P->ctx->sm_count, 256, 0, P->ctx->stream>>>(
+        a, P->d_wl, P->d_wl_count, P->wl_cap, P->d_acc);
     GW_LAUNCHED(P->ctx);
   }
   gw::KTimer tm(P->ctx, GW_K_DET_EPI);
@@ -302,7 +565,10 @@ extern "C" int gw_detector_debug_indices(gw_detector_plan *P, int32_t orient,
   int64_t *d = nullptr;
   GW_CUDA(gw::dev_malloc((void **)&d, npx * sizeof(int64_t)));
   DetArgs a = det_args(P);
-  k_det_debug<<<(npx + 255) / 256, 256, 0, P->ctx->stream>>>(a, orient, d);
+  if (P->p.exact)
+    k_det_debug<<<(npx + 255) / 256, 256, 0, P->ctx->stream>>>(a, orient, d);
+  else
+    k_det_debug_fast<<<(npx + 255) / 256, 256, 0, P->ctx->stream>>>(a, P->d_ot, orient, d);
   P->ctx->launches++;
   cudaError_t e = cudaMemcpyAsync(flat_idx, d, npx * sizeof(int64_t),
                                   cudaMemcpyDeviceToHost, P->ctx->stream);

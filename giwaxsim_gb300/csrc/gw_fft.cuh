@@ -1,17 +1,49 @@
-// Batched power-of-two complex FFTs in shared memory (Stockham autosort).
+// Batched power-of-two complex FFTs in shared memory (Stockham autosort,
+// radix-16 register butterflies).
 //
-// NB sequences of length M sit back to back in shared memory (buf[f*M+n]).
-// Each pass reads every butterfly's R inputs into registers, synchronises,
-// then writes the R outputs in Stockham order, so a single buffer suffices.
-// Passes are radix-4 with one radix-2 pass when log2(M) is odd.  Twiddles
-// come from a shared table tw[t] = exp(-2*pi*i*t/M) made in float64 on the
-// host, so no pass evaluates a transcendental.
+// NB sequences of length M are transformed together by one block.  A pass
+// with radix R and stride Ns reads, for butterfly j, the R values
+// j + r*(M/R), multiplies value r by exp(-+2 pi i r (j mod Ns) / (Ns R)),
+// does an R-point DFT in registers and writes output r to
+// (j / Ns) * Ns * R + (j mod Ns) + r * Ns; after the last pass the sequence
+// is in natural order.  M = 16^a * R_last with R_last in {2,4,8,16}, so a
+// 2048-point transform is three passes (16, 16, 8).
 //
-// Sizes and launch shapes: FftShape<M> gives NB (sequences per block) and
-// NT (threads) so that every radix-4 pass is 4 butterflies per thread.
+// Shared layout: element a of sequence f lives at f*ldm + a + (a >> 4).  With
+// that one-in-sixteen padding every pass's reads (consecutive j) and writes
+// (stride R when Ns = 1, consecutive otherwise) fall into 16 distinct 8-byte
+// bank pairs per half-warp, i.e. no bank conflicts.
+//
+// Twiddles come from per-pass tables tw[k*(R-1) + r-1] = W_{Ns R}^{r k}
+// made in float64 on the host; lanes read consecutive k at an odd stride
+// (R-1), again conflict-free.  No pass evaluates a transcendental.
+//
+// The first pass of a transform can read its inputs from a functor (global
+// memory) and the last pass can hand its outputs to a functor, so the
+// transform's input and output need no shared-memory round trip.
 #pragma once
 
 #include "gw_common.cuh"
+
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+__host__ __device__ constexpr int fft_pad(int a) { return a + (a >> 4); }
+
+// Pass plan: number of radix-16 passes and the last radix.
+template <int M>
+struct FftPlan {
+  static constexpr int L2 = ilog2(M);
+  static constexpr int N16 = (L2 % 4 == 0) ? L2 / 4 : L2 / 4;  // radix-16 passes
+  static constexpr int RLAST = 1 << (L2 - 4 * N16);          // 1 if none
+  static constexpr int NPASS = N16 + (RLAST > 1 ? 1 : 0);
+  static constexpr int LDM = fft_pad(M) + 4;  // floats2 per sequence (+4: see f-fastest maps)
+  // twiddle table length (passes with Ns > 1)
+  __host__ __device__ static constexpr int tw_len() {
+    int t = 0, ns = 16;
+    for (int p = 1; p < N16; ++p) { t += ns * 15; ns *= 16; }
+    if (RLAST > 1 && N16 >= 1) t += ns * (RLAST - 1);
+    return t;
+  }
+};
 
 template <int M>
 struct FftShape;
@@ -24,102 +56,202 @@ template <> struct FftShape<2048> { static constexpr int NB = 4,  NT = 512; };
 template <> struct FftShape<4096> { static constexpr int NB = 2,  NT = 512; };
 template <> struct FftShape<8192> { static constexpr int NB = 1,  NT = 512; };
 
-__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
-
 template <bool INV>
-__device__ __forceinline__ float2 twid(const float2 *tw, int t) {
-  float2 w = tw[t];
+__device__ __forceinline__ float2 conj_if(float2 w) {
   if (INV) w.y = -w.y;
   return w;
 }
 
-// In-place radix-4 DFT of (a0,a1,a2,a3); forward uses exp(-i), inverse exp(+i).
+// x * exp(-+ i pi/2): forward multiplies by -i, inverse by +i
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft2(float2 &a0, float2 &a1) {
+  const float2 s = cadd(a0, a1), d = csub(a0, a1);
+  a0 = s;
+  a1 = d;
+}
+
 template <bool INV>
 __device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2,
                                      float2 &a3) {
-  float2 s0 = cadd(a0, a2), d0 = csub(a0, a2);
-  float2 s1 = cadd(a1, a3), d1 = csub(a1, a3);
-  // d1 * (-i) forward, d1 * (+i) inverse
-  float2 r = INV ? make_float2(-d1.y, d1.x) : make_float2(d1.y, -d1.x);
+  const float2 s0 = cadd(a0, a2), d0 = csub(a0, a2);
+  const float2 s1 = cadd(a1, a3), d1 = mul_mi<INV>(csub(a1, a3));
   a0 = cadd(s0, s1);
   a2 = csub(s0, s1);
-  a1 = cadd(d0, r);
-  a3 = csub(d0, r);
+  a1 = cadd(d0, d1);
+  a3 = csub(d0, d1);
 }
 
-// All threads of the block must call this.  buf: NB*M complex values.
-template <int M, int NB, int NT, bool INV>
-__device__ __forceinline__ void fft_block(float2 *buf, const float2 *tw) {
-  constexpr int LOG2M = ilog2(M);
-  constexpr int Q = M / 4;
-  constexpr int BF = NB * Q;
-  constexpr int PER = BF / NT;
-  static_assert(BF % NT == 0, "radix-4 butterflies must split evenly");
-  const int tid = threadIdx.x;
-  int Ns = 1;
-#pragma unroll 1
-  for (int pass = 0; pass < LOG2M / 2; ++pass) {
-    float2 v[PER][4];
-    const int tstride = M / (4 * Ns);
-#pragma unroll
-    for (int e = 0; e < PER; ++e) {
-      const int b = tid + e * NT;
-      const int f = b / Q, j = b % Q;
-      const float2 *src = buf + f * M;
-      float2 a0 = src[j], a1 = src[j + Q], a2 = src[j + 2 * Q],
-             a3 = src[j + 3 * Q];
-      if (Ns > 1) {
-        const int k = j & (Ns - 1);
-        a1 = cmul(a1, twid<INV>(tw, k * tstride));
-        a2 = cmul(a2, twid<INV>(tw, 2 * k * tstride));
-        a3 = cmul(a3, twid<INV>(tw, 3 * k * tstride));
-      }
-      dft4<INV>(a0, a1, a2, a3);
-      v[e][0] = a0; v[e][1] = a1; v[e][2] = a2; v[e][3] = a3;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int e = 0; e < PER; ++e) {
-      const int b = tid + e * NT;
-      const int f = b / Q, j = b % Q;
-      const int k = j & (Ns - 1);
-      float2 *dst = buf + f * M + (j / Ns) * Ns * 4 + k;
-      dst[0] = v[e][0];
-      dst[Ns] = v[e][1];
-      dst[2 * Ns] = v[e][2];
-      dst[3 * Ns] = v[e][3];
-    }
-    __syncthreads();
-    Ns *= 4;
+// W_16^m (forward sign); m in 0..15
+__device__ __forceinline__ float2 w16(int m) {
+  constexpr float c1 = 0.92387953251128674f, s1 = 0.38268343236508978f;
+  constexpr float c2 = 0.70710678118654752f;
+  switch (m & 15) {
+    case 0: return make_float2(1.f, 0.f);
+    case 1: return make_float2(c1, -s1);
+    case 2: return make_float2(c2, -c2);
+    case 3: return make_float2(s1, -c1);
+    case 4: return make_float2(0.f, -1.f);
+    case 5: return make_float2(-s1, -c1);
+    case 6: return make_float2(-c2, -c2);
+    case 7: return make_float2(-c1, -s1);
+    case 8: return make_float2(-1.f, 0.f);
+    case 9: return make_float2(-c1, s1);
+    case 10: return make_float2(-c2, c2);
+    case 11: return make_float2(-s1, c1);
+    case 12: return make_float2(0.f, 1.f);
+    case 13: return make_float2(s1, c1);
+    case 14: return make_float2(c2, c2);
+    default: return make_float2(c1, s1);
   }
-  if (LOG2M & 1) {
-    // final radix-2 pass, Ns = M/2: butterfly j pairs (j, j+M/2), twiddle tw[j]
-    constexpr int H = M / 2;
-    constexpr int BF2 = NB * H;
-    constexpr int PER2 = (BF2 + NT - 1) / NT;
-    float2 v[PER2][2];
+}
+
+// In-register R-point DFT.  Output k ends in slot out_slot<R>(k).
+template <int R>
+__host__ __device__ constexpr int out_slot(int k) {
+  return R == 16 ? (k % 4) * 4 + k / 4 : R == 8 ? (k % 4) * 2 + k / 4 : k;
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 *v) {
+  if constexpr (R == 2) {
+    dft2<INV>(v[0], v[1]);
+  } else if constexpr (R == 4) {
+    dft4<INV>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    // n = 2 n1 + n2; four-point DFTs over n1, twiddle W8^{n2 k1}, pairs
 #pragma unroll
-    for (int e = 0; e < PER2; ++e) {
-      const int b = tid + e * NT;
-      if (BF2 % NT == 0 || b < BF2) {
-        const int f = b / H, j = b % H;
-        const float2 *src = buf + f * M;
-        float2 a0 = src[j];
-        float2 a1 = cmul(src[j + H], twid<INV>(tw, j));
-        v[e][0] = cadd(a0, a1);
-        v[e][1] = csub(a0, a1);
+    for (int n2 = 0; n2 < 2; ++n2) dft4<INV>(v[n2], v[n2 + 2], v[n2 + 4], v[n2 + 6]);
+#pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1) v[1 + 2 * k1] = cmul(v[1 + 2 * k1], conj_if<INV>(w16(2 * k1)));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft2<INV>(v[2 * k1], v[2 * k1 + 1]);
+  } else {
+    static_assert(R == 16, "radix");
+    // n = 4 n1 + n2; four-point DFTs over n1, twiddle W16^{n2 k1}, over n2
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2)
+      dft4<INV>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
+#pragma unroll
+    for (int n2 = 1; n2 < 4; ++n2)
+#pragma unroll
+      for (int k1 = 1; k1 < 4; ++k1)
+        v[n2 + 4 * k1] = cmul(v[n2 + 4 * k1], conj_if<INV>(w16(n2 * k1)));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+      dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+  }
+}
+
+// Twiddle-table offset of pass p (p >= 1) of a length-M plan.
+template <int M>
+__host__ __device__ constexpr int tw_offset(int p) {
+  int t = 0, ns = 16;
+  for (int q = 1; q < p; ++q) { t += ns * 15; ns *= 16; }
+  return t;
+}
+
+// Generic pass.  SRC: 0 = shared memory (optionally multiplied by pre[n]),
+// 1 = load(f, n).  DST: 0 = shared memory, 1 = store(f, m, value).
+// FFAST maps the sequence index f fastest across threads (column loads from
+// global memory); otherwise the butterfly index j is fastest.
+template <int M, int R, int NS, int NB, int NT, bool INV, int SRC, bool PREMUL,
+          int DST, bool FFAST, class Load, class Store>
+__device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
+                                         const float2 *pre, Load load,
+                                         Store store) {
+  constexpr int Q = M / R;
+  constexpr int BF = NB * Q;
+  constexpr int PER = (BF + NT - 1) / NT;
+  constexpr int LDM = FftPlan<M>::LDM;
+  float2 v[PER][R];
+#pragma unroll
+  for (int e = 0; e < PER; ++e) {
+    const int b = threadIdx.x + e * NT;
+    if (BF % NT == 0 || b < BF) {
+      const int f = FFAST ? b % NB : b / Q;
+      const int j = FFAST ? b / NB : b % Q;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int n = j + r * Q;
+        if (SRC == 0) {
+          float2 x = buf[f * LDM + fft_pad(n)];
+          if (PREMUL) x = cmul(x, __ldg(pre + n));
+          v[e][r] = x;
+        } else {
+          v[e][r] = load(f, n);
+        }
+      }
+      if (NS > 1) {
+        const int k = j % NS;
+        const float2 *t = tw + k * (R - 1) - 1;
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[e][r] = cmul(v[e][r], conj_if<INV>(t[r]));
+      }
+      dft<R, INV>(v[e]);
+    }
+  }
+  if (SRC == 0 && DST == 0) __syncthreads();
+#pragma unroll
+  for (int e = 0; e < PER; ++e) {
+    const int b = threadIdx.x + e * NT;
+    if (BF % NT == 0 || b < BF) {
+      const int f = FFAST ? b % NB : b / Q;
+      const int j = FFAST ? b / NB : b % Q;
+      const int k = j % NS;
+      const int base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int m = base + r * NS;
+        const float2 val = v[e][out_slot<R>(r)];
+        if (DST == 0) buf[f * LDM + fft_pad(m)] = val;
+        else store(f, m, val);
       }
     }
-    __syncthreads();
-#pragma unroll
-    for (int e = 0; e < PER2; ++e) {
-      const int b = tid + e * NT;
-      if (BF2 % NT == 0 || b < BF2) {
-        const int f = b / H, j = b % H;
-        buf[f * M + j] = v[e][0];
-        buf[f * M + j + H] = v[e][1];
-      }
+  }
+  if (DST == 0) __syncthreads();
+}
+
+struct NoLoad {
+  __device__ float2 operator()(int, int) const { return make_float2(0.f, 0.f); }
+};
+struct NoStore {
+  __device__ void operator()(int, int, float2) const {}
+};
+
+// Whole transform.  The first pass reads shared memory (SRC=0, times pre[n]
+// when PREMUL) or load(f, n) (SRC=1); the last pass writes shared memory
+// (DST=0) or calls store(f, m, value) (DST=1).  Middle passes stay in shared
+// memory.  A transform ending in shared memory leaves the block synchronised.
+template <int M, int NB, int NT, bool INV, int SRC, bool PREMUL, int DST,
+          bool FFAST_FIRST, class Load, class Store>
+__device__ __forceinline__ void fft_run(float2 *buf, const float2 *tw,
+                                        const float2 *pre, Load load,
+                                        Store store) {
+  using Pl = FftPlan<M>;
+  static_assert(Pl::N16 >= 1, "M >= 16");
+  if constexpr (Pl::NPASS == 1) {
+    fft_pass<M, 16, 1, NB, NT, INV, SRC, PREMUL, DST, FFAST_FIRST>(buf, tw, pre, load, store);
+  } else {
+    fft_pass<M, 16, 1, NB, NT, INV, SRC, PREMUL, 0, FFAST_FIRST>(buf, tw, pre, load, NoStore());
+    if constexpr (Pl::N16 >= 2) {
+      constexpr int dst = Pl::NPASS == 2 ? DST : 0;
+      fft_pass<M, 16, 16, NB, NT, INV, 0, false, dst, false>(
+          buf, tw + tw_offset<M>(1), nullptr, NoLoad(), store);
     }
-    __syncthreads();
+    if constexpr (Pl::N16 >= 3) {
+      constexpr int dst = Pl::NPASS == 3 ? DST : 0;
+      fft_pass<M, 16, 256, NB, NT, INV, 0, false, dst, false>(
+          buf, tw + tw_offset<M>(2), nullptr, NoLoad(), store);
+    }
+    if constexpr (Pl::RLAST > 1) {
+      constexpr int NSL = M / Pl::RLAST;
+      fft_pass<M, Pl::RLAST, NSL, NB, NT, INV, 0, false, DST, false>(
+          buf, tw + tw_offset<M>(Pl::N16), nullptr, NoLoad(), store);
+    }
   }
 }

@@ -59,6 +59,7 @@ struct SliceArgs {
   float2 *amo;
   float *my, *mz;
   const float *gw;  // gaussian weights, 2*radius+1
+  float4 *sconst;   // per slice: (Cbg.re, Cbg.im, Cd.re, Cd.im)
   int *err;
 };
 
@@ -103,6 +104,16 @@ __global__ void k_ymin(SliceArgs a, int slice0) {
   const int sl = slice0 + blockIdx.y;
   const int t = sl / a.n_phi, p = sl % a.n_phi;
   const gw_structure s = a.st[t];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // background constant C = avg_voxel_f * max_voxels (voxelgrids.py:358,365):
+    // Cbg is what the transformed window excludes (batched mode), Cd what
+    // stays inside it
+    const float2 c = make_float2((float)GW_DMUL(s.avg_f_re, s.max_voxels),
+                                 (float)GW_DMUL(s.avg_f_im, s.max_voxels));
+    const bool bg = !a.plain && (a.fill || a.smooth_on);
+    a.sconst[sl] = bg ? make_float4(c.x, c.y, 0.f, 0.f)
+                      : make_float4(0.f, 0.f, c.x, c.y);
+  }
   const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
   unsigned long long best = ~0ULL;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -271,52 +282,61 @@ struct SliceConst {
 };
 
 __device__ __forceinline__ SliceConst slice_const(const SliceArgs &a, int sl) {
-  const gw_structure s = a.st[sl / a.n_phi];
-  const float2 c = make_float2((float)GW_DMUL(s.avg_f_re, s.max_voxels),
-                               (float)GW_DMUL(s.avg_f_im, s.max_voxels));
+  const float4 v = a.sconst[sl];
   SliceConst k;
-  const bool bg = !a.plain && (a.fill || a.smooth_on);
-  k.cbg = bg ? c : make_float2(0.f, 0.f);
-  k.cd = bg ? make_float2(0.f, 0.f) : c;
+  k.cbg = make_float2(v.x, v.y);
+  k.cd = make_float2(v.z, v.w);
   return k;
 }
 
-// Row stage: for NB rows (slice, z) transform along y, keep Nc outputs.
+// Row stage: NB rows (slice, z) per block, transformed along y; Nc outputs
+// kept.  The forward FFT's first pass reads the deposit box directly (with
+// the fill/smoothing transform and the chirp A), the inverse FFT's first
+// pass multiplies by the filter spectrum H, and its last pass writes
+// F1 = B * result straight to global memory.
+template <int M>
+struct RowLoad {
+  const SliceArgs *a;
+  const CztArgs *cz;
+  int slice0, row0, n_rows;
+  __device__ float2 operator()(int f, int n) const {
+    const int row = row0 + f;
+    if (row >= n_rows || n >= cz->L) return make_float2(0.f, 0.f);
+    const int slot = row / a->Lz, zz = row % a->Lz;
+    const int sl = slice0 + slot;
+    const SliceConst k = slice_const(*a, sl);
+    const float2 dep = a->box[((size_t)slot * a->Lz + zz) * a->Ly + n];
+    return cmul(d_value(*a, slot, sl, zz, n, dep, k.cd, k.cbg, a->ext[sl]),
+                __ldg(cz->A + n));
+  }
+};
+
+struct RowStore {
+  const float2 *B;
+  float2 *F1;
+  int row0, n_rows, nc;
+  __device__ void operator()(int f, int m, float2 v) const {
+    const int row = row0 + f;
+    if (row < n_rows && m < nc) F1[(size_t)row * nc + m] = cmul(v, __ldg(B + m));
+  }
+};
+
 template <int M>
 __global__ void __launch_bounds__(FftShape<M>::NT)
 k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
           float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  constexpr int TWL = FftPlan<M>::tw_len();
   extern __shared__ float2 smem[];
-  float2 *buf = smem;
-  float2 *tw = smem + NB * M;
-  for (int t = threadIdx.x; t < M; t += NT) tw[t] = cz.tw[t];
+  float2 *tw = smem;
+  float2 *buf = smem + TWL;
+  for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
+  __syncthreads();
   const int row0 = blockIdx.x * NB;
-  for (int idx = threadIdx.x; idx < NB * M; idx += NT) {
-    const int f = idx / M, n = idx % M;
-    const int row = row0 + f;
-    float2 v = make_float2(0.f, 0.f);
-    if (row < n_rows && n < cz.L) {
-      const int slot = row / a.Lz, zz = row % a.Lz;
-      const int sl = slice0 + slot;
-      const SliceConst k = slice_const(a, sl);
-      const float2 dep = a.box[((size_t)slot * a.Lz + zz) * a.Ly + n];
-      v = cmul(d_value(a, slot, sl, zz, n, dep, k.cd, k.cbg, a.ext[sl]), cz.A[n]);
-    }
-    buf[idx] = v;
-  }
-  __syncthreads();
-  fft_block<M, NB, NT, false>(buf, tw);
-  for (int idx = threadIdx.x; idx < NB * M; idx += NT)
-    buf[idx] = cmul(buf[idx], cz.H[idx % M]);
-  __syncthreads();
-  fft_block<M, NB, NT, true>(buf, tw);
-  for (int idx = threadIdx.x; idx < NB * nc_out; idx += NT) {
-    const int f = idx / nc_out, m = idx % nc_out;
-    const int row = row0 + f;
-    if (row < n_rows)
-      F1[(size_t)row * nc_out + m] = cmul(buf[f * M + m], cz.B[m]);
-  }
+  RowLoad<M> ld{&a, &cz, slice0, row0, n_rows};
+  fft_run<M, NB, NT, false, 1, false, 0, false>(buf, tw, nullptr, ld, NoStore());
+  RowStore stv{cz.B, F1, row0, n_rows, nc_out};
+  fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), stv);
 }
 
 struct BinArgs {
@@ -346,15 +366,50 @@ __device__ __forceinline__ void kahan_add(float2 *addr, float x) {
   } while (old != assumed);
 }
 
-// Column stage: NB columns of one slice; transform along z, |.|^2, bin.
+// Column stage: NB columns of one slice, transformed along z.  The forward
+// FFT's first pass reads F1 columns (sequence index fastest across threads,
+// so a warp reads whole 32-byte sectors), and the inverse FFT's last pass
+// squares B * result and bins it into the float64 sum grid.
+struct ColLoad {
+  const float2 *src, *A;
+  int L, nc, m0;
+  __device__ float2 operator()(int f, int n) const {
+    if (n >= L || m0 + f >= nc) return make_float2(0.f, 0.f);
+    return cmul(src[(size_t)n * nc + m0 + f], __ldg(A + n));
+  }
+};
+
+struct ColBin {
+  const BinArgs *bn;
+  const int *cofs;
+  const float2 *B;
+  float2 cbg;
+  int nr, nc, m0;
+  __device__ void operator()(int f, int mr, float2 v) const {
+    const int m = m0 + f;
+    if (mr >= nr || m >= nc) return;
+    const int co = cofs[m], ro = bn->rowofs[mr];
+    if (co < 0 || ro < 0) return;
+    float2 X = cmul(v, __ldg(B + mr));
+    if (bn->k0 + m == 0 && bn->kz0 + mr == 0) {
+      X.x += cbg.x * bn->dc_scale;
+      X.y += cbg.y * bn->dc_scale;
+    }
+    const float I = X.x * X.x + X.y * X.y;
+    if (bn->kahan) kahan_add(bn->sumk + co + ro, I);
+    else atomicAdd(bn->sum + co + ro, (double)I);
+  }
+};
+
 template <int M>
 __global__ void __launch_bounds__(FftShape<M>::NT)
 k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
               const float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  constexpr int TWL = FftPlan<M>::tw_len();
   extern __shared__ float2 smem[];
-  float2 *buf = smem;
-  float2 *tw = smem + NB * M;
+  float2 *tw = smem;
+  float2 *buf = smem + TWL;
   const int slot = blockIdx.y, sl = slice0 + slot;
   const int p = sl % a.n_phi;
   const int m0 = blockIdx.x * NB;
@@ -364,39 +419,12 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
   for (int f = 0; f < NB; ++f)
     if (m0 + f < nc && cofs[m0 + f] >= 0) any = true;
   if (!any) return;
-  for (int t = threadIdx.x; t < M; t += NT) tw[t] = cz.tw[t];
-  const float2 *src = F1 + (size_t)slot * a.Lz * nc;
-  for (int idx = threadIdx.x; idx < NB * M; idx += NT) {
-    const int f = idx % NB, n = idx / NB;
-    float2 v = make_float2(0.f, 0.f);
-    if (n < cz.L && m0 + f < nc) v = cmul(src[(size_t)n * nc + m0 + f], cz.A[n]);
-    buf[f * M + n] = v;
-  }
+  for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   __syncthreads();
-  fft_block<M, NB, NT, false>(buf, tw);
-  for (int idx = threadIdx.x; idx < NB * M; idx += NT)
-    buf[idx] = cmul(buf[idx], cz.H[idx % M]);
-  __syncthreads();
-  fft_block<M, NB, NT, true>(buf, tw);
-  const SliceConst k = slice_const(a, sl);
-  const int nr = cz.N;
-  for (int idx = threadIdx.x; idx < NB * nr; idx += NT) {
-    const int f = idx / nr, mr = idx % nr;
-    const int m = m0 + f;
-    if (m >= nc) continue;
-    const int co = cofs[m], ro = bn.rowofs[mr];
-    if (co < 0 || ro < 0) continue;
-    float2 X = cmul(buf[f * M + mr], cz.B[mr]);
-    if (bn.k0 + m == 0 && bn.kz0 + mr == 0) {
-      X.x += k.cbg.x * bn.dc_scale;
-      X.y += k.cbg.y * bn.dc_scale;
-    }
-    const float I = X.x * X.x + X.y * X.y;
-    if (bn.kahan)
-      kahan_add(bn.sumk + co + ro, I);
-    else
-      atomicAdd(bn.sum + co + ro, (double)I);
-  }
+  ColLoad ld{F1 + (size_t)slot * a.Lz * nc, cz.A, cz.L, nc, m0};
+  fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
+  ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0};
+  fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), st);
 }
 
 // ---------------------------------------------------------- geometry tables
@@ -429,40 +457,49 @@ __global__ void k_col_tables(const gw_phi *ph, int g, int k0, int nc,
 
 // I = sum / count (0 where count == 0), crop, f0 factor (comparison.py:765-786,
 // voxelgrids.py:16-48, :828-857).  Output in crop coordinates (qy,qx,qz).
+// One block row per (qy, qx) line; threads run along qz, the contiguous
+// axis.  The count and the f0 factor are exact integers / float32 (the
+// factor's 1e-7 relative error is far inside the tolerance); the sum keeps
+// float64 and takes one float64 multiply.
 __global__ void k_finalize(const double *sum, const float2 *sumk, int kahan,
                            const unsigned int *C2, const int *C1, int W,
-                           int off, int Qc, double n_struct_div,
+                           int off, int Qc, float inv_nstruct,
                            const float *f0tab, int use_f0, float f0_c,
                            float f0_invz, double *out64, float *out32) {
-  const int64_t total = (int64_t)Qc * Qc * Qc;
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < total;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    const int iz = (int)(v % Qc);
-    const int ix = (int)((v / Qc) % Qc);
-    const int iy = (int)(v / ((int64_t)Qc * Qc));
-    const int wy = iy + off, wx = ix + off, wz = iz + off;
-    const size_t w = ((size_t)wy * W + wx) * W + wz;
-    const double cnt = (double)C2[(size_t)wy * W + wx] * (double)C1[wz];
+  const int line = blockIdx.x;  // iy * Qc + ix
+  const int iy = line / Qc, ix = line - iy * Qc;
+  const int wy = iy + off, wx = ix + off;
+  const unsigned c2 = C2[(size_t)wy * W + wx];
+  const size_t wbase = ((size_t)wy * W + wx) * W + off;
+  const size_t obase = (size_t)line * Qc;
+  float fxy[4];
+  if (use_f0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float *t = f0tab + i * 3 * Qc;
+      fxy[i] = t[ix] * t[Qc + iy];
+    }
+  }
+  for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
+    const unsigned cnt = c2 * (unsigned)C1[iz + off];
     double s;
     if (kahan) {
-      const float2 sc = sumk[w];
+      const float2 sc = sumk[wbase + iz];
       s = (double)sc.x - (double)sc.y;
     } else {
-      s = sum[w];
+      s = sum[wbase + iz];
     }
-    double I = cnt != 0.0 ? s / (cnt * n_struct_div) : 0.0;
+    float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
     if (use_f0) {
       float acc = f0_c;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const float *t = f0tab + i * 3 * Qc;
-        acc += t[ix] * t[Qc + iy] * t[2 * Qc + iz];
-      }
+      for (int i = 0; i < 4; ++i) acc += fxy[i] * f0tab[(i * 3 + 2) * Qc + iz];
       const float fq = acc * f0_invz;
-      I *= (double)(fq * fq);
+      scale *= fq * fq;
     }
-    out64[v] = I;
-    out32[v] = (float)I;
+    const double I = s * (double)scale;
+    out64[obase + iz] = I;
+    out32[obase + iz] = (float)I;
   }
 }
 
@@ -525,11 +562,34 @@ struct CztTables {
   std::vector<float2> A, H, B, tw;
 };
 
+// Per-pass twiddle tables of gw_fft.cuh's plan for length M: for every pass
+// with stride Ns > 1 and radix R, tw[k*(R-1) + r-1] = exp(-2 pi i r k/(Ns R)).
+std::vector<float2> fft_twiddles(int M) {
+  int l2 = 0;
+  while ((1 << l2) < M) ++l2;
+  const int n16 = l2 / 4, rlast = 1 << (l2 - 4 * n16);
+  std::vector<float2> tw;
+  auto add = [&](int ns, int R) {
+    const long long span = (long long)ns * R;
+    for (int k = 0; k < ns; ++k)
+      for (int r = 1; r < R; ++r) {
+        const long long e = ((long long)r * k) % span;
+        const double ang = -2.0 * M_PI * (double)e / (double)span;
+        tw.push_back(make_float2((float)std::cos(ang), (float)std::sin(ang)));
+      }
+  };
+  int ns = 16;
+  for (int p = 1; p < n16; ++p) { add(ns, 16); ns *= 16; }
+  if (rlast > 1) add(ns, rlast);
+  if (tw.empty()) tw.push_back(make_float2(1.f, 0.f));
+  return tw;
+}
+
 // X[k0+m] = sum_{n<L} x[lo+n] W^{(lo+n)(k0+m)}, W = exp(-2 pi i/g), via
 // B[m] * conv(x*A, h)[m], h[j] = W^{-j^2/2}, j in [-(L-1), N-1].
 CztTables make_czt(int g, int lo, int L, int k0, int N, int M) {
   CztTables t;
-  t.A.resize(L); t.B.resize(N); t.H.resize(M); t.tw.resize(M);
+  t.A.resize(L); t.B.resize(N); t.H.resize(M);
   for (int n = 0; n < L; ++n) {
     const cd w = chirp(2LL * n * k0 + 1LL * n * n, g);  // W^{n k0 + n^2/2}
     t.A[n] = make_float2((float)w.real(), (float)w.imag());
@@ -548,10 +608,7 @@ CztTables make_czt(int g, int lo, int L, int k0, int N, int M) {
     const cd v = h[i] / (double)M;
     t.H[i] = make_float2((float)v.real(), (float)v.imag());
   }
-  for (int i = 0; i < M; ++i) {
-    const double ang = -2.0 * M_PI * (double)i / (double)M;
-    t.tw[i] = make_float2((float)std::cos(ang), (float)std::sin(ang));
-  }
+  t.tw = fft_twiddles(M);
   return t;
 }
 
@@ -617,6 +674,7 @@ struct gw_voxel_plan {
   float *d_iq32 = nullptr;
   float2 *d_box = nullptr, *d_F1 = nullptr, *d_amo = nullptr;
   float *d_my = nullptr, *d_mz = nullptr;
+  float4 *d_sconst = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int64_t graph_kernels = 0;
@@ -634,7 +692,7 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
   a.ext = P->d_ext; a.box = P->d_box; a.amo = P->d_amo; a.my = P->d_my;
-  a.mz = P->d_mz; a.gw = P->d_gw; a.err = P->ctx->d_err;
+  a.mz = P->d_mz; a.gw = P->d_gw; a.sconst = P->d_sconst; a.err = P->ctx->d_err;
   return a;
 }
 
@@ -642,7 +700,7 @@ template <int M>
 int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                int slice0, int n_rows) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
-  const size_t smem = (size_t)(NB * M + M) * sizeof(float2);
+  const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
   static bool attr = false;
   if (!attr) {
     GW_CUDA(cudaFuncSetAttribute(k_row_czt<M>,
@@ -662,7 +720,7 @@ template <int M>
 int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                const BinArgs &bn, int slice0, int n_sl) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
-  const size_t smem = (size_t)(NB * M + M) * sizeof(float2);
+  const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
   static bool attr = false;
   if (!attr) {
     GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M>,
@@ -764,17 +822,17 @@ int enqueue(gw_voxel_plan *P) {
     GW_TRY(row_dispatch(P, a, cy, s0, n * P->Lz));
     GW_TRY(col_dispatch(P, a, cz, bn, s0, n));
   }
-  const int fin_blocks = std::max(1, std::min(
-      (int)(((int64_t)P->Qc * P->Qc * P->Qc + 255) / 256), 8 * ctx->sm_count));
+  const int fin_blocks = P->Qc * P->Qc;
   const float f0c = (float)P->p.f0_coef[8];
   const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
   {
     gw::KTimer tm(ctx, GW_K_FINALIZE);
-    k_finalize<<<fin_blocks, 256, 0, st>>>(
+    const int fin_threads = P->Qc >= 256 ? 256 : ((P->Qc + 31) / 32) * 32;
+    k_finalize<<<fin_blocks, fin_threads, 0, st>>>(
         P->d_sum, P->d_sumk, P->p.accum == GW_ACCUM_KAHAN32, P->d_C2, P->d_C1,
         P->W, P->lo - P->wlo, P->Qc,
-        P->p.average ? (double)P->n_struct : 1.0, P->d_f0, P->p.f0_z > 0, f0c,
-        f0iz, P->d_iq64, P->d_iq32);
+        P->p.average ? 1.0f / (float)P->n_struct : 1.0f, P->d_f0,
+        P->p.f0_z > 0, f0c, f0iz, P->d_iq64, P->d_iq32);
     GW_LAUNCHED(ctx);
   }
   return GW_OK;
@@ -963,6 +1021,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_zmin, n_struct, &B)) ||
       (st = alloc(&P->d_ymin, P->n_slices, &B)) ||
       (st = alloc(&P->d_ext, P->n_slices, &B)) ||
+      (st = alloc(&P->d_sconst, P->n_slices, &B)) ||
       (st = alloc(&P->d_colofs, (size_t)n_phi * P->Nc, &B)) ||
       (st = alloc(&P->d_C2, (size_t)P->W * P->W, &B)) ||
       (st = (p->accum == GW_ACCUM_KAHAN32 ? alloc(&P->d_sumk, W3, &B)
@@ -989,7 +1048,8 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_Hy, P->d_By, P->d_twy, P->d_Az, P->d_Hz, P->d_Bz,
                   P->d_twz, P->d_gw, P->d_colofs, P->d_rowofs, P->d_C1,
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
-                  P->d_iq32, P->d_box, P->d_F1, P->d_amo, P->d_my, P->d_mz};
+                  P->d_iq32, P->d_box, P->d_F1, P->d_amo, P->d_my, P->d_mz,
+                  P->d_sconst};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;

@@ -10,6 +10,8 @@ Keyword-only extensions (all default to the reference's behaviour):
   phis=            explicit rotation list instead of the automatic count
   mode=            'batched' (default) or 'plain' (per-rotation, full grid)
   accum=           'fp64' (default) or 'kahan32' accumulation
+  exact=           detector: replay the float64 index chain for every sample
+                   instead of only the samples the float32 path cannot decide
   weights=         per-atom occupancy multiplying the scattering factor
   ctx=             a giwaxsim_gb300._native.Context
 """
@@ -78,7 +80,8 @@ def _weights(path, angles):
 def detectormaker_fitting(iq, qx, qy, qz, num_pixels, max_q, angle_init_vals,
                           angle_init_axs, psis, psi_weights_path, phis,
                           phi_weights_path, thetas, theta_weights_path,
-                          mirror=True, *, accum="fp64", ctx=None):
+                          mirror=True, *, accum="fp64", exact=False,
+                          ctx=None):
     """Detector image summed over psi x phi x theta orientations; returns
     (det_sum (num_pixels, num_pixels), det_h, det_v) like the reference."""
     psis, phis, thetas = (np.atleast_1d(np.asarray(a)) for a in (psis, phis, thetas))
@@ -95,7 +98,7 @@ def detectormaker_fitting(iq, qx, qy, qz, num_pixels, max_q, angle_init_vals,
     plan = DetectorPlan(iq.shape, qx, qy, qz, num_pixels, max_q,
                         angle_init_vals, angle_init_axs, psis, psi_w, phis,
                         phi_w, thetas, theta_w, mirror=mirror, accum=accum,
-                        ctx=ctx)
+                        exact=exact, ctx=ctx)
     try:
         plan.set_iq(iq)
         plan.execute()

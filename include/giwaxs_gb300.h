@@ -173,7 +173,10 @@ typedef struct gw_detector_params {
   double dq;                /* np.diff(qz)[0]           detector.py:213   */
   int32_t mirror;           /* mirror_vertical_horizontal  comparison.py:857 */
   int32_t accum;            /* GW_ACCUM_FP64 | GW_ACCUM_KAHAN32           */
-  int32_t reserved[6];
+  int32_t exact;            /* 1: replay the float64 chain for every sample;
+                               0: float32 fast path with exact replay of the
+                               samples whose voxel it cannot decide        */
+  int32_t reserved[5];
 } gw_detector_params;
 
 typedef struct gw_detector_plan gw_detector_plan;

@@ -51,13 +51,19 @@ def test_detector_vs_oracle(case):
     assert rel_l2(got, ref) <= RTOL
 
 
-def test_gather_indices_bit_exact():
-    init, axs, psis, phis, thetas, mirror, npx = CASES[2]
+@pytest.mark.parametrize("exact", [False, True])
+@pytest.mark.parametrize("case", [0, 1, 2, 3])
+def test_gather_indices_bit_exact(case, exact):
+    """The voxel each pixel gathers, per orientation, equals the oracle's
+    (the fast path's float32 decisions plus its exact replays, and the
+    all-exact path)."""
+    init, axs, psis, phis, thetas, mirror, npx = CASES[case]
     iq, q = synthetic_iq()
     psis, phis, thetas = map(np.asarray, (psis, phis, thetas))
     w = lambda a: np.ones_like(a) / len(a)
     plan = F.DetectorPlan(iq.shape, q, q, q, npx, 1.5, init, axs, psis,
-                          w(psis), phis, w(phis), thetas, w(thetas), mirror)
+                          w(psis), phis, w(phis), thetas, w(thetas), mirror,
+                          exact=exact)
     plan.set_iq(iq)
     x0, y0, z0, _, _ = O.init_detector(npx, 1.5, init, axs)
     o = 0
@@ -115,3 +121,32 @@ def test_weights_and_errors(tmp_path):
         comparison.detectormaker_fitting(
             iq, q, q, q, 20, 1.5, (0, 0, 0), ("None",) * 3, psis, str(wpath),
             np.array([0.0]), None, np.array([0.0]), None)
+
+
+@pytest.mark.parametrize("cap", [None, "7"])
+def test_fast_path_matches_exact_path(cap, monkeypatch):
+    """Fast image == all-exact image to rounding (different summation order);
+    cap=7 forces the worklist to overflow so the in-kernel exact branch runs."""
+    if cap:
+        monkeypatch.setenv("GW_DET_WORKLIST_CAP", cap)
+    iq, q = synthetic_iq(seed=5)
+    init, axs, psis, phis, thetas, mirror, npx = CASES[2]
+    args = (iq, q, q, q, 64, 1.5, init, axs, psis, None, np.asarray(phis),
+            None, np.asarray(thetas), None)
+    fast, _, _ = comparison.detectormaker_fitting(*args, mirror=mirror)
+    exact, _, _ = comparison.detectormaker_fitting(*args, mirror=mirror,
+                                                   exact=True)
+    ref, _, _ = O.detector(*args, mirror=mirror)
+    assert rel_l2(fast, exact) <= 1e-6
+    assert rel_l2(fast, ref) <= RTOL
+
+
+def test_large_detector_vs_oracle():
+    """500 px, 91 orientations on a 203^3 grid (graphite-50A detector sizes)."""
+    iq, q = synthetic_iq(n=203, qmax=3.03, seed=7)
+    psis = np.linspace(0, 180, 91)
+    args = (iq, q, q, q, 500, 3.0, (0, 0, 0), ("None",) * 3, psis, None,
+            np.array([0.0]), None, np.array([0.0]), None)
+    got, _, _ = comparison.detectormaker_fitting(*args, mirror=True)
+    ref, _, _ = O.detector(*args, mirror=True)
+    assert rel_l2(got, ref) <= RTOL

@@ -172,3 +172,26 @@ def test_graph_replay_matches_eager():
     for _ in range(2):
         plan.execute()
         assert rel_l2(plan.iq(), eager) <= 1e-12
+
+
+@pytest.mark.parametrize("name,n_phi,expect_m", [("graphite-50A", 2, 2048),
+                                                 ("si-100A", 1, 4096),
+                                                 ("lamellar-200A", 1, 8192)])
+def test_plain_mode_large_transforms(name, n_phi, expect_m):
+    """Plain (full-grid) mode at full workload grid sizes: 2048-, 4096- and
+    8192-point transforms against the oracle's numpy fftn."""
+    structs = W.structures(name)
+    xyz, el, _ = structs[0]
+    w = W.WORKLOADS[name]
+    fv = F.element_f_values(el, w["energy"])
+    geom = F.VoxelGeometry(w["r"], w["dq"], w["max_q"])
+    phis = np.array([0.0, 61.0])[:n_phi]
+    ref = O.voxelgrid([(xyz, fv)], w["r"], w["dq"], w["max_q"], phis,
+                      w["fill_bkg"], w["smooth"])
+    got = gpu_run(geom, [(xyz, fv, None)], phis, w["fill_bkg"], w["smooth"],
+                  mode="plain")
+    assert got["info"]["My"] == expect_m
+    assert np.array_equal(got["counts"], ref["count"])
+    assert rel_l2(got["iq"], ref["iq"]) <= RTOL
+    bat = gpu_run(geom, [(xyz, fv, None)], phis, w["fill_bkg"], w["smooth"])
+    assert rel_l2(bat["iq"], ref["iq"]) <= RTOL
