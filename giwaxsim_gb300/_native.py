@@ -27,7 +27,8 @@ EXPORTS = [
     "gw_voxel_plan_create", "gw_voxel_plan_destroy", "gw_voxel_set_atoms",
     "gw_voxel_execute", "gw_voxel_capture_graph", "gw_voxel_get_iq",
     "gw_voxel_device_iq32", "gw_voxel_get_counts", "gw_voxel_get_sums",
-    "gw_voxel_info", "gw_voxel_debug_deposit", "gw_voxelgrid",
+    "gw_voxel_info", "gw_voxel_debug_deposit", "gw_voxel_debug_window",
+    "gw_voxelgrid",
     "gw_detector_plan_create", "gw_detector_plan_destroy",
     "gw_detector_set_iq", "gw_detector_set_iq32_device",
     "gw_detector_execute", "gw_detector_get", "gw_detector_debug_indices",
@@ -120,6 +121,7 @@ def _declare(lib):
         "gw_voxel_get_sums": ([P, P], ctypes.c_int),
         "gw_voxel_info": ([P, P, i32], ctypes.c_int),
         "gw_voxel_debug_deposit": ([P, i32, P, P], ctypes.c_int),
+        "gw_voxel_debug_window": ([P, i32, P], ctypes.c_int),
         "gw_voxelgrid": ([P, P, P, i32, P, i32, P, P, i64, P], ctypes.c_int),
         "gw_detector_plan_create": ([P, P, P, P, P, i32, P, P, P, i32, pp],
                                     ctypes.c_int),

@@ -195,7 +195,8 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
       dft<R, INV>(v[e]);
     }
   }
-  if (SRC == 0 && DST == 0) __syncthreads();
+  // a first pass may read inputs that alias its shared destination
+  if (DST == 0) __syncthreads();
 #pragma unroll
   for (int e = 0; e < PER; ++e) {
     const int b = threadIdx.x + e * NT;

@@ -47,15 +47,19 @@ struct SliceArgs {
   int radius;
   int plain;
   // arrays
-  const double *xyz;
+  const double *xyz;   // atoms in input order
   const float2 *f;
   const int *zidx;
+  const double *xyz_s; // atoms sorted by z index within each structure
+  const float2 *f_s;
+  const int *rowstart; // per structure: g+2 offsets into the sorted arrays
+  const int2 *zstat;   // per structure: (max valid z index, all z valid)
   const gw_structure *st;
   const gw_phi *ph;
   const double *clbase;  // per slice
-  unsigned long long *ymin_ord;
+  unsigned long long *ymin_ord, *ymax_ord;
+  int *extflag;          // per slice: 1 = extents need the exact pass
   int4 *ext;  // y_min, y_max, z_min, z_max (valid atoms)
-  float2 *box;
   float2 *amo;
   float *my, *mz;
   const float *gw;  // gaussian weights, 2*radius+1
@@ -80,17 +84,96 @@ __global__ void k_zmin(const double *xyz, const gw_structure *st,
 }
 
 // z index is phi independent: rotation about z leaves z unchanged
-// (fma(z,1,fma(y,0,x*0)) == z), utilities.py:303-317.
-__global__ void k_zidx(const double *xyz, const gw_structure *st,
-                       const unsigned long long *zmin_ord, double r,
-                       double inv_r, int *zidx) {
+// (fma(z,1,fma(y,0,x*0)) == z), utilities.py:303-317.  Atoms are counted per
+// z row (bin g collects z >= g, dropped by every slice's valid mask).
+__global__ void k_zidx_hist(const double *xyz, const gw_structure *st,
+                            const unsigned long long *zmin_ord, double r,
+                            double inv_r, int g, int *zidx, int *hist) {
   const gw_structure s = st[blockIdx.y];
   const double zmin = ord_dbl(zmin_ord[blockIdx.y]);
+  int *h = hist + (size_t)blockIdx.y * (g + 1);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
        i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t a = s.atom_begin + i;
-    double z = GW_DSUB(xyz[3 * a + 2], zmin);
-    zidx[a] = (int)floor_div_exact(z, r, inv_r);
+    const double z = GW_DSUB(xyz[3 * a + 2], zmin);
+    const int zi = (int)floor_div_exact(z, r, inv_r);
+    zidx[a] = zi;
+    atomicAdd(h + (zi >= 0 && zi < g ? zi : g), 1);
+  }
+}
+
+// Per structure: exclusive scan of the row histogram into absolute offsets
+// rowstart[0..g+1], scatter cursors, and (largest occupied row, all valid).
+__global__ void __launch_bounds__(1024)
+k_zscan(const gw_structure *st, int g, const int *hist, int *rowstart,
+        int *cursor, int2 *zstat) {
+  __shared__ int warp_sum[32];
+  const int t = blockIdx.x;
+  const int *h = hist + (size_t)t * (g + 1);
+  int *rs = rowstart + (size_t)t * (g + 2);
+  int *cur = cursor + (size_t)t * (g + 1);
+  const int nb = g + 1;
+  const int per = (nb + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per;
+  int local = 0, zmax = -1;
+  for (int k = 0; k < per; ++k) {
+    const int b = b0 + k;
+    if (b < nb) {
+      local += h[b];
+      if (b < g && h[b] > 0) zmax = b;
+    }
+  }
+  // block exclusive scan of `local`
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = local;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) warp_sum[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int ws = lane < (int)(blockDim.x >> 5) ? warp_sum[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += v;
+    }
+    warp_sum[lane] = ws;
+  }
+  __syncthreads();
+  int run = (int)st[t].atom_begin + (wid ? warp_sum[wid - 1] : 0) + incl - local;
+  for (int k = 0; k < per; ++k) {
+    const int b = b0 + k;
+    if (b < nb) {
+      rs[b] = run;
+      cur[b] = run;
+      run += h[b];
+    }
+  }
+  if (threadIdx.x == blockDim.x - 1) rs[nb] = (int)(st[t].atom_begin + st[t].atom_count);
+  zmax = __reduce_max_sync(0xffffffffu, zmax);
+  __shared__ int zm;
+  if (threadIdx.x == 0) zm = -1;
+  __syncthreads();
+  if (lane == 0) atomicMax(&zm, zmax);
+  __syncthreads();
+  if (threadIdx.x == 0) zstat[t] = make_int2(zm, h[g] == 0);
+}
+
+__global__ void k_zscatter(const double *xyz, const float2 *f,
+                           const gw_structure *st, const int *zidx, int g,
+                           int *cursor, double *xyz_s, float2 *f_s) {
+  const gw_structure s = st[blockIdx.y];
+  int *cur = cursor + (size_t)blockIdx.y * (g + 1);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = s.atom_begin + i;
+    const int zi = zidx[a];
+    const int pos = atomicAdd(cur + (zi >= 0 && zi < g ? zi : g), 1);
+    xyz_s[3 * (size_t)pos] = xyz[3 * a];
+    xyz_s[3 * (size_t)pos + 1] = xyz[3 * a + 1];
+    xyz_s[3 * (size_t)pos + 2] = xyz[3 * a + 2];
+    f_s[pos] = f[a];
   }
 }
 
@@ -100,7 +183,9 @@ __device__ __forceinline__ double rot_y(const double *p, double c, double s) {
   return GW_DFMA(p[1], c, GW_DMUL(p[0], s));
 }
 
-__global__ void k_ymin(SliceArgs a, int slice0) {
+// Per slice: min and max of the rotated y over all atoms (the shift to the
+// minimum, voxelgrids.py:323), and the slice's background constants.
+__global__ void k_yminmax(SliceArgs a, int slice0) {
   const int sl = slice0 + blockIdx.y;
   const int t = sl / a.n_phi, p = sl % a.n_phi;
   const gw_structure s = a.st[t];
@@ -115,25 +200,51 @@ __global__ void k_ymin(SliceArgs a, int slice0) {
                       : make_float4(0.f, 0.f, c.x, c.y);
   }
   const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
-  unsigned long long best = ~0ULL;
+  unsigned long long lo = ~0ULL, hi = 0ULL;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
        i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
-    best = min(best, dbl_ord(rot_y(a.xyz + 3 * (s.atom_begin + i), c, sn)));
+    const unsigned long long v = dbl_ord(rot_y(a.xyz_s + 3 * (s.atom_begin + i), c, sn));
+    lo = min(lo, v);
+    hi = max(hi, v);
   }
-  for (int o = 16; o > 0; o >>= 1)
-    best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-  if ((threadIdx.x & 31) == 0 && best != ~0ULL)
-    atomicMin(a.ymin_ord + sl, best);
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0 && lo != ~0ULL) {
+    atomicMin(a.ymin_ord + sl, lo);
+    atomicMax(a.ymax_ord + sl, hi);
+  }
 }
 
-// voxelgrids.py:321-341: shift, floor-divide, valid mask, np.add.at deposit.
-__global__ void k_deposit(SliceArgs a, int slice0) {
+// Per slice extents of the valid atoms (voxelgrids.py:346-349).  y indices
+// grow with y (the floor division is monotone), so when every atom is valid
+// the extents are (0, index of max y, 0, largest occupied z row); otherwise
+// k_ext_exact computes them atom by atom.
+__global__ void k_ext(SliceArgs a, int slice0, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sl = slice0 + i;
+  const int t = sl / a.n_phi;
+  const double ymin = ord_dbl(a.ymin_ord[sl]), ymax = ord_dbl(a.ymax_ord[sl]);
+  const double Y = floor_div_exact(GW_DSUB(ymax, ymin), a.r, a.inv_r);
+  const int2 zs = a.zstat[t];
+  if (Y < (double)a.g && zs.y) {
+    a.ext[sl] = make_int4(0, (int)Y, 0, zs.x);
+    a.extflag[sl] = 0;
+  } else {
+    a.ext[sl] = make_int4(INT_MAX, -1, INT_MAX, -1);
+    a.extflag[sl] = 1;
+  }
+}
+
+__global__ void k_ext_exact(SliceArgs a, int slice0) {
   const int sl = slice0 + blockIdx.y;
+  if (!a.extflag[sl]) return;
   const int t = sl / a.n_phi, p = sl % a.n_phi;
   const gw_structure s = a.st[t];
   const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
   const double ymin = ord_dbl(a.ymin_ord[sl]);
-  float2 *box = a.box + (size_t)blockIdx.y * a.Lz * a.Ly;
   int ymn = INT_MAX, ymx = -1, zmn = INT_MAX, zmx = -1;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
        i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
@@ -144,16 +255,6 @@ __global__ void k_deposit(SliceArgs a, int slice0) {
     if (yi >= 0 && yi < a.g && zi >= 0 && zi < a.g) {
       ymn = min(ymn, yi); ymx = max(ymx, yi);
       zmn = min(zmn, zi); zmx = max(zmx, zi);
-      int yy = yi - a.y_lo; if (yy >= a.g) yy -= a.g;
-      int zz = zi - a.z_lo; if (zz >= a.g) zz -= a.g;
-      if (yy < a.Ly && zz < a.Lz) {
-        float2 *dst = box + (size_t)zz * a.Ly + yy;
-        const float2 fv = a.f[at];
-        atomicAdd(&dst->x, fv.x);
-        atomicAdd(&dst->y, fv.y);
-      } else {
-        dev_error(a.err, GW_DEVERR_BOX);
-      }
     }
   }
   ymn = __reduce_min_sync(0xffffffffu, ymn);
@@ -290,14 +391,41 @@ __device__ __forceinline__ SliceConst slice_const(const SliceArgs &a, int sl) {
 }
 
 // Row stage: NB rows (slice, z) per block, transformed along y; Nc outputs
-// kept.  The forward FFT's first pass reads the deposit box directly (with
-// the fill/smoothing transform and the chirp A), the inverse FFT's first
-// pass multiplies by the filter spectrum H, and its last pass writes
-// F1 = B * result straight to global memory.
+// kept.  The block first deposits the atoms of its rows (contiguous in the
+// z-sorted arrays) into shared-memory row buffers with shared atomics
+// (voxelgrids.py:328-341: shift, floor division, valid mask, np.add.at).
+// The forward FFT's first pass reads those rows with the fill/smoothing
+// transform and the chirp A; the inverse FFT's first pass multiplies by the
+// filter spectrum H, and its last pass writes F1 = B * result to global
+// memory.  The row buffers share storage with the FFT buffer: the first pass
+// reads all its inputs before it writes.
+// Window column of sorted atom `at` in slice `sl`: false when the valid mask
+// drops it (y index outside [0, g)); yy >= Ly flags a window overflow.
+__device__ __forceinline__ bool deposit_column(const SliceArgs &a, int at,
+                                               int sl, int &yy) {
+  const int p = sl % a.n_phi;
+  const double ymin = ord_dbl(a.ymin_ord[sl]);
+  const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, a.ph[p].cos_phi,
+                                 a.ph[p].sin_phi), ymin);
+  const int yi = (int)floor_div_exact(y, a.r, a.inv_r);
+  if (yi < 0 || yi >= a.g) return false;
+  yy = yi - a.y_lo;
+  if (yy >= a.g) yy -= a.g;
+  return true;
+}
+
+__device__ __forceinline__ int window_row_to_z(const SliceArgs &a, int zz) {
+  int zi = a.z_lo + zz;
+  if (zi < 0) zi += a.g;
+  if (zi >= a.g) zi -= a.g;
+  return zi;
+}
+
 template <int M>
 struct RowLoad {
   const SliceArgs *a;
   const CztArgs *cz;
+  const float2 *rows;  // row f at rows + f * LDM
   int slice0, row0, n_rows;
   __device__ float2 operator()(int f, int n) const {
     const int row = row0 + f;
@@ -305,7 +433,7 @@ struct RowLoad {
     const int slot = row / a->Lz, zz = row % a->Lz;
     const int sl = slice0 + slot;
     const SliceConst k = slice_const(*a, sl);
-    const float2 dep = a->box[((size_t)slot * a->Lz + zz) * a->Ly + n];
+    const float2 dep = rows[f * FftPlan<M>::LDM + n];
     return cmul(d_value(*a, slot, sl, zz, n, dep, k.cd, k.cbg, a->ext[sl]),
                 __ldg(cz->A + n));
   }
@@ -327,13 +455,54 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
           float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   constexpr int TWL = FftPlan<M>::tw_len();
+  constexpr int LDM = FftPlan<M>::LDM;
   extern __shared__ float2 smem[];
   float2 *tw = smem;
   float2 *buf = smem + TWL;
+  __shared__ int r_lo[NB], r_cnt[NB + 1];
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
-  __syncthreads();
+  for (int t = threadIdx.x; t < NB * LDM; t += NT) buf[t] = make_float2(0.f, 0.f);
   const int row0 = blockIdx.x * NB;
-  RowLoad<M> ld{&a, &cz, slice0, row0, n_rows};
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int f = 0; f < NB; ++f) {
+      const int row = row0 + f;
+      int lo = 0, cnt = 0;
+      if (row < n_rows) {
+        const int slot = row / a.Lz, zz = row % a.Lz;
+        const int sl = slice0 + slot, t = sl / a.n_phi;
+        if (a.ext[sl].y < 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
+        const int zi = window_row_to_z(a, zz);
+        const int *rs = a.rowstart + (size_t)t * (a.g + 2);
+        lo = rs[zi];
+        cnt = rs[zi + 1] - lo;
+      }
+      r_lo[f] = lo;
+      r_cnt[f] = acc;
+      acc += cnt;
+    }
+    r_cnt[NB] = acc;
+  }
+  __syncthreads();
+  const int total = r_cnt[NB];
+  for (int i = threadIdx.x; i < total; i += NT) {
+    int f = 0;
+    while (f + 1 < NB && i >= r_cnt[f + 1]) ++f;
+    const int at = r_lo[f] + (i - r_cnt[f]);
+    const int sl = slice0 + (row0 + f) / a.Lz;
+    int yy;
+    if (deposit_column(a, at, sl, yy)) {
+      if (yy < a.Ly) {
+        const float2 fv = a.f_s[at];
+        atomicAdd(&buf[f * LDM + yy].x, fv.x);
+        atomicAdd(&buf[f * LDM + yy].y, fv.y);
+      } else {
+        dev_error(a.err, GW_DEVERR_BOX);
+      }
+    }
+  }
+  __syncthreads();
+  RowLoad<M> ld{&a, &cz, buf, slice0, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false>(buf, tw, nullptr, ld, NoStore());
   RowStore stv{cz.B, F1, row0, n_rows, nc_out};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), stv);
@@ -500,6 +669,23 @@ __global__ void k_finalize(const double *sum, const float2 *sumk, int kahan,
     const double I = s * (double)scale;
     out64[obase + iz] = I;
     out32[obase + iz] = (float)I;
+  }
+}
+
+// The deposited window of one slice (row zz, column yy) through the same
+// sorted arrays and index code the row kernel uses.
+__global__ void k_debug_window(SliceArgs a, int sl, float2 *win) {
+  const int t = sl / a.n_phi;
+  const int *rs = a.rowstart + (size_t)t * (a.g + 2);
+  for (int zz = blockIdx.x; zz < a.Lz; zz += gridDim.x) {
+    const int zi = window_row_to_z(a, zz);
+    for (int at = rs[zi] + threadIdx.x; at < rs[zi + 1]; at += blockDim.x) {
+      int yy;
+      if (deposit_column(a, at, sl, yy) && yy < a.Ly) {
+        atomicAdd(&win[(size_t)zz * a.Ly + yy].x, a.f_s[at].x);
+        atomicAdd(&win[(size_t)zz * a.Ly + yy].y, a.f_s[at].y);
+      }
+    }
   }
 }
 
@@ -672,7 +858,13 @@ struct gw_voxel_plan {
   float *d_f0 = nullptr;
   double *d_iq64 = nullptr;
   float *d_iq32 = nullptr;
-  float2 *d_box = nullptr, *d_F1 = nullptr, *d_amo = nullptr;
+  float2 *d_F1 = nullptr, *d_amo = nullptr;
+  double *d_xyz_s = nullptr;
+  float2 *d_f_s = nullptr;
+  int *d_zhist = nullptr, *d_rowstart = nullptr, *d_cursor = nullptr;
+  int2 *d_zstat = nullptr;
+  unsigned long long *d_ymax = nullptr;
+  int *d_extflag = nullptr;
   float *d_my = nullptr, *d_mz = nullptr;
   float4 *d_sconst = nullptr;
   cudaGraph_t graph = nullptr;
@@ -690,8 +882,10 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.fill = P->p.fill_bkg != 0; a.smooth_on = P->p.smooth != 0.0;
   a.sigma = (float)P->p.smooth; a.radius = P->radius; a.plain = P->plain;
   a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
+  a.xyz_s = P->d_xyz_s; a.f_s = P->d_f_s; a.rowstart = P->d_rowstart;
+  a.zstat = P->d_zstat; a.ymax_ord = P->d_ymax; a.extflag = P->d_extflag;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
-  a.ext = P->d_ext; a.box = P->d_box; a.amo = P->d_amo; a.my = P->d_my;
+  a.ext = P->d_ext; a.amo = P->d_amo; a.my = P->d_my;
   a.mz = P->d_mz; a.gw = P->d_gw; a.sconst = P->d_sconst; a.err = P->ctx->d_err;
   return a;
 }
@@ -770,6 +964,8 @@ int enqueue(gw_voxel_plan *P) {
   GW_CUDA(cudaMemsetAsync(P->d_C2, 0, (size_t)P->W * P->W * sizeof(unsigned), st));
   GW_CUDA(cudaMemsetAsync(P->d_zmin, 0xff, P->n_struct * sizeof(unsigned long long), st));
   GW_CUDA(cudaMemsetAsync(P->d_ymin, 0xff, P->n_slices * sizeof(unsigned long long), st));
+  GW_CUDA(cudaMemsetAsync(P->d_ymax, 0, P->n_slices * sizeof(unsigned long long), st));
+  GW_CUDA(cudaMemsetAsync(P->d_zhist, 0, (size_t)P->n_struct * (P->g + 1) * sizeof(int), st));
   int64_t max_atoms = 0;
   for (auto &s : P->structs) max_atoms = std::max(max_atoms, s.atom_count);
   const int nblk_at = (int)std::min<int64_t>(
@@ -781,8 +977,22 @@ int enqueue(gw_voxel_plan *P) {
   }
   {
     gw::KTimer tm(ctx, GW_K_PREP);
-    k_zidx<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(P->d_xyz, P->d_structs, P->d_zmin,
-                                                     P->r, P->inv_r, P->d_zidx);
+    k_zidx_hist<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(
+        P->d_xyz, P->d_structs, P->d_zmin, P->r, P->inv_r, P->g, P->d_zidx,
+        P->d_zhist);
+    GW_LAUNCHED(ctx);
+  }
+  {
+    gw::KTimer tm(ctx, GW_K_PREP);
+    k_zscan<<<P->n_struct, 1024, 0, st>>>(P->d_structs, P->g, P->d_zhist,
+                                          P->d_rowstart, P->d_cursor, P->d_zstat);
+    GW_LAUNCHED(ctx);
+  }
+  {
+    gw::KTimer tm(ctx, GW_K_PREP);
+    k_zscatter<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(
+        P->d_xyz, P->d_f, P->d_structs, P->d_zidx, P->g, P->d_cursor,
+        P->d_xyz_s, P->d_f_s);
     GW_LAUNCHED(ctx);
   }
   {
@@ -802,16 +1012,19 @@ int enqueue(gw_voxel_plan *P) {
              (float)((double)P->g * (double)P->g)};
   for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
     const int n = std::min(P->S, P->n_slices - s0);
-    GW_CUDA(cudaMemsetAsync(P->d_box, 0,
-                            (size_t)n * P->Lz * P->Ly * sizeof(float2), st));
     {
       gw::KTimer tm(ctx, GW_K_DEPOSIT);
-      k_ymin<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+      k_yminmax<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
       GW_LAUNCHED(ctx);
     }
     {
       gw::KTimer tm(ctx, GW_K_DEPOSIT);
-      k_deposit<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+      k_ext<<<(n + 127) / 128, 128, 0, st>>>(a, s0, n);
+      GW_LAUNCHED(ctx);
+    }
+    {
+      gw::KTimer tm(ctx, GW_K_DEPOSIT);
+      k_ext_exact<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
       GW_LAUNCHED(ctx);
     }
     if (a.fill || a.smooth_on) {
@@ -957,7 +1170,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
   }
   // batch size: keep the per-batch intermediates near L2 size
   {
-    const size_t per = (size_t)P->Lz * (P->Ly + P->Nc) * sizeof(float2) +
+    const size_t per = (size_t)P->Lz * P->Nc * sizeof(float2) +
                        (P->Ly + P->Lz) * 12;
     int S = p->batch_slices > 0 ? p->batch_slices
                                 : (int)std::max<size_t>(1, (96u << 20) / per);
@@ -1027,7 +1240,12 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = (p->accum == GW_ACCUM_KAHAN32 ? alloc(&P->d_sumk, W3, &B)
                                           : alloc(&P->d_sum, W3, &B))) ||
       (st = alloc(&P->d_iq64, Qc3, &B)) || (st = alloc(&P->d_iq32, Qc3, &B)) ||
-      (st = alloc(&P->d_box, (size_t)P->S * P->Lz * P->Ly, &B)) ||
+      (st = alloc(&P->d_ymax, P->n_slices, &B)) ||
+      (st = alloc(&P->d_extflag, P->n_slices, &B)) ||
+      (st = alloc(&P->d_zhist, (size_t)n_struct * (g + 1), &B)) ||
+      (st = alloc(&P->d_rowstart, (size_t)n_struct * (g + 2), &B)) ||
+      (st = alloc(&P->d_cursor, (size_t)n_struct * (g + 1), &B)) ||
+      (st = alloc(&P->d_zstat, n_struct, &B)) ||
       (st = alloc(&P->d_F1, (size_t)P->S * P->Lz * P->Nc, &B)) ||
       (st = alloc(&P->d_amo, (size_t)P->S * P->Ly, &B)) ||
       (st = alloc(&P->d_my, (size_t)P->S * P->Ly, &B)) ||
@@ -1048,8 +1266,9 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_Hy, P->d_By, P->d_twy, P->d_Az, P->d_Hz, P->d_Bz,
                   P->d_twz, P->d_gw, P->d_colofs, P->d_rowofs, P->d_C1,
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
-                  P->d_iq32, P->d_box, P->d_F1, P->d_amo, P->d_my, P->d_mz,
-                  P->d_sconst};
+                  P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
+                  P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_zhist, P->d_rowstart,
+                  P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -1063,11 +1282,17 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
     if (s.atom_begin < 0 || s.atom_count < 1 || s.atom_begin + s.atom_count > n)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: structure atom range outside the atom arrays");
   if (n != P->n_atoms) {
-    gw::dev_free(P->d_xyz); gw::dev_free(P->d_f); gw::dev_free(P->d_zidx);
+    void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_f_s};
+    for (void *q : old) gw::dev_free(q);
     P->d_xyz = nullptr; P->d_f = nullptr; P->d_zidx = nullptr;
+    P->d_xyz_s = nullptr; P->d_f_s = nullptr;
+    if (n > INT_MAX / 4)
+      return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: more than 2^29 atoms");
     GW_CUDA(gw::dev_malloc((void **)&P->d_xyz, (size_t)n * 3 * sizeof(double)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_f, (size_t)n * sizeof(float2)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_zidx, (size_t)n * sizeof(int)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_xyz_s, (size_t)n * 3 * sizeof(double)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_f_s, (size_t)n * sizeof(float2)));
     P->n_atoms = n;
     if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
     if (P->graph) { cudaGraphDestroy(P->graph); P->graph = nullptr; }
@@ -1222,4 +1447,26 @@ extern "C" int gw_voxelgrid(gw_ctx *ctx, const gw_voxel_params *p,
   if (st == GW_OK) st = gw_voxel_get_iq(P, iq_out, 0);
   gw_voxel_plan_destroy(P);
   return st;
+}
+
+extern "C" int gw_voxel_debug_window(gw_voxel_plan *P, int32_t slice,
+                                     float *window) {
+  if (!P || !window) return gw::fail(GW_ERR_ARG, "gw_voxel_debug_window: null argument");
+  if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_debug_window: plan not executed");
+  if (slice < 0 || slice >= P->n_slices) return gw::fail(GW_ERR_ARG, "gw_voxel_debug_window: slice out of range");
+  const size_t n = (size_t)P->Lz * P->Ly;
+  float2 *d = nullptr;
+  GW_CUDA(gw::dev_malloc((void **)&d, n * sizeof(float2)));
+  cudaError_t e = cudaMemsetAsync(d, 0, n * sizeof(float2), P->ctx->stream);
+  SliceArgs a = slice_args(P);
+  if (e == cudaSuccess) {
+    k_debug_window<<<256, 128, 0, P->ctx->stream>>>(a, slice, d);
+    P->ctx->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(window, d, n * sizeof(float2), cudaMemcpyDeviceToHost, P->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->ctx->stream);
+  gw::dev_free(d);
+  if (e != cudaSuccess) return gw::cuda_fail(e, "debug window", __FILE__, __LINE__);
+  return GW_OK;
 }

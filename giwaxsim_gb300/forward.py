@@ -229,6 +229,15 @@ class VoxelPlan:
                                                N.ptr(y), N.ptr(z)))
         return y, z
 
+    def debug_window(self, slice_index):
+        """Deposited (Lz, Ly) complex window of one slice and its origin
+        (z_lo, y_lo) in grid coordinates (cyclic)."""
+        info = self.info()
+        out = np.zeros((info["Lz"], info["Ly"]), dtype=np.complex64)
+        N.check(N.lib().gw_voxel_debug_window(self.handle, int(slice_index),
+                                              N.ptr(out.view(np.float32))))
+        return out, info["z_lo"], info["y_lo"]
+
     def close(self):
         if getattr(self, "handle", None):
             N.lib().gw_voxel_plan_destroy(self.handle)

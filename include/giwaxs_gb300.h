@@ -159,6 +159,10 @@ int gw_voxel_info(gw_voxel_plan *plan, int64_t *info, int32_t n);
  * (voxelgrids.py:328-335). */
 int gw_voxel_debug_deposit(gw_voxel_plan *plan, int32_t slice, int32_t *y_idx,
                            int32_t *z_idx);
+/* Parity hook: the deposited window of one slice before fill/smoothing,
+ * complex64 (Lz, Ly) (row z_lo+zz, column y_lo+yy of the grid, cyclic):
+ * np.add.at(grid[z, y], f) of voxelgrids.py:341 restricted to the window. */
+int gw_voxel_debug_window(gw_voxel_plan *plan, int32_t slice, float *window);
 /* One-shot: plan, upload, execute, download, destroy (host buffers). */
 int gw_voxelgrid(gw_ctx *ctx, const gw_voxel_params *p,
                  const gw_structure *structs, int32_t n_struct,
