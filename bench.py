@@ -302,10 +302,29 @@ def run_gb300(args, world, rank, local, pg):
                 weights=wt, ctx=ctx)
             t_e.append(time.perf_counter() - t0)
         te = float(np.mean(t_e[1:]))
+        # where the e2e time goes: the same call split into its phases
+        fv = F.element_f_values(el, w["energy"])
+        ph = {}
+        t0 = time.perf_counter()
+        pl = F.VoxelPlan(geom, [(xyz, fv, wt)], phis=phis,
+                         fill_bkg=w["fill_bkg"], smooth=w["smooth"], ctx=ctx)
+        ph["plan_s"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        pl.set_atoms()
+        pl.execute()
+        ctx.synchronize()
+        ph["upload_execute_s"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        out = np.empty((pl.Qc,) * 3)
+        ph["alloc_s"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        pl.iq(out)
+        ph["d2h_s"] = time.perf_counter() - t0
+        pl.close()
         e2e = {"value": world * n_slices / te, "unit": "slices/s",
                "h2d_bytes_per_step": int(xyz.size * 8 + len(xyz) * 8),
                "d2h_bytes_per_step": int(iq.size * 8),
-               "s_per_step": te}
+               "s_per_step": te, "phases": ph}
 
     # roofline of the dominant kernel
     peak, peak_kind = measured_peaks()

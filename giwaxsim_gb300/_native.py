@@ -32,7 +32,8 @@ EXPORTS = [
     "gw_detector_plan_create", "gw_detector_plan_destroy",
     "gw_detector_set_iq", "gw_detector_set_iq32_device",
     "gw_detector_execute", "gw_detector_get", "gw_detector_debug_indices",
-    "gw_detector_noalloc", "gw_detector",
+    "gw_detector_noalloc", "gw_detector", "gw_gather", "gw_bin_slice",
+    "gw_mirror", "gw_f0_scale", "gw_collapse_lengths",
 ]
 
 
@@ -134,12 +135,18 @@ def _declare(lib):
         "gw_detector_noalloc": ([P, P, P, P, P, i32, P, P, P, i32, P, P],
                                 ctypes.c_int),
         "gw_detector": ([P, P, P, P, P, P, i32, P, P, P, i32, P], ctypes.c_int),
+        "gw_gather": ([P, P, P, P, d, P, P, P, i64, P, i32, d, i32, P],
+                      ctypes.c_int),
+        "gw_bin_slice": ([P, P, i32, i32, P, P, P, i32, d, d, d, P, P],
+                         ctypes.c_int),
+        "gw_mirror": ([P, P, i32, i32, P], ctypes.c_int),
+        "gw_f0_scale": ([P, P, P, P, P, P, P, d, P], ctypes.c_int),
+        "gw_collapse_lengths": ([P, P, i64, d, d, P, P], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = res
-    del d
 
 
 def lib():

@@ -47,14 +47,17 @@ struct FftPlan {
 
 template <int M>
 struct FftShape;
-template <> struct FftShape<64>   { static constexpr int NB = 16, NT = 64; };
-template <> struct FftShape<128>  { static constexpr int NB = 16, NT = 128; };
-template <> struct FftShape<256>  { static constexpr int NB = 8,  NT = 128; };
-template <> struct FftShape<512>  { static constexpr int NB = 8,  NT = 256; };
-template <> struct FftShape<1024> { static constexpr int NB = 4,  NT = 256; };
-template <> struct FftShape<2048> { static constexpr int NB = 4,  NT = 512; };
-template <> struct FftShape<4096> { static constexpr int NB = 2,  NT = 512; };
-template <> struct FftShape<8192> { static constexpr int NB = 1,  NT = 512; };
+// MINB: blocks per SM the register budget is sized for (1024 threads per SM,
+// i.e. at most 64 registers per thread) so that latency is hidden by 32
+// resident warps.
+template <> struct FftShape<64>   { static constexpr int NB = 16, NT = 64,  MINB = 16; };
+template <> struct FftShape<128>  { static constexpr int NB = 16, NT = 128, MINB = 8; };
+template <> struct FftShape<256>  { static constexpr int NB = 8,  NT = 128, MINB = 8; };
+template <> struct FftShape<512>  { static constexpr int NB = 8,  NT = 256, MINB = 4; };
+template <> struct FftShape<1024> { static constexpr int NB = 4,  NT = 256, MINB = 4; };
+template <> struct FftShape<2048> { static constexpr int NB = 4,  NT = 512, MINB = 2; };
+template <> struct FftShape<4096> { static constexpr int NB = 2,  NT = 512, MINB = 2; };
+template <> struct FftShape<8192> { static constexpr int NB = 1,  NT = 512, MINB = 1; };
 
 template <bool INV>
 __device__ __forceinline__ float2 conj_if(float2 w) {

@@ -52,6 +52,7 @@ struct SliceArgs {
   const int *zidx;
   const double *xyz_s; // atoms sorted by z index within each structure
   const float2 *f_s;
+  const float2 *xy32_s; // float32 (x, y) of the sorted atoms
   const int *rowstart; // per structure: g+2 offsets into the sorted arrays
   const int2 *zstat;   // per structure: (max valid z index, all z valid)
   const gw_structure *st;
@@ -162,7 +163,8 @@ k_zscan(const gw_structure *st, int g, const int *hist, int *rowstart,
 
 __global__ void k_zscatter(const double *xyz, const float2 *f,
                            const gw_structure *st, const int *zidx, int g,
-                           int *cursor, double *xyz_s, float2 *f_s) {
+                           int *cursor, double *xyz_s, float2 *f_s,
+                           float2 *xy32_s) {
   const gw_structure s = st[blockIdx.y];
   int *cur = cursor + (size_t)blockIdx.y * (g + 1);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -174,6 +176,7 @@ __global__ void k_zscatter(const double *xyz, const float2 *f,
     xyz_s[3 * (size_t)pos + 1] = xyz[3 * a + 1];
     xyz_s[3 * (size_t)pos + 2] = xyz[3 * a + 2];
     f_s[pos] = f[a];
+    xy32_s[pos] = make_float2((float)xyz[3 * a], (float)xyz[3 * a + 1]);
   }
 }
 
@@ -401,13 +404,32 @@ __device__ __forceinline__ SliceConst slice_const(const SliceArgs &a, int sl) {
 // reads all its inputs before it writes.
 // Window column of sorted atom `at` in slice `sl`: false when the valid mask
 // drops it (y index outside [0, g)); yy >= Ly flags a window overflow.
+// The index is first estimated in float32: t = (x s + y c - ymin)/r with an
+// error below d = 10 u (|x s| + |y c| + |ymin|)/r + 1e-6 (u = 2^-24; the
+// input roundings, four arithmetic roundings and those of t -+ d total at
+// most 7 u times that sum).  Only when [t-d, t+d] contains an integer is the
+// exact float64 chain replayed.
 __device__ __forceinline__ bool deposit_column(const SliceArgs &a, int at,
                                                int sl, int &yy) {
   const int p = sl % a.n_phi;
+  const gw_phi &ph = a.ph[p];
   const double ymin = ord_dbl(a.ymin_ord[sl]);
-  const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, a.ph[p].cos_phi,
-                                 a.ph[p].sin_phi), ymin);
-  const int yi = (int)floor_div_exact(y, a.r, a.inv_r);
+  const float2 xy = a.xy32_s[at];
+  const float cs = (float)ph.cos_phi, sn = (float)ph.sin_phi;
+  const float ym = (float)ymin, ir = (float)a.inv_r;
+  const float t = (fmaf(xy.y, cs, xy.x * sn) - ym) * ir;
+  const float d = 10.f * 5.9604645e-8f *
+                      (fabsf(xy.x * sn) + fabsf(xy.y * cs) + fabsf(ym)) * ir +
+                  1e-6f;
+  const float klo = floorf(t - d), khi = floorf(t + d);
+  int yi;
+  if (klo == khi) {
+    yi = (int)klo;
+  } else {
+    const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, ph.cos_phi,
+                                   ph.sin_phi), ymin);
+    yi = (int)floor_div_exact(y, a.r, a.inv_r);
+  }
   if (yi < 0 || yi >= a.g) return false;
   yy = yi - a.y_lo;
   if (yy >= a.g) yy -= a.g;
@@ -450,7 +472,7 @@ struct RowStore {
 };
 
 template <int M>
-__global__ void __launch_bounds__(FftShape<M>::NT)
+__global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
 k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
           float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
@@ -571,7 +593,7 @@ struct ColBin {
 };
 
 template <int M>
-__global__ void __launch_bounds__(FftShape<M>::NT)
+__global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
 k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
               const float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
@@ -860,6 +882,7 @@ struct gw_voxel_plan {
   float *d_iq32 = nullptr;
   float2 *d_F1 = nullptr, *d_amo = nullptr;
   double *d_xyz_s = nullptr;
+  float2 *d_xy32_s = nullptr;
   float2 *d_f_s = nullptr;
   int *d_zhist = nullptr, *d_rowstart = nullptr, *d_cursor = nullptr;
   int2 *d_zstat = nullptr;
@@ -883,6 +906,7 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.sigma = (float)P->p.smooth; a.radius = P->radius; a.plain = P->plain;
   a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
   a.xyz_s = P->d_xyz_s; a.f_s = P->d_f_s; a.rowstart = P->d_rowstart;
+  a.xy32_s = P->d_xy32_s;
   a.zstat = P->d_zstat; a.ymax_ord = P->d_ymax; a.extflag = P->d_extflag;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
   a.ext = P->d_ext; a.amo = P->d_amo; a.my = P->d_my;
@@ -992,7 +1016,7 @@ int enqueue(gw_voxel_plan *P) {
     gw::KTimer tm(ctx, GW_K_PREP);
     k_zscatter<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(
         P->d_xyz, P->d_f, P->d_structs, P->d_zidx, P->g, P->d_cursor,
-        P->d_xyz_s, P->d_f_s);
+        P->d_xyz_s, P->d_f_s, P->d_xy32_s);
     GW_LAUNCHED(ctx);
   }
   {
@@ -1267,7 +1291,7 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_twz, P->d_gw, P->d_colofs, P->d_rowofs, P->d_C1,
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
                   P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
-                  P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_zhist, P->d_rowstart,
+                  P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
@@ -1282,16 +1306,17 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
     if (s.atom_begin < 0 || s.atom_count < 1 || s.atom_begin + s.atom_count > n)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: structure atom range outside the atom arrays");
   if (n != P->n_atoms) {
-    void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_f_s};
+    void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_f_s, P->d_xy32_s};
     for (void *q : old) gw::dev_free(q);
     P->d_xyz = nullptr; P->d_f = nullptr; P->d_zidx = nullptr;
-    P->d_xyz_s = nullptr; P->d_f_s = nullptr;
+    P->d_xyz_s = nullptr; P->d_f_s = nullptr; P->d_xy32_s = nullptr;
     if (n > INT_MAX / 4)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: more than 2^29 atoms");
     GW_CUDA(gw::dev_malloc((void **)&P->d_xyz, (size_t)n * 3 * sizeof(double)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_f, (size_t)n * sizeof(float2)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_zidx, (size_t)n * sizeof(int)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_xyz_s, (size_t)n * 3 * sizeof(double)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_xy32_s, (size_t)n * sizeof(float2)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_f_s, (size_t)n * sizeof(float2)));
     P->n_atoms = n;
     if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }

@@ -235,6 +235,37 @@ int gw_detector(gw_ctx *ctx, const gw_detector_params *p, const double *iq,
                 const double *rot_R, const double *weights, int32_t n_orient,
                 double *out);
 
+/* ---- per-slice and helper entry points (device, synchronous) ---------- */
+/* Gather I(q) at points (x,y,z) after applying n_R 3x3 rotations in order
+ * (BLAS fused order), with the reference's floor division by dq and clip:
+ * tools/detector.py:194-232 intersect_detector (n_R = 0, use_weight = 0) and
+ * tools/detector.py:278-300 generate_detector_ints (the psi/phi/theta
+ * matrices, weight = psi_w*phi_w*theta_w).  iq float64 (ny,nx,nz) host;
+ * qmin = (min qx, min qy, min qz); out float64 (n) host. */
+int gw_gather(gw_ctx *ctx, const double *iq, const int32_t *shape,
+              const double *qmin, double dq, const double *x, const double *y,
+              const double *z, int64_t n, const double *R, int32_t n_R,
+              double weight, int32_t use_weight, double *out);
+/* tools/voxelgrids.py:464-506 process_file2: bin one |F|^2 slice (nv,nh)
+ * with per-column (qx,qy) and per-row qz into sum/count grids (q_num^3,
+ * float64, host), added to what they hold. */
+int gw_bin_slice(gw_ctx *ctx, const double *iq2d, int32_t nv, int32_t nh,
+                 const double *hx, const double *hy, const double *vz,
+                 int32_t q_num, double q_min, double q_max, double dq,
+                 double *sum, double *count);
+/* tools/detector.py:246-275 mirror_vertical_horizontal (float64, host). */
+int gw_mirror(gw_ctx *ctx, const double *in, int32_t n_rows, int32_t n_cols,
+              double *out);
+/* tools/voxelgrids.py:828-857 add_f0_q_3d: iq (ny,nx,nz) times
+ * ((sum_i a_i exp(-b_i q^2/16pi^2) + c)/Z)^2; coef = (a1,b1,...,a4,b4,c). */
+int gw_f0_scale(gw_ctx *ctx, const double *iq, const int32_t *shape,
+                const double *qx, const double *qy, const double *qz,
+                const double *coef, double z, double *out);
+/* tools/voxelgrids.py:238-309 rectangular_collapse_lengths at x_vals for the
+ * slice scalars in ph (hor, ver before the phi > 90 swap). */
+int gw_collapse_lengths(gw_ctx *ctx, const double *x_vals, int64_t n,
+                        double hor, double ver, const gw_phi *ph, double *out);
+
 #ifdef __cplusplus
 }
 #endif
