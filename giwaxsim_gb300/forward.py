@@ -57,6 +57,26 @@ class VoxelGeometry:
         q_h = fftshift(fftfreq(self.grid_size, d=r_voxel_size) * 2 * np.pi)
         self.h_max = np.max(q_h)
 
+    @classmethod
+    def from_axes(cls, grid_size, r_voxel_size, q_axis):
+        """Geometry of the reference's per-slice worker, which receives the
+        grid size and the q axis instead of q_voxel_size and max_q
+        (voxelgrids.py:311-315).  The crop is the whole axis."""
+        g = cls.__new__(cls)
+        g.r_voxel_size = r_voxel_size
+        g.q_voxel_size = None
+        g.max_q = None
+        g.grid_size = int(grid_size)
+        g.q = np.asarray(q_axis, dtype=np.float64)
+        g.q_num = len(g.q)
+        g.auto_phis = None
+        g.crop_lo, g.crop_hi = 0, g.q_num - 1
+        g.q_crop = g.q
+        g.dq = np.diff(g.q)[0]
+        q_h = fftshift(fftfreq(g.grid_size, d=r_voxel_size) * 2 * np.pi)
+        g.h_max = np.max(q_h)
+        return g
+
     def check_bounds(self, coords):
         b = [np.max(coords[:, i]) - np.min(coords[:, i]) for i in range(3)]
         if self.grid_size * self.r_voxel_size < np.min(b):
@@ -118,7 +138,7 @@ class VoxelPlan:
 
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
-                 batch_slices=0, ctx=None):
+                 batch_slices=0, constants=None, ctx=None):
         self.geom = geom
         self.ctx = ctx or N.default_context()
         self.phis = geom.auto_phis if phis is None else np.asarray(phis, np.float64)
@@ -132,11 +152,17 @@ class VoxelPlan:
             coords = np.ascontiguousarray(coords, dtype=np.float64)
             if coords.ndim != 2 or coords.shape[1] != 3 or len(coords) == 0:
                 raise ValueError("coords must be a non-empty (N, 3) array")
-            geom.check_bounds(coords)
             fv = np.asarray(fv, dtype=complex)
             if w is not None:
                 fv = fv * np.asarray(w, dtype=np.float64)
-            xb, yb, zb, avg, mv = structure_constants(coords, fv, r)
+            if constants is not None:
+                # the per-slice worker receives the driver's constants
+                xb, yb, zb, avg = constants[i]
+                avg = complex(avg)
+                mv = float(np.sqrt(xb ** 2 + yb ** 2) // r)
+            else:
+                geom.check_bounds(coords)
+                xb, yb, zb, avg, mv = structure_constants(coords, fv, r)
             st[i] = (begin, len(coords), xb, yb, zb, avg.real, avg.imag, mv)
             begin += len(coords)
             xyz.append(coords)
@@ -275,6 +301,14 @@ class PlaneCorners:
     def __init__(self, h, v):
         self.pts = np.array([[0.0, h[0], v[0]], [0.0, h[-1], v[0]],
                              [0.0, h[0], v[-1]]])
+
+    @classmethod
+    def from_grids(cls, x, y, z):
+        c = cls.__new__(cls)
+        c.pts = np.array([[x[0, 0], y[0, 0], z[0, 0]],
+                          [x[0, -1], y[0, -1], z[0, -1]],
+                          [x[-1, 0], y[-1, 0], z[-1, 0]]], dtype=np.float64)
+        return c
 
     def matrix(self, kind, angle):
         p1, p2, p3 = self.pts

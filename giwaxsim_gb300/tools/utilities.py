@@ -187,3 +187,17 @@ def get_element_f1_f2_dict(energy, elements):
         except Exception as e:
             print(f"An error occurred for element '{el}': {e}")
     return out
+
+
+def create_shared_array(shape, name=None):
+    """float64 shared-memory block for `shape` (utilities.py:378-398); the
+    name is always a fresh 29-character uuid (macOS limit), as there."""
+    import uuid
+    from multiprocessing import shared_memory
+    size = int(np.prod(shape)) * np.dtype(np.float64).itemsize
+    name = uuid.uuid4().hex[:29]
+    try:
+        return shared_memory.SharedMemory(create=True, size=size, name=name)
+    except FileExistsError:
+        shared_memory.SharedMemory(name=name).unlink()
+        return shared_memory.SharedMemory(create=True, size=size, name=name)

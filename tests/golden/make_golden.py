@@ -3,6 +3,7 @@ GIWAXSim code itself (a Python package, imported from its checkout).
 
 Run in a container that has the reference checkout:
     python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference pm6   # PM6 example
 
 The reference imports matplotlib, mpl_toolkits, fabio, lmfit and xraydb and
 scipy.signal.tukey at module level; none of these is on the computation path
@@ -203,5 +204,50 @@ def main():
     print("fixtures written to", HERE)
 
 
+def pm6():
+    """The reference's shipped example (config_templates/
+    simulate_GIWAXS_config.txt on test_input_files/PM6_sample.pdb): the unit
+    cell, the reference's own result with f' = f'' = 0 (its shipped
+    output_data/PM6_sample/det_sum.npy was made with xraydb's f', f'' at
+    12.7 keV), and that shipped result.  Takes about two minutes."""
+    comparison, detector, utilities, voxelgrids = _import_reference()
+    cfg = utilities.parse_config_file(
+        os.path.join(REF, "config_templates", "simulate_GIWAXS_config.txt"))
+    pdb = os.path.join(REF, "test_input_files", "PM6_sample.pdb")
+    cell_xyz, cell_el = utilities.load_pdb(pdb)
+    cell = utilities.load_pdb_cell_params(pdb)
+    xs, ys, zs = (float(cfg[k]) for k in ("x_size", "y_size", "z_size"))
+    slab, slab_el = comparison.slabmaker_fitting(pdb, xs, ys, zs, *cell)
+    r, dq, mq = (float(cfg[k]) for k in ("r_voxel_size", "q_voxel_size", "max_q"))
+    iq, qx, qy, qz = comparison.voxelgridmaker_fitting(
+        slab, slab_el, r, dq, mq, float(cfg["energy"]), fill_bkg=True,
+        smooth=int(cfg["smooth"]))
+    psis = np.linspace(float(cfg["psi_start"]), float(cfg["psi_end"]),
+                       int(cfg["psi_num"]))
+    phis = np.linspace(float(cfg["phi_start"]), float(cfg["phi_end"]),
+                       int(cfg["phi_num"]))
+    thetas = np.linspace(float(cfg["theta_start"]), float(cfg["theta_end"]),
+                         int(cfg["theta_num"]))
+    init_vals = tuple(float(cfg[f"angle_init_val{i}"]) for i in (1, 2, 3))
+    init_axs = tuple(cfg[f"angle_init_ax{i}"] for i in (1, 2, 3))
+    det, h, v = comparison.detectormaker_fitting(
+        iq, qx, qy, qz, int(cfg["num_pixels"]), mq, init_vals, init_axs, psis,
+        None, phis, None, thetas, None, mirror=True)
+    kh, kv = np.where(h >= 0)[0], np.where(v >= 0)[0]
+    shipped = np.load(os.path.join(REF, "output_data", "PM6_sample",
+                                   "det_sum.npy"))
+    np.savez_compressed(
+        os.path.join(HERE, "golden_pm6.npz"), cell_xyz=cell_xyz,
+        cell_el=cell_el, cell=np.array(cell), slab_n=len(slab),
+        slab_sum=slab.sum(0), slab_head=slab[:16], config=np.array(
+            ["%s=%s" % kv_ for kv_ in cfg.items()]),
+        det_ref=det[np.ix_(kv, kh)], det_h=h[kh], det_v=v[kv],
+        det_shipped=shipped)
+    print("PM6 fixture written")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 2 and sys.argv[2] == "pm6":
+        pm6()
+    else:
+        main()
