@@ -46,6 +46,15 @@ def _import_reference():
         scipy.signal.tukey = scipy.signal.windows.tukey
     sys.path.insert(0, REF)
     from tools import comparison, detector, utilities, voxelgrids
+    # The drivers accumulate into shared memory from a ThreadPoolExecutor;
+    # concurrent np.add.at / += on the shared grids lose updates (on the PM6
+    # example 340 of the 8.4 M cropped voxels differ between a threaded and
+    # a serial run).  The fixtures run the reference's own drivers with a
+    # single worker so that they are deterministic.
+    import concurrent.futures as cf
+    serial = lambda *a, **k: cf.ThreadPoolExecutor(max_workers=1)
+    comparison.ThreadPoolExecutor = serial
+    voxelgrids.ThreadPoolExecutor = serial
     return comparison, detector, utilities, voxelgrids
 
 
@@ -209,7 +218,8 @@ def pm6():
     simulate_GIWAXS_config.txt on test_input_files/PM6_sample.pdb): the unit
     cell, the reference's own result with f' = f'' = 0 (its shipped
     output_data/PM6_sample/det_sum.npy was made with xraydb's f', f'' at
-    12.7 keV), and that shipped result.  Takes about two minutes."""
+    12.7 keV and a threaded run), and that shipped result.  Takes about six
+    minutes (single-worker drivers)."""
     comparison, detector, utilities, voxelgrids = _import_reference()
     cfg = utilities.parse_config_file(
         os.path.join(REF, "config_templates", "simulate_GIWAXS_config.txt"))
