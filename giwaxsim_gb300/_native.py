@@ -17,6 +17,7 @@ GW_OK, GW_ERR_ARG, GW_ERR_OOM, GW_ERR_CUDA = 0, 1, 2, 3
 GW_ERR_TIMEOUT, GW_ERR_BOUNDS, GW_ERR_STATE = 4, 5, 6
 GW_VOXEL_BATCHED, GW_VOXEL_PLAIN = 0, 1
 GW_ACCUM_FP64, GW_ACCUM_KAHAN32 = 0, 1
+GW_DEPOSIT_NEAREST, GW_DEPOSIT_BILINEAR = 0, 1
 
 # every symbol include/giwaxs_gb300.h declares
 EXPORTS = [
@@ -34,6 +35,7 @@ EXPORTS = [
     "gw_detector_execute", "gw_detector_get", "gw_detector_debug_indices",
     "gw_detector_noalloc", "gw_detector", "gw_gather", "gw_bin_slice",
     "gw_mirror", "gw_f0_scale", "gw_collapse_lengths",
+    "gw_detector_backward", "gw_voxel_backward", "gw_voxel_grad_buffer",
 ]
 
 
@@ -60,8 +62,8 @@ class VoxelParams(ctypes.Structure):
                 ("smooth", ctypes.c_double), ("mode", ctypes.c_int32),
                 ("accum", ctypes.c_int32), ("average", ctypes.c_int32),
                 ("f0_coef", ctypes.c_double * 9), ("f0_z", ctypes.c_double),
-                ("batch_slices", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 7)]
+                ("batch_slices", ctypes.c_int32), ("deposit", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 class Structure(ctypes.Structure):
@@ -142,6 +144,9 @@ def _declare(lib):
         "gw_mirror": ([P, P, i32, i32, P], ctypes.c_int),
         "gw_f0_scale": ([P, P, P, P, P, P, P, d, P], ctypes.c_int),
         "gw_collapse_lengths": ([P, P, i64, d, d, P, P], ctypes.c_int),
+        "gw_detector_backward": ([P, P, i32, P, i32], ctypes.c_int),
+        "gw_voxel_backward": ([P, P, i32, P, P, P, P], ctypes.c_int),
+        "gw_voxel_grad_buffer": ([P, pp], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -272,6 +272,80 @@ __global__ void k_detector_fix(DetArgs a, const int2 *wl, const int *wl_count,
   }
 }
 
+// ------------------------------------------------------------------ adjoint
+// Transpose of the epilogue: the image is out = 1e-6 * max'(mirror(acc))
+// with max' the NaN/<=0 -> 1e-6 clamp (zero derivative where it acts) and
+// mirror the sum over the four flips (a symmetric map: each output pixel
+// sums its orbit under the flips, with multiplicity).  Hence
+// dL/dacc[p] = 1e-6 * [v_p > 0] * sum over the flips q of p of dL/dout[q],
+// v = mirror(acc) being constant on the orbit.
+__global__ void k_det_epi_adj(const double *acc, const double *gout, int nv,
+                              int nh, int mirror, double *gpix) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= nv * nh) return;
+  const int i = pix / nh, j = pix % nh;
+  const int i2 = nv - 1 - i, j2 = nh - 1 - j;
+  const size_t q0 = (size_t)i * nh + j, q1 = (size_t)i * nh + j2,
+               q2 = (size_t)i2 * nh + j, q3 = (size_t)i2 * nh + j2;
+  double v, g;
+  if (mirror) {
+    v = ((acc[q0] + acc[q1]) + acc[q2]) + acc[q3];
+    g = gout[q0] + gout[q1] + gout[q2] + gout[q3];
+  } else {
+    v = acc[q0];
+    g = gout[q0];
+  }
+  gpix[pix] = (v == v && v > 0.0) ? 1e-6 * g : 0.0;
+}
+
+// Transpose of the orientation sum: every (pixel, orientation) sample adds
+// w_o dL/dacc[pixel] to dL/dI at the voxel it gathered.  Indices come from
+// the same float32 estimate with exact float64 replay as the forward (the
+// ambiguous samples are replayed inline), so they are the forward's.
+__global__ void __launch_bounds__(kDetThreads)
+k_detector_adj(DetArgs a, const OrientFast *ot, const double *gpix,
+               double *g_iq) {
+  __shared__ OrientFast s_ot[kDetChunk];
+  const int npx = a.nh * a.nv;
+  const int pix = blockIdx.x * kDetThreads + threadIdx.x;
+  const bool valid = pix < npx;
+  double x0 = 0.0, y0 = 0.0, z0 = 0.0, g = 0.0;
+  if (valid) {
+    base_point(a, pix / a.nh, pix % a.nh, x0, y0, z0);
+    g = gpix[pix];
+  }
+  const bool live = valid && g != 0.0;
+  const float xf = (float)x0, yf = (float)y0, zf = (float)z0;
+  for (int c0 = 0; c0 < a.n_orient; c0 += kDetChunk) {
+    const int nc = min(kDetChunk, a.n_orient - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * kOrientFloats; t += kDetThreads)
+      reinterpret_cast<float *>(s_ot)[t] = reinterpret_cast<const float *>(ot + c0)[t];
+    __syncthreads();
+    if (!live) continue;
+    for (int oo = 0; oo < nc; ++oo) {
+      const int o = c0 + oo;
+      int64_t idx;
+      if (!fast_index(s_ot[oo], a, xf, yf, zf, idx))
+        idx = gather_index(a, o, x0, y0, z0);
+      atomicAdd(g_iq + idx, g * a.w[o]);
+    }
+  }
+}
+
+// Exact-path adjoint (plans built with exact indices).
+__global__ void k_detector_adj_exact(DetArgs a, const double *gpix,
+                                     double *g_iq) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= a.nh * a.nv) return;
+  const double g = gpix[pix];
+  if (g == 0.0) return;
+  double x0, y0, z0;
+  base_point(a, pix / a.nh, pix % a.nh, x0, y0, z0);
+  for (int o = 0; o < a.n_orient; ++o)
+    atomicAdd(g_iq + gather_index(a, o, x0, y0, z0), g * a.w[o]);
+}
+
 __global__ void k_det_debug_fast(DetArgs a, const OrientFast *ot, int o,
                                  int64_t *idx) {
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -300,6 +374,7 @@ struct gw_detector_plan {
   int2 *d_wl = nullptr;         // exact-replay worklist
   int *d_wl_count = nullptr;
   int wl_cap = 0;
+  double *d_gout = nullptr, *d_gpix = nullptr, *d_giq = nullptr;  // adjoint
   bool executed = false;
 };
 
@@ -473,7 +548,7 @@ extern "C" int gw_detector_plan_destroy(gw_detector_plan *P) {
   if (!P) return GW_OK;
   void *ptrs[] = {P->d_h, P->d_v, P->d_init, P->d_rot, P->d_w, P->d_rs,
                   P->d_rn, P->d_iq_own, P->d_acc, P->d_out, P->d_ot, P->d_wl,
-                  P->d_wl_count};
+                  P->d_wl_count, P->d_gout, P->d_gpix, P->d_giq};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -554,6 +629,55 @@ extern "C" int gw_detector_get(gw_detector_plan *P, double *out, int32_t on_devi
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                           P->ctx->stream));
   return gw::check_device_error(P->ctx, "detector stage");
+}
+
+extern "C" int gw_detector_backward(gw_detector_plan *P, const double *g_out,
+                                    int32_t out_on_device, double *g_iq,
+                                    int32_t iq_on_device) {
+  if (!P || !g_out || !g_iq)
+    return gw::fail(GW_ERR_ARG, "gw_detector_backward: null argument");
+  if (!P->executed)
+    return gw::fail(GW_ERR_STATE, "gw_detector_backward: plan not executed");
+  GW_CUDA(cudaSetDevice(P->ctx->device));
+  const int npx = P->p.n_h * P->p.n_v;
+  const size_t niq = (size_t)P->p.iq_shape[0] * P->p.iq_shape[1] * P->p.iq_shape[2];
+  cudaStream_t st = P->ctx->stream;
+  if (!P->d_gpix) {
+    GW_CUDA(gw::dev_malloc((void **)&P->d_gpix, npx * sizeof(double)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_gout, npx * sizeof(double)));
+  }
+  const double *gout = g_out;
+  if (!out_on_device) {
+    GW_CUDA(cudaMemcpyAsync(P->d_gout, g_out, npx * sizeof(double),
+                            cudaMemcpyHostToDevice, st));
+    gout = P->d_gout;
+  }
+  double *giq = g_iq;
+  if (!iq_on_device) {
+    if (!P->d_giq) GW_CUDA(gw::dev_malloc((void **)&P->d_giq, niq * sizeof(double)));
+    giq = P->d_giq;
+  }
+  GW_CUDA(cudaMemsetAsync(giq, 0, niq * sizeof(double), st));
+  {
+    gw::KTimer tm(P->ctx, GW_K_DET_EPI);
+    k_det_epi_adj<<<(npx + 255) / 256, 256, 0, st>>>(P->d_acc, gout, P->p.n_v,
+                                                     P->p.n_h, P->p.mirror, P->d_gpix);
+    GW_LAUNCHED(P->ctx);
+  }
+  DetArgs a = det_args(P);
+  {
+    gw::KTimer tm(P->ctx, GW_K_DETECTOR);
+    if (P->p.exact)
+      k_detector_adj_exact<<<(npx + 127) / 128, 128, 0, st>>>(a, P->d_gpix, giq);
+    else
+      k_detector_adj<<<(npx + kDetThreads - 1) / kDetThreads, kDetThreads, 0, st>>>(
+          a, P->d_ot, P->d_gpix, giq);
+    GW_LAUNCHED(P->ctx);
+  }
+  if (!iq_on_device)
+    GW_CUDA(cudaMemcpyAsync(g_iq, giq, niq * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GW_CUDA(cudaStreamSynchronize(st));
+  return gw::check_device_error(P->ctx, "detector backward");
 }
 
 extern "C" int gw_detector_debug_indices(gw_detector_plan *P, int32_t orient,

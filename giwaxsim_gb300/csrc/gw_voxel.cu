@@ -28,45 +28,11 @@
 #include <cstring>
 #include <vector>
 
-#include "gw_common.cuh"
-#include "gw_fft.cuh"
-#include "gw_slice.cuh"
+#include "gw_voxel_impl.cuh"
+
+using namespace gwv;
 
 namespace {
-
-constexpr int kMinM = 64, kMaxM = 8192;
-
-struct SliceArgs {
-  // geometry
-  int g;
-  double r, inv_r;
-  int n_phi;
-  int y_lo, Ly, z_lo, Lz;
-  int fill, smooth_on;
-  float sigma;
-  int radius;
-  int plain;
-  // arrays
-  const double *xyz;   // atoms in input order
-  const float2 *f;
-  const int *zidx;
-  const double *xyz_s; // atoms sorted by z index within each structure
-  const float2 *f_s;
-  const float2 *xy32_s; // float32 (x, y) of the sorted atoms
-  const int *rowstart; // per structure: g+2 offsets into the sorted arrays
-  const int2 *zstat;   // per structure: (max valid z index, all z valid)
-  const gw_structure *st;
-  const gw_phi *ph;
-  const double *clbase;  // per slice
-  unsigned long long *ymin_ord, *ymax_ord;
-  int *extflag;          // per slice: 1 = extents need the exact pass
-  int4 *ext;  // y_min, y_max, z_min, z_max (valid atoms)
-  float2 *amo;
-  float *my, *mz;
-  const float *gw;  // gaussian weights, 2*radius+1
-  float4 *sconst;   // per slice: (Cbg.re, Cbg.im, Cd.re, Cd.im)
-  int *err;
-};
 
 // ------------------------------------------------------------ structure prep
 __global__ void k_zmin(const double *xyz, const gw_structure *st,
@@ -161,12 +127,17 @@ k_zscan(const gw_structure *st, int g, const int *hist, int *rowstart,
   if (threadIdx.x == 0) zstat[t] = make_int2(zm, h[g] == 0);
 }
 
+// Counting-sort scatter by z index.  Also records the permutation (sorted
+// position -> input index) and, for the bilinear deposit, the fractional z
+// position (z - zmin)/r - zi of each atom.
 __global__ void k_zscatter(const double *xyz, const float2 *f,
                            const gw_structure *st, const int *zidx, int g,
+                           const unsigned long long *zmin_ord, double inv_r,
                            int *cursor, double *xyz_s, float2 *f_s,
-                           float2 *xy32_s) {
+                           float2 *xy32_s, int *perm, float *fz_s) {
   const gw_structure s = st[blockIdx.y];
   int *cur = cursor + (size_t)blockIdx.y * (g + 1);
+  const double zmin = ord_dbl(zmin_ord[blockIdx.y]);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
        i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t a = s.atom_begin + i;
@@ -177,15 +148,15 @@ __global__ void k_zscatter(const double *xyz, const float2 *f,
     xyz_s[3 * (size_t)pos + 2] = xyz[3 * a + 2];
     f_s[pos] = f[a];
     xy32_s[pos] = make_float2((float)xyz[3 * a], (float)xyz[3 * a + 1]);
+    perm[pos] = (int)a;
+    if (fz_s) {
+      const double v = GW_DMUL(GW_DSUB(xyz[3 * a + 2], zmin), inv_r);
+      fz_s[pos] = fminf(fmaxf((float)(v - (double)zi), 0.f), 1.f);
+    }
   }
 }
 
 // ------------------------------------------------------------ per slice
-__device__ __forceinline__ double rot_y(const double *p, double c, double s) {
-  // column 1 of np.dot(coords, Rz.T): fma(z,0,fma(y,c,x*s)) == fma(y,c,x*s)
-  return GW_DFMA(p[1], c, GW_DMUL(p[0], s));
-}
-
 // Per slice: min and max of the rotated y over all atoms (the shift to the
 // minimum, voxelgrids.py:323), and the slice's background constants.
 __global__ void k_yminmax(SliceArgs a, int slice0) {
@@ -271,29 +242,6 @@ __global__ void k_ext_exact(SliceArgs a, int slice0) {
   }
 }
 
-// Python slice normalisation of [start:stop] on a length-n axis.
-__device__ __forceinline__ void py_slice(int start, int stop, int n, int &s,
-                                         int &e) {
-  if (start < 0) { start += n; if (start < 0) start = 0; }
-  else if (start > n) start = n;
-  if (stop < 0) { stop += n; if (stop < 0) stop = 0; }
-  else if (stop > n) stop = n;
-  s = start;
-  e = stop;
-}
-
-// gaussian_filter1d(mask, sigma, mode='wrap') of the plateau [ms, me).
-__device__ float smooth_at(int i, int ms, int me, int g, int radius,
-                           const float *w) {
-  float acc = 0.f;
-  for (int j = -radius; j <= radius; ++j) {
-    int k = i + j;
-    k %= g; if (k < 0) k += g;
-    if (k >= ms && k < me) acc += w[j + radius];
-  }
-  return acc;
-}
-
 // Per-slice profiles: fill_bkg column term (minus the background) and the
 // two separable smoothing masks (voxelgrids.py:344-379).
 __global__ void k_profile(SliceArgs a, int slice0) {
@@ -324,10 +272,8 @@ __global__ void k_profile(SliceArgs a, int slice0) {
     }
   }
   if (a.smooth_on) {
-    const float sg = a.sigma;
     int ys, ye, zs, ze;
-    py_slice((int)ceilf((float)e.x + sg), (int)ceilf((float)e.y - sg), a.g, ys, ye);
-    py_slice((int)ceilf((float)e.z + sg), (int)ceilf((float)e.w - sg), a.g, zs, ze);
+    plateau(a, e, ys, ye, zs, ze);
     for (int yy = threadIdx.x; yy < a.Ly; yy += blockDim.x) {
       int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
       a.my[(size_t)blockIdx.x * a.Ly + yy] = smooth_at(yi, ys, ye, a.g, a.radius, a.gw);
@@ -355,44 +301,6 @@ __global__ void k_profile(SliceArgs a, int slice0) {
 }
 
 // --------------------------------------------------------------- CZT stages
-struct CztArgs {
-  int M;
-  int L, N;  // input length, output length
-  const float2 *A, *H, *B, *tw;
-};
-
-// D value of box element (zz, yy) of slice slot `slot`.
-__device__ __forceinline__ float2 d_value(const SliceArgs &a, int slot, int sl,
-                                          int zz, int yy, float2 dep, float2 cd,
-                                          float2 cbg, int4 e) {
-  float2 v;
-  if (a.fill) {
-    int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
-    int zi = a.z_lo + zz; if (zi < 0) zi += a.g; if (zi >= a.g) zi -= a.g;
-    const bool inside = zi >= e.z && zi < e.w && yi > e.x && yi < e.y;
-    v = inside ? cadd(dep, a.amo[(size_t)slot * a.Ly + yy]) : cd;
-  } else {
-    v = csub(dep, cbg);
-  }
-  if (a.smooth_on) {
-    const float m = a.mz[(size_t)slot * a.Lz + zz] * a.my[(size_t)slot * a.Ly + yy];
-    v = make_float2(v.x * m + cd.x * (1.f - m), v.y * m + cd.y * (1.f - m));
-  }
-  return v;
-}
-
-struct SliceConst {
-  float2 cbg, cd;
-};
-
-__device__ __forceinline__ SliceConst slice_const(const SliceArgs &a, int sl) {
-  const float4 v = a.sconst[sl];
-  SliceConst k;
-  k.cbg = make_float2(v.x, v.y);
-  k.cd = make_float2(v.z, v.w);
-  return k;
-}
-
 // Row stage: NB rows (slice, z) per block, transformed along y; Nc outputs
 // kept.  The block first deposits the atoms of its rows (contiguous in the
 // z-sorted arrays) into shared-memory row buffers with shared atomics
@@ -402,47 +310,6 @@ __device__ __forceinline__ SliceConst slice_const(const SliceArgs &a, int sl) {
 // filter spectrum H, and its last pass writes F1 = B * result to global
 // memory.  The row buffers share storage with the FFT buffer: the first pass
 // reads all its inputs before it writes.
-// Window column of sorted atom `at` in slice `sl`: false when the valid mask
-// drops it (y index outside [0, g)); yy >= Ly flags a window overflow.
-// The index is first estimated in float32: t = (x s + y c - ymin)/r with an
-// error below d = 10 u (|x s| + |y c| + |ymin|)/r + 1e-6 (u = 2^-24; the
-// input roundings, four arithmetic roundings and those of t -+ d total at
-// most 7 u times that sum).  Only when [t-d, t+d] contains an integer is the
-// exact float64 chain replayed.
-__device__ __forceinline__ bool deposit_column(const SliceArgs &a, int at,
-                                               int sl, int &yy) {
-  const int p = sl % a.n_phi;
-  const gw_phi &ph = a.ph[p];
-  const double ymin = ord_dbl(a.ymin_ord[sl]);
-  const float2 xy = a.xy32_s[at];
-  const float cs = (float)ph.cos_phi, sn = (float)ph.sin_phi;
-  const float ym = (float)ymin, ir = (float)a.inv_r;
-  const float t = (fmaf(xy.y, cs, xy.x * sn) - ym) * ir;
-  const float d = 10.f * 5.9604645e-8f *
-                      (fabsf(xy.x * sn) + fabsf(xy.y * cs) + fabsf(ym)) * ir +
-                  1e-6f;
-  const float klo = floorf(t - d), khi = floorf(t + d);
-  int yi;
-  if (klo == khi) {
-    yi = (int)klo;
-  } else {
-    const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, ph.cos_phi,
-                                   ph.sin_phi), ymin);
-    yi = (int)floor_div_exact(y, a.r, a.inv_r);
-  }
-  if (yi < 0 || yi >= a.g) return false;
-  yy = yi - a.y_lo;
-  if (yy >= a.g) yy -= a.g;
-  return true;
-}
-
-__device__ __forceinline__ int window_row_to_z(const SliceArgs &a, int zz) {
-  int zi = a.z_lo + zz;
-  if (zi < 0) zi += a.g;
-  if (zi >= a.g) zi -= a.g;
-  return zi;
-}
-
 template <int M>
 struct RowLoad {
   const SliceArgs *a;
@@ -471,7 +338,19 @@ struct RowStore {
   }
 };
 
-template <int M>
+// Add w * fv at grid column i of a shared-memory row.
+__device__ __forceinline__ void deposit_at(const SliceArgs &a, float2 *row,
+                                           int i, float2 fv, float w) {
+  const int yy = window_col(a, i);
+  if (yy < a.Ly) {
+    atomicAdd(&row[yy].x, fv.x * w);
+    atomicAdd(&row[yy].y, fv.y * w);
+  } else {
+    dev_error(a.err, GW_DEVERR_BOX);
+  }
+}
+
+template <int M, bool BIL>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
 k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
           float2 *F1) {
@@ -481,7 +360,7 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
   extern __shared__ float2 smem[];
   float2 *tw = smem;
   float2 *buf = smem + TWL;
-  __shared__ int r_lo[NB], r_cnt[NB + 1];
+  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1];
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   for (int t = threadIdx.x; t < NB * LDM; t += NT) buf[t] = make_float2(0.f, 0.f);
   const int row0 = blockIdx.x * NB;
@@ -489,19 +368,17 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
     int acc = 0;
     for (int f = 0; f < NB; ++f) {
       const int row = row0 + f;
-      int lo = 0, cnt = 0;
+      int lo = 0, mid = 0, hi = 0;
       if (row < n_rows) {
         const int slot = row / a.Lz, zz = row % a.Lz;
         const int sl = slice0 + slot, t = sl / a.n_phi;
         if (a.ext[sl].y < 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
-        const int zi = window_row_to_z(a, zz);
-        const int *rs = a.rowstart + (size_t)t * (a.g + 2);
-        lo = rs[zi];
-        cnt = rs[zi + 1] - lo;
+        row_atoms(a, t, zz, lo, mid, hi);
       }
       r_lo[f] = lo;
+      r_mid[f] = mid;
       r_cnt[f] = acc;
-      acc += cnt;
+      acc += hi - lo;
     }
     r_cnt[NB] = acc;
   }
@@ -512,14 +389,26 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
     while (f + 1 < NB && i >= r_cnt[f + 1]) ++f;
     const int at = r_lo[f] + (i - r_cnt[f]);
     const int sl = slice0 + (row0 + f) / a.Lz;
-    int yy;
-    if (deposit_column(a, at, sl, yy)) {
-      if (yy < a.Ly) {
+    if constexpr (!BIL) {
+      int yy;
+      if (deposit_column(a, at, sl, yy)) {
+        if (yy < a.Ly) {
+          const float2 fv = a.f_s[at];
+          atomicAdd(&buf[f * LDM + yy].x, fv.x);
+          atomicAdd(&buf[f * LDM + yy].y, fv.y);
+        } else {
+          dev_error(a.err, GW_DEVERR_BOX);
+        }
+      }
+    } else {
+      int i0;
+      float fu;
+      if (bilinear_column(a, at, sl, i0, fu)) {
+        const float fz = a.fz_s[at];
+        const float wz = at >= r_mid[f] ? 1.f - fz : fz;
         const float2 fv = a.f_s[at];
-        atomicAdd(&buf[f * LDM + yy].x, fv.x);
-        atomicAdd(&buf[f * LDM + yy].y, fv.y);
-      } else {
-        dev_error(a.err, GW_DEVERR_BOX);
+        deposit_at(a, buf + f * LDM, i0, fv, wz * (1.f - fu));
+        if (i0 + 1 < a.g) deposit_at(a, buf + f * LDM, i0 + 1, fv, wz * fu);
       }
     }
   }
@@ -529,16 +418,6 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
   RowStore stv{cz.B, F1, row0, n_rows, nc_out};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), stv);
 }
-
-struct BinArgs {
-  const int *colofs;  // [n_phi][Nc], -1 = not binned
-  const int *rowofs;  // [Nr], -1 = not binned
-  double *sum;        // window^3 float64
-  float2 *sumk;       // window^3 (sum, compensation) for Kahan float32
-  int kahan;
-  int k0, kz0;        // frequency of output column 0 / row 0
-  float dc_scale;     // g*g
-};
 
 __device__ __forceinline__ void kahan_add(float2 *addr, float x) {
   unsigned long long *p = reinterpret_cast<unsigned long long *>(addr);
@@ -698,14 +577,33 @@ __global__ void k_finalize(const double *sum, const float2 *sumk, int kahan,
 // sorted arrays and index code the row kernel uses.
 __global__ void k_debug_window(SliceArgs a, int sl, float2 *win) {
   const int t = sl / a.n_phi;
-  const int *rs = a.rowstart + (size_t)t * (a.g + 2);
   for (int zz = blockIdx.x; zz < a.Lz; zz += gridDim.x) {
-    const int zi = window_row_to_z(a, zz);
-    for (int at = rs[zi] + threadIdx.x; at < rs[zi + 1]; at += blockDim.x) {
-      int yy;
-      if (deposit_column(a, at, sl, yy) && yy < a.Ly) {
-        atomicAdd(&win[(size_t)zz * a.Ly + yy].x, a.f_s[at].x);
-        atomicAdd(&win[(size_t)zz * a.Ly + yy].y, a.f_s[at].y);
+    int lo, mid, hi;
+    row_atoms(a, t, zz, lo, mid, hi);
+    float2 *row = win + (size_t)zz * a.Ly;
+    for (int at = lo + threadIdx.x; at < hi; at += blockDim.x) {
+      if (!a.bil) {
+        int yy;
+        if (deposit_column(a, at, sl, yy) && yy < a.Ly) {
+          atomicAdd(&row[yy].x, a.f_s[at].x);
+          atomicAdd(&row[yy].y, a.f_s[at].y);
+        }
+      } else {
+        int i0;
+        float fu;
+        if (bilinear_column(a, at, sl, i0, fu)) {
+          const float wz = at >= mid ? 1.f - a.fz_s[at] : a.fz_s[at];
+          const float2 fv = a.f_s[at];
+          for (int c = 0; c < 2; ++c) {
+            const int i = i0 + c;
+            const int yy = window_col(a, i);
+            const float w = wz * (c ? fu : 1.f - fu);
+            if (i < a.g && yy < a.Ly) {
+              atomicAdd(&row[yy].x, fv.x * w);
+              atomicAdd(&row[yy].y, fv.y * w);
+            }
+          }
+        }
       }
     }
   }
@@ -766,10 +664,6 @@ cd chirp(long long e, long long g) {
   return cd(std::cos(ang), std::sin(ang));
 }
 
-struct CztTables {
-  std::vector<float2> A, H, B, tw;
-};
-
 // Per-pass twiddle tables of gw_fft.cuh's plan for length M: for every pass
 // with stride Ns > 1 and radix R, tw[k*(R-1) + r-1] = exp(-2 pi i r k/(Ns R)).
 std::vector<float2> fft_twiddles(int M) {
@@ -793,8 +687,10 @@ std::vector<float2> fft_twiddles(int M) {
   return tw;
 }
 
-// X[k0+m] = sum_{n<L} x[lo+n] W^{(lo+n)(k0+m)}, W = exp(-2 pi i/g), via
-// B[m] * conv(x*A, h)[m], h[j] = W^{-j^2/2}, j in [-(L-1), N-1].
+}  // namespace
+
+namespace gwv {
+
 CztTables make_czt(int g, int lo, int L, int k0, int N, int M) {
   CztTables t;
   t.A.resize(L); t.B.resize(N); t.H.resize(M);
@@ -826,78 +722,6 @@ int next_pow2(int n) {
   return m;
 }
 
-template <typename T>
-int upload(T **dst, const std::vector<T> &v, size_t *bytes) {
-  if (v.empty()) { *dst = nullptr; return GW_OK; }
-  GW_CUDA(gw::dev_malloc((void **)dst, v.size() * sizeof(T)));
-  *bytes += v.size() * sizeof(T);
-  GW_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T),
-                     cudaMemcpyHostToDevice));
-  return GW_OK;
-}
-
-template <typename T>
-int alloc(T **dst, size_t n, size_t *bytes) {
-  if (n == 0) { *dst = nullptr; return GW_OK; }
-  GW_CUDA(gw::dev_malloc((void **)dst, n * sizeof(T)));
-  *bytes += n * sizeof(T);
-  return GW_OK;
-}
-
-}  // namespace
-
-// ================================================================== plan
-struct gw_voxel_plan {
-  gw_ctx *ctx = nullptr;
-  gw_voxel_params p{};
-  int n_struct = 0, n_phi = 0, n_slices = 0;
-  std::vector<gw_structure> structs;
-  std::vector<gw_phi> phis;
-  int g = 0, plain = 0, Qc = 0, lo = 0, hi = 0, wlo = 0, whi = 0, W = 0;
-  double r = 0, inv_r = 0, dq = 0, inv_dq = 0;
-  int radius = 0;
-  int y_lo = 0, Ly = 0, z_lo = 0, Lz = 0, k0 = 0, Nc = 0, kz0 = 0, Nr = 0;
-  int My = 0, Mz = 0, S = 1;
-  int64_t n_atoms = -1;
-  size_t bytes = 0;
-  std::vector<int> C1host;
-  // device
-  double *d_xyz = nullptr;
-  float2 *d_f = nullptr;
-  int *d_zidx = nullptr;
-  gw_structure *d_structs = nullptr;
-  gw_phi *d_phis = nullptr;
-  double *d_clbase = nullptr;
-  unsigned long long *d_zmin = nullptr, *d_ymin = nullptr;
-  int4 *d_ext = nullptr;
-  float2 *d_Ay = nullptr, *d_Hy = nullptr, *d_By = nullptr, *d_twy = nullptr;
-  float2 *d_Az = nullptr, *d_Hz = nullptr, *d_Bz = nullptr, *d_twz = nullptr;
-  float *d_gw = nullptr;
-  int *d_colofs = nullptr, *d_rowofs = nullptr, *d_C1 = nullptr;
-  unsigned int *d_C2 = nullptr;
-  double *d_sum = nullptr;
-  float2 *d_sumk = nullptr;
-  float *d_f0 = nullptr;
-  double *d_iq64 = nullptr;
-  float *d_iq32 = nullptr;
-  float2 *d_F1 = nullptr, *d_amo = nullptr;
-  double *d_xyz_s = nullptr;
-  float2 *d_xy32_s = nullptr;
-  float2 *d_f_s = nullptr;
-  int *d_zhist = nullptr, *d_rowstart = nullptr, *d_cursor = nullptr;
-  int2 *d_zstat = nullptr;
-  unsigned long long *d_ymax = nullptr;
-  int *d_extflag = nullptr;
-  float *d_my = nullptr, *d_mz = nullptr;
-  float4 *d_sconst = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  int64_t graph_kernels = 0;
-  bool executed = false;
-};
-
-namespace {
-
 SliceArgs slice_args(gw_voxel_plan *P) {
   SliceArgs a{};
   a.g = P->g; a.r = P->r; a.inv_r = P->inv_r; a.n_phi = P->n_phi;
@@ -906,7 +730,7 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.sigma = (float)P->p.smooth; a.radius = P->radius; a.plain = P->plain;
   a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
   a.xyz_s = P->d_xyz_s; a.f_s = P->d_f_s; a.rowstart = P->d_rowstart;
-  a.xy32_s = P->d_xy32_s;
+  a.xy32_s = P->d_xy32_s; a.fz_s = P->d_fz_s; a.bil = P->bil;
   a.zstat = P->d_zstat; a.ymax_ord = P->d_ymax; a.extflag = P->d_extflag;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
   a.ext = P->d_ext; a.amo = P->d_amo; a.my = P->d_my;
@@ -914,24 +738,31 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   return a;
 }
 
-template <int M>
-int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-               int slice0, int n_rows) {
+template <int M, bool BIL>
+int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                 int slice0, int n_rows) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
   static bool attr = false;
   if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_row_czt<M>,
+    GW_CUDA(cudaFuncSetAttribute(k_row_czt<M, BIL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
     attr = true;
   }
   const int blocks = (n_rows + NB - 1) / NB;
   gw::KTimer tm(P->ctx, GW_K_ROW);
-  k_row_czt<M><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_rows,
-                                                     P->Nc, P->d_F1);
+  k_row_czt<M, BIL><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_rows,
+                                                          P->Nc, P->d_F1);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
+}
+
+template <int M>
+int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+               int slice0, int n_rows) {
+  return a.bil ? launch_row_t<M, true>(P, a, cz, slice0, n_rows)
+               : launch_row_t<M, false>(P, a, cz, slice0, n_rows);
 }
 
 template <int M>
@@ -954,19 +785,6 @@ int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   return GW_OK;
 }
 
-#define GW_DISPATCH_M(M_, fn, ...)                                        \
-  switch (M_) {                                                         \
-    case 64: return fn<64>(__VA_ARGS__);                                \
-    case 128: return fn<128>(__VA_ARGS__);                              \
-    case 256: return fn<256>(__VA_ARGS__);                              \
-    case 512: return fn<512>(__VA_ARGS__);                              \
-    case 1024: return fn<1024>(__VA_ARGS__);                            \
-    case 2048: return fn<2048>(__VA_ARGS__);                            \
-    case 4096: return fn<4096>(__VA_ARGS__);                            \
-    case 8192: return fn<8192>(__VA_ARGS__);                            \
-    default: return gw::fail(GW_ERR_ARG, "unsupported FFT size");       \
-  }
-
 int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  int s0, int n) {
   GW_DISPATCH_M(P->My, launch_row, P, a, cz, s0, n)
@@ -976,24 +794,24 @@ int col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   GW_DISPATCH_M(P->Mz, launch_col, P, a, cz, bn, s0, n)
 }
 
-// Enqueue the whole chain (no synchronisation).
-int enqueue(gw_voxel_plan *P) {
+int atom_blocks(gw_voxel_plan *P) {
+  int64_t max_atoms = 0;
+  for (auto &s : P->structs) max_atoms = std::max(max_atoms, s.atom_count);
+  return (int)std::min<int64_t>(std::max<int64_t>(1, (max_atoms + 255) / 256),
+                                4 * P->ctx->sm_count);
+}
+
+int enqueue_prep(gw_voxel_plan *P) {
   gw_ctx *ctx = P->ctx;
   cudaStream_t st = ctx->stream;
-  const size_t W3 = (size_t)P->W * P->W * P->W;
-  if (P->p.accum == GW_ACCUM_KAHAN32)
-    GW_CUDA(cudaMemsetAsync(P->d_sumk, 0, W3 * sizeof(float2), st));
-  else
-    GW_CUDA(cudaMemsetAsync(P->d_sum, 0, W3 * sizeof(double), st));
+  k_ext_init<<<(P->n_slices + 255) / 256, 256, 0, st>>>(P->d_ext, P->n_slices);
+  GW_LAUNCHED(ctx);
   GW_CUDA(cudaMemsetAsync(P->d_C2, 0, (size_t)P->W * P->W * sizeof(unsigned), st));
   GW_CUDA(cudaMemsetAsync(P->d_zmin, 0xff, P->n_struct * sizeof(unsigned long long), st));
   GW_CUDA(cudaMemsetAsync(P->d_ymin, 0xff, P->n_slices * sizeof(unsigned long long), st));
   GW_CUDA(cudaMemsetAsync(P->d_ymax, 0, P->n_slices * sizeof(unsigned long long), st));
   GW_CUDA(cudaMemsetAsync(P->d_zhist, 0, (size_t)P->n_struct * (P->g + 1) * sizeof(int), st));
-  int64_t max_atoms = 0;
-  for (auto &s : P->structs) max_atoms = std::max(max_atoms, s.atom_count);
-  const int nblk_at = (int)std::min<int64_t>(
-      std::max<int64_t>(1, (max_atoms + 255) / 256), 4 * ctx->sm_count);
+  const int nblk_at = atom_blocks(P);
   {
     gw::KTimer tm(ctx, GW_K_PREP);
     k_zmin<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(P->d_xyz, P->d_structs, P->d_zmin);
@@ -1015,8 +833,8 @@ int enqueue(gw_voxel_plan *P) {
   {
     gw::KTimer tm(ctx, GW_K_PREP);
     k_zscatter<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(
-        P->d_xyz, P->d_f, P->d_structs, P->d_zidx, P->g, P->d_cursor,
-        P->d_xyz_s, P->d_f_s, P->d_xy32_s);
+        P->d_xyz, P->d_f, P->d_structs, P->d_zidx, P->g, P->d_zmin, P->inv_r,
+        P->d_cursor, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_perm, P->d_fz_s);
     GW_LAUNCHED(ctx);
   }
   {
@@ -1027,7 +845,46 @@ int enqueue(gw_voxel_plan *P) {
                                            P->d_colofs, P->d_C2);
     GW_LAUNCHED(ctx);
   }
+  return GW_OK;
+}
 
+int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
+  gw_ctx *ctx = P->ctx;
+  cudaStream_t st = ctx->stream;
+  const int nblk_at = atom_blocks(P);
+  {
+    gw::KTimer tm(ctx, GW_K_DEPOSIT);
+    k_yminmax<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+    GW_LAUNCHED(ctx);
+  }
+  {
+    gw::KTimer tm(ctx, GW_K_DEPOSIT);
+    k_ext<<<(n + 127) / 128, 128, 0, st>>>(a, s0, n);
+    GW_LAUNCHED(ctx);
+  }
+  {
+    gw::KTimer tm(ctx, GW_K_DEPOSIT);
+    k_ext_exact<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+    GW_LAUNCHED(ctx);
+  }
+  if (a.fill || a.smooth_on) {
+    gw::KTimer tm(ctx, GW_K_PROFILE);
+    k_profile<<<n, 256, 0, st>>>(a, s0);
+    GW_LAUNCHED(ctx);
+  }
+  return GW_OK;
+}
+
+// Enqueue the whole chain (no synchronisation).
+int enqueue(gw_voxel_plan *P) {
+  gw_ctx *ctx = P->ctx;
+  cudaStream_t st = ctx->stream;
+  const size_t W3 = (size_t)P->W * P->W * P->W;
+  if (P->p.accum == GW_ACCUM_KAHAN32)
+    GW_CUDA(cudaMemsetAsync(P->d_sumk, 0, W3 * sizeof(float2), st));
+  else
+    GW_CUDA(cudaMemsetAsync(P->d_sum, 0, W3 * sizeof(double), st));
+  GW_TRY(enqueue_prep(P));
   SliceArgs a = slice_args(P);
   CztArgs cy{P->My, P->Ly, P->Nc, P->d_Ay, P->d_Hy, P->d_By, P->d_twy};
   CztArgs cz{P->Mz, P->Lz, P->Nr, P->d_Az, P->d_Hz, P->d_Bz, P->d_twz};
@@ -1036,26 +893,7 @@ int enqueue(gw_voxel_plan *P) {
              (float)((double)P->g * (double)P->g)};
   for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
     const int n = std::min(P->S, P->n_slices - s0);
-    {
-      gw::KTimer tm(ctx, GW_K_DEPOSIT);
-      k_yminmax<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
-      GW_LAUNCHED(ctx);
-    }
-    {
-      gw::KTimer tm(ctx, GW_K_DEPOSIT);
-      k_ext<<<(n + 127) / 128, 128, 0, st>>>(a, s0, n);
-      GW_LAUNCHED(ctx);
-    }
-    {
-      gw::KTimer tm(ctx, GW_K_DEPOSIT);
-      k_ext_exact<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
-      GW_LAUNCHED(ctx);
-    }
-    if (a.fill || a.smooth_on) {
-      gw::KTimer tm(ctx, GW_K_PROFILE);
-      k_profile<<<n, 256, 0, st>>>(a, s0);
-      GW_LAUNCHED(ctx);
-    }
+    GW_TRY(enqueue_slice_setup(P, a, s0, n));
     GW_TRY(row_dispatch(P, a, cy, s0, n * P->Lz));
     GW_TRY(col_dispatch(P, a, cz, bn, s0, n));
   }
@@ -1091,6 +929,10 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: invalid geometry");
   if (p->smooth < 0)
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: smooth must be >= 0");
+  if (p->deposit != GW_DEPOSIT_NEAREST && p->deposit != GW_DEPOSIT_BILINEAR)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: unknown deposit mode");
+  if (p->deposit == GW_DEPOSIT_BILINEAR && p->mode == GW_VOXEL_PLAIN)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: the bilinear deposit needs the batched mode");
   GW_CUDA(cudaSetDevice(ctx->device));
   auto *P = new gw_voxel_plan();
   P->ctx = ctx;
@@ -1102,6 +944,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
   P->phis.assign(phis, phis + n_phi);
   P->g = p->grid_size;
   P->plain = p->mode == GW_VOXEL_PLAIN;
+  P->bil = p->deposit == GW_DEPOSIT_BILINEAR;
   P->r = p->r_voxel_size;
   P->inv_r = 1.0 / P->r;
   P->dq = p->dq;
@@ -1285,13 +1128,15 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
   if (!P) return GW_OK;
   if (P->gexec) cudaGraphExecDestroy(P->gexec);
   if (P->graph) cudaGraphDestroy(P->graph);
+  gwv::grad_state_destroy(P->grad);
   void *ptrs[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_structs, P->d_phis,
                   P->d_clbase, P->d_zmin, P->d_ymin, P->d_ext, P->d_Ay,
                   P->d_Hy, P->d_By, P->d_twy, P->d_Az, P->d_Hz, P->d_Bz,
                   P->d_twz, P->d_gw, P->d_colofs, P->d_rowofs, P->d_C1,
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
                   P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
-                  P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_zhist, P->d_rowstart,
+                  P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_fz_s,
+                  P->d_perm, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
@@ -1306,10 +1151,13 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
     if (s.atom_begin < 0 || s.atom_count < 1 || s.atom_begin + s.atom_count > n)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: structure atom range outside the atom arrays");
   if (n != P->n_atoms) {
-    void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_f_s, P->d_xy32_s};
+    void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_f_s,
+                   P->d_xy32_s, P->d_perm, P->d_fz_s};
     for (void *q : old) gw::dev_free(q);
     P->d_xyz = nullptr; P->d_f = nullptr; P->d_zidx = nullptr;
     P->d_xyz_s = nullptr; P->d_f_s = nullptr; P->d_xy32_s = nullptr;
+    P->d_perm = nullptr; P->d_fz_s = nullptr;
+    P->n_atoms = -1;
     if (n > INT_MAX / 4)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: more than 2^29 atoms");
     GW_CUDA(gw::dev_malloc((void **)&P->d_xyz, (size_t)n * 3 * sizeof(double)));
@@ -1318,6 +1166,9 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
     GW_CUDA(gw::dev_malloc((void **)&P->d_xyz_s, (size_t)n * 3 * sizeof(double)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_xy32_s, (size_t)n * sizeof(float2)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_f_s, (size_t)n * sizeof(float2)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_perm, (size_t)n * sizeof(int)));
+    if (P->bil)
+      GW_CUDA(gw::dev_malloc((void **)&P->d_fz_s, (size_t)n * sizeof(float)));
     P->n_atoms = n;
     if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
     if (P->graph) { cudaGraphDestroy(P->graph); P->graph = nullptr; }
@@ -1328,11 +1179,7 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
   return GW_OK;
 }
 
-static int voxel_enqueue_all(gw_voxel_plan *P) {
-  k_ext_init<<<(P->n_slices + 255) / 256, 256, 0, P->ctx->stream>>>(P->d_ext, P->n_slices);
-  GW_LAUNCHED(P->ctx);
-  return enqueue(P);
-}
+static int voxel_enqueue_all(gw_voxel_plan *P) { return enqueue(P); }
 
 extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
   if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_execute: null plan");

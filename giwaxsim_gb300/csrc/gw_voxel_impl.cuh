@@ -1,0 +1,327 @@
+// Internal declarations of the voxel stage shared by the forward kernels
+// (gw_voxel.cu) and the adjoint kernels (gw_grad.cu): the per-slice argument
+// block, the chirp-z argument block, the plan object, and the device helpers
+// that both sides must evaluate identically (deposit index, window mapping,
+// smoothing profile).
+#pragma once
+
+#include <algorithm>
+#include <climits>
+#include <complex>
+#include <vector>
+
+#include "gw_common.cuh"
+#include "gw_fft.cuh"
+#include "gw_slice.cuh"
+
+namespace gwv {
+
+constexpr int kMinM = 64, kMaxM = 8192;
+
+struct SliceArgs {
+  // geometry
+  int g;
+  double r, inv_r;
+  int n_phi;
+  int y_lo, Ly, z_lo, Lz;
+  int fill, smooth_on;
+  float sigma;
+  int radius;
+  int plain;
+  int bil;             // bilinear deposit (two rows x two columns per atom)
+  // arrays
+  const double *xyz;   // atoms in input order
+  const float2 *f;
+  const int *zidx;
+  const double *xyz_s; // atoms sorted by z index within each structure
+  const float2 *f_s;
+  const float2 *xy32_s; // float32 (x, y) of the sorted atoms
+  const float *fz_s;   // bilinear: fractional z position of the sorted atoms
+  const int *rowstart; // per structure: g+2 offsets into the sorted arrays
+  const int2 *zstat;   // per structure: (max valid z index, all z valid)
+  const gw_structure *st;
+  const gw_phi *ph;
+  const double *clbase;  // per slice
+  unsigned long long *ymin_ord, *ymax_ord;
+  int *extflag;          // per slice: 1 = extents need the exact pass
+  int4 *ext;  // y_min, y_max, z_min, z_max (valid atoms)
+  float2 *amo;
+  float *my, *mz;
+  const float *gw;  // gaussian weights, 2*radius+1
+  float4 *sconst;   // per slice: (Cbg.re, Cbg.im, Cd.re, Cd.im)
+  int *err;
+};
+
+struct CztArgs {
+  int M;
+  int L, N;  // input length, output length
+  const float2 *A, *H, *B, *tw;
+};
+
+struct BinArgs {
+  const int *colofs;  // [n_phi][Nc], -1 = not binned
+  const int *rowofs;  // [Nr], -1 = not binned
+  double *sum;        // window^3 float64
+  float2 *sumk;       // window^3 (sum, compensation) for Kahan float32
+  int kahan;
+  int k0, kz0;        // frequency of output column 0 / row 0
+  float dc_scale;     // g*g
+};
+
+struct SliceConst {
+  float2 cbg, cd;
+};
+
+__device__ __forceinline__ SliceConst slice_const(const SliceArgs &a, int sl) {
+  const float4 v = a.sconst[sl];
+  SliceConst k;
+  k.cbg = make_float2(v.x, v.y);
+  k.cd = make_float2(v.z, v.w);
+  return k;
+}
+
+__device__ __forceinline__ double rot_y(const double *p, double c, double s) {
+  // column 1 of np.dot(coords, Rz.T): fma(z,0,fma(y,c,x*s)) == fma(y,c,x*s)
+  return GW_DFMA(p[1], c, GW_DMUL(p[0], s));
+}
+
+// Python slice normalisation of [start:stop] on a length-n axis.
+__device__ __forceinline__ void py_slice(int start, int stop, int n, int &s,
+                                         int &e) {
+  if (start < 0) { start += n; if (start < 0) start = 0; }
+  else if (start > n) start = n;
+  if (stop < 0) { stop += n; if (stop < 0) stop = 0; }
+  else if (stop > n) stop = n;
+  s = start;
+  e = stop;
+}
+
+// gaussian_filter1d(mask, sigma, mode='wrap') of the plateau [ms, me), with
+// the kernel weights w (or their sigma derivative).
+__device__ __forceinline__ float smooth_at(int i, int ms, int me, int g,
+                                           int radius, const float *w) {
+  float acc = 0.f;
+  for (int j = -radius; j <= radius; ++j) {
+    int k = i + j;
+    k %= g; if (k < 0) k += g;
+    if (k >= ms && k < me) acc += w[j + radius];
+  }
+  return acc;
+}
+
+// Smoothing plateau bounds of slice extents e (voxelgrids.py:369-370, with
+// ceil() for non-integer sigma).
+__device__ __forceinline__ void plateau(const SliceArgs &a, int4 e, int &ys,
+                                        int &ye, int &zs, int &ze) {
+  const float sg = a.sigma;
+  py_slice((int)ceilf((float)e.x + sg), (int)ceilf((float)e.y - sg), a.g, ys, ye);
+  py_slice((int)ceilf((float)e.z + sg), (int)ceilf((float)e.w - sg), a.g, zs, ze);
+}
+
+__device__ __forceinline__ int window_row_to_z(const SliceArgs &a, int zz) {
+  int zi = a.z_lo + zz;
+  if (zi < 0) zi += a.g;
+  if (zi >= a.g) zi -= a.g;
+  return zi;
+}
+
+// Window column of grid column yi (yi in [0, g)); >= Ly flags an overflow.
+__device__ __forceinline__ int window_col(const SliceArgs &a, int yi) {
+  int yy = yi - a.y_lo;
+  if (yy >= a.g) yy -= a.g;
+  return yy;
+}
+
+// D value of box element (zz, yy) of slice slot `slot`.
+__device__ __forceinline__ float2 d_value(const SliceArgs &a, int slot, int sl,
+                                          int zz, int yy, float2 dep, float2 cd,
+                                          float2 cbg, int4 e) {
+  float2 v;
+  if (a.fill) {
+    int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
+    int zi = a.z_lo + zz; if (zi < 0) zi += a.g; if (zi >= a.g) zi -= a.g;
+    const bool inside = zi >= e.z && zi < e.w && yi > e.x && yi < e.y;
+    v = inside ? cadd(dep, a.amo[(size_t)slot * a.Ly + yy]) : cd;
+  } else {
+    v = csub(dep, cbg);
+  }
+  if (a.smooth_on) {
+    const float m = a.mz[(size_t)slot * a.Lz + zz] * a.my[(size_t)slot * a.Ly + yy];
+    v = make_float2(v.x * m + cd.x * (1.f - m), v.y * m + cd.y * (1.f - m));
+  }
+  return v;
+}
+
+// Window column of sorted atom `at` in slice `sl` (nearest-bin deposit):
+// false when the valid mask drops it (y index outside [0, g)); yy >= Ly
+// flags a window overflow.
+// The index is first estimated in float32: t = (x s + y c - ymin)/r with an
+// error below d = 10 u (|x s| + |y c| + |ymin|)/r + 1e-6 (u = 2^-24; the
+// input roundings, four arithmetic roundings and those of t -+ d total at
+// most 7 u times that sum).  Only when [t-d, t+d] contains an integer is the
+// exact float64 chain replayed.
+__device__ __forceinline__ bool deposit_column(const SliceArgs &a, int at,
+                                               int sl, int &yy) {
+  const int p = sl % a.n_phi;
+  const gw_phi &ph = a.ph[p];
+  const double ymin = ord_dbl(a.ymin_ord[sl]);
+  const float2 xy = a.xy32_s[at];
+  const float cs = (float)ph.cos_phi, sn = (float)ph.sin_phi;
+  const float ym = (float)ymin, ir = (float)a.inv_r;
+  const float t = (fmaf(xy.y, cs, xy.x * sn) - ym) * ir;
+  const float d = 10.f * 5.9604645e-8f *
+                      (fabsf(xy.x * sn) + fabsf(xy.y * cs) + fabsf(ym)) * ir +
+                  1e-6f;
+  const float klo = floorf(t - d), khi = floorf(t + d);
+  int yi;
+  if (klo == khi) {
+    yi = (int)klo;
+  } else {
+    const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, ph.cos_phi,
+                                   ph.sin_phi), ymin);
+    yi = (int)floor_div_exact(y, a.r, a.inv_r);
+  }
+  if (yi < 0 || yi >= a.g) return false;
+  yy = window_col(a, yi);
+  return true;
+}
+
+// Bilinear deposit of sorted atom `at` in slice `sl`: the atom's shifted
+// position u = (y' - ymin)/r splits between columns i0 = floor(u) (weight
+// 1-fu) and i0+1 (weight fu).  The atom is valid when i0 is inside the grid
+// (the nearest-bin valid mask); a corner at g is dropped.
+__device__ __forceinline__ bool bilinear_column(const SliceArgs &a, int at,
+                                                int sl, int &i0, float &fu) {
+  const gw_phi &ph = a.ph[sl % a.n_phi];
+  const double ymin = ord_dbl(a.ymin_ord[sl]);
+  const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, ph.cos_phi,
+                                 ph.sin_phi), ymin);
+  const double k = floor_div_exact(y, a.r, a.inv_r);
+  if (k < 0.0 || k >= (double)a.g) return false;
+  i0 = (int)k;
+  const float t = (float)(GW_DMUL(y, a.inv_r) - k);
+  fu = fminf(fmaxf(t, 0.f), 1.f);
+  return true;
+}
+
+// Atom range of window row zz: nearest-bin rows hold the atoms of z index
+// zi; bilinear rows also those of zi-1 (their upper z corner).  `mid` is the
+// first atom of index zi.
+__device__ __forceinline__ void row_atoms(const SliceArgs &a, int t, int zz,
+                                          int &lo, int &mid, int &hi) {
+  const int zi = window_row_to_z(a, zz);
+  const int *rs = a.rowstart + (size_t)t * (a.g + 2);
+  mid = rs[zi];
+  hi = rs[zi + 1];
+  lo = (a.bil && zi > 0) ? rs[zi - 1] : mid;
+}
+
+// ------------------------------------------------------------ host helpers
+struct CztTables {
+  std::vector<float2> A, H, B, tw;
+};
+
+// X[k0+m] = sum_{n<L} x[lo+n] W^{(lo+n)(k0+m)}, W = exp(-2 pi i/g), via
+// B[m] * conv(x*A, h)[m], h[j] = W^{-j^2/2}, j in [-(L-1), N-1].
+CztTables make_czt(int g, int lo, int L, int k0, int N, int M);
+int next_pow2(int n);
+
+template <typename T>
+int upload(T **dst, const std::vector<T> &v, size_t *bytes) {
+  if (v.empty()) { *dst = nullptr; return GW_OK; }
+  GW_CUDA(gw::dev_malloc((void **)dst, v.size() * sizeof(T)));
+  *bytes += v.size() * sizeof(T);
+  GW_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T),
+                     cudaMemcpyHostToDevice));
+  return GW_OK;
+}
+
+template <typename T>
+int alloc(T **dst, size_t n, size_t *bytes) {
+  if (n == 0) { *dst = nullptr; return GW_OK; }
+  GW_CUDA(gw::dev_malloc((void **)dst, n * sizeof(T)));
+  *bytes += n * sizeof(T);
+  return GW_OK;
+}
+
+}  // namespace gwv
+
+struct gw_grad_state;
+
+// ================================================================== plan
+struct gw_voxel_plan {
+  gw_ctx *ctx = nullptr;
+  gw_voxel_params p{};
+  int n_struct = 0, n_phi = 0, n_slices = 0;
+  std::vector<gw_structure> structs;
+  std::vector<gw_phi> phis;
+  int g = 0, plain = 0, Qc = 0, lo = 0, hi = 0, wlo = 0, whi = 0, W = 0;
+  double r = 0, inv_r = 0, dq = 0, inv_dq = 0;
+  int radius = 0, bil = 0;
+  int y_lo = 0, Ly = 0, z_lo = 0, Lz = 0, k0 = 0, Nc = 0, kz0 = 0, Nr = 0;
+  int My = 0, Mz = 0, S = 1;
+  int64_t n_atoms = -1;
+  size_t bytes = 0;
+  std::vector<int> C1host;
+  // device
+  double *d_xyz = nullptr;
+  float2 *d_f = nullptr;
+  int *d_zidx = nullptr;
+  gw_structure *d_structs = nullptr;
+  gw_phi *d_phis = nullptr;
+  double *d_clbase = nullptr;
+  unsigned long long *d_zmin = nullptr, *d_ymin = nullptr;
+  int4 *d_ext = nullptr;
+  float2 *d_Ay = nullptr, *d_Hy = nullptr, *d_By = nullptr, *d_twy = nullptr;
+  float2 *d_Az = nullptr, *d_Hz = nullptr, *d_Bz = nullptr, *d_twz = nullptr;
+  float *d_gw = nullptr;
+  int *d_colofs = nullptr, *d_rowofs = nullptr, *d_C1 = nullptr;
+  unsigned int *d_C2 = nullptr;
+  double *d_sum = nullptr;
+  float2 *d_sumk = nullptr;
+  float *d_f0 = nullptr;
+  double *d_iq64 = nullptr;
+  float *d_iq32 = nullptr;
+  float2 *d_F1 = nullptr, *d_amo = nullptr;
+  double *d_xyz_s = nullptr;
+  float2 *d_xy32_s = nullptr;
+  float2 *d_f_s = nullptr;
+  float *d_fz_s = nullptr;
+  int *d_perm = nullptr;   // sorted position -> input atom index
+  int *d_zhist = nullptr, *d_rowstart = nullptr, *d_cursor = nullptr;
+  int2 *d_zstat = nullptr;
+  unsigned long long *d_ymax = nullptr;
+  int *d_extflag = nullptr;
+  float *d_my = nullptr, *d_mz = nullptr;
+  float4 *d_sconst = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_kernels = 0;
+  bool executed = false;
+  gw_grad_state *grad = nullptr;  // adjoint workspace (gw_grad.cu)
+};
+
+namespace gwv {
+SliceArgs slice_args(gw_voxel_plan *P);
+// Structure preparation: extents reset, z sort, column tables.
+int enqueue_prep(gw_voxel_plan *P);
+// Per-slice min/max, extents and profiles of slices [s0, s0+n).
+int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n);
+// Row transforms of n_rows window rows starting at slice s0, into d_F1.
+int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                 int s0, int n_rows);
+void grad_state_destroy(gw_grad_state *g);
+}  // namespace gwv
+
+#define GW_DISPATCH_M(M_, fn, ...)                                        \
+  switch (M_) {                                                         \
+    case 64: return fn<64>(__VA_ARGS__);                                \
+    case 128: return fn<128>(__VA_ARGS__);                              \
+    case 256: return fn<256>(__VA_ARGS__);                              \
+    case 512: return fn<512>(__VA_ARGS__);                              \
+    case 1024: return fn<1024>(__VA_ARGS__);                            \
+    case 2048: return fn<2048>(__VA_ARGS__);                            \
+    case 4096: return fn<4096>(__VA_ARGS__);                            \
+    case 8192: return fn<8192>(__VA_ARGS__);                            \
+    default: return gw::fail(GW_ERR_ARG, "unsupported FFT size");       \
+  }

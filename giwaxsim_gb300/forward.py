@@ -138,7 +138,7 @@ class VoxelPlan:
 
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
-                 batch_slices=0, constants=None, ctx=None):
+                 batch_slices=0, constants=None, deposit="nearest", ctx=None):
         self.geom = geom
         self.ctx = ctx or N.default_context()
         self.phis = geom.auto_phis if phis is None else np.asarray(phis, np.float64)
@@ -189,6 +189,8 @@ class VoxelPlan:
             p.f0_coef[i] = coef[i]
         p.f0_z = z
         p.batch_slices = int(batch_slices)
+        p.deposit = {"nearest": N.GW_DEPOSIT_NEAREST,
+                     "bilinear": N.GW_DEPOSIT_BILINEAR}[deposit]
         self.params = p
         h = ctypes.c_void_p()
         N.check(N.lib().gw_voxel_plan_create(
@@ -254,6 +256,37 @@ class VoxelPlan:
         N.check(N.lib().gw_voxel_debug_deposit(self.handle, int(slice_index),
                                                N.ptr(y), N.ptr(z)))
         return y, z
+
+    def grad_buffer(self):
+        """Device address of the plan's dL/dI(q) buffer (Qc^3 float64)."""
+        p = ctypes.c_void_p()
+        N.check(N.lib().gw_voxel_grad_buffer(self.handle, ctypes.byref(p)))
+        return p.value
+
+    def backward(self, g_iq, iq_on_device=False, want_xyz=False):
+        """Vector-Jacobian product of the voxel stage (gw_voxel_backward):
+        g_iq is dL/dI(q) on the cropped cube (host array, or a device
+        pointer with iq_on_device).  Returns dict(g_f (N,) complex: dL/d of
+        every atom's deposited f with the structure constants held fixed,
+        g_xyz (N,3) or None, g_sigma float, g_c (n_struct,) complex: dL/d of
+        each structure's background constant avg_voxel_f * max_voxels)."""
+        n = len(self.xyz)
+        g_f = np.empty(2 * n)
+        g_xyz = np.empty((n, 3)) if want_xyz else None
+        g_sigma = np.zeros(1)
+        g_c = np.zeros(2 * len(self.structs))
+        if iq_on_device:
+            src, flag = ctypes.c_void_p(g_iq), 1
+        else:
+            g_iq = np.ascontiguousarray(g_iq, dtype=np.float64)
+            if g_iq.shape != (self.Qc,) * 3:
+                raise ValueError("g_iq must have shape %s" % ((self.Qc,) * 3,))
+            src, flag = N.ptr(g_iq), 0
+        N.check(N.lib().gw_voxel_backward(self.handle, src, flag, N.ptr(g_f),
+                                          N.ptr(g_xyz), N.ptr(g_sigma),
+                                          N.ptr(g_c)))
+        return dict(g_f=g_f.view(complex), g_xyz=g_xyz, g_sigma=float(g_sigma[0]),
+                    g_c=g_c.view(complex))
 
     def debug_window(self, slice_index):
         """Deposited (Lz, Ly) complex window of one slice and its origin
@@ -411,6 +444,22 @@ class DetectorPlan:
     def result(self):
         out = np.empty((self.params.n_v, self.params.n_h))
         N.check(N.lib().gw_detector_get(self.handle, N.ptr(out), 0))
+        return out
+
+    def backward(self, g_image, g_iq_device=None):
+        """dL/dI(q) from dL/d(image of result()) (gw_detector_backward).
+        Written to the device buffer g_iq_device when given, else returned
+        as a host array of the plan's I(q) shape."""
+        g = np.ascontiguousarray(g_image, dtype=np.float64)
+        if g.shape != (self.params.n_v, self.params.n_h):
+            raise ValueError("g_image must have the detector's shape")
+        if g_iq_device is not None:
+            N.check(N.lib().gw_detector_backward(self.handle, N.ptr(g), 0,
+                                                 ctypes.c_void_p(g_iq_device), 1))
+            return None
+        out = np.empty(self.iq_shape)
+        N.check(N.lib().gw_detector_backward(self.handle, N.ptr(g), 0,
+                                             N.ptr(out), 0))
         return out
 
     def debug_indices(self, orient):

@@ -85,6 +85,7 @@ int gw_collapse_base(const double *ver, const double *cos_t, int64_t n,
 /* ---- voxel stage: I(qx,qy,qz) from atoms ----------------------------- */
 enum { GW_VOXEL_BATCHED = 0, GW_VOXEL_PLAIN = 1 };
 enum { GW_ACCUM_FP64 = 0, GW_ACCUM_KAHAN32 = 1 };
+enum { GW_DEPOSIT_NEAREST = 0, GW_DEPOSIT_BILINEAR = 1 };
 
 typedef struct gw_voxel_params {
   int32_t grid_size;    /* g = ceil(2pi/(dq*r))          comparison.py:710 */
@@ -104,7 +105,12 @@ typedef struct gw_voxel_params {
   double f0_coef[9];    /* Cromer-Mann a1,b1,..,a4,b4,c  voxelgrids.py:849 */
   double f0_z;          /* Z of the f0 element; <= 0 skips the f0 factor   */
   int32_t batch_slices; /* slices per batch, 0 = automatic                 */
-  int32_t reserved[7];
+  int32_t deposit;      /* GW_DEPOSIT_NEAREST (the reference's np.add.at of
+                           floor-divided indices, voxelgrids.py:328-341) |
+                           GW_DEPOSIT_BILINEAR (each atom split over two
+                           rows x two columns; differentiable in the
+                           coordinates; no counterpart in the reference)    */
+  int32_t reserved[6];
 } gw_voxel_params;
 
 typedef struct gw_structure {
@@ -228,6 +234,41 @@ int gw_detector_noalloc(const gw_detector_params *p, const float *iq32,
                         const int32_t *n_rot, const double *rot_R,
                         const double *weights, int32_t n_orient, double *out,
                         void *stream);
+/* ---- adjoints (vector-Jacobian products) -------------------------------
+ * No counterpart in the reference, which has no gradients; they give the
+ * gradient of a scalar misfit of the detector image (the scale + flat
+ * background least squares of tools/comparison.py:873-882 is one) with
+ * respect to the inputs of the forward path.  Complex gradients are
+ * dL/dRe + i dL/dIm.
+ *
+ * Detector: g_out is dL/d(image returned by gw_detector_get), (n_v, n_h)
+ * float64; g_iq receives dL/dI(q) (ny*nx*nz float64).  The plan must have
+ * been executed on the I(q) the gradient is taken at (the clamp of the
+ * epilogue is evaluated on that image).  Synchronous. */
+int gw_detector_backward(gw_detector_plan *plan, const double *g_out,
+                         int32_t out_on_device, double *g_iq,
+                         int32_t iq_on_device);
+/* Voxel stage (batched mode, fill_bkg off): g_iq is dL/dI(q) on the
+ * cropped cube (Qc^3 float64, host or device).  Every slice is recomputed
+ * from the atoms set on the plan, one batch at a time (nothing per slice is
+ * kept from the forward).  Outputs (host):
+ *   g_f      n_atoms x 2: dL/d f of every atom's deposited scattering factor
+ *            (input order), the constants of the structures held fixed;
+ *   g_xyz    n_atoms x 3 or NULL: dL/d coordinates (GW_DEPOSIT_BILINEAR
+ *            only), including the shift of every slice to its minimum
+ *            rotated y and of the z axis to the minimum z;
+ *   g_sigma  1 or NULL: dL/d smooth (sigma in voxels; plateau bounds and the
+ *            kernel radius are piecewise constant and contribute nothing);
+ *   g_c      n_struct x 2 or NULL: dL/d of each structure's background
+ *            constant avg_voxel_f * max_voxels (smoothing on; else 0).
+ * Synchronous. */
+int gw_voxel_backward(gw_voxel_plan *plan, const double *g_iq,
+                      int32_t iq_on_device, double *g_f, double *g_xyz,
+                      double *g_sigma, double *g_c);
+/* Plan-owned device buffer (Qc^3 float64) for dL/dI(q), so that the
+ * detector adjoint can write it and gw_voxel_backward read it without a
+ * host round trip.  Valid until the plan is destroyed. */
+int gw_voxel_grad_buffer(gw_voxel_plan *plan, double **g_iq_dev);
 /* One-shot with host buffers. */
 int gw_detector(gw_ctx *ctx, const gw_detector_params *p, const double *iq,
                 const double *h_axis, const double *v_axis,
