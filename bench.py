@@ -30,6 +30,13 @@ sys.path.insert(0, ROOT)
 METRIC = "slices/s & s/detector image: batched vs plain on 1 GB300 at <=1e-5 rel err vs FP64"
 L2_BYTES = 129 * 1024 * 1024
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# one ncu --set full capture of the kernel on the same workload and batch
+# shape (51-slice batches of si-100A); the summaries with their commands are
+# profiles/k_row_czt_2048_si-100A.md and profiles/k_col_czt_bin_1024_si-100A.md.
+NCU_TRAFFIC = {("si-100A", "row_czt"): (1.6 + 247.2) * 1e6,
+               ("si-100A", "col_czt_bin"): (148.5 + 39.5) * 1e6}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -41,6 +48,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the five-workload batched/plain table")
+    ap.add_argument("--no-grad", action="store_true",
+                    help="skip the forward+backward timing")
     ap.add_argument("--phis", type=int, default=0,
                     help="use this many slices instead of the workload's")
     ap.add_argument("--profile", action="store_true",
@@ -269,24 +280,24 @@ def run_gb300(args, world, rank, local, pg):
     eager.close()
 
     # plain per-rotation path: one slice per launch sequence, full grid
+    # (per-slice cost from 8- and 24-slice plans; their difference removes
+    # the per-execute memset, preparation and finalize, counted once)
     plain = None
     if not args.no_plain:
-        n_plain = min(len(phis), 24)
-        pp = F.VoxelPlan(geom, items[:1], phis=phis[:n_plain],
-                         fill_bkg=w["fill_bkg"], smooth=w["smooth"],
-                         mode="plain", ctx=ctx)
-        pp.set_atoms()
-        pp.execute()
-        ctx.synchronize()
-        p0 = torch.cuda.Event(enable_timing=True)
-        p1 = torch.cuda.Event(enable_timing=True)
-        p0.record(ts)
-        pp.execute()
-        p1.record(ts)
-        torch.cuda.synchronize()
-        plain_ms = p0.elapsed_time(p1)
-        plain = n_plain / (plain_ms / 1e3)
-        pp.close()
+        t = {}
+        for k in (min(len(phis), 8), min(len(phis), 24)):
+            pp = F.VoxelPlan(geom, items[:1], phis=phis[:k],
+                             fill_bkg=w["fill_bkg"], smooth=w["smooth"],
+                             mode="plain", ctx=ctx)
+            pp.set_atoms()
+            pp.execute()
+            ctx.synchronize()
+            t[k] = _event_ms(ts, pp.execute, 2)
+            pp.close()
+        (k1, t1), (k2, t2) = sorted(t.items())
+        per_slice = (t2 - t1) / (k2 - k1) if k2 > k1 else t2 / k2
+        fixed = max(0.0, t1 - k1 * per_slice)
+        plain = n_slices / ((fixed + per_slice * n_slices) / 1e3)
 
     # e2e through the public API with host arrays
     e2e = None
@@ -338,10 +349,21 @@ def run_gb300(args, world, rank, local, pg):
         roof = {"kernel": name, "bound": "hbm", "achieved": achieved,
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": None, "avg_launch_ms": avg_ms,
+                "traffic": NCU_TRAFFIC.get((args.workload, name)),
+                "traffic_source": "ncu capture (profiles/)"
+                if (args.workload, name) in NCU_TRAFFIC else None,
+                "avg_launch_ms": avg_ms,
                 "algorithmic_bytes_per_launch": algo}
     kernel_share = {k: {"ms": round(v[0], 4), "launches": v[1]}
                     for k, v in kt.items()}
+
+    # the five workloads: seconds per detector image, batched vs plain
+    table = None
+    if not args.no_workloads:
+        table = {}
+        for name in WORKLOAD_NAMES:
+            table[name] = workload_summary(name, ctx, ts, do_flush)
+    grad = None if args.no_grad else grad_timing(ctx)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -369,11 +391,130 @@ def run_gb300(args, world, rank, local, pg):
         "gpu_launches": int(launches),
         "e2e": e2e, "roofline": roof, "kernel_ms": kernel_share,
         "cpu_baseline": cpu, "clocks": clk,
+        "workloads": table, "gradient": grad,
     }
     if rank == 0:
         print(json.dumps(out))
     for p_ in (det, plan):
         p_.close()
+
+
+WORKLOAD_NAMES = ("graphite-50A", "si-100A", "graphite-64", "si-60A-occ",
+                  "lamellar-200A")
+
+
+def _event_ms(ts, fn, reps, flush=None):
+    import torch
+    tot = 0.0
+    for _ in range(reps):
+        if flush:
+            flush()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ts)
+        fn()
+        e1.record(ts)
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    return tot / reps
+
+
+def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8):
+    """Seconds per detector image of one workload: batched (graph replay of
+    the voxel stage over all slices + detector) and plain (the per-rotation
+    path, timed on n_plain slices and scaled to all slices, + detector)."""
+    from giwaxsim_gb300 import forward as F
+    w, structs, geom, phis, items = load_workload(name)
+    n_slices = len(items) * len(phis)
+    plan = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
+                       smooth=w["smooth"], ctx=ctx)
+    plan.set_atoms()
+    plan.execute()
+    ctx.synchronize()
+    plan.capture_graph()
+    plan.execute()
+    ctx.synchronize()
+    vox_ms = _event_ms(ts, plan.execute, reps, flush)
+    dargs = detector_args(w, geom)
+    q = geom.q_crop
+    det = F.DetectorPlan((plan.Qc,) * 3, q, q, q, dargs["num_pixels"],
+                         dargs["max_q"], dargs["angle_init_vals"],
+                         dargs["angle_init_axs"], dargs["psis"],
+                         dargs["psi_weights"], dargs["phis"],
+                         dargs["phi_weights"], dargs["thetas"],
+                         dargs["theta_weights"], mirror=True, ctx=ctx)
+    det.set_iq_device32(plan.device_iq32())
+    det.execute()
+    ctx.synchronize()
+    det_ms = _event_ms(ts, det.execute, reps)
+    info = plan.info()
+    det.close()
+    plan.close()
+    # plain: per-slice cost from two sample sizes (the difference removes the
+    # per-execute memset, structure preparation and finalize), plus one
+    # fixed cost
+    n = min(n_plain, len(phis))
+    n1 = max(1, n // 3)
+    t = {}
+    for k in (n1, n):
+        pp = F.VoxelPlan(geom, items[:1], phis=phis[:k], fill_bkg=w["fill_bkg"],
+                         smooth=w["smooth"], mode="plain", ctx=ctx)
+        pp.set_atoms()
+        pp.execute()
+        ctx.synchronize()
+        t[k] = _event_ms(ts, pp.execute, 2)
+        pp.close()
+    per_slice = (t[n] - t[n1]) / (n - n1) if n > n1 else t[n] / n
+    fixed = max(0.0, t[n1] - n1 * per_slice)
+    plain_ms = fixed + per_slice * n_slices
+    batched = (vox_ms + det_ms) / 1e3
+    plain = (plain_ms + det_ms) / 1e3
+    return {"slices": n_slices, "atoms": int(sum(len(x[0]) for x in items)),
+            "grid": geom.grid_size, "crop": info["crop"],
+            "fft_y": info["My"], "fft_z": info["Mz"],
+            "voxel_ms": round(vox_ms, 4), "detector_ms": round(det_ms, 4),
+            "slices_per_s": n_slices / (vox_ms / 1e3),
+            "s_per_image_batched": batched, "s_per_image_plain": plain,
+            "plain_ms_per_slice": round(per_slice, 4),
+            "plain_fixed_ms": round(fixed, 4),
+            "plain_sample_slices": [n1, n], "batched_vs_plain": plain / batched}
+
+
+def grad_timing(ctx, steps=3):
+    """Forward + backward of the scale/offset misfit on si-60A-occ
+    (bilinear deposit, checkpoint interval 16): wall seconds per step."""
+    import torch
+    from giwaxsim_gb300 import workloads as W
+    from giwaxsim_gb300.autograd import (DetectorModel, detector_image,
+                                         scale_offset_misfit)
+    w = W.WORKLOADS["si-60A-occ"]
+    (xyz, el, hidden), = W.structures("si-60A-occ")
+    model = DetectorModel(el, w["energy"], w["r"], w["dq"], w["max_q"],
+                          w["num_pixels"], psis=np.linspace(*w["psis"]),
+                          phis=W.phis_linspace(w["n_phi"]), deposit="bilinear",
+                          checkpoint_every=16, ctx=ctx)
+    target = torch.from_numpy(model.forward(xyz, hidden, 1.5)[0])
+    X = torch.tensor(xyz, requires_grad=True)
+    fw, bw = [], []
+    for k in range(steps + 1):
+        occ = torch.ones(len(xyz), dtype=torch.float64, requires_grad=True)
+        sig = torch.tensor(1.2, dtype=torch.float64, requires_grad=True)
+        t0 = time.perf_counter()
+        loss, _, _ = scale_offset_misfit(detector_image(model, occ, sig, X),
+                                         target)
+        t1 = time.perf_counter()
+        loss.backward()
+        t2 = time.perf_counter()
+        if k:
+            fw.append(t1 - t0)
+            bw.append(t2 - t1)
+    model.close()
+    f, b = float(np.mean(fw)), float(np.mean(bw))
+    return {"workload": "si-60A-occ", "deposit": "bilinear",
+            "checkpoint_every": 16, "atoms": int(len(xyz)),
+            "parameters": int(4 * len(xyz) + 1), "forward_s": f,
+            "backward_s": b, "step_s": f + b,
+            "backward_over_forward": b / f}
 
 
 def run_profile(args, w, geom, phis, items, ctx):

@@ -88,7 +88,7 @@ class DetectorParams(ctypes.Structure):
                 ("qmin_y", ctypes.c_double), ("qmin_z", ctypes.c_double),
                 ("dq", ctypes.c_double), ("mirror", ctypes.c_int32),
                 ("accum", ctypes.c_int32), ("exact", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("no_plane", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 _lib = None

@@ -258,6 +258,128 @@ k_detector_fast(DetArgs a, const OrientFast *ot, double *acc_out, int2 *wl,
   }
 }
 
+// ------------------------------------------------------------ plane mode
+// When every orientation keeps the same axis at a fixed index (the plane
+// rotated about its own normal, the reference's psi rotations), all samples
+// lie in one plane of I(q).  The plane is copied to a compact nu x nv array
+// (u, v the two free axes in memory order) and each block gathers from it:
+// from shared memory when the plane fits, else from global memory through
+// L1.  Blocks own 16 x 32 pixel tiles, so that per orientation a block's
+// samples cover a compact patch of the plane.  Indices, worklist decisions
+// and the per-pixel accumulation order are those of k_detector_fast; only
+// the order in which k_detector_fix atomically adds the replayed samples
+// differs (it is scheduling order in both).
+struct PlaneArgs {
+  int fa, fi;   // fixed axis (0 x, 1 y, 2 z) and its index
+  int ua, va;   // free axes, slower and faster in memory
+  int nu, nv;
+  const float *P;
+};
+constexpr int kPlTW = 32, kPlTH = 16, kPlThreads = 256;
+constexpr size_t kPlaneSmemMax = 200 * 1024;
+
+__global__ void k_plane_extract(DetArgs a, PlaneArgs pa, float *P) {
+  const int64_t n = (int64_t)pa.nu * pa.nv;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int idx[3];
+    idx[pa.fa] = pa.fi;
+    idx[pa.ua] = (int)(t / pa.nv);
+    idx[pa.va] = (int)(t % pa.nv);
+    P[t] = a.iq[((int64_t)idx[1] * a.nx + idx[0]) * a.nz + idx[2]];
+  }
+}
+
+__device__ __forceinline__ bool plane_index(const OrientFast &T,
+                                            const PlaneArgs &pa, float x,
+                                            float y, float z, int &iu,
+                                            int &iv) {
+  const float *Au = T.A + 3 * pa.ua, *Av = T.A + 3 * pa.va;
+  const float tu = fmaf(Au[0], x, fmaf(Au[1], y, fmaf(Au[2], z, T.b[pa.ua])));
+  const float tv = fmaf(Av[0], x, fmaf(Av[1], y, fmaf(Av[2], z, T.b[pa.va])));
+  return fast_axis(tu, T.d[pa.ua], pa.nu, iu) & fast_axis(tv, T.d[pa.va], pa.nv, iv);
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kPlThreads)
+k_detector_plane(DetArgs a, const OrientFast *ot, PlaneArgs pa,
+                 double *acc_out, int2 *wl, int *wl_count, int wl_cap) {
+  extern __shared__ float s_plane[];
+  __shared__ OrientFast s_ot[kDetChunk];
+  constexpr int KP = kPlTH * kPlTW / kPlThreads;  // pixels per thread
+  const int lane = threadIdx.x & 31;
+  const int tiles_x = (a.nh + kPlTW - 1) / kPlTW;
+  const int j = (blockIdx.x % tiles_x) * kPlTW + (threadIdx.x % kPlTW);
+  const int ib = (blockIdx.x / tiles_x) * kPlTH + threadIdx.x / kPlTW;
+  const float *src = pa.P;
+  if (SMEM) {
+    const int n = pa.nu * pa.nv;
+    for (int t = threadIdx.x; t < n; t += kPlThreads) s_plane[t] = pa.P[t];
+    src = s_plane;
+  }
+  int pix[KP];
+  bool valid[KP];
+  float xf[KP], yf[KP], zf[KP];
+  double acc[KP];
+  float part[KP];
+#pragma unroll
+  for (int k = 0; k < KP; ++k) {
+    const int i = ib + k * (kPlThreads / kPlTW);
+    valid[k] = i < a.nv && j < a.nh;
+    pix[k] = valid[k] ? i * a.nh + j : 0;
+    double x0 = 0.0, y0 = 0.0, z0 = 0.0;
+    if (valid[k]) base_point(a, i, j, x0, y0, z0);
+    xf[k] = (float)x0; yf[k] = (float)y0; zf[k] = (float)z0;
+    acc[k] = 0.0;
+    part[k] = 0.f;
+  }
+  for (int c0 = 0; c0 < a.n_orient; c0 += kDetChunk) {
+    const int nc = min(kDetChunk, a.n_orient - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * kOrientFloats; t += kPlThreads)
+      reinterpret_cast<float *>(s_ot)[t] = reinterpret_cast<const float *>(ot + c0)[t];
+    __syncthreads();
+    for (int oo = 0; oo < nc; ++oo) {
+      const OrientFast &T = s_ot[oo];
+      const int o = c0 + oo;
+#pragma unroll
+      for (int k = 0; k < KP; ++k) {
+        int iu, iv;
+        const bool ok = plane_index(T, pa, xf[k], yf[k], zf[k], iu, iv);
+        const bool need = valid[k] && !ok;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        bool inline_exact = false;
+        if (m) {
+          int base = 0;
+          const int leader = __ffs(m) - 1;
+          if (lane == leader) base = atomicAdd(wl_count, __popc(m));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (need) {
+            const int slot = base + __popc(m & ((1u << lane) - 1u));
+            if (slot < wl_cap) wl[slot] = make_int2(pix[k], o);
+            else inline_exact = true;
+          }
+        }
+        float v = 0.f;
+        if (valid[k] && ok) v = SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv);
+        if (inline_exact) {
+          double x, y, z;
+          base_point(a, pix[k] / a.nh, pix[k] % a.nh, x, y, z);
+          v = __ldg(a.iq + gather_index(a, o, x, y, z));
+        }
+        if (valid[k] && (ok || inline_exact)) part[k] = fmaf(v, T.w, part[k]);
+      }
+      if ((o + 1) % kDetFlush == 0) {
+#pragma unroll
+        for (int k = 0; k < KP; ++k) { acc[k] += (double)part[k]; part[k] = 0.f; }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < KP; ++k)
+    if (valid[k]) acc_out[pix[k]] = acc[k] + (double)part[k];
+}
+
 // Exact float64 replay of the worklist's (pixel, orientation) pairs.
 __global__ void k_detector_fix(DetArgs a, const int2 *wl, const int *wl_count,
                                int wl_cap, double *acc) {
@@ -375,6 +497,8 @@ struct gw_detector_plan {
   int *d_wl_count = nullptr;
   int wl_cap = 0;
   double *d_gout = nullptr, *d_gpix = nullptr, *d_giq = nullptr;  // adjoint
+  PlaneArgs plane{-1, -1, 0, 0, 0, 0, nullptr};  // plane mode when fa >= 0
+  float *d_plane = nullptr;
   bool executed = false;
 };
 
@@ -539,6 +663,28 @@ extern "C" int gw_detector_plan_create(gw_ctx *ctx, const gw_detector_params *p,
       gw_detector_plan_destroy(P);
       return gw::cuda_fail(e, "detector worklist", __FILE__, __LINE__);
     }
+    // plane mode: one axis at the same fixed index in every orientation
+    if (p->accum != GW_ACCUM_KAHAN32 && !p->no_plane) {
+      for (int c = 0; c < 3 && P->plane.fa < 0; ++c) {
+        bool same = true;
+        for (int o = 0; o < n_orient && same; ++o)
+          same = ot[o].fix[c] >= 0 && ot[o].fix[c] == ot[0].fix[c];
+        if (!same) continue;
+        // free axes in memory order (y, x, z)
+        const int order[3] = {1, 0, 2};
+        int fr[2], k = 0;
+        for (int q : order)
+          if (q != c) fr[k++] = q;
+        PlaneArgs pa{c, ot[0].fix[c], fr[0], fr[1], dims[fr[0]], dims[fr[1]], nullptr};
+        e = gw::dev_malloc((void **)&P->d_plane, (size_t)pa.nu * pa.nv * sizeof(float));
+        if (e != cudaSuccess) {
+          gw_detector_plan_destroy(P);
+          return gw::cuda_fail(e, "detector plane", __FILE__, __LINE__);
+        }
+        pa.P = P->d_plane;
+        P->plane = pa;
+      }
+    }
   }
   *out = P;
   return GW_OK;
@@ -548,7 +694,7 @@ extern "C" int gw_detector_plan_destroy(gw_detector_plan *P) {
   if (!P) return GW_OK;
   void *ptrs[] = {P->d_h, P->d_v, P->d_init, P->d_rot, P->d_w, P->d_rs,
                   P->d_rn, P->d_iq_own, P->d_acc, P->d_out, P->d_ot, P->d_wl,
-                  P->d_wl_count, P->d_gout, P->d_gpix, P->d_giq};
+                  P->d_wl_count, P->d_gout, P->d_gpix, P->d_giq, P->d_plane};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -601,7 +747,34 @@ extern "C" int gw_detector_execute(gw_detector_plan *P) {
     GW_LAUNCHED(P->ctx);
   } else {
     GW_CUDA(cudaMemsetAsync(P->d_wl_count, 0, sizeof(int), P->ctx->stream));
-    {
+    if (P->plane.fa >= 0) {
+      const PlaneArgs &pa = P->plane;
+      {
+        gw::KTimer tm(P->ctx, GW_K_MISC);
+        const int64_t n = (int64_t)pa.nu * pa.nv;
+        k_plane_extract<<<(int)std::min<int64_t>((n + 255) / 256, 4 * P->ctx->sm_count),
+                          256, 0, P->ctx->stream>>>(a, pa, P->d_plane);
+        GW_LAUNCHED(P->ctx);
+      }
+      const size_t smem = (size_t)pa.nu * pa.nv * sizeof(float);
+      const int tiles = ((P->p.n_h + kPlTW - 1) / kPlTW) * ((P->p.n_v + kPlTH - 1) / kPlTH);
+      gw::KTimer tm(P->ctx, GW_K_DETECTOR);
+      if (smem <= kPlaneSmemMax) {
+        static bool attr = false;
+        if (!attr) {
+          GW_CUDA(cudaFuncSetAttribute(k_detector_plane<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kPlaneSmemMax));
+          attr = true;
+        }
+        k_detector_plane<true><<<tiles, kPlThreads, smem, P->ctx->stream>>>(
+            a, P->d_ot, pa, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);
+      } else {
+        k_detector_plane<false><<<tiles, kPlThreads, 0, P->ctx->stream>>>(
+            a, P->d_ot, pa, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);
+      }
+      GW_LAUNCHED(P->ctx);
+    } else {
       gw::KTimer tm(P->ctx, GW_K_DETECTOR);
       const int per = kDetThreads * kDetPix;
       k_detector_fast<<<(npx + per - 1) / per, kDetThreads, 0, P->ctx->stream>>>(

@@ -371,7 +371,7 @@ class DetectorPlan:
     def __init__(self, iq_shape, qx, qy, qz, num_pixels, max_q,
                  angle_init_vals, angle_init_axs, psis, psi_weights, phis,
                  phi_weights, thetas, theta_weights, mirror=True,
-                 accum="fp64", exact=False, ctx=None):
+                 accum="fp64", exact=False, plane=True, ctx=None):
         self.ctx = ctx or N.default_context()
         nh = nv = int(num_pixels)
         h = np.linspace(-max_q, max_q, nh)
@@ -413,6 +413,7 @@ class DetectorPlan:
         p.mirror = int(bool(mirror))
         p.accum = {"fp64": N.GW_ACCUM_FP64, "kahan32": N.GW_ACCUM_KAHAN32}[accum]
         p.exact = int(bool(exact))
+        p.no_plane = int(not plane)
         self.params = p
         self._h = np.ascontiguousarray(h)
         self._v = np.ascontiguousarray(v)

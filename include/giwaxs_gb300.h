@@ -186,7 +186,10 @@ typedef struct gw_detector_params {
   int32_t exact;            /* 1: replay the float64 chain for every sample;
                                0: float32 fast path with exact replay of the
                                samples whose voxel it cannot decide        */
-  int32_t reserved[5];
+  int32_t no_plane;         /* 1: never use the plane gather (taken by the
+                               fast path when every orientation keeps one
+                               axis at a fixed index); same image either way */
+  int32_t reserved[4];
 } gw_detector_params;
 
 typedef struct gw_detector_plan gw_detector_plan;

@@ -150,3 +150,35 @@ def test_large_detector_vs_oracle():
     got, _, _ = comparison.detectormaker_fitting(*args, mirror=True)
     ref, _, _ = O.detector(*args, mirror=True)
     assert rel_l2(got, ref) <= RTOL
+
+
+@pytest.mark.parametrize("n,npx,cap", [(41, 31, None), (41, 40, "7"),
+                                       (203, 500, None), (260, 300, None)])
+def test_plane_gather_bit_identical(n, npx, cap, monkeypatch):
+    """Orientations that keep x = 0 (rotations about the detector normal)
+    take the plane gather -- from shared memory (plane <= 200 KB) or global
+    memory (260^2 floats) -- and gather the same samples as the general fast
+    path: the images agree to the order of the float64 atomic adds of the
+    exactly replayed samples (1e-12).  cap=7 overflows the worklist into the
+    in-kernel exact branch; which samples overflow depends on push order, and
+    those go into the float32 partial sums (1e-7)."""
+    if cap:
+        monkeypatch.setenv("GW_DET_WORKLIST_CAP", cap)
+    iq, q = synthetic_iq(n=n, qmax=1.5 * (n - 1) / 40, seed=3)
+    psis = np.linspace(0, 180, 37)
+    one = np.array([0.0])
+    for init, axs in (((0, 0, 0), ("None",) * 3),
+                      ((90.0, 0, 0), ("psi", "None", "None"))):
+        imgs, launches = [], []
+        for plane in (True, False):
+            p = F.DetectorPlan(iq.shape, q, q, q, npx, q[-1], init, axs, psis,
+                               np.ones_like(psis) / len(psis), one, one + 1,
+                               one, one + 1, mirror=True, plane=plane)
+            p.set_iq(iq)
+            c0 = p.ctx.launch_count()
+            p.execute()
+            launches.append(p.ctx.launch_count() - c0)
+            imgs.append(p.result())
+            p.close()
+        assert launches[0] == launches[1] + 1  # + the plane copy
+        assert rel_l2(imgs[0], imgs[1]) <= (1e-7 if cap else 1e-12)
