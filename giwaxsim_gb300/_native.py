@@ -63,7 +63,8 @@ class VoxelParams(ctypes.Structure):
                 ("accum", ctypes.c_int32), ("average", ctypes.c_int32),
                 ("f0_coef", ctypes.c_double * 9), ("f0_z", ctypes.c_double),
                 ("batch_slices", ctypes.c_int32), ("deposit", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("fft_y", ctypes.c_int32), ("fft_z", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 class Structure(ctypes.Structure):

@@ -1,22 +1,24 @@
-// Batched power-of-two complex FFTs in shared memory (Stockham autosort,
-// radix-16 register butterflies).
+// Batched mixed-radix complex FFTs in shared memory (Stockham autosort,
+// register butterflies of radix 16, 8, 4, 2, 5 and 3).
 //
 // NB sequences of length M are transformed together by one block.  A pass
 // with radix R and stride Ns reads, for butterfly j, the R values
 // j + r*(M/R), multiplies value r by exp(-+2 pi i r (j mod Ns) / (Ns R)),
 // does an R-point DFT in registers and writes output r to
 // (j / Ns) * Ns * R + (j mod Ns) + r * Ns; after the last pass the sequence
-// is in natural order.  M = 16^a * R_last with R_last in {2,4,8,16}, so a
-// 2048-point transform is three passes (16, 16, 8).
+// is in natural order.  M = 16^a * R2 * F with R2 in {1,2,4,8} and F in
+// {1,3,5}; the passes are a radix-16 passes, then R2, then F, so a
+// 2048-point transform is (16, 16, 8) and a 1280-point one (16, 16, 5).
 //
 // Shared layout: element a of sequence f lives at f*ldm + a + (a >> 4).  With
 // that one-in-sixteen padding every pass's reads (consecutive j) and writes
 // (stride R when Ns = 1, consecutive otherwise) fall into 16 distinct 8-byte
 // bank pairs per half-warp, i.e. no bank conflicts.
 //
-// Twiddles come from per-pass tables tw[k*(R-1) + r-1] = W_{Ns R}^{r k}
-// made in float64 on the host; lanes read consecutive k at an odd stride
-// (R-1), again conflict-free.  No pass evaluates a transcendental.
+// Twiddles come from per-pass tables made in float64 on the host:
+// tw[k*(R-1) + r-1] = W_{Ns R}^{r k} for even R (lanes read consecutive k at
+// the odd stride R-1, conflict-free) and tw[(r-1)*Ns + k] for odd R (lanes
+// read consecutive k).  No pass evaluates a transcendental.
 //
 // The first pass of a transform can read its inputs from a functor (global
 // memory) and the last pass can hand its outputs to a functor, so the
@@ -27,37 +29,66 @@
 
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
 __host__ __device__ constexpr int fft_pad(int a) { return a + (a >> 4); }
+// odd factor of a supported length (1, 3 or 5)
+__host__ __device__ constexpr int fft_odd(int m) { return (m & 1) ? m : fft_odd(m >> 1); }
 
-// Pass plan: number of radix-16 passes and the last radix.
+// Pass plan: a radix-16 passes, then R2 (pow2 remainder), then F (odd).
 template <int M>
 struct FftPlan {
-  static constexpr int L2 = ilog2(M);
-  static constexpr int N16 = (L2 % 4 == 0) ? L2 / 4 : L2 / 4;  // radix-16 passes
-  static constexpr int RLAST = 1 << (L2 - 4 * N16);          // 1 if none
-  static constexpr int NPASS = N16 + (RLAST > 1 ? 1 : 0);
+  static constexpr int F = fft_odd(M);
+  static_assert(F == 1 || F == 3 || F == 5, "M = 2^k, 3*2^k or 5*2^k");
+  static constexpr int P2 = M / F;
+  static constexpr int L2 = ilog2(P2);
+  static constexpr int N16 = L2 / 4;                 // radix-16 passes
+  static constexpr int R2 = 1 << (L2 - 4 * N16);    // 1 if none
+  static constexpr int NPASS = N16 + (R2 > 1) + (F > 1);
   static constexpr int LDM = fft_pad(M) + 4;  // floats2 per sequence (+4: see f-fastest maps)
   // twiddle table length (passes with Ns > 1)
   __host__ __device__ static constexpr int tw_len() {
     int t = 0, ns = 16;
     for (int p = 1; p < N16; ++p) { t += ns * 15; ns *= 16; }
-    if (RLAST > 1 && N16 >= 1) t += ns * (RLAST - 1);
+    if (R2 > 1) { t += ns * (R2 - 1); ns *= R2; }
+    if (F > 1) t += ns * (F - 1);
+    return t > 0 ? t : 1;
+  }
+  // table offsets of the R2 and F passes
+  __host__ __device__ static constexpr int tw_r2() {
+    int t = 0, ns = 16;
+    for (int p = 1; p < N16; ++p) { t += ns * 15; ns *= 16; }
     return t;
+  }
+  __host__ __device__ static constexpr int tw_f() {
+    return tw_r2() + (R2 > 1 ? (1 << (4 * N16)) * (R2 - 1) : 0);
   }
 };
 
 template <int M>
 struct FftShape;
-// MINB: blocks per SM the register budget is sized for (1024 threads per SM,
-// i.e. at most 64 registers per thread) so that latency is hidden by 32
-// resident warps.
+// NB sequences per block, NT threads: every thread holds about 16 points
+// per pass.  MINB: blocks per SM the register budget is sized for (about
+// 1024 threads per SM, i.e. at most 64 registers per thread) so that
+// latency is hidden by ~32 resident warps.
 template <> struct FftShape<64>   { static constexpr int NB = 16, NT = 64,  MINB = 16; };
 template <> struct FftShape<128>  { static constexpr int NB = 16, NT = 128, MINB = 8; };
 template <> struct FftShape<256>  { static constexpr int NB = 8,  NT = 128, MINB = 8; };
+template <> struct FftShape<384>  { static constexpr int NB = 8,  NT = 192, MINB = 5; };
 template <> struct FftShape<512>  { static constexpr int NB = 8,  NT = 256, MINB = 4; };
+template <> struct FftShape<640>  { static constexpr int NB = 8,  NT = 320, MINB = 3; };
+template <> struct FftShape<768>  { static constexpr int NB = 4,  NT = 192, MINB = 5; };
 template <> struct FftShape<1024> { static constexpr int NB = 4,  NT = 256, MINB = 4; };
+template <> struct FftShape<1280> { static constexpr int NB = 4,  NT = 320, MINB = 3; };
+template <> struct FftShape<1536> { static constexpr int NB = 4,  NT = 384, MINB = 2; };
 template <> struct FftShape<2048> { static constexpr int NB = 4,  NT = 512, MINB = 2; };
+template <> struct FftShape<2560> { static constexpr int NB = 2,  NT = 320, MINB = 3; };
+template <> struct FftShape<3072> { static constexpr int NB = 2,  NT = 384, MINB = 2; };
 template <> struct FftShape<4096> { static constexpr int NB = 2,  NT = 512, MINB = 2; };
+template <> struct FftShape<5120> { static constexpr int NB = 1,  NT = 320, MINB = 3; };
+template <> struct FftShape<6144> { static constexpr int NB = 1,  NT = 384, MINB = 2; };
 template <> struct FftShape<8192> { static constexpr int NB = 1,  NT = 512, MINB = 1; };
+
+// The supported lengths, ascending.
+constexpr int kFftSizes[] = {64, 128, 256, 384, 512, 640, 768, 1024, 1280,
+                             1536, 2048, 2560, 3072, 4096, 5120, 6144, 8192};
 
 template <bool INV>
 __device__ __forceinline__ float2 conj_if(float2 w) {
@@ -119,10 +150,52 @@ __host__ __device__ constexpr int out_slot(int k) {
   return R == 16 ? (k % 4) * 4 + k / 4 : R == 8 ? (k % 4) * 2 + k / 4 : k;
 }
 
+// 3-point DFT: y0 = a0+a1+a2, y1,2 = a0 - (a1+a2)/2 -+ i s (a1-a2) with
+// s = sin(2 pi/3) (forward; the inverse swaps the sign of i).
+template <bool INV>
+__device__ __forceinline__ void dft3(float2 *v) {
+  constexpr float s = 0.86602540378443865f;
+  const float2 t1 = cadd(v[1], v[2]);
+  const float2 t2 = make_float2(v[0].x - 0.5f * t1.x, v[0].y - 0.5f * t1.y);
+  const float2 d = csub(v[1], v[2]);
+  const float2 m = INV ? make_float2(-s * d.y, s * d.x) : make_float2(s * d.y, -s * d.x);
+  v[0] = cadd(v[0], t1);
+  v[1] = cadd(t2, m);
+  v[2] = csub(t2, m);
+}
+
+// 5-point DFT with c_k = cos(2 pi k/5), s_k = sin(2 pi k/5):
+// b1 = a0 + c1 (a1+a4) + c2 (a2+a3), b2 = a0 + c2 (a1+a4) + c1 (a2+a3),
+// d1 = s1 (a1-a4) + s2 (a2-a3), d2 = s2 (a1-a4) - s1 (a2-a3);
+// forward y1 = b1 - i d1, y4 = b1 + i d1, y2 = b2 - i d2, y3 = b2 + i d2.
+template <bool INV>
+__device__ __forceinline__ void dft5(float2 *v) {
+  constexpr float c1 = 0.30901699437494742f, c2 = -0.80901699437494742f;
+  constexpr float s1 = 0.95105651629515357f, s2 = 0.58778525229247313f;
+  const float2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+  const float2 t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+  const float2 b1 = make_float2(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
+  const float2 b2 = make_float2(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
+  const float2 d1 = make_float2(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+  const float2 d2 = make_float2(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+  // -i d = (d.y, -d.x); +i d = (-d.y, d.x)
+  const float2 m1 = INV ? make_float2(-d1.y, d1.x) : make_float2(d1.y, -d1.x);
+  const float2 m2 = INV ? make_float2(-d2.y, d2.x) : make_float2(d2.y, -d2.x);
+  v[0] = cadd(v[0], cadd(t1, t2));
+  v[1] = cadd(b1, m1);
+  v[4] = csub(b1, m1);
+  v[2] = cadd(b2, m2);
+  v[3] = csub(b2, m2);
+}
+
 template <int R, bool INV>
 __device__ __forceinline__ void dft(float2 *v) {
   if constexpr (R == 2) {
     dft2<INV>(v[0], v[1]);
+  } else if constexpr (R == 3) {
+    dft3<INV>(v);
+  } else if constexpr (R == 5) {
+    dft5<INV>(v);
   } else if constexpr (R == 4) {
     dft4<INV>(v[0], v[1], v[2], v[3]);
   } else if constexpr (R == 8) {
@@ -150,7 +223,7 @@ __device__ __forceinline__ void dft(float2 *v) {
   }
 }
 
-// Twiddle-table offset of pass p (p >= 1) of a length-M plan.
+// Twiddle-table offset of radix-16 pass p (p >= 1) of a length-M plan.
 template <int M>
 __host__ __device__ constexpr int tw_offset(int p) {
   int t = 0, ns = 16;
@@ -191,9 +264,15 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
       }
       if (NS > 1) {
         const int k = j % NS;
-        const float2 *t = tw + k * (R - 1) - 1;
+        if constexpr (R & 1) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[e][r] = cmul(v[e][r], conj_if<INV>(t[r]));
+          for (int r = 1; r < R; ++r)
+            v[e][r] = cmul(v[e][r], conj_if<INV>(tw[(r - 1) * NS + k]));
+        } else {
+          const float2 *t = tw + k * (R - 1) - 1;
+#pragma unroll
+          for (int r = 1; r < R; ++r) v[e][r] = cmul(v[e][r], conj_if<INV>(t[r]));
+        }
       }
       dft<R, INV>(v[e]);
     }
@@ -252,10 +331,15 @@ __device__ __forceinline__ void fft_run(float2 *buf, const float2 *tw,
       fft_pass<M, 16, 256, NB, NT, INV, 0, false, dst, false>(
           buf, tw + tw_offset<M>(2), nullptr, NoLoad(), store);
     }
-    if constexpr (Pl::RLAST > 1) {
-      constexpr int NSL = M / Pl::RLAST;
-      fft_pass<M, Pl::RLAST, NSL, NB, NT, INV, 0, false, DST, false>(
-          buf, tw + tw_offset<M>(Pl::N16), nullptr, NoLoad(), store);
+    if constexpr (Pl::R2 > 1) {
+      constexpr int NS2 = 1 << (4 * Pl::N16);
+      constexpr int dst = Pl::F == 1 ? DST : 0;
+      fft_pass<M, Pl::R2, NS2, NB, NT, INV, 0, false, dst, false>(
+          buf, tw + Pl::tw_r2(), nullptr, NoLoad(), store);
+    }
+    if constexpr (Pl::F > 1) {
+      fft_pass<M, Pl::F, Pl::P2, NB, NT, INV, 0, false, DST, false>(
+          buf, tw + Pl::tw_f(), nullptr, NoLoad(), store);
     }
   }
 }

@@ -635,24 +635,33 @@ __global__ void k_debug_deposit(SliceArgs a, int sl, int *yo, int *zo) {
 // ------------------------------------------------------------ host tables
 using cd = std::complex<double>;
 
+// Forward DFT (exp(-2 pi i/n)) in float64 for n = 2^k * odd: radix-2
+// decimation in time down to the odd length, done directly.
 void fft_inplace_host(std::vector<cd> &a) {
   const size_t n = a.size();
-  for (size_t i = 1, j = 0; i < n; ++i) {
-    size_t bit = n >> 1;
-    for (; j & bit; bit >>= 1) j ^= bit;
-    j ^= bit;
-    if (i < j) std::swap(a[i], a[j]);
-  }
-  for (size_t len = 2; len <= n; len <<= 1) {
-    for (size_t i = 0; i < n; i += len) {
-      for (size_t k = 0; k < len / 2; ++k) {
-        const double ang = -2.0 * M_PI * (double)k / (double)len;
-        const cd w(std::cos(ang), std::sin(ang));
-        const cd u = a[i + k], v = a[i + k + len / 2] * w;
-        a[i + k] = u + v;
-        a[i + k + len / 2] = u - v;
+  if (n <= 1) return;
+  if (n & 1) {
+    std::vector<cd> out(n);
+    for (size_t k = 0; k < n; ++k) {
+      cd s(0, 0);
+      for (size_t j = 0; j < n; ++j) {
+        const double ang = -2.0 * M_PI * (double)((j * k) % n) / (double)n;
+        s += a[j] * cd(std::cos(ang), std::sin(ang));
       }
+      out[k] = s;
     }
+    a.swap(out);
+    return;
+  }
+  std::vector<cd> ev(n / 2), od(n / 2);
+  for (size_t i = 0; i < n / 2; ++i) { ev[i] = a[2 * i]; od[i] = a[2 * i + 1]; }
+  fft_inplace_host(ev);
+  fft_inplace_host(od);
+  for (size_t k = 0; k < n / 2; ++k) {
+    const double ang = -2.0 * M_PI * (double)k / (double)n;
+    const cd t = cd(std::cos(ang), std::sin(ang)) * od[k];
+    a[k] = ev[k] + t;
+    a[k + n / 2] = ev[k] - t;
   }
 }
 
@@ -666,23 +675,33 @@ cd chirp(long long e, long long g) {
 
 // Per-pass twiddle tables of gw_fft.cuh's plan for length M: for every pass
 // with stride Ns > 1 and radix R, tw[k*(R-1) + r-1] = exp(-2 pi i r k/(Ns R)).
+// Odd-radix passes store their table r-major: tw[(r-1)*Ns + k].
 std::vector<float2> fft_twiddles(int M) {
+  int F = M;
+  while (!(F & 1)) F >>= 1;
+  const int P2 = M / F;
   int l2 = 0;
-  while ((1 << l2) < M) ++l2;
-  const int n16 = l2 / 4, rlast = 1 << (l2 - 4 * n16);
+  while ((1 << l2) < P2) ++l2;
+  const int n16 = l2 / 4, r2 = 1 << (l2 - 4 * n16);
   std::vector<float2> tw;
+  auto w = [](long long e, long long span) {
+    const double ang = -2.0 * M_PI * (double)(e % span) / (double)span;
+    return make_float2((float)std::cos(ang), (float)std::sin(ang));
+  };
   auto add = [&](int ns, int R) {
     const long long span = (long long)ns * R;
-    for (int k = 0; k < ns; ++k)
-      for (int r = 1; r < R; ++r) {
-        const long long e = ((long long)r * k) % span;
-        const double ang = -2.0 * M_PI * (double)e / (double)span;
-        tw.push_back(make_float2((float)std::cos(ang), (float)std::sin(ang)));
-      }
+    if (R & 1) {
+      for (int r = 1; r < R; ++r)
+        for (int k = 0; k < ns; ++k) tw.push_back(w((long long)r * k, span));
+    } else {
+      for (int k = 0; k < ns; ++k)
+        for (int r = 1; r < R; ++r) tw.push_back(w((long long)r * k, span));
+    }
   };
   int ns = 16;
   for (int p = 1; p < n16; ++p) { add(ns, 16); ns *= 16; }
-  if (rlast > 1) add(ns, rlast);
+  if (r2 > 1) { add(ns, r2); ns *= r2; }
+  if (F > 1) add(ns, F);
   if (tw.empty()) tw.push_back(make_float2(1.f, 0.f));
   return tw;
 }
@@ -716,10 +735,16 @@ CztTables make_czt(int g, int lo, int L, int k0, int N, int M) {
   return t;
 }
 
-int next_pow2(int n) {
-  int m = kMinM;
-  while (m < n) m <<= 1;
-  return m;
+int next_fft_size(int n, bool pow2_only) {
+  for (int m : kFftSizes)
+    if (m >= n && m >= kMinM && (!pow2_only || (m & (m - 1)) == 0)) return m;
+  return 0;
+}
+
+bool fft_size_supported(int m) {
+  for (int s : kFftSizes)
+    if (s == m) return true;
+  return false;
 }
 
 SliceArgs slice_args(gw_voxel_plan *P) {
@@ -1029,11 +1054,19 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     P->Lz = zbound + tail - lo_off + 1;
     if (P->Lz >= g) { P->Lz = g; P->z_lo = 0; }
   }
-  P->My = next_pow2(P->Ly + P->Nc - 1);
-  P->Mz = next_pow2(P->Lz + P->Nr - 1);
-  if (P->My > kMaxM || P->Mz > kMaxM) {
+  // transform lengths: the smallest supported >= L+N-1, or the caller's
+  // choice (an autotuner compares the candidates)
+  const int need_y = P->Ly + P->Nc - 1, need_z = P->Lz + P->Nr - 1;
+  P->My = p->fft_y > 0 ? p->fft_y : next_fft_size(need_y, false);
+  P->Mz = p->fft_z > 0 ? p->fft_z : next_fft_size(need_z, false);
+  if (P->My == 0 || P->Mz == 0) {
     delete P;
     return gw::fail(GW_ERR_ARG, "slice transform larger than 8192 points");
+  }
+  if (!fft_size_supported(P->My) || !fft_size_supported(P->Mz) ||
+      P->My < need_y || P->Mz < need_z) {
+    delete P;
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: fft_y/fft_z must be a supported length >= L+N-1");
   }
   // batch size: keep the per-batch intermediates near L2 size
   {

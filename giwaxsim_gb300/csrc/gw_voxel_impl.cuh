@@ -224,7 +224,9 @@ struct CztTables {
 // X[k0+m] = sum_{n<L} x[lo+n] W^{(lo+n)(k0+m)}, W = exp(-2 pi i/g), via
 // B[m] * conv(x*A, h)[m], h[j] = W^{-j^2/2}, j in [-(L-1), N-1].
 CztTables make_czt(int g, int lo, int L, int k0, int N, int M);
-int next_pow2(int n);
+// Smallest supported transform length >= n (0 if none).
+int next_fft_size(int n, bool pow2_only);
+bool fft_size_supported(int m);
 
 template <typename T>
 int upload(T **dst, const std::vector<T> &v, size_t *bytes) {
@@ -318,10 +320,19 @@ void grad_state_destroy(gw_grad_state *g);
     case 64: return fn<64>(__VA_ARGS__);                                \
     case 128: return fn<128>(__VA_ARGS__);                              \
     case 256: return fn<256>(__VA_ARGS__);                              \
+    case 384: return fn<384>(__VA_ARGS__);                              \
     case 512: return fn<512>(__VA_ARGS__);                              \
+    case 640: return fn<640>(__VA_ARGS__);                              \
+    case 768: return fn<768>(__VA_ARGS__);                              \
     case 1024: return fn<1024>(__VA_ARGS__);                            \
+    case 1280: return fn<1280>(__VA_ARGS__);                            \
+    case 1536: return fn<1536>(__VA_ARGS__);                            \
     case 2048: return fn<2048>(__VA_ARGS__);                            \
+    case 2560: return fn<2560>(__VA_ARGS__);                            \
+    case 3072: return fn<3072>(__VA_ARGS__);                            \
     case 4096: return fn<4096>(__VA_ARGS__);                            \
+    case 5120: return fn<5120>(__VA_ARGS__);                            \
+    case 6144: return fn<6144>(__VA_ARGS__);                            \
     case 8192: return fn<8192>(__VA_ARGS__);                            \
     default: return gw::fail(GW_ERR_ARG, "unsupported FFT size");       \
   }

@@ -138,7 +138,8 @@ class VoxelPlan:
 
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
-                 batch_slices=0, constants=None, deposit="nearest", ctx=None):
+                 batch_slices=0, constants=None, deposit="nearest", fft_y=0,
+                 fft_z=0, ctx=None):
         self.geom = geom
         self.ctx = ctx or N.default_context()
         self.phis = geom.auto_phis if phis is None else np.asarray(phis, np.float64)
@@ -191,6 +192,7 @@ class VoxelPlan:
         p.batch_slices = int(batch_slices)
         p.deposit = {"nearest": N.GW_DEPOSIT_NEAREST,
                      "bilinear": N.GW_DEPOSIT_BILINEAR}[deposit]
+        p.fft_y, p.fft_z = int(fft_y), int(fft_z)
         self.params = p
         h = ctypes.c_void_p()
         N.check(N.lib().gw_voxel_plan_create(

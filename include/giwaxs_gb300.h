@@ -110,7 +110,10 @@ typedef struct gw_voxel_params {
                            GW_DEPOSIT_BILINEAR (each atom split over two
                            rows x two columns; differentiable in the
                            coordinates; no counterpart in the reference)    */
-  int32_t reserved[6];
+  int32_t fft_y, fft_z; /* chirp-z convolution lengths along y and z: 0 =
+                           the smallest supported length >= L+N-1; else one
+                           of 2^k, 3*2^k, 5*2^k in [64, 8192] and >= L+N-1 */
+  int32_t reserved[4];
 } gw_voxel_params;
 
 typedef struct gw_structure {

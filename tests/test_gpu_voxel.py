@@ -174,12 +174,14 @@ def test_graph_replay_matches_eager():
         assert rel_l2(plan.iq(), eager) <= 1e-12
 
 
-@pytest.mark.parametrize("name,n_phi,expect_m", [("graphite-50A", 2, 2048),
-                                                 ("si-100A", 1, 4096),
-                                                 ("lamellar-200A", 1, 8192)])
-def test_plain_mode_large_transforms(name, n_phi, expect_m):
-    """Plain (full-grid) mode at full workload grid sizes: 2048-, 4096- and
-    8192-point transforms against the oracle's numpy fftn."""
+@pytest.mark.parametrize("name,n_phi,force,expect_m", [
+    ("graphite-50A", 2, 0, 1536), ("graphite-50A", 2, 2048, 2048),
+    ("si-100A", 1, 0, 2560), ("si-100A", 1, 4096, 4096),
+    ("lamellar-200A", 1, 0, 5120), ("lamellar-200A", 1, 8192, 8192)])
+def test_plain_mode_large_transforms(name, n_phi, force, expect_m):
+    """Plain (full-grid) mode at full workload grid sizes: the automatic
+    1536-, 2560- and 5120-point transforms and forced 2048-, 4096- and
+    8192-point ones against the oracle's numpy fftn."""
     structs = W.structures(name)
     xyz, el, _ = structs[0]
     w = W.WORKLOADS[name]
@@ -189,7 +191,7 @@ def test_plain_mode_large_transforms(name, n_phi, expect_m):
     ref = O.voxelgrid([(xyz, fv)], w["r"], w["dq"], w["max_q"], phis,
                       w["fill_bkg"], w["smooth"])
     got = gpu_run(geom, [(xyz, fv, None)], phis, w["fill_bkg"], w["smooth"],
-                  mode="plain")
+                  mode="plain", fft_y=force, fft_z=force)
     assert got["info"]["My"] == expect_m
     assert np.array_equal(got["counts"], ref["count"])
     assert rel_l2(got["iq"], ref["iq"]) <= RTOL
@@ -223,3 +225,22 @@ def test_deposit_window_bit_exact(name, n_phi):
             ref = grid[np.ix_(zi, yi)]
             assert np.array_equal(win.astype(np.complex128), ref), (t, phi)
             assert np.abs(ref).sum() == np.abs(grid).sum()  # window holds all
+
+
+FFT_SIZES = [128, 256, 384, 512, 640, 768, 1024, 1280, 1536, 2048, 2560,
+             3072, 4096, 5120, 6144, 8192]
+
+
+@pytest.mark.parametrize("m", FFT_SIZES)
+def test_every_transform_length(m):
+    """Each supported chirp-z length (2^k, 3*2^k, 5*2^k: radix-16/8/4/2
+    passes plus a radix-3 or radix-5 pass) forced on both axes of a small
+    smoothed case gives the oracle's I(q)."""
+    xyz, fv = small_case(seed=4)
+    geom = F.VoxelGeometry(0.5, 0.15, 1.5)
+    phis = np.array([0.0, 31.0, 90.0, 151.0])
+    ref = O.voxelgrid([(xyz, fv)], 0.5, 0.15, 1.5, phis, False, 1.5)
+    got = gpu_run(geom, [(xyz, fv, None)], phis, False, 1.5, fft_y=m, fft_z=m)
+    assert (got["info"]["My"], got["info"]["Mz"]) == (m, m)
+    assert np.array_equal(got["counts"], ref["count"])
+    assert rel_l2(got["iq"], ref["iq"]) <= RTOL
