@@ -175,11 +175,22 @@ __global__ void k_yminmax(SliceArgs a, int slice0) {
   }
   const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
   unsigned long long lo = ~0ULL, hi = 0ULL;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long v = dbl_ord(rot_y(a.xyz_s + 3 * (s.atom_begin + i), c, sn));
-    lo = min(lo, v);
-    hi = max(hi, v);
+  const int2 co = a.cand_off ? a.cand_off[t] : make_int2(0, -1);
+  if (co.y >= 0) {
+    // only the atoms near the (x, y) hull can hold the extremes
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < co.y;
+         i += gridDim.x * blockDim.x) {
+      const unsigned long long v = dbl_ord(rot_y(a.xyz + 3 * (size_t)a.cand[co.x + i], c, sn));
+      lo = min(lo, v);
+      hi = max(hi, v);
+    }
+  } else {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+         i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+      const unsigned long long v = dbl_ord(rot_y(a.xyz_s + 3 * (s.atom_begin + i), c, sn));
+      lo = min(lo, v);
+      hi = max(hi, v);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
@@ -756,6 +767,8 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
   a.xyz_s = P->d_xyz_s; a.f_s = P->d_f_s; a.rowstart = P->d_rowstart;
   a.xy32_s = P->d_xy32_s; a.fz_s = P->d_fz_s; a.bil = P->bil;
+  a.cand = P->d_cand;
+  a.cand_off = P->d_cand_off;
   a.zstat = P->d_zstat; a.ymax_ord = P->d_ymax; a.extflag = P->d_extflag;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
   a.ext = P->d_ext; a.amo = P->d_amo; a.my = P->d_my;
@@ -879,7 +892,10 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
   const int nblk_at = atom_blocks(P);
   {
     gw::KTimer tm(ctx, GW_K_DEPOSIT);
-    k_yminmax<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+    const int nblk_mm = P->cand_max >= 0
+        ? (int)std::min<int64_t>(std::max<int64_t>(1, (P->cand_max + 255) / 256), nblk_at)
+        : nblk_at;
+    k_yminmax<<<dim3(nblk_mm, n), 256, 0, st>>>(a, s0);
     GW_LAUNCHED(ctx);
   }
   {
@@ -1169,11 +1185,67 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
                   P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
                   P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_fz_s,
-                  P->d_perm, P->d_zhist, P->d_rowstart,
+                  P->d_perm, P->d_cand, P->d_cand_off, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
+}
+
+// Atoms of one structure that can hold the minimum or maximum of the
+// rotated y = x sin(phi) + y cos(phi) for some phi: the minimum of a linear
+// function over the atoms is attained on the convex hull of their (x, y)
+// projection, and an atom farther than D inside the hull exceeds the
+// minimum by more than D for every direction.  D = 1e-9 (1 + max|x|,|y|)
+// is far above the float64 rounding of the rotated coordinate (a few ulp of
+// |x| + |y|), so the exact float64 minimum over the candidates equals the
+// minimum over all atoms.  Points on or outside the computed hull (rounding
+// in the hull itself) are candidates too.  Appends input indices to out.
+static void hull_candidates(const double *xyz, int64_t begin, int64_t count,
+                            std::vector<int> &out) {
+  std::vector<int64_t> id(count);
+  for (int64_t i = 0; i < count; ++i) id[i] = begin + i;
+  auto X = [&](int64_t a) { return xyz[3 * a]; };
+  auto Y = [&](int64_t a) { return xyz[3 * a + 1]; };
+  std::sort(id.begin(), id.end(), [&](int64_t a, int64_t b) {
+    return X(a) < X(b) || (X(a) == X(b) && Y(a) < Y(b));
+  });
+  auto cross = [&](int64_t o, int64_t a, int64_t b) {
+    return (X(a) - X(o)) * (Y(b) - Y(o)) - (Y(a) - Y(o)) * (X(b) - X(o));
+  };
+  std::vector<int64_t> h(2 * count + 1);
+  int64_t k = 0;
+  for (int64_t i = 0; i < count; ++i) {  // lower hull
+    while (k >= 2 && cross(h[k - 2], h[k - 1], id[i]) <= 0) --k;
+    h[k++] = id[i];
+  }
+  for (int64_t i = count - 2, lo = k + 1; i >= 0; --i) {  // upper hull
+    while (k >= lo && cross(h[k - 2], h[k - 1], id[i]) <= 0) --k;
+    h[k++] = id[i];
+  }
+  const int64_t nh = k - 1;  // counter-clockwise, last == first
+  if (nh < 3) {
+    for (int64_t i = 0; i < count; ++i) out.push_back((int)(begin + i));
+    return;
+  }
+  double scale = 0.0;
+  for (int64_t i = 0; i < count; ++i)
+    scale = std::max(scale, std::max(std::fabs(X(begin + i)), std::fabs(Y(begin + i))));
+  const double D = 1e-9 * (1.0 + scale);
+  std::vector<double> ex(nh), ey(nh), nx(nh), ny(nh);
+  for (int64_t e = 0; e < nh; ++e) {
+    const double dx = X(h[e + 1]) - X(h[e]), dy = Y(h[e + 1]) - Y(h[e]);
+    const double len = std::sqrt(dx * dx + dy * dy);
+    ex[e] = X(h[e]); ey[e] = Y(h[e]);
+    nx[e] = -dy / len; ny[e] = dx / len;  // inward unit normal
+  }
+  for (int64_t i = 0; i < count; ++i) {
+    const double px = X(begin + i), py = Y(begin + i);
+    double d = HUGE_VAL;
+    for (int64_t e = 0; e < nh && d > D; ++e)
+      d = std::min(d, (px - ex[e]) * nx[e] + (py - ey[e]) * ny[e]);
+    if (d <= D) out.push_back((int)(begin + i));
+  }
 }
 
 extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
@@ -1185,11 +1257,11 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: structure atom range outside the atom arrays");
   if (n != P->n_atoms) {
     void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_f_s,
-                   P->d_xy32_s, P->d_perm, P->d_fz_s};
+                   P->d_xy32_s, P->d_perm, P->d_fz_s, P->d_cand};
     for (void *q : old) gw::dev_free(q);
     P->d_xyz = nullptr; P->d_f = nullptr; P->d_zidx = nullptr;
     P->d_xyz_s = nullptr; P->d_f_s = nullptr; P->d_xy32_s = nullptr;
-    P->d_perm = nullptr; P->d_fz_s = nullptr;
+    P->d_perm = nullptr; P->d_fz_s = nullptr; P->d_cand = nullptr;
     P->n_atoms = -1;
     if (n > INT_MAX / 4)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: more than 2^29 atoms");
@@ -1209,6 +1281,34 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   GW_CUDA(cudaMemcpyAsync(P->d_xyz, xyz, (size_t)n * 3 * sizeof(double), kind, P->ctx->stream));
   GW_CUDA(cudaMemcpyAsync(P->d_f, f, (size_t)n * sizeof(float2), kind, P->ctx->stream));
+  // hull-near atoms per structure (host coordinates only; device-resident
+  // atoms keep the full scan).  The arrays keep their addresses, so a
+  // captured graph stays valid.
+  if (!P->d_cand) GW_CUDA(gw::dev_malloc((void **)&P->d_cand, (size_t)n * sizeof(int)));
+  if (!P->d_cand_off)
+    GW_CUDA(gw::dev_malloc((void **)&P->d_cand_off, P->n_struct * sizeof(int2)));
+  P->cand_host.clear();
+  P->cand_off_host.assign(P->n_struct, make_int2(0, -1));
+  P->cand_max = -1;
+  if (!on_device) {
+    int64_t mx = 0;
+    for (int t = 0; t < P->n_struct; ++t) {
+      const int begin = (int)P->cand_host.size();
+      hull_candidates(xyz, P->structs[t].atom_begin, P->structs[t].atom_count,
+                      P->cand_host);
+      const int cnt = (int)P->cand_host.size() - begin;
+      P->cand_off_host[t] = make_int2(begin, cnt);
+      mx = std::max<int64_t>(mx, cnt);
+    }
+    P->cand_max = mx;
+    if (!P->cand_host.empty())
+      GW_CUDA(cudaMemcpyAsync(P->d_cand, P->cand_host.data(),
+                              P->cand_host.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, P->ctx->stream));
+  }
+  GW_CUDA(cudaMemcpyAsync(P->d_cand_off, P->cand_off_host.data(),
+                          P->n_struct * sizeof(int2), cudaMemcpyHostToDevice,
+                          P->ctx->stream));
   return GW_OK;
 }
 

@@ -37,6 +37,8 @@ struct SliceArgs {
   const float2 *f_s;
   const float2 *xy32_s; // float32 (x, y) of the sorted atoms
   const float *fz_s;   // bilinear: fractional z position of the sorted atoms
+  const int *cand;     // atoms (input order) near each structure's (x,y) hull
+  const int2 *cand_off; // per structure (begin, count); count < 0: all atoms
   const int *rowstart; // per structure: g+2 offsets into the sorted arrays
   const int2 *zstat;   // per structure: (max valid z index, all z valid)
   const gw_structure *st;
@@ -290,6 +292,11 @@ struct gw_voxel_plan {
   float2 *d_f_s = nullptr;
   float *d_fz_s = nullptr;
   int *d_perm = nullptr;   // sorted position -> input atom index
+  int *d_cand = nullptr;   // hull-near atoms of every structure (capacity n)
+  int2 *d_cand_off = nullptr;
+  int64_t cand_max = -1;   // largest per-structure count; < 0: none
+  std::vector<int> cand_host;
+  std::vector<int2> cand_off_host;
   int *d_zhist = nullptr, *d_rowstart = nullptr, *d_cursor = nullptr;
   int2 *d_zstat = nullptr;
   unsigned long long *d_ymax = nullptr;
