@@ -31,11 +31,12 @@ METRIC = "slices/s & s/detector image: batched vs plain on 1 GB300 at <=1e-5 rel
 L2_BYTES = 129 * 1024 * 1024
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# one ncu --set full capture of the kernel on the same workload and batch
-# shape (51-slice batches of si-100A); the summaries with their commands are
-# profiles/k_row_czt_2048_si-100A.md and profiles/k_col_czt_bin_1024_si-100A.md.
-NCU_TRAFFIC = {("si-100A", "row_czt"): (1.6 + 247.2) * 1e6,
-               ("si-100A", "col_czt_bin"): (148.5 + 39.5) * 1e6}
+# one ncu --set full capture of the kernel on the same workload and plan
+# shape (workload, kernel, fft_y, fft_z, batch); the summaries with their
+# commands are profiles/k_row_czt_1280_si-100A.md and
+# profiles/k_col_czt_bin_1024_si-100A.md.
+NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024, 51): (1.49 + 38.11) * 1e6,
+               ("si-100A", "col_czt_bin", 1280, 1024, 51): (148.56 + 39.38) * 1e6}
 
 
 def parse():
@@ -50,6 +51,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-workloads", action="store_true",
                     help="skip the five-workload batched/plain table")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="use the default transform lengths and batch size")
     ap.add_argument("--no-grad", action="store_true",
                     help="skip the forward+backward timing")
     ap.add_argument("--phis", type=int, default=0,
@@ -193,7 +196,7 @@ def run_gb300(args, world, rank, local, pg):
         run_profile(args, w, geom, phis, items, ctx)
         return
     plan = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
-                       smooth=w["smooth"], ctx=ctx)
+                       smooth=w["smooth"], tune=not args.no_tune, ctx=ctx)
     plan.set_atoms()
     plan.execute()
     ctx.synchronize()
@@ -268,7 +271,9 @@ def run_gb300(args, world, rank, local, pg):
 
     # per-kernel device times (eager, instrumented replica of the same work)
     eager = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
-                        smooth=w["smooth"], ctx=ctx)
+                        smooth=w["smooth"], fft_y=plan.params.fft_y,
+                        fft_z=plan.params.fft_z,
+                        batch_slices=plan.params.batch_slices, ctx=ctx)
     eager.set_atoms()
     eager.execute()
     ctx.synchronize()
@@ -346,14 +351,26 @@ def run_gb300(args, world, rank, local, pg):
         avg_ms = ms_tot / max(nl, 1)
         algo = algorithmic_bytes(name, info, w, n_slices, dargs, plan.Qc)
         achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
+        tkey = (args.workload, name, info["My"], info["Mz"], info["batch"])
         roof = {"kernel": name, "bound": "hbm", "achieved": achieved,
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": NCU_TRAFFIC.get((args.workload, name)),
+                "traffic": NCU_TRAFFIC.get(tkey),
                 "traffic_source": "ncu capture (profiles/)"
-                if (args.workload, name) in NCU_TRAFFIC else None,
+                if tkey in NCU_TRAFFIC else None,
                 "avg_launch_ms": avg_ms,
                 "algorithmic_bytes_per_launch": algo}
+        if name in ("row_czt", "col_czt_bin"):
+            # the transforms' own limiter: shared-memory passes
+            m = info["My"] if name == "row_czt" else info["Mz"]
+            units = info["batch"] * (info["Lz"] if name == "row_czt" else info["Nc"])
+            sb = units * 2 * fft_passes(m) * m * 16
+            speak = 152 * 128 * 2070e6 / 1e12
+            roof["shared"] = {"achieved": sb / (avg_ms / 1e3) / 1e12,
+                              "peak": speak, "unit": "TB/s",
+                              "frac": sb / (avg_ms / 1e3) / 1e12 / speak,
+                              "peak_kind": "nominal: 152 SMs x 128 B/clk x 2070 MHz",
+                              "bytes_per_launch": sb}
     kernel_share = {k: {"ms": round(v[0], 4), "launches": v[1]}
                     for k, v in kt.items()}
 
@@ -362,7 +379,8 @@ def run_gb300(args, world, rank, local, pg):
     if not args.no_workloads:
         table = {}
         for name in WORKLOAD_NAMES:
-            table[name] = workload_summary(name, ctx, ts, do_flush)
+            table[name] = workload_summary(name, ctx, ts, do_flush,
+                                           tune=not args.no_tune)
     grad = None if args.no_grad else grad_timing(ctx)
 
     cpu = None
@@ -381,7 +399,7 @@ def run_gb300(args, world, rank, local, pg):
                    "detector_px": w["num_pixels"],
                    "orientations": int(det.n_orient),
                    "l2": "flushed between timed iterations (2x L2 write)",
-                   "plan": info},
+                   "plan": info, "tuned": plan.tuned},
         "s_per_detector_image": {
             "batched": ms_per_step / 1e3 / len(items) + det_ms / 1e3,
             "detector_only_s": det_ms / 1e3,
@@ -403,6 +421,16 @@ WORKLOAD_NAMES = ("graphite-50A", "si-100A", "graphite-64", "si-60A-occ",
                   "lamellar-200A")
 
 
+def fft_passes(m):
+    """Stockham passes of a length-m transform (radix-16 passes, then the
+    power-of-two remainder, then the odd factor 3 or 5)."""
+    odd = m
+    while odd % 2 == 0:
+        odd //= 2
+    l2 = (m // odd).bit_length() - 1
+    return l2 // 4 + (1 if l2 % 4 else 0) + (1 if odd > 1 else 0)
+
+
 def _event_ms(ts, fn, reps, flush=None):
     import torch
     tot = 0.0
@@ -419,7 +447,7 @@ def _event_ms(ts, fn, reps, flush=None):
     return tot / reps
 
 
-def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8):
+def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8, tune=True):
     """Seconds per detector image of one workload: batched (graph replay of
     the voxel stage over all slices + detector) and plain (the per-rotation
     path, timed on n_plain slices and scaled to all slices, + detector)."""
@@ -427,7 +455,7 @@ def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8):
     w, structs, geom, phis, items = load_workload(name)
     n_slices = len(items) * len(phis)
     plan = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
-                       smooth=w["smooth"], ctx=ctx)
+                       smooth=w["smooth"], tune=tune, ctx=ctx)
     plan.set_atoms()
     plan.execute()
     ctx.synchronize()
@@ -471,7 +499,8 @@ def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8):
     plain = (plain_ms + det_ms) / 1e3
     return {"slices": n_slices, "atoms": int(sum(len(x[0]) for x in items)),
             "grid": geom.grid_size, "crop": info["crop"],
-            "fft_y": info["My"], "fft_z": info["Mz"],
+            "fft_y": info["My"], "fft_z": info["Mz"], "batch": info["batch"],
+            "tuned": plan.tuned is not None,
             "voxel_ms": round(vox_ms, 4), "detector_ms": round(det_ms, 4),
             "slices_per_s": n_slices / (vox_ms / 1e3),
             "s_per_image_batched": batched, "s_per_image_plain": plain,

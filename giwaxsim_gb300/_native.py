@@ -36,6 +36,7 @@ EXPORTS = [
     "gw_detector_noalloc", "gw_detector", "gw_gather", "gw_bin_slice",
     "gw_mirror", "gw_f0_scale", "gw_collapse_lengths",
     "gw_detector_backward", "gw_voxel_backward", "gw_voxel_grad_buffer",
+    "gw_ctx_device_name", "gw_ctx_mark", "gw_ctx_elapsed_ms",
 ]
 
 
@@ -148,6 +149,9 @@ def _declare(lib):
         "gw_detector_backward": ([P, P, i32, P, i32], ctypes.c_int),
         "gw_voxel_backward": ([P, P, i32, P, P, P, P], ctypes.c_int),
         "gw_voxel_grad_buffer": ([P, pp], ctypes.c_int),
+        "gw_ctx_device_name": ([P, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+        "gw_ctx_mark": ([P, i32], ctypes.c_int),
+        "gw_ctx_elapsed_ms": ([P, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -211,6 +215,22 @@ class Context:
 
     def launch_count(self):
         return int(lib().gw_ctx_launch_count(self.handle))
+
+    def device_name(self):
+        buf = ctypes.create_string_buffer(256)
+        check(lib().gw_ctx_device_name(self.handle, buf, 256))
+        return buf.value.decode()
+
+    def time_ms(self, fn, reps=1):
+        """Device milliseconds per call of fn() (work on this context's
+        stream), timed between two events on the stream."""
+        check(lib().gw_ctx_mark(self.handle, 0))
+        for _ in range(reps):
+            fn()
+        check(lib().gw_ctx_mark(self.handle, 1))
+        ms = ctypes.c_float()
+        check(lib().gw_ctx_elapsed_ms(self.handle, ctypes.byref(ms)))
+        return ms.value / reps
 
     def set_timing(self, on):
         check(lib().gw_ctx_set_timing(self.handle, int(bool(on))))

@@ -200,6 +200,8 @@ int gw_ctx_destroy(gw_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   gw::collect(c);
   for (cudaEvent_t e : c->ev_free) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->mark)
+    if (e) cudaEventDestroy(e);
   gw::dev_free(c->d_err);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -219,6 +221,32 @@ int gw_ctx_stream(gw_ctx *c, void **stream) {
 }
 
 int64_t gw_ctx_launch_count(gw_ctx *c) { return c ? c->launches : -1; }
+
+int gw_ctx_device_name(gw_ctx *c, char *buf, size_t n) {
+  if (!c || !buf || n == 0) return gw::fail(GW_ERR_ARG, "gw_ctx_device_name: invalid argument");
+  cudaDeviceProp prop;
+  GW_CUDA(cudaGetDeviceProperties(&prop, c->device));
+  snprintf(buf, n, "%s sm_%d%d x%d", prop.name, prop.major, prop.minor,
+           prop.multiProcessorCount);
+  return GW_OK;
+}
+
+int gw_ctx_mark(gw_ctx *c, int32_t slot) {
+  if (!c || slot < 0 || slot > 1) return gw::fail(GW_ERR_ARG, "gw_ctx_mark: invalid argument");
+  GW_CUDA(cudaSetDevice(c->device));
+  if (!c->mark[slot]) GW_CUDA(cudaEventCreate(&c->mark[slot]));
+  GW_CUDA(cudaEventRecord(c->mark[slot], c->stream));
+  return GW_OK;
+}
+
+int gw_ctx_elapsed_ms(gw_ctx *c, float *ms) {
+  if (!c || !ms) return gw::fail(GW_ERR_ARG, "gw_ctx_elapsed_ms: null argument");
+  if (!c->mark[0] || !c->mark[1])
+    return gw::fail(GW_ERR_STATE, "gw_ctx_elapsed_ms: marks 0 and 1 not recorded");
+  GW_CUDA(cudaEventSynchronize(c->mark[1]));
+  GW_CUDA(cudaEventElapsedTime(ms, c->mark[0], c->mark[1]));
+  return GW_OK;
+}
 
 int gw_rotate_points(const double *R, const double *pts, int64_t n,
                      double *out) {

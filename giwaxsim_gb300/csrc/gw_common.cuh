@@ -128,6 +128,7 @@ struct gw_ctx {
   std::vector<Pending> pending;
   double kms[GW_K_COUNT] = {};
   int64_t kn[GW_K_COUNT] = {};
+  cudaEvent_t mark[2] = {nullptr, nullptr};  // gw_ctx_mark / gw_ctx_elapsed_ms
 };
 
 namespace gw {

@@ -139,9 +139,24 @@ class VoxelPlan:
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
                  batch_slices=0, constants=None, deposit="nearest", fft_y=0,
-                 fft_z=0, ctx=None):
+                 fft_z=0, tune=False, ctx=None):
         self.geom = geom
         self.ctx = ctx or N.default_context()
+        self.tuned = None
+        if tune and mode == "batched":
+            from . import autotune
+
+            def make(**choice):
+                return VoxelPlan(geom, structures, phis=phis, fill_bkg=fill_bkg,
+                                 smooth=smooth, mode=mode, accum=accum,
+                                 average=average, f0_element=f0_element,
+                                 constants=constants, deposit=deposit,
+                                 ctx=self.ctx, **choice)
+
+            self.tuned = autotune.tune(make, len(structures), fill_bkg, smooth,
+                                       deposit, ctx=self.ctx)
+            fft_y, fft_z = self.tuned["fft_y"], self.tuned["fft_z"]
+            batch_slices = self.tuned["batch_slices"]
         self.phis = geom.auto_phis if phis is None else np.asarray(phis, np.float64)
         if len(self.phis) < 1:
             raise ValueError("at least one phi is required")

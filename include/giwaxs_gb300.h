@@ -58,6 +58,13 @@ int gw_ctx_stream(gw_ctx *ctx, void **stream);
 /* Number of kernels this library launched on the context so far (graph
  * replays count the kernels inside the graph). */
 int64_t gw_ctx_launch_count(gw_ctx *ctx);
+/* "<device name> sm_XY xN" of the context's device (keys tuning caches). */
+int gw_ctx_device_name(gw_ctx *ctx, char *buf, size_t n);
+/* Device-side stopwatch on the context stream: record mark 0 and mark 1
+ * (gw_ctx_mark), then gw_ctx_elapsed_ms waits for mark 1 and returns the
+ * time between them. */
+int gw_ctx_mark(gw_ctx *ctx, int32_t slot);
+int gw_ctx_elapsed_ms(gw_ctx *ctx, float *ms);
 
 /* Per-kernel device timing.  When on, every kernel launch of the library on
  * this context is bracketed by CUDA events on the context stream (eager

@@ -244,3 +244,21 @@ def test_every_transform_length(m):
     assert (got["info"]["My"], got["info"]["Mz"]) == (m, m)
     assert np.array_equal(got["counts"], ref["count"])
     assert rel_l2(got["iq"], ref["iq"]) <= RTOL
+
+
+def test_autotuned_plan_vs_oracle(tmp_path, monkeypatch):
+    """A tuned plan (lengths and batch chosen by timing) gives the oracle's
+    I(q); the choice is cached for the next plan of the same shape."""
+    monkeypatch.setenv("GIWAXSIM_GB300_TUNE_CACHE", str(tmp_path / "t.json"))
+    xyz, fv = small_case(seed=6)
+    geom = F.VoxelGeometry(0.5, 0.15, 1.5)
+    phis = np.linspace(0.0, 180.0, 24, endpoint=False)
+    ref = O.voxelgrid([(xyz, fv)], 0.5, 0.15, 1.5, phis, False, 1.5)
+    got = gpu_run(geom, [(xyz, fv, None)], phis, False, 1.5, tune=True)
+    plan = got["plan"]
+    assert set(plan.tuned) == {"fft_y", "fft_z", "batch_slices"}
+    assert (got["info"]["My"], got["info"]["Mz"]) == (plan.tuned["fft_y"],
+                                                      plan.tuned["fft_z"])
+    assert np.array_equal(got["counts"], ref["count"])
+    assert rel_l2(got["iq"], ref["iq"]) <= RTOL
+    assert (tmp_path / "t.json").exists()
