@@ -275,7 +275,12 @@ struct PlaneArgs {
   int nu, nv;
   const float *P;
 };
-constexpr int kPlTW = 32, kPlTH = 16, kPlThreads = 256;
+// The two free rows of an orientation's affine map, packed for three
+// 16-byte shared loads: (A_u, b_u), (A_v, b_v), (d_u, d_v, w, -).
+struct PlaneOrient {
+  float4 u, v, e;
+};
+constexpr int kPlTW = 32, kPlTH = 32, kPlThreads = 512;
 constexpr size_t kPlaneSmemMax = 200 * 1024;
 
 __global__ void k_plane_extract(DetArgs a, PlaneArgs pa, float *P) {
@@ -290,22 +295,22 @@ __global__ void k_plane_extract(DetArgs a, PlaneArgs pa, float *P) {
   }
 }
 
-__device__ __forceinline__ bool plane_index(const OrientFast &T,
+// Same operation order as fast_index on those rows.
+__device__ __forceinline__ bool plane_index(const PlaneOrient &T,
                                             const PlaneArgs &pa, float x,
                                             float y, float z, int &iu,
                                             int &iv) {
-  const float *Au = T.A + 3 * pa.ua, *Av = T.A + 3 * pa.va;
-  const float tu = fmaf(Au[0], x, fmaf(Au[1], y, fmaf(Au[2], z, T.b[pa.ua])));
-  const float tv = fmaf(Av[0], x, fmaf(Av[1], y, fmaf(Av[2], z, T.b[pa.va])));
-  return fast_axis(tu, T.d[pa.ua], pa.nu, iu) & fast_axis(tv, T.d[pa.va], pa.nv, iv);
+  const float tu = fmaf(T.u.x, x, fmaf(T.u.y, y, fmaf(T.u.z, z, T.u.w)));
+  const float tv = fmaf(T.v.x, x, fmaf(T.v.y, y, fmaf(T.v.z, z, T.v.w)));
+  return fast_axis(tu, T.e.x, pa.nu, iu) & fast_axis(tv, T.e.y, pa.nv, iv);
 }
 
 template <bool SMEM>
 __global__ void __launch_bounds__(kPlThreads)
-k_detector_plane(DetArgs a, const OrientFast *ot, PlaneArgs pa,
+k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
                  double *acc_out, int2 *wl, int *wl_count, int wl_cap) {
   extern __shared__ float s_plane[];
-  __shared__ OrientFast s_ot[kDetChunk];
+  __shared__ PlaneOrient s_ot[kDetChunk];
   constexpr int KP = kPlTH * kPlTW / kPlThreads;  // pixels per thread
   const int lane = threadIdx.x & 31;
   const int tiles_x = (a.nh + kPlTW - 1) / kPlTW;
@@ -336,11 +341,11 @@ k_detector_plane(DetArgs a, const OrientFast *ot, PlaneArgs pa,
   for (int c0 = 0; c0 < a.n_orient; c0 += kDetChunk) {
     const int nc = min(kDetChunk, a.n_orient - c0);
     __syncthreads();
-    for (int t = threadIdx.x; t < nc * kOrientFloats; t += kPlThreads)
-      reinterpret_cast<float *>(s_ot)[t] = reinterpret_cast<const float *>(ot + c0)[t];
+    for (int t = threadIdx.x; t < nc * 3; t += kPlThreads)
+      reinterpret_cast<float4 *>(s_ot)[t] = reinterpret_cast<const float4 *>(ot + c0)[t];
     __syncthreads();
     for (int oo = 0; oo < nc; ++oo) {
-      const OrientFast &T = s_ot[oo];
+      const PlaneOrient T = s_ot[oo];
       const int o = c0 + oo;
 #pragma unroll
       for (int k = 0; k < KP; ++k) {
@@ -367,7 +372,7 @@ k_detector_plane(DetArgs a, const OrientFast *ot, PlaneArgs pa,
           base_point(a, pix[k] / a.nh, pix[k] % a.nh, x, y, z);
           v = __ldg(a.iq + gather_index(a, o, x, y, z));
         }
-        if (valid[k] && (ok || inline_exact)) part[k] = fmaf(v, T.w, part[k]);
+        if (valid[k] && (ok || inline_exact)) part[k] = fmaf(v, T.e.z, part[k]);
       }
       if ((o + 1) % kDetFlush == 0) {
 #pragma unroll
@@ -499,6 +504,7 @@ struct gw_detector_plan {
   double *d_gout = nullptr, *d_gpix = nullptr, *d_giq = nullptr;  // adjoint
   PlaneArgs plane{-1, -1, 0, 0, 0, 0, nullptr};  // plane mode when fa >= 0
   float *d_plane = nullptr;
+  PlaneOrient *d_po = nullptr;
   bool executed = false;
 };
 
@@ -683,6 +689,17 @@ extern "C" int gw_detector_plan_create(gw_ctx *ctx, const gw_detector_params *p,
         }
         pa.P = P->d_plane;
         P->plane = pa;
+        std::vector<PlaneOrient> po(n_orient);
+        for (int o = 0; o < n_orient; ++o) {
+          const OrientFast &T = ot[o];
+          po[o].u = make_float4(T.A[3 * pa.ua], T.A[3 * pa.ua + 1], T.A[3 * pa.ua + 2], T.b[pa.ua]);
+          po[o].v = make_float4(T.A[3 * pa.va], T.A[3 * pa.va + 1], T.A[3 * pa.va + 2], T.b[pa.va]);
+          po[o].e = make_float4(T.d[pa.ua], T.d[pa.va], T.w, 0.f);
+        }
+        if ((st = up(&P->d_po, po.data(), po.size()))) {
+          gw_detector_plan_destroy(P);
+          return st;
+        }
       }
     }
   }
@@ -694,7 +711,8 @@ extern "C" int gw_detector_plan_destroy(gw_detector_plan *P) {
   if (!P) return GW_OK;
   void *ptrs[] = {P->d_h, P->d_v, P->d_init, P->d_rot, P->d_w, P->d_rs,
                   P->d_rn, P->d_iq_own, P->d_acc, P->d_out, P->d_ot, P->d_wl,
-                  P->d_wl_count, P->d_gout, P->d_gpix, P->d_giq, P->d_plane};
+                  P->d_wl_count, P->d_gout, P->d_gpix, P->d_giq, P->d_plane,
+                  P->d_po};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -768,10 +786,10 @@ extern "C" int gw_detector_execute(gw_detector_plan *P) {
           attr = true;
         }
         k_detector_plane<true><<<tiles, kPlThreads, smem, P->ctx->stream>>>(
-            a, P->d_ot, pa, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);
+            a, P->d_po, pa, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);
       } else {
         k_detector_plane<false><<<tiles, kPlThreads, 0, P->ctx->stream>>>(
-            a, P->d_ot, pa, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);
+            a, P->d_po, pa, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);
       }
       GW_LAUNCHED(P->ctx);
     } else {

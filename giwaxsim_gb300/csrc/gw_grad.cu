@@ -206,7 +206,9 @@ k_col_bwd(SliceArgs a, CztArgs cz, BinArgs bn, GradCol gc, int slice0, int nc,
   const int *cofs = bn.colofs + (size_t)p * nc;
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   __syncthreads();
-  ColLoadF1 ld{F1 + (size_t)slot * a.Lz * nc, cz.A, cz.L, nc, m0};
+  int first, rows;
+  slice_rows(a, slice0, sl, first, rows);
+  ColLoadF1 ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
   fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
   fft_run<M, NB, NT, true, 0, true, 0, false>(buf, tw, cz.H, NoLoad(), NoStore());
   const float2 cbg = slice_const(a, sl).cbg;
@@ -255,11 +257,12 @@ template <int M>
 struct RowLoadAdj {
   const SliceArgs *a;
   const GradRow *gr;
+  const int *r_slot, *r_zz;
   int row0, n_rows;
   __device__ float2 operator()(int f, int n) const {
     const int row = row0 + f;
     if (row >= n_rows || n >= gr->nc) return make_float2(0.f, 0.f);
-    const int slot = row / a->Lz, zz = row - slot * a->Lz;
+    const int slot = r_slot[f], zz = r_zz[f];
     const float2 g = gr->G1[((size_t)slot * gr->nc + n) * a->Lz + zz];
     return cmul(conjf2(g), __ldg(gr->Aa + n));
   }
@@ -269,14 +272,14 @@ struct RowLoadAdj {
 // the rows gather G_D at their cells; per-row sums go to the slice scalars.
 template <int M, bool BIL>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
-k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_rows) {
+k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_sl, int n_rows) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   constexpr int TWL = FftPlan<M>::tw_len();
   constexpr int LDM = FftPlan<M>::LDM;
   extern __shared__ float2 smem[];
   float2 *tw = smem;
   float2 *buf = smem + TWL;
-  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1];
+  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1], r_slot[NB], r_zz[NB];
   __shared__ float racc[NB][7];
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = gr.tw[t];
   const int row0 = blockIdx.x * NB;
@@ -285,21 +288,23 @@ k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_rows) {
     int acc = 0;
     for (int f = 0; f < NB; ++f) {
       const int row = row0 + f;
-      int lo = 0, mid = 0, hi = 0;
+      int lo = 0, mid = 0, hi = 0, slot = 0, zz = 0;
       if (row < n_rows) {
-        const int slot = row / a.Lz, zz = row % a.Lz;
+        row_slot(a, slice0, n_sl, row, slot, zz);
         const int sl = slice0 + slot, t = sl / a.n_phi;
         row_atoms(a, t, zz, lo, mid, hi);
       }
       r_lo[f] = lo;
       r_mid[f] = mid;
       r_cnt[f] = acc;
+      r_slot[f] = slot;
+      r_zz[f] = zz;
       acc += hi - lo;
     }
     r_cnt[NB] = acc;
   }
   __syncthreads();
-  RowLoadAdj<M> ld{&a, &gr, row0, n_rows};
+  RowLoadAdj<M> ld{&a, &gr, r_slot, r_zz, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
   fft_run<M, NB, NT, true, 0, true, 0, false>(buf, tw, gr.Ha, NoLoad(), NoStore());
   // G_D on the window, and the per-row sums of G_D m and G_D dm/dsigma
@@ -311,7 +316,7 @@ k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_rows) {
     const float2 v = conjf2(cmul(*q, __ldg(gr.Ba + yy)));
     *q = v;
     if (a.smooth_on) {
-      const int slot = row / a.Lz, zz = row - slot * a.Lz;
+      const int slot = r_slot[f], zz = r_zz[f];
       const float mz = a.mz[(size_t)slot * a.Lz + zz], my = a.my[(size_t)slot * a.Ly + yy];
       const float dm = gr.dmz[(size_t)slot * a.Lz + zz] * my +
                        mz * gr.dmy[(size_t)slot * a.Ly + yy];
@@ -328,8 +333,7 @@ k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_rows) {
     int f = 0;
     while (f + 1 < NB && i >= r_cnt[f + 1]) ++f;
     const int at = r_lo[f] + (i - r_cnt[f]);
-    const int row = row0 + f;
-    const int slot = row / a.Lz, zz = row - slot * a.Lz;
+    const int slot = r_slot[f], zz = r_zz[f];
     const int sl = slice0 + slot;
     const float mz = a.smooth_on ? a.mz[(size_t)slot * a.Lz + zz] : 1.f;
     const float dmz = a.smooth_on ? gr.dmz[(size_t)slot * a.Lz + zz] : 0.f;
@@ -393,7 +397,7 @@ k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_rows) {
   if (threadIdx.x < NB) {
     const int f = threadIdx.x, row = row0 + f;
     if (row < n_rows) {
-      const int sl = slice0 + row / a.Lz;
+      const int sl = slice0 + r_slot[f];
       double *s = gr.sc + (size_t)sl * SC_N;
       if (a.smooth_on) {
         atomicAdd(s + SC_SM_RE, (double)racc[f][0]);
@@ -451,7 +455,8 @@ int launch_col_bwd(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
 
 template <int M, bool BIL>
 int launch_row_bwd_t(gw_voxel_plan *P, const SliceArgs &a, const GradRow &gr,
-                     int s0, int n_rows) {
+                     int s0, int n_sl) {
+  const int n_rows = batch_rows(P, s0, n_sl);
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = fft_smem<M>();
   static bool attr = false;
@@ -461,16 +466,17 @@ int launch_row_bwd_t(gw_voxel_plan *P, const SliceArgs &a, const GradRow &gr,
     attr = true;
   }
   gw::KTimer tm(P->ctx, GW_K_ROW);
-  k_row_bwd<M, BIL><<<(n_rows + NB - 1) / NB, NT, smem, P->ctx->stream>>>(a, gr, s0, n_rows);
+  k_row_bwd<M, BIL><<<(n_rows + NB - 1) / NB, NT, smem, P->ctx->stream>>>(a, gr, s0, n_sl,
+                                                                          n_rows);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
 }
 
 template <int M>
 int launch_row_bwd(gw_voxel_plan *P, const SliceArgs &a, const GradRow &gr,
-                   int s0, int n_rows) {
-  return a.bil ? launch_row_bwd_t<M, true>(P, a, gr, s0, n_rows)
-               : launch_row_bwd_t<M, false>(P, a, gr, s0, n_rows);
+                   int s0, int n_sl) {
+  return a.bil ? launch_row_bwd_t<M, true>(P, a, gr, s0, n_sl)
+               : launch_row_bwd_t<M, false>(P, a, gr, s0, n_sl);
 }
 
 int col_bwd_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
@@ -478,8 +484,8 @@ int col_bwd_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   GW_DISPATCH_M(P->Mz, launch_col_bwd, P, a, cz, bn, gc, s0, n)
 }
 int row_bwd_dispatch(gw_voxel_plan *P, const SliceArgs &a, const GradRow &gr,
-                     int s0, int n_rows) {
-  GW_DISPATCH_M(P->My, launch_row_bwd, P, a, gr, s0, n_rows)
+                     int s0, int n_sl) {
+  GW_DISPATCH_M(P->My, launch_row_bwd, P, a, gr, s0, n_sl)
 }
 
 int grad_state_init(gw_voxel_plan *P) {
@@ -629,9 +635,9 @@ extern "C" int gw_voxel_backward(gw_voxel_plan *P, const double *g_iq,
       k_argmin_y<<<dim3(nblk_at, nb), 256, 0, st>>>(a, s0, P->d_perm, G->d_amy);
       GW_LAUNCHED(ctx);
     }
-    GW_TRY(row_dispatch(P, a, cy, s0, nb * P->Lz));
+    GW_TRY(row_dispatch(P, a, cy, s0, nb));
     GW_TRY(col_bwd_dispatch(P, a, cz, bn, gc, s0, nb));
-    GW_TRY(row_bwd_dispatch(P, a, gr, s0, nb * P->Lz));
+    GW_TRY(row_bwd_dispatch(P, a, gr, s0, nb));
   }
   {
     gw::KTimer tm(ctx, GW_K_MISC);

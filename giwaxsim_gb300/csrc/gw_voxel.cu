@@ -302,8 +302,9 @@ __global__ void k_profile(SliceArgs a, int slice0) {
         dev_error(a.err, GW_DEVERR_MASK_WRAP);
     }
     if (threadIdx.x == 0 && a.Lz < a.g) {
+      const int rows = a.roff ? a.roff[sl + 1] - a.roff[sl] : a.Lz;
       int l = a.z_lo - 1; if (l < 0) l += a.g;
-      int r = a.z_lo + a.Lz; r %= a.g; if (r < 0) r += a.g;
+      int r = a.z_lo + rows; r %= a.g; if (r < 0) r += a.g;
       if (smooth_at(l, zs, ze, a.g, a.radius, a.gw) != 0.f ||
           smooth_at(r, zs, ze, a.g, a.radius, a.gw) != 0.f)
         dev_error(a.err, GW_DEVERR_MASK_WRAP);
@@ -326,11 +327,12 @@ struct RowLoad {
   const SliceArgs *a;
   const CztArgs *cz;
   const float2 *rows;  // row f at rows + f * LDM
+  const int *r_slot, *r_zz;  // per block row: slot and window row
   int slice0, row0, n_rows;
   __device__ float2 operator()(int f, int n) const {
     const int row = row0 + f;
     if (row >= n_rows || n >= cz->L) return make_float2(0.f, 0.f);
-    const int slot = row / a->Lz, zz = row % a->Lz;
+    const int slot = r_slot[f], zz = r_zz[f];
     const int sl = slice0 + slot;
     const SliceConst k = slice_const(*a, sl);
     const float2 dep = rows[f * FftPlan<M>::LDM + n];
@@ -363,15 +365,15 @@ __device__ __forceinline__ void deposit_at(const SliceArgs &a, float2 *row,
 
 template <int M, bool BIL>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
-k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
-          float2 *F1) {
+k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
+          int nc_out, float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   constexpr int TWL = FftPlan<M>::tw_len();
   constexpr int LDM = FftPlan<M>::LDM;
   extern __shared__ float2 smem[];
   float2 *tw = smem;
   float2 *buf = smem + TWL;
-  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1];
+  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1], r_slot[NB], r_zz[NB];
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   for (int t = threadIdx.x; t < NB * LDM; t += NT) buf[t] = make_float2(0.f, 0.f);
   const int row0 = blockIdx.x * NB;
@@ -379,9 +381,9 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
     int acc = 0;
     for (int f = 0; f < NB; ++f) {
       const int row = row0 + f;
-      int lo = 0, mid = 0, hi = 0;
+      int lo = 0, mid = 0, hi = 0, slot = 0, zz = 0;
       if (row < n_rows) {
-        const int slot = row / a.Lz, zz = row % a.Lz;
+        row_slot(a, slice0, n_sl, row, slot, zz);
         const int sl = slice0 + slot, t = sl / a.n_phi;
         if (a.ext[sl].y < 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
         row_atoms(a, t, zz, lo, mid, hi);
@@ -389,6 +391,8 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
       r_lo[f] = lo;
       r_mid[f] = mid;
       r_cnt[f] = acc;
+      r_slot[f] = slot;
+      r_zz[f] = zz;
       acc += hi - lo;
     }
     r_cnt[NB] = acc;
@@ -399,7 +403,7 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
     int f = 0;
     while (f + 1 < NB && i >= r_cnt[f + 1]) ++f;
     const int at = r_lo[f] + (i - r_cnt[f]);
-    const int sl = slice0 + (row0 + f) / a.Lz;
+    const int sl = slice0 + r_slot[f];
     if constexpr (!BIL) {
       int yy;
       if (deposit_column(a, at, sl, yy)) {
@@ -424,7 +428,7 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_rows, int nc_out,
     }
   }
   __syncthreads();
-  RowLoad<M> ld{&a, &cz, buf, slice0, row0, n_rows};
+  RowLoad<M> ld{&a, &cz, buf, r_slot, r_zz, slice0, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false>(buf, tw, nullptr, ld, NoStore());
   RowStore stv{cz.B, F1, row0, n_rows, nc_out};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), stv);
@@ -502,7 +506,9 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
   if (!any) return;
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   __syncthreads();
-  ColLoad ld{F1 + (size_t)slot * a.Lz * nc, cz.A, cz.L, nc, m0};
+  int first, rows;
+  slice_rows(a, slice0, sl, first, rows);
+  ColLoad ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
   fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
   ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), st);
@@ -581,6 +587,66 @@ __global__ void k_finalize(const double *sum, const float2 *sumk, int kahan,
     const double I = s * (double)scale;
     out64[obase + iz] = I;
     out32[obase + iz] = (float)I;
+  }
+}
+
+// Batched-mode finalize: the window is the crop (W = Qc, offset 0), so sum
+// and output share the flat index; each thread takes two consecutive voxels
+// with 16-byte loads and stores.  Same per-voxel arithmetic as k_finalize.
+__global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan,
+                                const unsigned int *C2, const int *C1, int Qc,
+                                float inv_nstruct, const float *f0tab,
+                                int use_f0, float f0_c, float f0_invz,
+                                double *out64, float *out32) {
+  const int n = Qc * Qc * Qc;  // < 2^31 (checked by the caller)
+  const int npair = (n + 1) / 2;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npair;
+       p += gridDim.x * blockDim.x) {
+    const int i0 = 2 * p;
+    const bool two = i0 + 1 < n;
+    // (line, iz) of the pair's first voxel; the second is the next voxel
+    const int line0 = i0 / Qc, iz0 = i0 - line0 * Qc;
+    double s[2] = {0.0, 0.0};
+    if (kahan) {
+      for (int e = 0; e < 2; ++e)
+        if (e == 0 || two) {
+          const float2 sc = sumk[i0 + e];
+          s[e] = (double)sc.x - (double)sc.y;
+        }
+    } else if (two) {
+      const double2 v = reinterpret_cast<const double2 *>(sum)[p];
+      s[0] = v.x; s[1] = v.y;
+    } else {
+      s[0] = sum[i0];
+    }
+    double I[2] = {0.0, 0.0};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      if (e == 1 && !two) break;
+      int line = line0, iz = iz0 + e;
+      if (iz == Qc) { iz = 0; ++line; }
+      const unsigned cnt = C2[line] * (unsigned)C1[iz];
+      float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
+      if (use_f0) {
+        const int iy = line / Qc, ix = line - iy * Qc;
+        float acc = f0_c;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float *t = f0tab + k * 3 * Qc;
+          acc += (t[ix] * t[Qc + iy]) * t[2 * Qc + iz];
+        }
+        const float fq = acc * f0_invz;
+        scale *= fq * fq;
+      }
+      I[e] = s[e] * (double)scale;
+    }
+    if (two) {
+      reinterpret_cast<double2 *>(out64)[p] = make_double2(I[0], I[1]);
+      reinterpret_cast<float2 *>(out32)[p] = make_float2((float)I[0], (float)I[1]);
+    } else {
+      out64[i0] = I[0];
+      out32[i0] = (float)I[0];
+    }
   }
 }
 
@@ -758,6 +824,11 @@ bool fft_size_supported(int m) {
   return false;
 }
 
+int batch_rows(gw_voxel_plan *P, int s0, int n) {
+  if (P->roff_host.empty()) return n * P->Lz;
+  return P->roff_host[s0 + n] - P->roff_host[s0];
+}
+
 SliceArgs slice_args(gw_voxel_plan *P) {
   SliceArgs a{};
   a.g = P->g; a.r = P->r; a.inv_r = P->inv_r; a.n_phi = P->n_phi;
@@ -769,6 +840,7 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.xy32_s = P->d_xy32_s; a.fz_s = P->d_fz_s; a.bil = P->bil;
   a.cand = P->d_cand;
   a.cand_off = P->d_cand_off;
+  a.roff = P->d_roff;
   a.zstat = P->d_zstat; a.ymax_ord = P->d_ymax; a.extflag = P->d_extflag;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
   a.ext = P->d_ext; a.amo = P->d_amo; a.my = P->d_my;
@@ -778,7 +850,8 @@ SliceArgs slice_args(gw_voxel_plan *P) {
 
 template <int M, bool BIL>
 int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-                 int slice0, int n_rows) {
+                 int slice0, int n_sl) {
+  const int n_rows = batch_rows(P, slice0, n_sl);
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
   static bool attr = false;
@@ -790,17 +863,17 @@ int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   }
   const int blocks = (n_rows + NB - 1) / NB;
   gw::KTimer tm(P->ctx, GW_K_ROW);
-  k_row_czt<M, BIL><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_rows,
-                                                          P->Nc, P->d_F1);
+  k_row_czt<M, BIL><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_sl,
+                                                          n_rows, P->Nc, P->d_F1);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
 }
 
 template <int M>
 int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-               int slice0, int n_rows) {
-  return a.bil ? launch_row_t<M, true>(P, a, cz, slice0, n_rows)
-               : launch_row_t<M, false>(P, a, cz, slice0, n_rows);
+               int slice0, int n_sl) {
+  return a.bil ? launch_row_t<M, true>(P, a, cz, slice0, n_sl)
+               : launch_row_t<M, false>(P, a, cz, slice0, n_sl);
 }
 
 template <int M>
@@ -844,7 +917,6 @@ int enqueue_prep(gw_voxel_plan *P) {
   cudaStream_t st = ctx->stream;
   k_ext_init<<<(P->n_slices + 255) / 256, 256, 0, st>>>(P->d_ext, P->n_slices);
   GW_LAUNCHED(ctx);
-  GW_CUDA(cudaMemsetAsync(P->d_C2, 0, (size_t)P->W * P->W * sizeof(unsigned), st));
   GW_CUDA(cudaMemsetAsync(P->d_zmin, 0xff, P->n_struct * sizeof(unsigned long long), st));
   GW_CUDA(cudaMemsetAsync(P->d_ymin, 0xff, P->n_slices * sizeof(unsigned long long), st));
   GW_CUDA(cudaMemsetAsync(P->d_ymax, 0, P->n_slices * sizeof(unsigned long long), st));
@@ -875,14 +947,6 @@ int enqueue_prep(gw_voxel_plan *P) {
         P->d_cursor, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_perm, P->d_fz_s);
     GW_LAUNCHED(ctx);
   }
-  {
-    gw::KTimer tm(ctx, GW_K_TABLES);
-    k_col_tables<<<P->n_phi, 256, 0, st>>>(P->d_phis, P->g, P->k0, P->Nc,
-                                           P->p.q_min, P->p.q_max, P->dq,
-                                           P->inv_dq, P->wlo, P->whi, P->W,
-                                           P->d_colofs, P->d_C2);
-    GW_LAUNCHED(ctx);
-  }
   return GW_OK;
 }
 
@@ -905,7 +969,9 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
   }
   {
     gw::KTimer tm(ctx, GW_K_DEPOSIT);
-    k_ext_exact<<<dim3(nblk_at, n), 256, 0, st>>>(a, s0);
+    // rarely needed (a slice with atoms outside the grid): a small grid
+    // that exits at once otherwise
+    k_ext_exact<<<dim3(std::min(nblk_at, 16), n), 256, 0, st>>>(a, s0);
     GW_LAUNCHED(ctx);
   }
   if (a.fill || a.smooth_on) {
@@ -935,20 +1001,29 @@ int enqueue(gw_voxel_plan *P) {
   for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
     const int n = std::min(P->S, P->n_slices - s0);
     GW_TRY(enqueue_slice_setup(P, a, s0, n));
-    GW_TRY(row_dispatch(P, a, cy, s0, n * P->Lz));
+    GW_TRY(row_dispatch(P, a, cy, s0, n));
     GW_TRY(col_dispatch(P, a, cz, bn, s0, n));
   }
   const int fin_blocks = P->Qc * P->Qc;
   const float f0c = (float)P->p.f0_coef[8];
   const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
-  {
+  const float inv_ns = P->p.average ? 1.0f / (float)P->n_struct : 1.0f;
+  const int kahan = P->p.accum == GW_ACCUM_KAHAN32;
+  if (P->W == P->Qc && P->lo == P->wlo &&
+      (int64_t)P->Qc * P->Qc * P->Qc < ((int64_t)1 << 31) - 2) {
+    gw::KTimer tm(ctx, GW_K_FINALIZE);
+    const int64_t pairs = ((int64_t)P->Qc * P->Qc * P->Qc + 1) / 2;
+    const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
+    k_finalize_flat<<<blocks, 256, 0, st>>>(
+        P->d_sum, P->d_sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0,
+        P->p.f0_z > 0, f0c, f0iz, P->d_iq64, P->d_iq32);
+    GW_LAUNCHED(ctx);
+  } else {
     gw::KTimer tm(ctx, GW_K_FINALIZE);
     const int fin_threads = P->Qc >= 256 ? 256 : ((P->Qc + 31) / 32) * 32;
     k_finalize<<<fin_blocks, fin_threads, 0, st>>>(
-        P->d_sum, P->d_sumk, P->p.accum == GW_ACCUM_KAHAN32, P->d_C2, P->d_C1,
-        P->W, P->lo - P->wlo, P->Qc,
-        P->p.average ? 1.0f / (float)P->n_struct : 1.0f, P->d_f0,
-        P->p.f0_z > 0, f0c, f0iz, P->d_iq64, P->d_iq32);
+        P->d_sum, P->d_sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo,
+        P->Qc, inv_ns, P->d_f0, P->p.f0_z > 0, f0c, f0iz, P->d_iq64, P->d_iq32);
     GW_LAUNCHED(ctx);
   }
   return GW_OK;
@@ -1069,6 +1144,22 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     P->z_lo = lo_off;
     P->Lz = zbound + tail - lo_off + 1;
     if (P->Lz >= g) { P->Lz = g; P->z_lo = 0; }
+    // structures of uneven height: each keeps the rows of its own z window
+    // (same origin z_lo; the window never wraps the grid when Lz < g)
+    if (P->Lz < g && n_struct > 1) {
+      std::vector<int> lz(n_struct);
+      bool uneven = false;
+      for (int t = 0; t < n_struct; ++t) {
+        const int zb = (int)std::floor(structs[t].z_bound * P->inv_r + 1e-6) + 1;
+        lz[t] = std::min(P->Lz, zb + tail - lo_off + 1);
+        uneven = uneven || lz[t] != P->Lz;
+      }
+      if (uneven) {
+        P->roff_host.assign((size_t)P->n_slices + 1, 0);
+        for (int sl = 0; sl < P->n_slices; ++sl)
+          P->roff_host[sl + 1] = P->roff_host[sl] + lz[sl / n_phi];
+      }
+    }
   }
   // transform lengths: the smallest supported >= L+N-1, or the caller's
   // choice (an autotuner compares the candidates)
@@ -1165,9 +1256,28 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_F1, (size_t)P->S * P->Lz * P->Nc, &B)) ||
       (st = alloc(&P->d_amo, (size_t)P->S * P->Ly, &B)) ||
       (st = alloc(&P->d_my, (size_t)P->S * P->Ly, &B)) ||
-      (st = alloc(&P->d_mz, (size_t)P->S * P->Lz, &B))) {
+      (st = alloc(&P->d_mz, (size_t)P->S * P->Lz, &B)) ||
+      (st = upload(&P->d_roff, P->roff_host, &B))) {
     gw_voxel_plan_destroy(P);
     return st;
+  }
+  // column bin tables and the (qy,qx) count factor: geometry only, made once
+  {
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMemsetAsync(P->d_C2, 0, (size_t)P->W * P->W * sizeof(unsigned), s);
+    if (e == cudaSuccess) {
+      k_col_tables<<<P->n_phi, 256, 0, s>>>(P->d_phis, P->g, P->k0, P->Nc,
+                                           P->p.q_min, P->p.q_max, P->dq,
+                                           P->inv_dq, P->wlo, P->whi, P->W,
+                                           P->d_colofs, P->d_C2);
+      ctx->launches++;
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      gw_voxel_plan_destroy(P);
+      return gw::cuda_fail(e, "column tables", __FILE__, __LINE__);
+    }
   }
   *out = P;
   return GW_OK;
@@ -1185,7 +1295,7 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
                   P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
                   P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_fz_s,
-                  P->d_perm, P->d_cand, P->d_cand_off, P->d_zhist, P->d_rowstart,
+                  P->d_perm, P->d_cand, P->d_cand_off, P->d_roff, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;

@@ -39,6 +39,8 @@ struct SliceArgs {
   const float *fz_s;   // bilinear: fractional z position of the sorted atoms
   const int *cand;     // atoms (input order) near each structure's (x,y) hull
   const int2 *cand_off; // per structure (begin, count); count < 0: all atoms
+  const int *roff;     // per slice: first window row (n_slices+1 entries),
+                       // when structures have their own z windows; else null
   const int *rowstart; // per structure: g+2 offsets into the sorted arrays
   const int2 *zstat;   // per structure: (max valid z index, all z valid)
   const gw_structure *st;
@@ -118,6 +120,39 @@ __device__ __forceinline__ void plateau(const SliceArgs &a, int4 e, int &ys,
   const float sg = a.sigma;
   py_slice((int)ceilf((float)e.x + sg), (int)ceilf((float)e.y - sg), a.g, ys, ye);
   py_slice((int)ceilf((float)e.z + sg), (int)ceilf((float)e.w - sg), a.g, zs, ze);
+}
+
+// Batch-relative window row -> (slot, zz).  Every slice has Lz rows, or,
+// with per-structure windows, roff[s+1] - roff[s] rows.
+__device__ __forceinline__ void row_slot(const SliceArgs &a, int slice0,
+                                         int n_sl, int row, int &slot,
+                                         int &zz) {
+  if (!a.roff) {
+    slot = row / a.Lz;
+    zz = row - slot * a.Lz;
+    return;
+  }
+  const int R = a.roff[slice0] + row;
+  int lo = 0, hi = n_sl - 1;  // last slot whose first row is <= R
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (a.roff[slice0 + mid] <= R) lo = mid;
+    else hi = mid - 1;
+  }
+  slot = lo;
+  zz = R - a.roff[slice0 + lo];
+}
+
+// Window rows of slice sl and the first of them relative to slice0.
+__device__ __forceinline__ void slice_rows(const SliceArgs &a, int slice0,
+                                           int sl, int &first, int &count) {
+  if (!a.roff) {
+    first = (sl - slice0) * a.Lz;
+    count = a.Lz;
+  } else {
+    first = a.roff[sl] - a.roff[slice0];
+    count = a.roff[sl + 1] - a.roff[sl];
+  }
 }
 
 __device__ __forceinline__ int window_row_to_z(const SliceArgs &a, int zz) {
@@ -297,6 +332,8 @@ struct gw_voxel_plan {
   int64_t cand_max = -1;   // largest per-structure count; < 0: none
   std::vector<int> cand_host;
   std::vector<int2> cand_off_host;
+  std::vector<int> roff_host;  // per-slice first window row (n_slices+1)
+  int *d_roff = nullptr;       // null when every slice has Lz rows
   int *d_zhist = nullptr, *d_rowstart = nullptr, *d_cursor = nullptr;
   int2 *d_zstat = nullptr;
   unsigned long long *d_ymax = nullptr;
@@ -316,9 +353,11 @@ SliceArgs slice_args(gw_voxel_plan *P);
 int enqueue_prep(gw_voxel_plan *P);
 // Per-slice min/max, extents and profiles of slices [s0, s0+n).
 int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n);
-// Row transforms of n_rows window rows starting at slice s0, into d_F1.
+// Row transforms of the window rows of slices [s0, s0+n_sl), into d_F1.
 int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-                 int s0, int n_rows);
+                 int s0, int n_sl);
+// Number of window rows of slices [s0, s0+n).
+int batch_rows(gw_voxel_plan *P, int s0, int n);
 void grad_state_destroy(gw_grad_state *g);
 }  // namespace gwv
 
