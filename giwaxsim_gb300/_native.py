@@ -37,6 +37,8 @@ EXPORTS = [
     "gw_mirror", "gw_f0_scale", "gw_collapse_lengths",
     "gw_detector_backward", "gw_voxel_backward", "gw_voxel_grad_buffer",
     "gw_ctx_device_name", "gw_ctx_mark", "gw_ctx_elapsed_ms",
+    "gw_slab_create", "gw_slab_destroy", "gw_slab_info", "gw_slab_get",
+    "gw_slab_device_xyz",
 ]
 
 
@@ -152,6 +154,11 @@ def _declare(lib):
         "gw_ctx_device_name": ([P, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
         "gw_ctx_mark": ([P, i32], ctypes.c_int),
         "gw_ctx_elapsed_ms": ([P, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+        "gw_slab_create": ([P, P, i32, P, P, pp], ctypes.c_int),
+        "gw_slab_destroy": ([P], ctypes.c_int),
+        "gw_slab_info": ([P, P, P], ctypes.c_int),
+        "gw_slab_get": ([P, P, P, i32], ctypes.c_int),
+        "gw_slab_device_xyz": ([P, pp], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -326,6 +326,56 @@ class VoxelPlan:
             pass
 
 
+# ------------------------------------------------------------------ slab
+class Slab:
+    """Owner of a gw_slab: a unit cell tiled and cropped on the device
+    (comparison.py:595-671).  cell_xyz (n_cell, 3); vecs the cell vectors
+    a, b, c (calc_real_space_abc); size (x, y, z)."""
+
+    def __init__(self, cell_xyz, vecs, size, ctx=None):
+        self.ctx = ctx or N.default_context()
+        cell = np.ascontiguousarray(cell_xyz, dtype=np.float64).reshape(-1, 3)
+        v = np.ascontiguousarray(np.asarray(vecs, dtype=np.float64).reshape(3, 3))
+        sz = np.ascontiguousarray(np.asarray(size, dtype=np.float64).reshape(3))
+        h = ctypes.c_void_p()
+        st = N.lib().gw_slab_create(self.ctx.handle, N.ptr(cell), len(cell),
+                                    N.ptr(v), N.ptr(sz), ctypes.byref(h))
+        if st != 0:
+            msg = N.last_error()
+            if "must be greater than" in msg:
+                raise AssertionError(msg.split(": ", 1)[-1])
+            N.check(st)
+        self.handle = h
+        n = ctypes.c_int64()
+        b = np.zeros(3)
+        N.check(N.lib().gw_slab_info(self.handle, ctypes.byref(n), N.ptr(b)))
+        self.n = int(n.value)
+        self.bounds = b
+
+    def coords(self):
+        """(n, 3) float64 coordinates and (n,) cell-atom indices (host)."""
+        xyz = np.empty((self.n, 3))
+        src = np.empty(self.n, dtype=np.int32)
+        N.check(N.lib().gw_slab_get(self.handle, N.ptr(xyz), N.ptr(src), 0))
+        return xyz, src
+
+    def device_xyz(self):
+        p = ctypes.c_void_p()
+        N.check(N.lib().gw_slab_device_xyz(self.handle, ctypes.byref(p)))
+        return p.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            N.lib().gw_slab_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------------ detector
 def rotation_matrix(u, theta):
     """Rodrigues rotation (utilities.py:222-245), same expression trees."""

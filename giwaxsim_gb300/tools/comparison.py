@@ -3,7 +3,7 @@
 
   voxelgridmaker_fitting   comparison.py:673-788  -> GPU voxel plan
   detectormaker_fitting    comparison.py:790-870  -> GPU detector plan
-  slabmaker_fitting        comparison.py:595-671  (host: unit-cell tiling)
+  slabmaker_fitting        comparison.py:595-671  -> GPU slab (gw_slab)
   optimize_scale_offset    comparison.py:873-882  (host least squares)
 
 Keyword-only extensions (all default to the reference's behaviour):
@@ -17,7 +17,7 @@ Keyword-only extensions (all default to the reference's behaviour):
 """
 import numpy as np
 
-from ..forward import (DetectorPlan, VoxelGeometry, VoxelPlan,
+from ..forward import (DetectorPlan, Slab, VoxelGeometry, VoxelPlan,
                        element_f_values)
 from .utilities import calc_real_space_abc, load_pdb, load_xyz
 
@@ -109,43 +109,23 @@ def detectormaker_fitting(iq, qx, qy, qz, num_pixels, max_q, angle_init_vals,
 
 
 def slabmaker_fitting(input_filepath, x_size, y_size, z_size, a, b, c, alpha,
-                      beta, gamma):
-    """Tile a unit cell into a slab of x/y/z size (comparison.py:595-671)."""
+                      beta, gamma, *, ctx=None):
+    """Tile a unit cell into a slab of x/y/z size (comparison.py:595-671),
+    on the device (gw_slab): same coordinates bit for bit, same atom order,
+    same AssertionError messages."""
     if input_filepath.lower().endswith(".xyz"):
         coords, elements = load_xyz(input_filepath)
     elif input_filepath.lower().endswith(".pdb"):
         coords, elements = load_pdb(input_filepath)
     else:
         raise Exception("Files must be a .pdb or .xyz file")
-    av, bv, cv = calc_real_space_abc(a, b, c, alpha, beta, gamma)
-    nx = int(np.ceil(2 * x_size / av[0]))
-    ny = int(np.ceil(2 * y_size / bv[1]))
-    nz = int(np.ceil(2 * z_size / cv[2]))
-    # the reference appends shifted copies axis by axis; keep its order
-    for n, shift in ((nx, lambda i: np.array([av[0] * i, 0, 0])),
-                     (ny, lambda i: np.array([bv[0] * i, bv[1] * i, 0])),
-                     (nz, lambda i: np.array([cv[0] * i, cv[1] * i, cv[2] * i]))):
-        base, base_el = coords.copy(), elements.copy()
-        blocks, els = [coords], [elements]
-        for i in range(n):
-            blocks.append(base + shift(i + 1))
-            els.append(base_el)
-        coords = np.concatenate(blocks, axis=0)
-        elements = np.concatenate(els, axis=0)
-    ext = [np.max(coords[:, k]) - np.min(coords[:, k]) for k in range(3)]
-    assert ext[0] > x_size, "x_max must be greater than x_size"
-    assert ext[1] > y_size, "y_max must be greater than y_size"
-    assert ext[2] > z_size, "z_max must be greater than z_size"
-    buf = [(ext[0] - x_size) / 2, (ext[1] - y_size) / 2, (ext[2] - z_size) / 2]
-    for k in range(3):
-        coords[:, k] -= np.min(coords[:, k])
-    keep = np.ones(len(coords), dtype=bool)
-    for k in range(3):
-        keep &= (coords[:, k] >= buf[k]) & (coords[:, k] <= ext[k] - buf[k])
-    coords, elements = coords[keep], elements[keep]
-    for k in range(3):
-        coords[:, k] -= np.min(coords[:, k])
-    return coords, elements
+    vecs = np.array(calc_real_space_abc(a, b, c, alpha, beta, gamma))
+    slab = Slab(coords, vecs, (x_size, y_size, z_size), ctx=ctx)
+    try:
+        xyz, src = slab.coords()
+    finally:
+        slab.close()
+    return xyz, np.asarray(elements)[src]
 
 
 def optimize_scale_offset(sim_map, rebin_map, rebin_mask):

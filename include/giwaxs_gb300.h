@@ -289,6 +289,27 @@ int gw_detector(gw_ctx *ctx, const gw_detector_params *p, const double *iq,
                 const double *rot_R, const double *weights, int32_t n_orient,
                 double *out);
 
+/* ---- slab construction (tools/comparison.py:595-671 slabmaker_fitting) -- */
+/* A unit cell of n_cell atoms (cell_xyz, (n_cell, 3) float64 host) is
+ * replicated along the cell vectors vecs = (a, b, c) (3x3 row-major, from
+ * calc_real_space_abc; a_y = a_z = b_z = 0 as there), shifted to the origin,
+ * cropped to the central size[0] x size[1] x size[2] box and shifted again,
+ * bit for bit as the reference does it and in its atom order.  The result
+ * stays on the device.  GW_ERR_ARG with the reference's message ("x_max
+ * must be greater than x_size", ...) when the replicated slab is too small. */
+typedef struct gw_slab gw_slab;
+int gw_slab_create(gw_ctx *ctx, const double *cell_xyz, int32_t n_cell,
+                   const double *vecs, const double *size, gw_slab **out);
+int gw_slab_destroy(gw_slab *slab);
+/* Number of atoms kept and their x/y/z extents (max - min per axis). */
+int gw_slab_info(gw_slab *slab, int64_t *n, double *bounds);
+/* Copy out the (n, 3) float64 coordinates and, if src is not NULL, the cell
+ * atom (0..n_cell-1) of each atom; host or device destination. */
+int gw_slab_get(gw_slab *slab, double *xyz, int32_t *src, int32_t on_device);
+/* Device address of the coordinates (valid until gw_slab_destroy), for
+ * gw_voxel_set_atoms(..., on_device = 1). */
+int gw_slab_device_xyz(gw_slab *slab, const double **xyz);
+
 /* ---- per-slice and helper entry points (device, synchronous) ---------- */
 /* Gather I(q) at points (x,y,z) after applying n_R 3x3 rotations in order
  * (BLAS fused order), with the reference's floor division by dq and clip:

@@ -502,3 +502,42 @@ def detector(iq, qx, qy, qz, num_pixels, max_q, angle_init_vals,
     det[det <= 0] = 1e-6
     det *= 1e-6
     return det, h, v
+
+
+# ------------------------------------------------------------------ slab
+def slabmaker(cell_xyz, cell_elements, vecs, size):
+    """comparison.py:595-671 (slabmaker_fitting) after the file is loaded:
+    copies appended axis by axis (x, then y, then z) with the reference's
+    float64 shift vectors, shift to the origin, crop to the central box,
+    shift again.  vecs = (a, b, c) from calc_real_space_abc."""
+    av, bv, cv = (np.asarray(v, dtype=np.float64) for v in vecs)
+    coords = np.array(cell_xyz, dtype=np.float64)
+    elements = np.asarray(cell_elements)
+    x_size, y_size, z_size = size
+    nx = int(np.ceil(2 * x_size / av[0]))
+    ny = int(np.ceil(2 * y_size / bv[1]))
+    nz = int(np.ceil(2 * z_size / cv[2]))
+    for n, shift in ((nx, lambda i: np.array([av[0] * i, 0, 0])),
+                     (ny, lambda i: np.array([bv[0] * i, bv[1] * i, 0])),
+                     (nz, lambda i: np.array([cv[0] * i, cv[1] * i, cv[2] * i]))):
+        base, base_el = coords.copy(), elements.copy()
+        blocks, els = [coords], [elements]
+        for i in range(n):
+            blocks.append(base + shift(i + 1))
+            els.append(base_el)
+        coords = np.concatenate(blocks, axis=0)
+        elements = np.concatenate(els, axis=0)
+    ext = [np.max(coords[:, k]) - np.min(coords[:, k]) for k in range(3)]
+    assert ext[0] > x_size, "x_max must be greater than x_size"
+    assert ext[1] > y_size, "y_max must be greater than y_size"
+    assert ext[2] > z_size, "z_max must be greater than z_size"
+    buf = [(ext[0] - x_size) / 2, (ext[1] - y_size) / 2, (ext[2] - z_size) / 2]
+    for k in range(3):
+        coords[:, k] -= np.min(coords[:, k])
+    keep = np.ones(len(coords), dtype=bool)
+    for k in range(3):
+        keep &= (coords[:, k] >= buf[k]) & (coords[:, k] <= ext[k] - buf[k])
+    coords, elements = coords[keep], elements[keep]
+    for k in range(3):
+        coords[:, k] -= np.min(coords[:, k])
+    return coords, elements

@@ -256,8 +256,63 @@ def pm6():
     print("PM6 fixture written")
 
 
+SLAB_CASES = [
+    # (name, cell source, cell parameters a b c alpha beta gamma, size)
+    ("pm6", "pdb", None, (60.0, 40.0, 50.0)),
+    ("graphite", "xyz", (2.46, 2.46, 6.70, 90.0, 90.0, 120.0), (20.0, 20.0, 20.0)),
+    ("graphite_odd", "xyz", (2.46, 2.46, 6.70, 90.0, 90.0, 120.0), (33.3, 41.7, 25.0)),
+    ("triclinic", "xyz", (4.1, 5.3, 6.2, 81.0, 95.0, 104.0), (27.5, 22.0, 31.0)),
+]
+
+
+def slab():
+    """The reference's slabmaker_fitting (comparison.py:595-671) on the PM6
+    cell and on small cells written as .xyz files (hexagonal graphite and a
+    triclinic cell, so that b_x, c_x and c_y are not zero): atom count,
+    a SHA-256 of the float64 coordinates and of the element names, and the
+    first rows.  Seconds."""
+    import hashlib
+    import tempfile
+    comparison, detector, utilities, voxelgrids = _import_reference()
+    out = {}
+    for name, kind, cellp, size in SLAB_CASES:
+        if kind == "pdb":
+            path = os.path.join(REF, "test_input_files", "PM6_sample.pdb")
+            cellp = utilities.load_pdb_cell_params(path)
+            cell_xyz, cell_el = utilities.load_pdb(path)
+        else:
+            av, bv, cv = utilities.calc_real_space_abc(*cellp)
+            frac = np.array([[0, 0, 0.25], [0, 0, 0.75], [1 / 3, 2 / 3, 0.25],
+                             [2 / 3, 1 / 3, 0.75], [0.1, 0.45, 0.6]])
+            cell_xyz = frac @ np.array([av, bv, cv])
+            cell_el = np.array(["C", "C", "C", "C", "S"])
+            fd, path = tempfile.mkstemp(suffix=".xyz")
+            with os.fdopen(fd, "w") as fh:
+                fh.write("%d\ncell\n" % len(cell_xyz))
+                for e, (x, y, z) in zip(cell_el, cell_xyz):
+                    fh.write("%s %.17g %.17g %.17g\n" % (e, x, y, z))
+            cell_xyz, cell_el = utilities.load_xyz(path)
+        coords, els = comparison.slabmaker_fitting(path, *size, *cellp)
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        out[name + "_cell_xyz"] = cell_xyz
+        out[name + "_cell_el"] = np.asarray(cell_el)
+        out[name + "_cellp"] = np.array(cellp, dtype=np.float64)
+        out[name + "_size"] = np.array(size)
+        out[name + "_n"] = len(coords)
+        out[name + "_sha"] = hashlib.sha256(coords.tobytes()).hexdigest()
+        out[name + "_el_sha"] = hashlib.sha256(
+            "".join(np.asarray(els).tolist()).encode()).hexdigest()
+        out[name + "_head"] = coords[:8]
+        if kind != "pdb":
+            os.remove(path)
+    np.savez_compressed(os.path.join(HERE, "golden_slab.npz"), **out)
+    print("slab fixture written")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "pm6":
         pm6()
+    elif len(sys.argv) > 2 and sys.argv[2] == "slab":
+        slab()
     else:
         main()

@@ -114,3 +114,26 @@ def test_f0_and_downselect():
     assert np.allclose(got, d["f0"], rtol=1e-14, atol=0)
     sub, x, _, _ = O.downselect_voxelgrid(d["grid"], q, q, q, 1.1)
     assert np.array_equal(sub, d["ds_grid"]) and np.array_equal(x, d["ds_x"])
+
+
+SLAB_CASES = ["pm6", "graphite", "graphite_odd", "triclinic"]
+
+
+def _slab_sha(coords, els):
+    import hashlib
+    return (hashlib.sha256(np.ascontiguousarray(coords, dtype=np.float64).tobytes()).hexdigest(),
+            hashlib.sha256("".join(np.asarray(els).tolist()).encode()).hexdigest())
+
+
+@pytest.mark.parametrize("name", SLAB_CASES)
+def test_slabmaker_vs_reference(name):
+    """The oracle's slab (and the package's cell vectors) against the
+    reference's slabmaker_fitting, every coordinate bit for bit."""
+    from giwaxsim_gb300.tools.utilities import calc_real_space_abc
+    d = golden("golden_slab.npz")
+    vecs = calc_real_space_abc(*d[name + "_cellp"])
+    coords, els = O.slabmaker(d[name + "_cell_xyz"], d[name + "_cell_el"], vecs,
+                              tuple(d[name + "_size"]))
+    assert len(coords) == int(d[name + "_n"])
+    assert np.array_equal(coords[:8], d[name + "_head"])
+    assert _slab_sha(coords, els) == (str(d[name + "_sha"]), str(d[name + "_el_sha"]))
