@@ -39,6 +39,8 @@ EXPORTS = [
     "gw_ctx_device_name", "gw_ctx_mark", "gw_ctx_elapsed_ms",
     "gw_slab_create", "gw_slab_destroy", "gw_slab_info", "gw_slab_get",
     "gw_slab_device_xyz",
+    "gw_compare_create", "gw_compare_destroy", "gw_compare_target",
+    "gw_compare_eval",
 ]
 
 
@@ -159,6 +161,11 @@ def _declare(lib):
         "gw_slab_info": ([P, P, P], ctypes.c_int),
         "gw_slab_get": ([P, P, P, i32], ctypes.c_int),
         "gw_slab_device_xyz": ([P, pp], ctypes.c_int),
+        "gw_compare_create": ([P, i32, i32, i32, i32, i32, i32, P, P, P, P, i64, pp],
+                              ctypes.c_int),
+        "gw_compare_destroy": ([P], ctypes.c_int),
+        "gw_compare_target": ([P, P, P], ctypes.c_int),
+        "gw_compare_eval": ([P, P, i32, P, P], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

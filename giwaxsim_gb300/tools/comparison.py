@@ -128,10 +128,175 @@ def slabmaker_fitting(input_filepath, x_size, y_size, z_size, a, b, c, alpha,
     return xyz, np.asarray(elements)[src]
 
 
-def optimize_scale_offset(sim_map, rebin_map, rebin_mask):
-    """Least-squares scale and offset of sim onto rebin where mask == 0."""
-    sim = sim_map[rebin_mask == 0].ravel()
-    reb = rebin_map[rebin_mask == 0].ravel()
-    A = np.vstack([sim, np.ones_like(sim)]).T
-    coeffs, _, _, _ = np.linalg.lstsq(A, reb, rcond=None)
-    return coeffs[0], coeffs[1]
+def trim_sim_data(sim_det_ints, det_h, det_v, exp_qxy, exp_qz):
+    """Rows/columns of the simulated image inside the experiment's q range
+    (comparison.py:161-191)."""
+    h_mask, v_mask = _trim_masks(det_h, det_v, exp_qxy, exp_qz)
+    return (np.asarray(sim_det_ints)[v_mask, :][:, h_mask], det_h[h_mask],
+            det_v[v_mask])
+
+
+def _trim_masks(det_h, det_v, exp_qxy, exp_qz):
+    h_mask = (det_h >= np.min(exp_qxy)) & (det_h <= np.max(exp_qxy))
+    v_mask = (det_v >= np.min(exp_qz)) & (det_v <= np.max(exp_qz))
+    return h_mask, v_mask
+
+
+def rebin_weights(qxy1, qz1, qxy2, qz2):
+    """The linear interpolation griddata(points2, values, grid1) performs
+    (comparison.py:425-438: a Delaunay triangulation of the experimental
+    (qxy, qz) points and barycentric weights in the containing triangle),
+    as 3 (index, weight) pairs per target pixel of the (qz1, qxy1) grid;
+    index -1 outside the triangulation (griddata's NaN)."""
+    from scipy.spatial import Delaunay
+    g1x, g1z = np.meshgrid(qxy1, qz1)
+    g2x, g2z = np.meshgrid(qxy2, qz2)
+    points2 = np.vstack((g2x.ravel(), g2z.ravel())).T
+    tri = Delaunay(points2)
+    xi = np.stack([g1x.ravel(), g1z.ravel()], 1)
+    s = tri.find_simplex(xi)
+    T = tri.transform[s]
+    d = xi - T[:, 2]
+    c0 = T[:, 0, 0] * d[:, 0] + T[:, 0, 1] * d[:, 1]
+    c1 = T[:, 1, 0] * d[:, 0] + T[:, 1, 1] * d[:, 1]
+    w = np.stack([c0, c1, (1.0 - c0) - c1], 1)
+    idx = tri.simplices[s].astype(np.int32)
+    idx[s < 0] = -1
+    w[s < 0] = 0.0
+    return np.ascontiguousarray(idx), np.ascontiguousarray(w)
+
+
+class Comparison:
+    """Device plan of the experimental comparison: the experiment rebinned
+    once onto the trimmed simulation grid, then per simulated image the
+    scale + offset least squares and residuals over the unmasked pixels
+    (comparison.py:161-191, :406-445, :873-882; fit_slabsize.py:43-44)."""
+
+    def __init__(self, det_h, det_v, exp_img, exp_qxy, exp_qz, exp_mask,
+                 weights=None, ctx=None):
+        import ctypes
+        from .. import _native as N
+        self._N = N
+        self.ctx = ctx or N.default_context()
+        det_h, det_v = np.asarray(det_h), np.asarray(det_v)
+        h_mask, v_mask = _trim_masks(det_h, det_v, exp_qxy, exp_qz)
+        hi, vi = np.where(h_mask)[0], np.where(v_mask)[0]
+        if len(hi) == 0 or len(vi) == 0:
+            raise ValueError("the simulated image does not overlap the experiment")
+        self.h0, self.v0 = int(hi[0]), int(vi[0])
+        self.rows, self.cols = len(vi), len(hi)
+        self.n_v, self.n_h = len(det_v), len(det_h)
+        self.det_h_trim, self.det_v_trim = det_h[hi], det_v[vi]
+        if weights is None:
+            weights = rebin_weights(self.det_h_trim, self.det_v_trim, exp_qxy, exp_qz)
+        idx, w = weights
+        vals = np.ascontiguousarray(np.asarray(exp_img, dtype=np.float64).ravel())
+        mvals = np.ascontiguousarray(np.asarray(exp_mask, dtype=np.float64).ravel())
+        h = ctypes.c_void_p()
+        N.check(N.lib().gw_compare_create(
+            self.ctx.handle, self.n_v, self.n_h, self.v0, self.h0, self.rows,
+            self.cols, N.ptr(idx), N.ptr(w), N.ptr(vals), N.ptr(mvals),
+            len(vals), ctypes.byref(h)))
+        self.handle = h
+
+    def target(self):
+        """(rebinned map, rebinned mask) on the trimmed grid."""
+        t = np.empty((self.rows, self.cols))
+        m = np.empty((self.rows, self.cols), dtype=np.uint8)
+        self._N.check(self._N.lib().gw_compare_target(self.handle, self._N.ptr(t),
+                                                      self._N.ptr(m)))
+        return t, m.astype(int)
+
+    def evaluate(self, sim, on_device=False, residual=False):
+        """(scale, offset, misfit, pixels used[, residual map]) for a whole
+        simulated image (host (n_v, n_h) array or a device pointer)."""
+        import ctypes
+        N = self._N
+        out = np.zeros(4)
+        res = np.empty((self.rows, self.cols)) if residual else None
+        if on_device:
+            src = ctypes.c_void_p(sim)
+        else:
+            sim = np.ascontiguousarray(sim, dtype=np.float64)
+            if sim.shape != (self.n_v, self.n_h):
+                raise ValueError("sim must be the whole (n_v, n_h) image")
+            src = N.ptr(sim)
+        N.check(N.lib().gw_compare_eval(self.handle, src, int(bool(on_device)),
+                                        N.ptr(out), N.ptr(res)))
+        r = (float(out[0]), float(out[1]), float(out[2]), int(out[3]))
+        return r + (res,) if residual else r
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._N.lib().gw_compare_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _identity(shape):
+    n = int(np.prod(shape))
+    idx = np.repeat(np.arange(n, dtype=np.int32), 3).reshape(n, 3)
+    w = np.zeros((n, 3))
+    w[:, 0] = 1.0
+    return idx, w
+
+
+def rebin_qmap_and_mask(qxy1, qz1, qmap2, qxy2, qz2, qmap2_mask, *, ctx=None):
+    """qmap2 and its mask rebinned onto the (qz1, qxy1) grid by linear
+    interpolation (comparison.py:406-445); the weights are made on the host
+    (Delaunay), the interpolation runs on the device."""
+    c = _whole_grid(np.asarray(qxy1), np.asarray(qz1), qmap2, qxy2, qz2,
+                    qmap2_mask, ctx)
+    try:
+        return c.target()
+    finally:
+        c.close()
+
+
+def _whole_grid(qxy1, qz1, qmap2, qxy2, qz2, qmap2_mask, ctx):
+    """A Comparison whose window is the whole (qz1, qxy1) grid."""
+    c = Comparison.__new__(Comparison)
+    import ctypes
+    from .. import _native as N
+    c._N = N
+    c.ctx = ctx or N.default_context()
+    c.v0 = c.h0 = 0
+    c.rows, c.cols = len(qz1), len(qxy1)
+    c.n_v, c.n_h = c.rows, c.cols
+    idx, w = rebin_weights(qxy1, qz1, qxy2, qz2)
+    vals = np.ascontiguousarray(np.asarray(qmap2, dtype=np.float64).ravel())
+    mvals = np.ascontiguousarray(np.asarray(qmap2_mask, dtype=np.float64).ravel())
+    h = ctypes.c_void_p()
+    N.check(N.lib().gw_compare_create(c.ctx.handle, c.n_v, c.n_h, 0, 0, c.rows,
+                                      c.cols, N.ptr(idx), N.ptr(w), N.ptr(vals),
+                                      N.ptr(mvals), len(vals), ctypes.byref(h)))
+    c.handle = h
+    return c
+
+
+def optimize_scale_offset(sim_map, rebin_map, rebin_mask, *, ctx=None):
+    """Least-squares scale and offset of sim onto rebin where mask == 0
+    (comparison.py:873-882), as a device reduction."""
+    import ctypes
+    from .. import _native as N
+    sim = np.ascontiguousarray(sim_map, dtype=np.float64)
+    ctx = ctx or N.default_context()
+    idx, w = _identity(sim.shape)
+    vals = np.ascontiguousarray(np.asarray(rebin_map, dtype=np.float64).ravel())
+    mvals = np.ascontiguousarray((np.asarray(rebin_mask) != 0).astype(np.float64).ravel())
+    h = ctypes.c_void_p()
+    rows, cols = sim.shape
+    N.check(N.lib().gw_compare_create(ctx.handle, rows, cols, 0, 0, rows, cols,
+                                      N.ptr(idx), N.ptr(w), N.ptr(vals),
+                                      N.ptr(mvals), len(vals), ctypes.byref(h)))
+    out = np.zeros(4)
+    try:
+        N.check(N.lib().gw_compare_eval(h, N.ptr(sim), 0, N.ptr(out), None))
+    finally:
+        N.lib().gw_compare_destroy(h)
+    return out[0], out[1]

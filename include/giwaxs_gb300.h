@@ -310,6 +310,30 @@ int gw_slab_get(gw_slab *slab, double *xyz, int32_t *src, int32_t on_device);
  * gw_voxel_set_atoms(..., on_device = 1). */
 int gw_slab_device_xyz(gw_slab *slab, const double **xyz);
 
+/* ---- experimental comparison (tools/comparison.py:161-191 trim_sim_data,
+ * :406-445 rebin_qmap_and_mask, :873-882 optimize_scale_offset) ---------- */
+/* The experimental map (n_src values and mask values) is rebinned onto the
+ * rows x cols trimmed window [v0, v0+rows) x [h0, h0+cols) of an n_v x n_h
+ * simulated image by the sparse weights idx/w (3 per target pixel, row-major
+ * over the window; idx[3i] < 0 marks a pixel outside the triangulation:
+ * NaN).  The mask is thresholded (> 0).  Made once per experiment. */
+typedef struct gw_compare gw_compare;
+int gw_compare_create(gw_ctx *ctx, int32_t n_v, int32_t n_h, int32_t v0,
+                      int32_t h0, int32_t rows, int32_t cols,
+                      const int32_t *idx, const double *w,
+                      const double *exp_values, const double *exp_mask,
+                      int64_t n_src, gw_compare **out);
+int gw_compare_destroy(gw_compare *cmp);
+/* The rebinned map (rows x cols float64) and mask (uint8) (host). */
+int gw_compare_target(gw_compare *cmp, double *target, uint8_t *mask);
+/* Least-squares scale and offset of the trimmed simulated image onto the
+ * target over the unmasked pixels; out = (scale, offset, misfit = sum of
+ * squared residuals, number of pixels used).  sim is the whole n_v x n_h
+ * image (host, or device with sim_on_device).  residual (host rows x cols,
+ * or NULL) receives target - (scale sim + offset), 0 where masked. */
+int gw_compare_eval(gw_compare *cmp, const double *sim, int32_t sim_on_device,
+                    double *out, double *residual);
+
 /* ---- per-slice and helper entry points (device, synchronous) ---------- */
 /* Gather I(q) at points (x,y,z) after applying n_R 3x3 rotations in order
  * (BLAS fused order), with the reference's floor division by dq and clip:

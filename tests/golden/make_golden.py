@@ -309,10 +309,48 @@ def slab():
     print("slab fixture written")
 
 
+def compare():
+    """The reference's experimental-comparison step on synthetic maps:
+    trim_sim_data, rebin_qmap_and_mask (griddata, linear), the masking of
+    fit_slabsize.py:142, optimize_scale_offset and the residual of
+    fit_slabsize.py:43-44."""
+    comparison, detector, utilities, voxelgrids = _import_reference()
+    rng = np.random.default_rng(21)
+    exp_qxy = np.linspace(0.05, 2.2, 97)
+    exp_qz = np.linspace(0.02, 1.9, 83)
+    gx, gz = np.meshgrid(exp_qxy, exp_qz)
+    exp_img = (np.exp(-((np.hypot(gx, gz) - 1.4) / 0.08) ** 2) + 0.1 * gz
+               + 0.02 * rng.random(gx.shape))
+    mask = (rng.random(gx.shape) < 0.08).astype(int)
+    mask[:, :4] = 1
+    det_h = np.linspace(-2.5, 2.5, 120)
+    det_v = np.linspace(-2.5, 2.5, 110)
+    hx, vz = np.meshgrid(det_h, det_v)
+    sim = (np.exp(-((np.hypot(hx, vz) - 1.38) / 0.09) ** 2) + 0.05
+           + 0.01 * rng.random(hx.shape))
+    sim_trim, h_trim, v_trim = comparison.trim_sim_data(sim, det_h, det_v,
+                                                        exp_qxy, exp_qz)
+    rebin_raw, rebin_mask = comparison.rebin_qmap_and_mask(
+        h_trim, v_trim, exp_img, exp_qxy, exp_qz, mask)
+    rebin_map = rebin_raw.copy()
+    rebin_map[rebin_mask == 1] = 0
+    scale, offset = comparison.optimize_scale_offset(sim_trim, rebin_map, rebin_mask)
+    residual = (rebin_map - (scale * sim_trim + offset)) * (rebin_mask == 0)
+    np.savez_compressed(
+        os.path.join(HERE, "golden_compare.npz"), exp_qxy=exp_qxy,
+        exp_qz=exp_qz, exp_img=exp_img, mask=mask, det_h=det_h, det_v=det_v,
+        sim=sim, sim_trim=sim_trim, h_trim=h_trim, v_trim=v_trim,
+        rebin_raw=rebin_raw, rebin_mask=rebin_mask, scale=scale,
+        offset=offset, residual=residual)
+    print("comparison fixture written")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "pm6":
         pm6()
     elif len(sys.argv) > 2 and sys.argv[2] == "slab":
         slab()
+    elif len(sys.argv) > 2 and sys.argv[2] == "compare":
+        compare()
     else:
         main()

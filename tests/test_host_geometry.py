@@ -75,15 +75,6 @@ def test_detector_corner_matrices_match_full_plane():
         c = c.rotate(Rc)
 
 
-def test_slabmaker_and_lstsq():
-    rng = np.random.default_rng(0)
-    sim = rng.uniform(0, 1, (20, 20))
-    mask = (rng.uniform(0, 1, (20, 20)) > 0.8).astype(int)
-    reb = 3.0 * sim + 0.25
-    s, o = comparison.optimize_scale_offset(sim, reb, mask)
-    assert abs(s - 3.0) < 1e-12 and abs(o - 0.25) < 1e-12
-
-
 def test_config_parsing(tmp_path):
     p = tmp_path / "cfg.txt"
     p.write_text("# comment\nr_voxel_size=0.3\nfill_bkg=True\nkey=a=b\n\n")
@@ -94,3 +85,18 @@ def test_config_parsing(tmp_path):
     assert utilities.str_to_bool("maybe") is False
     with pytest.raises(ValueError):
         utilities.str_to_bool("maybe", default=None)
+
+
+def test_trim_and_rebin_weights_vs_reference():
+    """trim_sim_data and the griddata weights (host parts of the
+    comparison step) against the reference's own outputs, bit for bit."""
+    from giwaxsim_gb300.tools.comparison import rebin_weights, trim_sim_data
+    d = golden("golden_compare.npz")
+    s, h, v = trim_sim_data(d["sim"], d["det_h"], d["det_v"], d["exp_qxy"], d["exp_qz"])
+    assert np.array_equal(s, d["sim_trim"]) and np.array_equal(h, d["h_trim"])
+    assert np.array_equal(v, d["v_trim"])
+    idx, w = rebin_weights(h, v, d["exp_qxy"], d["exp_qz"])
+    val = d["exp_img"].ravel()
+    out = ((w[:, 0] * val[idx[:, 0]]) + w[:, 1] * val[idx[:, 1]]) + w[:, 2] * val[idx[:, 2]]
+    out[idx[:, 0] < 0] = np.nan
+    assert np.array_equal(out.reshape(s.shape), d["rebin_raw"], equal_nan=True)
