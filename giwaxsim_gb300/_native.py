@@ -40,7 +40,7 @@ EXPORTS = [
     "gw_slab_create", "gw_slab_destroy", "gw_slab_info", "gw_slab_get",
     "gw_slab_device_xyz",
     "gw_compare_create", "gw_compare_destroy", "gw_compare_target",
-    "gw_compare_eval",
+    "gw_compare_eval", "gw_detector_device_out",
 ]
 
 
@@ -125,7 +125,7 @@ def _declare(lib):
         "gw_voxel_execute": ([P], ctypes.c_int),
         "gw_voxel_capture_graph": ([P], ctypes.c_int),
         "gw_voxel_get_iq": ([P, P, i32], ctypes.c_int),
-        "gw_voxel_device_iq32": ([P, pp], ctypes.c_int),
+        "gw_voxel_device_iq32": ([P, ctypes.c_int32, pp], ctypes.c_int),
         "gw_voxel_get_counts": ([P, P], ctypes.c_int),
         "gw_voxel_get_sums": ([P, P], ctypes.c_int),
         "gw_voxel_info": ([P, P, i32], ctypes.c_int),
@@ -166,6 +166,7 @@ def _declare(lib):
         "gw_compare_destroy": ([P], ctypes.c_int),
         "gw_compare_target": ([P, P, P], ctypes.c_int),
         "gw_compare_eval": ([P, P, i32, P, P], ctypes.c_int),
+        "gw_detector_device_out": ([P, pp], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -812,6 +812,12 @@ extern "C" int gw_detector_execute(gw_detector_plan *P) {
   return GW_OK;
 }
 
+extern "C" int gw_detector_device_out(gw_detector_plan *P, const double **out) {
+  if (!P || !out) return gw::fail(GW_ERR_ARG, "gw_detector_device_out: null argument");
+  *out = P->d_out;
+  return GW_OK;
+}
+
 extern "C" int gw_detector_get(gw_detector_plan *P, double *out, int32_t on_device) {
   if (!P || !out) return gw::fail(GW_ERR_ARG, "gw_detector_get: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_detector_get: plan not executed");

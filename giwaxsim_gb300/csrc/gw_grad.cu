@@ -569,6 +569,8 @@ extern "C" int gw_voxel_backward(gw_voxel_plan *P, const double *g_iq,
     return gw::fail(GW_ERR_ARG, "gw_voxel_backward: needs the batched mode");
   if (P->p.fill_bkg)
     return gw::fail(GW_ERR_ARG, "gw_voxel_backward: fill_bkg is not differentiated");
+  if (P->n_out > 1)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_backward: separate structures are not differentiated");
   if (g_xyz && !P->bil)
     return gw::fail(GW_ERR_ARG, "gw_voxel_backward: coordinate gradients need the bilinear deposit");
   if (P->n_atoms < 0)
@@ -617,7 +619,7 @@ extern "C" int gw_voxel_backward(gw_voxel_plan *P, const double *g_iq,
   CztArgs cy{P->My, P->Ly, P->Nc, P->d_Ay, P->d_Hy, P->d_By, P->d_twy};
   CztArgs cz{P->Mz, P->Lz, P->Nr, P->d_Az, P->d_Hz, P->d_Bz, P->d_twz};
   BinArgs bn{P->d_colofs, P->d_rowofs, P->d_sum, P->d_sumk, 0, P->k0, P->kz0,
-             (float)((double)P->g * (double)P->g)};
+             (float)((double)P->g * (double)P->g), 0};
   GradCol gc{G->d_gsum, G->d_Az, G->d_Hz, G->d_Bz, G->d_G1, G->d_sc,
              (float)((double)P->g * (double)P->g)};
   GradRow gr{G->d_Ay, G->d_Hy, G->d_By, P->d_twy, G->d_G1, G->d_dmy, G->d_dmz,

@@ -470,6 +470,7 @@ struct ColBin {
   const float2 *B;
   float2 cbg;
   int nr, nc, m0;
+  int64_t soff;  // sum-grid offset of the slice's structure (separate mode)
   __device__ void operator()(int f, int mr, float2 v) const {
     const int m = m0 + f;
     if (mr >= nr || m >= nc) return;
@@ -481,8 +482,8 @@ struct ColBin {
       X.y += cbg.y * bn->dc_scale;
     }
     const float I = X.x * X.x + X.y * X.y;
-    if (bn->kahan) kahan_add(bn->sumk + co + ro, I);
-    else atomicAdd(bn->sum + co + ro, (double)I);
+    if (bn->kahan) kahan_add(bn->sumk + soff + co + ro, I);
+    else atomicAdd(bn->sum + soff + co + ro, (double)I);
   }
 };
 
@@ -510,7 +511,8 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
   slice_rows(a, slice0, sl, first, rows);
   ColLoad ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
   fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
-  ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0};
+  ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0,
+            bn.sstride * (int64_t)(sl / a.n_phi)};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), st);
 }
 
@@ -986,18 +988,18 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
 int enqueue(gw_voxel_plan *P) {
   gw_ctx *ctx = P->ctx;
   cudaStream_t st = ctx->stream;
-  const size_t W3 = (size_t)P->W * P->W * P->W;
   if (P->p.accum == GW_ACCUM_KAHAN32)
-    GW_CUDA(cudaMemsetAsync(P->d_sumk, 0, W3 * sizeof(float2), st));
+    GW_CUDA(cudaMemsetAsync(P->d_sumk, 0, P->sum_stride * P->n_out * sizeof(float2), st));
   else
-    GW_CUDA(cudaMemsetAsync(P->d_sum, 0, W3 * sizeof(double), st));
+    GW_CUDA(cudaMemsetAsync(P->d_sum, 0, P->sum_stride * P->n_out * sizeof(double), st));
   GW_TRY(enqueue_prep(P));
   SliceArgs a = slice_args(P);
   CztArgs cy{P->My, P->Ly, P->Nc, P->d_Ay, P->d_Hy, P->d_By, P->d_twy};
   CztArgs cz{P->Mz, P->Lz, P->Nr, P->d_Az, P->d_Hz, P->d_Bz, P->d_twz};
   BinArgs bn{P->d_colofs, P->d_rowofs, P->d_sum, P->d_sumk,
              P->p.accum == GW_ACCUM_KAHAN32, P->k0, P->kz0,
-             (float)((double)P->g * (double)P->g)};
+             (float)((double)P->g * (double)P->g),
+             P->n_out > 1 ? (int64_t)P->sum_stride : 0};
   for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
     const int n = std::min(P->S, P->n_slices - s0);
     GW_TRY(enqueue_slice_setup(P, a, s0, n));
@@ -1007,24 +1009,30 @@ int enqueue(gw_voxel_plan *P) {
   const int fin_blocks = P->Qc * P->Qc;
   const float f0c = (float)P->p.f0_coef[8];
   const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
-  const float inv_ns = P->p.average ? 1.0f / (float)P->n_struct : 1.0f;
+  const float inv_ns = P->p.average == GW_STRUCTS_AVERAGE ? 1.0f / (float)P->n_struct : 1.0f;
   const int kahan = P->p.accum == GW_ACCUM_KAHAN32;
-  if (P->W == P->Qc && P->lo == P->wlo &&
-      (int64_t)P->Qc * P->Qc * P->Qc < ((int64_t)1 << 31) - 2) {
-    gw::KTimer tm(ctx, GW_K_FINALIZE);
-    const int64_t pairs = ((int64_t)P->Qc * P->Qc * P->Qc + 1) / 2;
-    const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
-    k_finalize_flat<<<blocks, 256, 0, st>>>(
-        P->d_sum, P->d_sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0,
-        P->p.f0_z > 0, f0c, f0iz, P->d_iq64, P->d_iq32);
-    GW_LAUNCHED(ctx);
-  } else {
-    gw::KTimer tm(ctx, GW_K_FINALIZE);
-    const int fin_threads = P->Qc >= 256 ? 256 : ((P->Qc + 31) / 32) * 32;
-    k_finalize<<<fin_blocks, fin_threads, 0, st>>>(
-        P->d_sum, P->d_sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo,
-        P->Qc, inv_ns, P->d_f0, P->p.f0_z > 0, f0c, f0iz, P->d_iq64, P->d_iq32);
-    GW_LAUNCHED(ctx);
+  const size_t Qc3 = (size_t)P->Qc * P->Qc * P->Qc;
+  for (int t = 0; t < P->n_out; ++t) {  // one I(q) per structure when separate
+    double *sum = P->d_sum ? P->d_sum + t * P->sum_stride : nullptr;
+    float2 *sumk = P->d_sumk ? P->d_sumk + t * P->sum_stride : nullptr;
+    double *o64 = P->d_iq64 + t * P->iq_stride;
+    float *o32 = P->d_iq32 + t * P->iq_stride;
+    if (P->W == P->Qc && P->lo == P->wlo && (int64_t)Qc3 < ((int64_t)1 << 31) - 2) {
+      gw::KTimer tm(ctx, GW_K_FINALIZE);
+      const int64_t pairs = ((int64_t)Qc3 + 1) / 2;
+      const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
+      k_finalize_flat<<<blocks, 256, 0, st>>>(
+          sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0,
+          P->p.f0_z > 0, f0c, f0iz, o64, o32);
+      GW_LAUNCHED(ctx);
+    } else {
+      gw::KTimer tm(ctx, GW_K_FINALIZE);
+      const int fin_threads = P->Qc >= 256 ? 256 : ((P->Qc + 31) / 32) * 32;
+      k_finalize<<<fin_blocks, fin_threads, 0, st>>>(
+          sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
+          inv_ns, P->d_f0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
+      GW_LAUNCHED(ctx);
+    }
   }
   return GW_OK;
 }
@@ -1061,6 +1069,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
   P->g = p->grid_size;
   P->plain = p->mode == GW_VOXEL_PLAIN;
   P->bil = p->deposit == GW_DEPOSIT_BILINEAR;
+  P->n_out = p->average == GW_STRUCTS_SEPARATE ? n_struct : 1;
   P->r = p->r_voxel_size;
   P->inv_r = 1.0 / P->r;
   P->dq = p->dq;
@@ -1228,6 +1237,8 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
   CztTables tz = make_czt(g, P->z_lo, P->Lz, P->kz0, P->Nr, P->Mz);
   const size_t W3 = (size_t)P->W * P->W * P->W;
   const size_t Qc3 = (size_t)P->Qc * P->Qc * P->Qc;
+  P->sum_stride = (W3 + 3) & ~(size_t)3;
+  P->iq_stride = (Qc3 + 3) & ~(size_t)3;
   if ((st = upload(&P->d_structs, P->structs, &B)) ||
       (st = upload(&P->d_phis, P->phis, &B)) ||
       (st = upload(&P->d_clbase, clbase, &B)) ||
@@ -1244,9 +1255,11 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_sconst, P->n_slices, &B)) ||
       (st = alloc(&P->d_colofs, (size_t)n_phi * P->Nc, &B)) ||
       (st = alloc(&P->d_C2, (size_t)P->W * P->W, &B)) ||
-      (st = (p->accum == GW_ACCUM_KAHAN32 ? alloc(&P->d_sumk, W3, &B)
-                                          : alloc(&P->d_sum, W3, &B))) ||
-      (st = alloc(&P->d_iq64, Qc3, &B)) || (st = alloc(&P->d_iq32, Qc3, &B)) ||
+      (st = (p->accum == GW_ACCUM_KAHAN32
+                 ? alloc(&P->d_sumk, P->sum_stride * P->n_out, &B)
+                 : alloc(&P->d_sum, P->sum_stride * P->n_out, &B))) ||
+      (st = alloc(&P->d_iq64, P->iq_stride * P->n_out, &B)) ||
+      (st = alloc(&P->d_iq32, P->iq_stride * P->n_out, &B)) ||
       (st = alloc(&P->d_ymax, P->n_slices, &B)) ||
       (st = alloc(&P->d_extflag, P->n_slices, &B)) ||
       (st = alloc(&P->d_zhist, (size_t)n_struct * (g + 1), &B)) ||
@@ -1464,15 +1477,23 @@ extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) 
   if (!P || !iq) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq: plan not executed");
   const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
-  GW_CUDA(cudaMemcpyAsync(iq, P->d_iq64, n * sizeof(double),
-                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                          P->ctx->stream));
+  // one 2-D copy packs the structures' padded grids back to back
+  GW_CUDA(cudaMemcpy2DAsync(iq, n * sizeof(double), P->d_iq64,
+                            P->iq_stride * sizeof(double), n * sizeof(double),
+                            P->n_out,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                            P->ctx->stream));
   return gw::check_device_error(P->ctx, "voxel stage");
 }
 
-extern "C" int gw_voxel_device_iq32(gw_voxel_plan *P, const float **iq32) {
+extern "C" int gw_voxel_device_iq32(gw_voxel_plan *P, int32_t structure,
+                                    const float **iq32) {
   if (!P || !iq32) return gw::fail(GW_ERR_ARG, "gw_voxel_device_iq32: null argument");
-  *iq32 = P->d_iq32;
+  if (structure < 0 || structure >= P->n_out)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_device_iq32: structure " +
+                                    std::to_string(structure) + " outside [0, " +
+                                    std::to_string(P->n_out) + ")");
+  *iq32 = P->d_iq32 + (size_t)structure * P->iq_stride;
   return GW_OK;
 }
 

@@ -70,6 +70,7 @@ struct BinArgs {
   int kahan;
   int k0, kz0;        // frequency of output column 0 / row 0
   float dc_scale;     // g*g
+  int64_t sstride;    // window^3 per structure in separate mode, else 0
 };
 
 struct SliceConst {
@@ -299,6 +300,11 @@ struct gw_voxel_plan {
   int radius = 0, bil = 0;
   int y_lo = 0, Ly = 0, z_lo = 0, Lz = 0, k0 = 0, Nc = 0, kz0 = 0, Nr = 0;
   int My = 0, Mz = 0, S = 1;
+  int n_out = 1;           // I(q) grids produced: n_struct in separate mode
+  // element strides between the structures' sum and I(q) grids, rounded up
+  // to 4 so that every grid starts 16-byte aligned for the vector loads and
+  // stores of the finalize kernel
+  size_t sum_stride = 0, iq_stride = 0;
   int64_t n_atoms = -1;
   size_t bytes = 0;
   std::vector<int> C1host;

@@ -199,7 +199,9 @@ class VoxelPlan:
         p.smooth = float(smooth) if smooth else 0.0
         p.mode = {"batched": N.GW_VOXEL_BATCHED, "plain": N.GW_VOXEL_PLAIN}[mode]
         p.accum = {"fp64": N.GW_ACCUM_FP64, "kahan32": N.GW_ACCUM_KAHAN32}[accum]
-        p.average = int(bool(average))
+        # True/False: average/sum over structures; "separate": one I(q) each
+        p.average = 2 if average == "separate" else int(bool(average))
+        self.n_out = len(structures) if average == "separate" else 1
         coef, z = f0_params(f0_element)
         for i in range(9):
             p.f0_coef[i] = coef[i]
@@ -235,16 +237,21 @@ class VoxelPlan:
         N.check(N.lib().gw_voxel_capture_graph(self.handle))
 
     def iq(self, out=None):
-        out = np.empty((self.Qc,) * 3) if out is None else out
+        """I(q) (Qc, Qc, Qc); (n_struct, Qc, Qc, Qc) for separate structures."""
+        shape = (self.Qc,) * 3 if self.n_out == 1 else (self.n_out,) + (self.Qc,) * 3
+        out = np.empty(shape) if out is None else out
         N.check(N.lib().gw_voxel_get_iq(self.handle, N.ptr(out), 0))
         return out
 
     def iq_to_device(self, dev_ptr):
         N.check(N.lib().gw_voxel_get_iq(self.handle, ctypes.c_void_p(dev_ptr), 1))
 
-    def device_iq32(self):
+    def device_iq32(self, structure=0):
+        """Device address of the float32 I(q) (of one structure when they
+        are separate)."""
         p = ctypes.c_void_p()
-        N.check(N.lib().gw_voxel_device_iq32(self.handle, ctypes.byref(p)))
+        N.check(N.lib().gw_voxel_device_iq32(self.handle, int(structure),
+                                             ctypes.byref(p)))
         return p.value
 
     def counts(self):
@@ -513,6 +520,12 @@ class DetectorPlan:
         out = np.empty((self.params.n_v, self.params.n_h))
         N.check(N.lib().gw_detector_get(self.handle, N.ptr(out), 0))
         return out
+
+    def device_result(self):
+        """Device address of the image the last execute wrote."""
+        p = ctypes.c_void_p()
+        N.check(N.lib().gw_detector_device_out(self.handle, ctypes.byref(p)))
+        return p.value
 
     def backward(self, g_image, g_iq_device=None):
         """dL/dI(q) from dL/d(image of result()) (gw_detector_backward).

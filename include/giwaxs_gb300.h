@@ -92,6 +92,7 @@ int gw_collapse_base(const double *ver, const double *cos_t, int64_t n,
 /* ---- voxel stage: I(qx,qy,qz) from atoms ----------------------------- */
 enum { GW_VOXEL_BATCHED = 0, GW_VOXEL_PLAIN = 1 };
 enum { GW_ACCUM_FP64 = 0, GW_ACCUM_KAHAN32 = 1 };
+enum { GW_STRUCTS_SUM = 0, GW_STRUCTS_AVERAGE = 1, GW_STRUCTS_SEPARATE = 2 };
 enum { GW_DEPOSIT_NEAREST = 0, GW_DEPOSIT_BILINEAR = 1 };
 
 typedef struct gw_voxel_params {
@@ -107,8 +108,11 @@ typedef struct gw_voxel_params {
   double smooth;        /* sigma in r-voxels, 0 = off    voxelgrids.py:364 */
   int32_t mode;         /* GW_VOXEL_BATCHED | GW_VOXEL_PLAIN               */
   int32_t accum;        /* GW_ACCUM_FP64 | GW_ACCUM_KAHAN32                */
-  int32_t average;      /* 1: divide by the number of structures
-                           (old_modules/voxelgridmaker.py:56-61)           */
+  int32_t average;      /* GW_STRUCTS_AVERAGE: one I(q) averaged over the
+                           structures (old_modules/voxelgridmaker.py:56-61);
+                           GW_STRUCTS_SUM: their sum; GW_STRUCTS_SEPARATE:
+                           one I(q) per structure, concatenated (candidates
+                           of a fit evaluated in one pass)                 */
   double f0_coef[9];    /* Cromer-Mann a1,b1,..,a4,b4,c  voxelgrids.py:849 */
   double f0_z;          /* Z of the f0 element; <= 0 skips the f0 factor   */
   int32_t batch_slices; /* slices per batch, 0 = automatic                 */
@@ -158,11 +162,15 @@ int gw_voxel_set_atoms(gw_voxel_plan *plan, const double *xyz, const float *f,
  * replay when gw_voxel_capture_graph succeeded). */
 int gw_voxel_execute(gw_voxel_plan *plan);
 int gw_voxel_capture_graph(gw_voxel_plan *plan);
-/* Results (synchronous).  iq: crop^3 float64, C order (qy,qx,qz).
+/* Results (synchronous).  iq: crop^3 float64, C order (qy,qx,qz); in
+ * GW_STRUCTS_SEPARATE mode n_struct such grids back to back.
  * on_device: write to a device pointer instead of host memory. */
 int gw_voxel_get_iq(gw_voxel_plan *plan, double *iq, int32_t on_device);
-/* Device pointer to the float32 copy of I(q) the detector gathers from. */
-int gw_voxel_device_iq32(gw_voxel_plan *plan, const float **iq32);
+/* Device pointer to the float32 copy of I(q) the detector gathers from
+ * (of structure `structure` in GW_STRUCTS_SEPARATE mode, else 0).  Each
+ * grid starts 16-byte aligned. */
+int gw_voxel_device_iq32(gw_voxel_plan *plan, int32_t structure,
+                         const float **iq32);
 /* Parity hooks: the cropped count and sum grids (float64, crop^3). */
 int gw_voxel_get_counts(gw_voxel_plan *plan, double *counts);
 int gw_voxel_get_sums(gw_voxel_plan *plan, double *sums);
@@ -224,6 +232,9 @@ int gw_detector_set_iq32_device(gw_detector_plan *plan, const float *iq32);
 int gw_detector_execute(gw_detector_plan *plan);
 /* (n_v, n_h) float64 image after the epilogue (comparison.py:857-868). */
 int gw_detector_get(gw_detector_plan *plan, double *out, int32_t on_device);
+/* Device address of the plan's image (n_v, n_h) float64, valid until the
+ * plan is destroyed and rewritten by every execute. */
+int gw_detector_device_out(gw_detector_plan *plan, const double **out);
 /* Flat (y*nx+x)*nz+z voxel index each pixel gathers for orientation o. */
 int gw_detector_debug_indices(gw_detector_plan *plan, int32_t orient,
                               int64_t *flat_idx);
