@@ -571,6 +571,8 @@ extern "C" int gw_voxel_backward(gw_voxel_plan *P, const double *g_iq,
     return gw::fail(GW_ERR_ARG, "gw_voxel_backward: fill_bkg is not differentiated");
   if (P->n_out > 1)
     return gw::fail(GW_ERR_ARG, "gw_voxel_backward: separate structures are not differentiated");
+  if (P->n_shells > 0)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_backward: multi-q shells are not differentiated");
   if (g_xyz && !P->bil)
     return gw::fail(GW_ERR_ARG, "gw_voxel_backward: coordinate gradients need the bilinear deposit");
   if (P->n_atoms < 0)

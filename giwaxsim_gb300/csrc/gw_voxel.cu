@@ -476,6 +476,7 @@ struct ColBin {
     if (mr >= nr || m >= nc) return;
     const int co = cofs[m], ro = bn->rowofs[mr];
     if (co < 0 || ro < 0) return;
+    if (bn->shell && !shell_member(bn->shell[co + ro], bn->shell_k)) return;
     float2 X = cmul(v, __ldg(B + mr));
     if (bn->k0 + m == 0 && bn->kz0 + mr == 0) {
       X.x += cbg.x * bn->dc_scale;
@@ -648,6 +649,51 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
     } else {
       out64[i0] = I[0];
       out32[i0] = (float)I[0];
+    }
+  }
+}
+
+// Shell code of every window voxel (voxelgrids.py:651-652, :659-664, :706):
+// |q| = sqrt((qx^2 + qy^2) + qz^2) as numpy evaluates the meshgrid sum, and
+// shell k holds lower[k] < |q| <= upper[k].  Shells are increasing, so a
+// voxel lies in at most two adjacent ones.
+__global__ void k_shell_codes(const double *qw, int W, const double *lower,
+                              const double *upper, int K, unsigned short *codes) {
+  const int64_t n = (int64_t)W * W * W;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(i % W);
+    const int64_t line = i / W;
+    const int ix = (int)(line % W), iy = (int)(line / W);
+    const double qx = qw[ix], qy = qw[iy], qz = qw[iz];
+    const double qr = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(qx, qx), __dmul_rn(qy, qy)),
+                                           __dmul_rn(qz, qz)));
+    unsigned short c = kNoShell;
+    for (int k = 0; k < K; ++k)
+      if (qr <= upper[k] && qr > lower[k]) {
+        const bool next = k + 1 < K && qr <= upper[k + 1] && qr > lower[k + 1];
+        c = (unsigned short)(2 * k + (next ? 1 : 0));
+        break;
+      }
+    codes[i] = c;
+  }
+}
+
+// The reference's multi-q result (voxelgrids.py:703-707): the last shell's
+// I(q) everywhere, doubled inside that shell.  Doubling is exact in float64
+// and float32.
+__global__ void k_shell_double(const unsigned short *codes, int W, int off,
+                               int Qc, int k, double *out64, float *out32) {
+  const int64_t n = (int64_t)Qc * Qc * Qc;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(i % Qc);
+    const int64_t line = i / Qc;
+    const int ix = (int)(line % Qc), iy = (int)(line / Qc);
+    const int64_t w = ((int64_t)(iy + off) * W + (ix + off)) * W + (iz + off);
+    if (shell_member(codes[w], k)) {
+      out64[i] *= 2.0;
+      out32[i] *= 2.f;
     }
   }
 }
@@ -992,19 +1038,37 @@ int enqueue(gw_voxel_plan *P) {
     GW_CUDA(cudaMemsetAsync(P->d_sumk, 0, P->sum_stride * P->n_out * sizeof(float2), st));
   else
     GW_CUDA(cudaMemsetAsync(P->d_sum, 0, P->sum_stride * P->n_out * sizeof(double), st));
-  GW_TRY(enqueue_prep(P));
   SliceArgs a = slice_args(P);
   CztArgs cy{P->My, P->Ly, P->Nc, P->d_Ay, P->d_Hy, P->d_By, P->d_twy};
   CztArgs cz{P->Mz, P->Lz, P->Nr, P->d_Az, P->d_Hz, P->d_Bz, P->d_twz};
   BinArgs bn{P->d_colofs, P->d_rowofs, P->d_sum, P->d_sumk,
              P->p.accum == GW_ACCUM_KAHAN32, P->k0, P->kz0,
              (float)((double)P->g * (double)P->g),
-             P->n_out > 1 ? (int64_t)P->sum_stride : 0};
-  for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
-    const int n = std::min(P->S, P->n_slices - s0);
-    GW_TRY(enqueue_slice_setup(P, a, s0, n));
-    GW_TRY(row_dispatch(P, a, cy, s0, n));
-    GW_TRY(col_dispatch(P, a, cz, bn, s0, n));
+             P->n_out > 1 ? (int64_t)P->sum_stride : 0, nullptr, 0};
+  // Multi-q form factors: one pass per shell with that shell's atom f
+  // values and average voxel f, binning only the shell's voxels into the
+  // common sums (GW_SHELLS_PER_SHELL); or the reference's single pass with
+  // the last shell's values (GW_SHELLS_REFERENCE).
+  const int K = P->n_shells;
+  const int k_first = K > 0 && P->shell_mode == GW_SHELLS_PER_SHELL ? 0 : K - 1;
+  for (int k = std::max(k_first, 0); k < std::max(K, 1); ++k) {
+    if (K > 0) {
+      GW_CUDA(cudaMemcpyAsync(P->d_f, P->d_f_shells + (size_t)k * P->n_atoms,
+                              (size_t)P->n_atoms * sizeof(float2),
+                              cudaMemcpyDeviceToDevice, st));
+      GW_CUDA(cudaMemcpyAsync(P->d_structs, P->d_structs_shells + (size_t)k * P->n_struct,
+                              (size_t)P->n_struct * sizeof(gw_structure),
+                              cudaMemcpyDeviceToDevice, st));
+      bn.shell = P->shell_mode == GW_SHELLS_PER_SHELL ? P->d_shell : nullptr;
+      bn.shell_k = k;
+    }
+    GW_TRY(enqueue_prep(P));
+    for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
+      const int n = std::min(P->S, P->n_slices - s0);
+      GW_TRY(enqueue_slice_setup(P, a, s0, n));
+      GW_TRY(row_dispatch(P, a, cy, s0, n));
+      GW_TRY(col_dispatch(P, a, cz, bn, s0, n));
+    }
   }
   const int fin_blocks = P->Qc * P->Qc;
   const float f0c = (float)P->p.f0_coef[8];
@@ -1031,6 +1095,13 @@ int enqueue(gw_voxel_plan *P) {
       k_finalize<<<fin_blocks, fin_threads, 0, st>>>(
           sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
           inv_ns, P->d_f0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
+      GW_LAUNCHED(ctx);
+    }
+    if (K > 0 && P->shell_mode == GW_SHELLS_REFERENCE) {
+      gw::KTimer tm(ctx, GW_K_FINALIZE);
+      const int blocks = (int)std::min<int64_t>(((int64_t)Qc3 + 255) / 256, 16 * ctx->sm_count);
+      k_shell_double<<<blocks, 256, 0, st>>>(P->d_shell, P->W, P->lo - P->wlo,
+                                             P->Qc, K - 1, o64, o32);
       GW_LAUNCHED(ctx);
     }
   }
@@ -1309,7 +1380,8 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
                   P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_fz_s,
                   P->d_perm, P->d_cand, P->d_cand_off, P->d_roff, P->d_zhist, P->d_rowstart,
-                  P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag};
+                  P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
+                  P->d_shell, P->d_f_shells, P->d_structs_shells};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -1404,6 +1476,7 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   GW_CUDA(cudaMemcpyAsync(P->d_xyz, xyz, (size_t)n * 3 * sizeof(double), kind, P->ctx->stream));
   GW_CUDA(cudaMemcpyAsync(P->d_f, f, (size_t)n * sizeof(float2), kind, P->ctx->stream));
+  P->f_stale = false;
   // hull-near atoms per structure (host coordinates only; device-resident
   // atoms keep the full scan).  The arrays keep their addresses, so a
   // captured graph stays valid.
@@ -1435,11 +1508,108 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
   return GW_OK;
 }
 
+extern "C" int gw_voxel_set_shells(gw_voxel_plan *P, int32_t n_shells,
+                                   int32_t mode, const double *q_axis,
+                                   const double *lower, const double *upper,
+                                   const float *f, const double *avg_f) {
+  if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: null plan");
+  auto drop = [P]() {
+    gw::dev_free(P->d_shell); gw::dev_free(P->d_f_shells);
+    gw::dev_free(P->d_structs_shells);
+    P->d_shell = nullptr; P->d_f_shells = nullptr; P->d_structs_shells = nullptr;
+    if (P->n_shells > 0) P->f_stale = true;
+    P->n_shells = 0;
+    P->shell_atoms = -1;
+    if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    if (P->graph) { cudaGraphDestroy(P->graph); P->graph = nullptr; }
+  };
+  GW_CUDA(cudaSetDevice(P->ctx->device));
+  GW_CUDA(cudaStreamSynchronize(P->ctx->stream));  // no pass reads the tables
+  if (n_shells == 0) { drop(); return GW_OK; }
+  if (n_shells < 0 || n_shells > 32767)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: n_shells outside [0, 32767]");
+  if (mode != GW_SHELLS_PER_SHELL && mode != GW_SHELLS_REFERENCE)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: unknown mode");
+  if (!q_axis || !lower || !upper || !f || !avg_f)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: null argument");
+  if (P->n_atoms < 1)
+    return gw::fail(GW_ERR_STATE, "gw_voxel_set_shells: set the atoms first");
+  if (P->grad) return gw::fail(GW_ERR_STATE, "gw_voxel_set_shells: plan has gradient state");
+  for (int k = 0; k < n_shells; ++k) {
+    if (!(lower[k] < upper[k]))
+      return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: shell with lower >= upper");
+    if (k + 1 < n_shells && !(lower[k + 1] > lower[k] && upper[k + 1] > upper[k]))
+      return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: shells must increase");
+    if (k + 2 < n_shells && !(lower[k + 2] >= upper[k]))
+      return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: a shell overlaps the one after next");
+  }
+  drop();
+  const int K = n_shells;
+  const size_t W3 = (size_t)P->W * P->W * P->W;
+  std::vector<gw_structure> st((size_t)K * P->n_struct);
+  for (int k = 0; k < K; ++k)
+    for (int t = 0; t < P->n_struct; ++t) {
+      gw_structure s = P->structs[t];
+      s.avg_f_re = avg_f[2 * ((size_t)k * P->n_struct + t)];
+      s.avg_f_im = avg_f[2 * ((size_t)k * P->n_struct + t) + 1];
+      st[(size_t)k * P->n_struct + t] = s;
+    }
+  std::vector<double> qw(q_axis + P->wlo, q_axis + P->whi + 1);
+  std::vector<double> bounds(lower, lower + K);
+  bounds.insert(bounds.end(), upper, upper + K);
+  double *d_qw = nullptr, *d_bounds = nullptr;
+  cudaStream_t s = P->ctx->stream;
+  cudaError_t e = gw::dev_malloc((void **)&P->d_shell, W3 * sizeof(unsigned short));
+  if (e == cudaSuccess) e = gw::dev_malloc((void **)&P->d_f_shells, (size_t)K * P->n_atoms * sizeof(float2));
+  if (e == cudaSuccess) e = gw::dev_malloc((void **)&P->d_structs_shells, st.size() * sizeof(gw_structure));
+  if (e == cudaSuccess) e = gw::dev_malloc((void **)&d_qw, qw.size() * sizeof(double));
+  if (e == cudaSuccess) e = gw::dev_malloc((void **)&d_bounds, bounds.size() * sizeof(double));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->d_f_shells, f, (size_t)K * P->n_atoms * sizeof(float2),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->d_structs_shells, st.data(), st.size() * sizeof(gw_structure),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_qw, qw.data(), qw.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_bounds, bounds.data(), bounds.size() * sizeof(double),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    const int blocks = (int)std::min<int64_t>(((int64_t)W3 + 255) / 256, 16 * P->ctx->sm_count);
+    k_shell_codes<<<blocks, 256, 0, s>>>(d_qw, P->W, d_bounds, d_bounds + K, K, P->d_shell);
+    P->ctx->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  gw::dev_free(d_qw);
+  gw::dev_free(d_bounds);
+  if (e != cudaSuccess) {
+    drop();
+    return gw::cuda_fail(e, "gw_voxel_set_shells", __FILE__, __LINE__);
+  }
+  P->n_shells = K;
+  P->shell_mode = mode;
+  P->shell_atoms = P->n_atoms;
+  return GW_OK;
+}
+
 static int voxel_enqueue_all(gw_voxel_plan *P) { return enqueue(P); }
+
+static int shell_state(gw_voxel_plan *P, const char *who) {
+  if (P->n_shells > 0 && P->shell_atoms != P->n_atoms)
+    return gw::fail(GW_ERR_STATE, std::string(who) +
+                                      ": the atom count changed after gw_voxel_set_shells");
+  if (P->n_shells == 0 && P->f_stale)
+    return gw::fail(GW_ERR_STATE, std::string(who) +
+                                      ": shells were cleared; set the atoms again");
+  return GW_OK;
+}
 
 extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
   if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_execute: null plan");
   if (P->n_atoms < 0) return gw::fail(GW_ERR_STATE, "gw_voxel_execute: atoms not set");
+  GW_TRY(shell_state(P, "gw_voxel_execute"));
   GW_CUDA(cudaSetDevice(P->ctx->device));
   if (P->gexec) {
     GW_CUDA(cudaGraphLaunch(P->gexec, P->ctx->stream));
@@ -1454,6 +1624,7 @@ extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
 extern "C" int gw_voxel_capture_graph(gw_voxel_plan *P) {
   if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_capture_graph: null plan");
   if (P->n_atoms < 0) return gw::fail(GW_ERR_STATE, "gw_voxel_capture_graph: atoms not set");
+  GW_TRY(shell_state(P, "gw_voxel_capture_graph"));
   if (P->gexec) return GW_OK;
   GW_CUDA(cudaSetDevice(P->ctx->device));
   // first-launch attributes must be set outside capture

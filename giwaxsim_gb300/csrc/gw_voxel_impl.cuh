@@ -71,7 +71,20 @@ struct BinArgs {
   int k0, kz0;        // frequency of output column 0 / row 0
   float dc_scale;     // g*g
   int64_t sstride;    // window^3 per structure in separate mode, else 0
+  // q-shell pass (multi-q form factors): bin only the voxels of shell
+  // shell_k; null = every voxel
+  const unsigned short *shell;
+  int shell_k;
 };
+
+// Shell code of a voxel: 2 k + 1 if it lies in shells k and k + 1 (a
+// boundary rounding case), 2 k if in shell k only, kNoShell if in none.
+constexpr unsigned short kNoShell = 0xFFFF;
+__device__ __forceinline__ bool shell_member(unsigned short c, int k) {
+  if (c == kNoShell) return false;
+  const int k1 = c >> 1;
+  return k == k1 || ((c & 1) && k == k1 + 1);
+}
 
 struct SliceConst {
   float2 cbg, cd;
@@ -305,6 +318,14 @@ struct gw_voxel_plan {
   // to 4 so that every grid starts 16-byte aligned for the vector loads and
   // stores of the finalize kernel
   size_t sum_stride = 0, iq_stride = 0;
+  // multi-q form factors: n_shells passes with per-shell atom f values and
+  // structure tables (0 = off)
+  int n_shells = 0, shell_mode = 0;
+  int64_t shell_atoms = -1;    // n_atoms the shell tables were made for
+  bool f_stale = false;        // d_f holds a shell's f values, not the atoms'
+  unsigned short *d_shell = nullptr;  // window^3 shell codes
+  float2 *d_f_shells = nullptr;       // [n_shells][n_atoms]
+  gw_structure *d_structs_shells = nullptr;  // [n_shells][n_struct]
   int64_t n_atoms = -1;
   size_t bytes = 0;
   std::vector<int> C1host;

@@ -230,6 +230,36 @@ class VoxelPlan:
             N.check(N.lib().gw_voxel_set_atoms(self.handle, N.ptr(xyz), N.ptr(f),
                                                len(xyz), 0))
 
+    def set_shells(self, q_axis, lower, upper, f_shells, avg_shells,
+                   mode="per_shell"):
+        """Multi-q form factors (voxelgrids.py:650-707): shell k (lower[k] <
+        |q| <= upper[k]) takes its I(q) from a pass with the per-atom f
+        values f_shells[k] (n_atoms complex, in the plan's atom order) and
+        the per-structure avg_voxel_f avg_shells[k].  mode "per_shell" or
+        "reference" (the reference's own output, see gw_voxel_set_shells).
+        Call after set_atoms; set_shells(None) clears them (set the atoms
+        again afterwards)."""
+        if q_axis is None:
+            N.check(N.lib().gw_voxel_set_shells(self.handle, 0, 0, None, None,
+                                                None, None, None))
+            return
+        lower = np.ascontiguousarray(lower, dtype=np.float64)
+        upper = np.ascontiguousarray(upper, dtype=np.float64)
+        K = len(lower)
+        f = np.ascontiguousarray(np.asarray(f_shells, dtype=np.complex64)
+                                 .reshape(K, len(self.xyz)))
+        avg = np.ascontiguousarray(np.asarray(avg_shells, dtype=np.complex128)
+                                   .reshape(K, len(self.structs)))
+        q = np.ascontiguousarray(q_axis, dtype=np.float64)
+        if len(q) != self.params.q_num or len(upper) != K:
+            raise ValueError("q_axis must be the full q axis and lower/upper "
+                             "one value per shell")
+        m = {"per_shell": N.GW_SHELLS_PER_SHELL,
+             "reference": N.GW_SHELLS_REFERENCE}[mode]
+        N.check(N.lib().gw_voxel_set_shells(self.handle, K, m, N.ptr(q),
+                                            N.ptr(lower), N.ptr(upper),
+                                            N.ptr(f), N.ptr(avg)))
+
     def execute(self):
         N.check(N.lib().gw_voxel_execute(self.handle))
 

@@ -153,6 +153,9 @@ def rotate_coords_z(coords, phi):
 
 
 def get_element_f0_dict(q_val, elements):
+    """f0 per element at q_val (utilities.py:318-340): the Cromer-Mann sum
+    with the exponent -b q / (16 pi^2), q and not q^2, as the reference
+    writes it (its multi-q shells call this)."""
     out = {}
     for el in set(elements):
         a = aff_dict[el]

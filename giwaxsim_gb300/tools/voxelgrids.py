@@ -5,7 +5,8 @@
   rotate_project_fft_coords    voxelgrids.py:311-416 -> one-slice plain plan,
                                accumulated into the named shared-memory grids
   process_file2                voxelgrids.py:464-506 -> gw_bin_slice
-  generate_voxel_grid_low_mem  voxelgrids.py:535-722 (aff_num_qs == 1)
+  generate_voxel_grid_low_mem  voxelgrids.py:535-722 (aff_num_qs >= 1; the
+                               multi-q shells -> gw_voxel_set_shells)
   add_f0_q_3d                  voxelgrids.py:828-857 -> gw_f0_scale
 
 The per-slice functions keep the reference's calling convention (shared
@@ -21,7 +22,8 @@ import numpy as np
 from .. import _native as N
 from ..forward import VoxelGeometry, VoxelPlan, element_f_values
 from .ptable_dict import aff_dict, ptable
-from .utilities import load_pdb, load_xyz
+from .utilities import (get_element_f0_dict, get_element_f1_f2_dict, load_pdb,
+                        load_xyz)
 
 
 def _axes_identical(qx, qy, qz):
@@ -137,18 +139,47 @@ def add_f0_q_3d(iq, qx_axis, qy_axis, qz_axis, element, ctx=None):
     return out
 
 
+def aff_shell_tables(q_axis, aff_num_qs, elements, energy, f1f2=None):
+    """Shell bounds and per-shell atom f values of the multi-q branch
+    (voxelgrids.py:659-669): K = aff_num_qs shells of width
+    step = max_q_diag / K over (0, max_q_diag], shell k centred at
+    q_k = step/2 + k step, atoms scattering with f0(q_k) + f' + i f''.
+    Returns (lower, upper, f (K, n_atoms) complex)."""
+    K = int(aff_num_qs)
+    max_q_diag = q_axis[-1]
+    step = max_q_diag / K
+    elements = np.asarray(elements)
+    d = f1f2 if f1f2 is not None else get_element_f1_f2_dict(energy, elements)
+    lower, upper, f = [], [], []
+    for k in range(K):
+        q_val = 0.5 * step + k * step
+        upper.append(q_val + step / 2)
+        lower.append(q_val - step / 2)
+        f0 = get_element_f0_dict(q_val, elements)
+        f.append(np.array([f0[e] for e in elements])
+                 + np.array([d[e] for e in elements]))
+    return np.array(lower), np.array(upper), np.array(f, dtype=complex)
+
+
 def generate_voxel_grid_low_mem(input_path, r_voxel_size, q_voxel_size, max_q,
                                 aff_num_qs, energy, gen_name, output_dir=None,
                                 scratch_folder=None, num_cpus=None,
                                 fill_bkg=False, smooth=0, *, phis=None,
-                                ctx=None):
+                                aff_mode="reference", f1f2=None, ctx=None):
     """Full q_num^3 I(q) of one structure file (voxelgrids.py:535-722).
-    Only aff_num_qs == 1 is provided: the reference's multi-q branch
-    accumulates the grid onto itself (voxelgrids.py:707)."""
-    if int(aff_num_qs) != 1:
-        if int(aff_num_qs) < 1:
-            raise Exception("Invalid aff_num_qs value. Must be non-negative integer")
-        raise NotImplementedError("aff_num_qs > 1 is not provided")
+
+    aff_num_qs > 1 evaluates the atomic form factors per q shell
+    (voxelgrids.py:650-707).  aff_mode "reference" returns what the
+    reference returns: its loop overwrites the grid with every shell's I(q)
+    and adds the shell-masked grid to itself (:703-707), i.e. the last
+    shell's I(q) over the whole grid, doubled inside the last shell.
+    aff_mode "per_shell" gives each voxel the I(q) of its own shell (the
+    evident intent; 0 outside every shell), in one device pass per shell.
+    f1f2: element -> f' + i f'' (default: the xraydb lookup)."""
+    if int(aff_num_qs) < 1:
+        raise Exception("Invalid aff_num_qs value. Must be non-negative integer")
+    if aff_mode not in ("reference", "per_shell"):
+        raise ValueError("aff_mode must be 'reference' or 'per_shell'")
     geom = VoxelGeometry(r_voxel_size, q_voxel_size, max_q)
     if input_path[-3:] == "xyz":
         coords, elements = load_xyz(input_path)
@@ -158,12 +189,20 @@ def generate_voxel_grid_low_mem(input_path, r_voxel_size, q_voxel_size, max_q,
         raise Exception("files must be a .pdb or .xyz file")
     geom.check_bounds(coords)
     full = VoxelGeometry.from_axes(geom.grid_size, r_voxel_size, geom.q)
-    fv = element_f_values(elements, energy)
+    fv = element_f_values(elements, energy, f1f2)
     plan = VoxelPlan(full, [(coords, fv, None)],
                      phis=geom.auto_phis if phis is None else phis,
                      fill_bkg=fill_bkg, smooth=smooth, f0_element=None, ctx=ctx)
     try:
         plan.set_atoms()
+        if int(aff_num_qs) > 1:
+            lower, upper, fk = aff_shell_tables(geom.q, aff_num_qs, elements,
+                                                energy, f1f2)
+            r3 = r_voxel_size ** 3
+            b = plan.structs[0]
+            vol = b["x_bound"] * b["y_bound"] * b["z_bound"]
+            avg = np.array([[(np.sum(f) / vol) * r3] for f in fk])
+            plan.set_shells(geom.q, lower, upper, fk, avg, mode=aff_mode)
         plan.execute()
         iq = plan.iq()
     finally:

@@ -94,6 +94,7 @@ enum { GW_VOXEL_BATCHED = 0, GW_VOXEL_PLAIN = 1 };
 enum { GW_ACCUM_FP64 = 0, GW_ACCUM_KAHAN32 = 1 };
 enum { GW_STRUCTS_SUM = 0, GW_STRUCTS_AVERAGE = 1, GW_STRUCTS_SEPARATE = 2 };
 enum { GW_DEPOSIT_NEAREST = 0, GW_DEPOSIT_BILINEAR = 1 };
+enum { GW_SHELLS_PER_SHELL = 1, GW_SHELLS_REFERENCE = 2 };
 
 typedef struct gw_voxel_params {
   int32_t grid_size;    /* g = ceil(2pi/(dq*r))          comparison.py:710 */
@@ -158,6 +159,26 @@ int gw_voxel_plan_destroy(gw_voxel_plan *plan);
  * (device pointers are copied into the plan). */
 int gw_voxel_set_atoms(gw_voxel_plan *plan, const double *xyz, const float *f,
                        int64_t n_atoms, int32_t on_device);
+/* Multi-q atomic form factors (voxelgrids.py:650-707, aff_num_qs > 1).
+ * Shell k holds the voxels with lower[k] < |q| <= upper[k], |q| taken from
+ * q_axis (the full q axis, q_num values) as numpy's meshgrid sum does; f is
+ * n_shells x n_atoms complex float32 (f0(q_k) + f' + i f'' per atom) and
+ * avg_f n_shells x n_struct complex float64 (avg_voxel_f per shell).
+ *   GW_SHELLS_PER_SHELL  one pass per shell, each voxel's I(q) from the
+ *                        pass of its own shell (of both shells for a voxel
+ *                        on a rounding boundary), voxels in no shell 0;
+ *   GW_SHELLS_REFERENCE  what the reference returns: the last shell's pass
+ *                        over every voxel, doubled inside the last shell
+ *                        (voxelgrids.py:703-707 overwrite the grid each
+ *                        shell and add the masked grid to itself).
+ * Call after gw_voxel_set_atoms; n_shells = 0 clears the shells (the atoms
+ * must then be set again: the passes overwrite the plan's copy of f).
+ * Shells must increase, and shell k + 2 must start at or above the end of
+ * shell k. */
+int gw_voxel_set_shells(gw_voxel_plan *plan, int32_t n_shells, int32_t mode,
+                        const double *q_axis, const double *lower,
+                        const double *upper, const float *f,
+                        const double *avg_f);
 /* Enqueue the whole forward chain on the context stream (a CUDA graph
  * replay when gw_voxel_capture_graph succeeded). */
 int gw_voxel_execute(gw_voxel_plan *plan);

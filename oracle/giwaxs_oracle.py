@@ -100,6 +100,18 @@ def fma_xyz(x, y, z, R):
 Z_OF = {"H": 1, "C": 6, "N": 7, "O": 8, "F": 9, "Si": 14, "S": 16}
 CROMER_MANN = {
     "C": (2.31, 20.8439, 1.02, 10.2075, 1.5886, 0.5687, 0.865, 51.6512, 0.2156),
+    "H": (0.489918, 20.6593, 0.262003, 7.74039, 0.196767, 49.5519, 0.049879,
+          2.20159, 0.001305),
+    "N": (12.2126, 0.0057, 3.1322, 9.8933, 2.0125, 28.9975, 1.1663, 0.5826,
+          -11.529),
+    "O": (3.0485, 13.2771, 2.2868, 5.7011, 1.5463, 0.3239, 0.867, 32.9089,
+          0.2508),
+    "F": (3.5392, 10.2825, 2.6412, 4.2944, 1.517, 0.2615, 1.0243, 26.1476,
+          0.2776),
+    "Si": (6.2915, 2.4386, 3.0353, 32.3337, 1.9891, 0.6785, 1.541, 81.6937,
+           1.1407),
+    "S": (6.9053, 1.4679, 5.2034, 22.2151, 1.4379, 0.2536, 1.5863, 56.172,
+          0.8669),
 }
 
 
@@ -354,6 +366,86 @@ def voxelgrid(structures, r_voxel_size, q_voxel_size, max_q, phis=None,
     if keep_full:
         out["full_sum"], out["full_count"] = vsum, vcnt
     return out
+
+
+# --------------------------------------------------------------------------
+# multi-q form factors (generate_voxel_grid_low_mem with aff_num_qs > 1)
+
+def element_f0_at(q_val, element):
+    """utilities.py:318-340 get_element_f0_dict for one element: the
+    Cromer-Mann sum with exponent -b q/(16 pi^2) (q, not q^2, as the
+    reference writes it)."""
+    a = CROMER_MANN[element]
+    s = 16 * np.pi ** 2
+    return (a[0] * np.exp(-a[1] * q_val / s) + a[2] * np.exp(-a[3] * q_val / s)
+            + a[4] * np.exp(-a[5] * q_val / s) + a[6] * np.exp(-a[7] * q_val / s)
+            + a[8])
+
+
+def aff_shells(max_q_diag, aff_num_qs):
+    """voxelgrids.py:659-664: shell centres and (lower, upper] bounds."""
+    K = int(aff_num_qs)
+    step = max_q_diag / K
+    q_vals = np.array([0.5 * step + k * step for k in range(K)])
+    return q_vals, q_vals - step / 2, q_vals + step / 2
+
+
+def shell_masks(q, lower, upper):
+    """voxelgrids.py:651-652, :706: (qr <= upper) & (qr > lower) per shell on
+    the meshgrid |q| of the full axis."""
+    qx, qy, qz = np.meshgrid(q, q, q)
+    qr = np.sqrt(qx ** 2 + qy ** 2 + qz ** 2)
+    return [(qr <= u) & (qr > l) for l, u in zip(lower, upper)]
+
+
+def voxelgrid_multi_q(coords, elements, f1f2, r_voxel_size, q_voxel_size,
+                      max_q, aff_num_qs, phis=None, fill_bkg=False, smooth=0,
+                      mode="reference"):
+    """voxelgrids.py:535-722 with aff_num_qs > 1 on the full q grid.  f1f2:
+    element -> f' + i f''.  Per shell k the atoms scatter with f0(q_k) + f'
+    + i f'' (no Z: the reference's multi-q branch, :665-669) and the average
+    voxel f follows (:671-674).
+
+    mode "reference": what the reference returns.  Its loop overwrites the
+    grid with each shell's I(q) and then adds the shell-masked grid to
+    itself (:703-707), so the result is the last shell's I(q) with the last
+    shell doubled.
+    mode "per_shell": the evident intent, sum over k of shell k's I(q) masked
+    to shell k.
+
+    Returns dict(iq, q, masks, shell_iq) with shell_iq the per-shell grids."""
+    grid_size, q, auto_phis = voxel_geometry(r_voxel_size, q_voxel_size, max_q,
+                                             coords)
+    if phis is None:
+        phis = auto_phis
+    q_vals, lower, upper = aff_shells(q[-1], aff_num_qs)
+    masks = shell_masks(q, lower, upper)
+    elements = np.asarray(elements)
+    qn = len(q)
+    shells = range(len(q_vals)) if mode == "per_shell" else [len(q_vals) - 1]
+    shell_iq = {}
+    for k in shells:
+        fv = np.array([element_f0_at(q_vals[k], e) + f1f2[e] for e in elements],
+                      dtype=complex)
+        xb, yb, zb, avg = structure_constants(coords, fv, r_voxel_size)
+        vsum = np.zeros((qn, qn, qn))
+        vcnt = np.zeros((qn, qn, qn))
+        for phi in phis:
+            grid, _ = project_slice(coords, fv, phi, grid_size, r_voxel_size,
+                                    avg, xb, yb, zb, fill_bkg, smooth)
+            hx, hy, vz = slice_axes(grid_size, r_voxel_size, phi)
+            bin_slice(slice_intensity(grid), hx, hy, vz, q, q, q, vsum, vcnt)
+        shell_iq[k] = np.divide(vsum, vcnt, out=np.zeros_like(vsum),
+                                where=vcnt != 0)
+    if mode == "per_shell":
+        iq = np.zeros((qn, qn, qn))
+        for k, m in enumerate(masks):
+            iq += np.where(m, shell_iq[k], 0)
+    else:
+        last = shell_iq[len(q_vals) - 1]
+        iq = last + np.where(masks[-1], last, 0)
+    return dict(iq=iq, q=q, masks=masks, shell_iq=shell_iq, lower=lower,
+                upper=upper, q_vals=q_vals, phis=np.asarray(phis))
 
 
 # --------------------------------------------------------------------------

@@ -4,6 +4,7 @@ GIWAXSim code itself (a Python package, imported from its checkout).
 Run in a container that has the reference checkout:
     python tests/golden/make_golden.py [/path/to/reference]
     python tests/golden/make_golden.py /path/to/reference pm6   # PM6 example
+    (other fixture groups: slab, compare, multiq)
 
 The reference imports matplotlib, mpl_toolkits, fabio, lmfit and xraydb and
 scipy.signal.tukey at module level; none of these is on the computation path
@@ -345,6 +346,46 @@ def compare():
     print("comparison fixture written")
 
 
+MULTIQ_CASES = [
+    # (name, fill_bkg, smooth, aff_num_qs)
+    ("plain", False, 0, 3),
+    ("fillsmooth", True, 1, 4),
+]
+
+
+def multiq():
+    """The reference's generate_voxel_grid_low_mem (voxelgrids.py:535-722)
+    with aff_num_qs > 1 on a small graphite slab in which every fifth atom is
+    relabelled O (two elements, so the per-shell f values differ by more
+    than a common factor), read back from an .xyz file.  f' = f'' = 0 (the
+    xraydb stub), so f = f0(q_k).  Seconds."""
+    import tempfile
+    comparison, detector, utilities, voxelgrids = _import_reference()
+    xyz = small_graphite(seed=5, size=(12.0, 11.0, 13.0))
+    els = np.array(["O" if i % 5 == 0 else "C" for i in range(len(xyz))])
+    fd, path = tempfile.mkstemp(suffix=".xyz")
+    with os.fdopen(fd, "w") as fh:
+        fh.write("%d\nslab\n" % len(xyz))
+        for e, (x, y, z) in zip(els, xyz):
+            fh.write("%s %.17g %.17g %.17g\n" % (e, x, y, z))
+    coords, elements = utilities.load_xyz(path)
+    r, dq, max_q = 0.5, 0.15, 1.0
+    out = dict(coords=coords, elements=np.asarray(elements), r=r, dq=dq,
+               max_q=max_q)
+    for name, fill, smooth, K in MULTIQ_CASES:
+        iq, qx, qy, qz = voxelgrids.generate_voxel_grid_low_mem(
+            path, r, dq, max_q, K, 10000.0, "mq", output_dir=None,
+            fill_bkg=fill, smooth=smooth)
+        out[name + "_iq"] = iq
+        out[name + "_K"] = K
+        out[name + "_fill"] = fill
+        out[name + "_smooth"] = smooth
+        out["q"] = qx
+    os.remove(path)
+    np.savez_compressed(os.path.join(HERE, "golden_multiq.npz"), **out)
+    print("multi-q fixture written")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "pm6":
         pm6()
@@ -352,5 +393,7 @@ if __name__ == "__main__":
         slab()
     elif len(sys.argv) > 2 and sys.argv[2] == "compare":
         compare()
+    elif len(sys.argv) > 2 and sys.argv[2] == "multiq":
+        multiq()
     else:
         main()

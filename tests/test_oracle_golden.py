@@ -137,3 +137,22 @@ def test_slabmaker_vs_reference(name):
     assert len(coords) == int(d[name + "_n"])
     assert np.array_equal(coords[:8], d[name + "_head"])
     assert _slab_sha(coords, els) == (str(d[name + "_sha"]), str(d[name + "_el_sha"]))
+
+
+@pytest.mark.parametrize("name", ["plain", "fillsmooth"])
+def test_multi_q_vs_reference(name):
+    """generate_voxel_grid_low_mem with aff_num_qs > 1, bit for bit."""
+    d = golden("golden_multiq.npz")
+    r = O.voxelgrid_multi_q(d["coords"], d["elements"], {"C": 0j, "O": 0j},
+                            float(d["r"]), float(d["dq"]), float(d["max_q"]),
+                            int(d[name + "_K"]), fill_bkg=bool(d[name + "_fill"]),
+                            smooth=int(d[name + "_smooth"]))
+    assert np.array_equal(r["q"], d["q"])
+    assert np.array_equal(r["iq"], d[name + "_iq"])
+    # shells cover (0, max_q_diag]: the centre voxel and the cube's corners
+    # lie in none, every other voxel in exactly one
+    n_in = sum(m.astype(int) for m in r["masks"])
+    qx, qy, qz = np.meshgrid(r["q"], r["q"], r["q"])
+    qr = np.sqrt(qx ** 2 + qy ** 2 + qz ** 2)
+    assert n_in.max() == 1
+    assert np.array_equal(n_in == 1, (qr > 0) & (qr <= r["q"][-1]))
