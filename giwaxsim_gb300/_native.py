@@ -42,7 +42,8 @@ EXPORTS = [
     "gw_slab_create", "gw_slab_destroy", "gw_slab_info", "gw_slab_get",
     "gw_slab_device_xyz",
     "gw_compare_create", "gw_compare_destroy", "gw_compare_target",
-    "gw_compare_eval", "gw_detector_device_out",
+    "gw_compare_eval", "gw_detector_device_out", "gw_warp_create",
+    "gw_warp_destroy", "gw_warp_apply", "gw_compare_set_warp",
 ]
 
 
@@ -169,6 +170,10 @@ def _declare(lib):
         "gw_compare_destroy": ([P], ctypes.c_int),
         "gw_compare_target": ([P, P, P], ctypes.c_int),
         "gw_compare_eval": ([P, P, i32, P, P], ctypes.c_int),
+        "gw_warp_create": ([P, i32, i32, i32, i32, P, P, P, P, P, pp], ctypes.c_int),
+        "gw_warp_destroy": ([P], ctypes.c_int),
+        "gw_warp_apply": ([P, P, i32, P, i32], ctypes.c_int),
+        "gw_compare_set_warp": ([P, P], ctypes.c_int),
         "gw_detector_device_out": ([P, pp], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():

@@ -14,8 +14,12 @@ experiment, rebinned once (gw_compare).  Optimisers:
   method="grid"         rounds of K candidates evaluated together on a
                         shrinking grid around the best one.
 
-Not provided: shift_peak (the reference's polar-warp padding of the pi-pi
-peak, comparison.py:566-592); the simulated image is compared as trimmed.
+shift=(pad_width, pad_range) applies shift_peak (the polar-warp padding of
+the pi-pi peak, comparison.py:566-592) to every trimmed image on the device
+before the comparison, as fullfit_model does (fit_slabsize.py:36).
+
+fullfit_model below keeps the reference's signature and return value (the
+residual vector lmfit minimises) and runs on a cached SlabFit.
 """
 import itertools
 
@@ -34,7 +38,9 @@ class SlabFit:
                  angle_init_vals=(0, 0, 0), angle_init_axs=("None",) * 3,
                  psis=(0.0,), psi_weights=None, det_phis=(0.0,),
                  det_phi_weights=None, thetas=(0.0,), theta_weights=None,
-                 mirror=True, f1f2=None, ctx=None):
+                 mirror=True, f1f2=None, shift=None, rebinned=False, ctx=None):
+        """rebinned=True: exp_img / exp_mask are already on the trimmed
+        simulation grid (rebin_map / rebin_mask of fit_slabsize.py:140-142)."""
         self.ctx = ctx or N.default_context()
         self.cell_xyz = np.asarray(cell_xyz, dtype=np.float64)
         self.cell_f = element_f_values(cell_elements, energy, f1f2)
@@ -55,8 +61,13 @@ class SlabFit:
         self.det = DetectorPlan((Qc,) * 3, q, q, q, num_pixels, max_q,
                                 angle_init_vals, angle_init_axs, psis, pw, dph,
                                 hw, th, tw, mirror=mirror, ctx=self.ctx)
+        weights = None
+        if rebinned:
+            from .tools.comparison import _identity
+            weights = _identity(np.shape(exp_img))
         self.cmp = Comparison(self.det.det_h, self.det.det_v, exp_img, exp_qxy,
-                              exp_qz, exp_mask, ctx=self.ctx)
+                              exp_qz, exp_mask, weights=weights, shift=shift,
+                              ctx=self.ctx)
         self.evaluations = 0
 
     def images(self, sizes):
@@ -68,7 +79,11 @@ class SlabFit:
         candidates in one batched voxel pass."""
         return [m for _, m in self._run(sizes, keep_images=False)]
 
-    def _run(self, sizes, keep_images):
+    def residuals(self, size):
+        """The residual map of one candidate (fit_slabsize.py:43-44)."""
+        return self._run([size], keep_images=False, residual=True)[0][1][3]
+
+    def _run(self, sizes, keep_images, residual=False):
         sizes = [tuple(float(v) for v in s) for s in sizes]
         items = []
         for s in sizes:
@@ -89,10 +104,10 @@ class SlabFit:
             for k in range(len(sizes)):
                 self.det.set_iq_device32(plan.device_iq32(k))
                 self.det.execute()
-                s, o, mis, _ = self.cmp.evaluate(self.det.device_result(),
-                                                 on_device=True)
+                r = self.cmp.evaluate(self.det.device_result(), on_device=True,
+                                      residual=residual)
                 img = self.det.result() if keep_images else None
-                out.append((img, (s, o, mis)))
+                out.append((img, r[:3] + (r[4],) if residual else r[:3]))
         finally:
             plan.close()
         self.evaluations += len(sizes)
@@ -158,3 +173,70 @@ class SlabFit:
     def close(self):
         self.det.close()
         self.cmp.close()
+
+
+_MODELS = {}
+
+
+def _model_key(*parts):
+    import hashlib
+    h = hashlib.sha256()
+    for p in parts:
+        a = np.asarray(p) if not isinstance(p, str) else None
+        if a is not None and a.dtype != object:
+            h.update(str(a.dtype).encode() + str(a.shape).encode())
+            h.update(np.ascontiguousarray(a).tobytes())
+        else:
+            h.update(repr(p).encode())
+    return h.hexdigest()
+
+
+def fullfit_model(params, fixed_slab_params, fixed_voxelgrid_params,
+                  fixed_detectormaker_params, fixed_exp_params, *, ctx=None):
+    """fit_slabsize.py:19-46 with the reference's arguments and return value
+    (the residual vector, flattened, that lmfit minimises): slab of
+    params['x_size'/'y_size'/'z_size'], I(q), detector image (mirror=True),
+    trim, shift_peak, scale + offset, residuals where rebin_mask == 0.  The
+    device plans of one set of fixed parameters are made on the first call
+    and reused."""
+    from .tools.utilities import load_pdb, load_xyz
+    size = tuple(float(params[k]) for k in ("x_size", "y_size", "z_size"))
+    input_filepath, a, b, c, alpha, beta, gamma = fixed_slab_params
+    r_voxel_size, q_voxel_size, max_q, energy, fill_bkg, smooth = fixed_voxelgrid_params
+    (num_pixels, angle_init_vals, angle_init_axs, psis, psi_weights_path, phis,
+     phi_weights_path, thetas, theta_weights_path) = fixed_detectormaker_params
+    rebin_map, rebin_mask, exp_qxy, exp_qz, pad_width, pad_range = fixed_exp_params
+    key = _model_key(input_filepath, (a, b, c, alpha, beta, gamma),
+                     fixed_voxelgrid_params, num_pixels, angle_init_vals,
+                     angle_init_axs, psis, psi_weights_path, phis,
+                     phi_weights_path, thetas, theta_weights_path, rebin_map,
+                     rebin_mask, exp_qxy, exp_qz, pad_width, pad_range, id(ctx))
+    fit = _MODELS.get(key)
+    if fit is None:
+        if input_filepath.lower().endswith(".xyz"):
+            cell_xyz, cell_el = load_xyz(input_filepath)
+        elif input_filepath.lower().endswith(".pdb"):
+            cell_xyz, cell_el = load_pdb(input_filepath)
+        else:
+            raise Exception("Files must be a .pdb or .xyz file")
+
+        def wts(path, ang):
+            ang = np.atleast_1d(np.asarray(ang, dtype=np.float64))
+            return ang, (np.load(path) if path else np.ones_like(ang) / len(ang))
+
+        ps, pw = wts(psi_weights_path, psis)
+        ph, hw = wts(phi_weights_path, phis)
+        th, tw = wts(theta_weights_path, thetas)
+        if len(_MODELS) >= 4:
+            for m in _MODELS.values():
+                m.close()
+            _MODELS.clear()
+        fit = _MODELS[key] = SlabFit(
+            cell_xyz, cell_el, (a, b, c, alpha, beta, gamma), r_voxel_size,
+            q_voxel_size, max_q, energy, num_pixels, rebin_map, exp_qxy, exp_qz,
+            rebin_mask, fill_bkg=fill_bkg, smooth=smooth,
+            angle_init_vals=angle_init_vals, angle_init_axs=angle_init_axs,
+            psis=ps, psi_weights=pw, det_phis=ph, det_phi_weights=hw,
+            thetas=th, theta_weights=tw, mirror=True,
+            shift=(pad_width, pad_range), rebinned=True, ctx=ctx)
+    return fit.residuals(size).ravel()

@@ -166,6 +166,153 @@ def rebin_weights(qxy1, qz1, qxy2, qz2):
     return np.ascontiguousarray(idx), np.ascontiguousarray(w)
 
 
+def _bilinear_map(shape_in, rows, cols):
+    """map_coordinates(image, (rows, cols), order=1, cval=0) for every image
+    of shape `shape_in` as (idx (n, 4) int32 flat input indices, -1 unused;
+    w (n, 4)): the four neighbours (r0, c0), (r0, c0+1), (r0+1, c0),
+    (r0+1, c0+1), r0 = floor(row).  The weights are scipy's own: an image
+    that is 1 on the pixels of one (row, column) parity class and 0 elsewhere
+    returns, at each point, the weight of its one neighbour in that class."""
+    from scipy.ndimage import map_coordinates
+    H, W = shape_in
+    rows = np.asarray(rows, dtype=np.float64).ravel()
+    cols = np.asarray(cols, dtype=np.float64).ravel()
+    r0 = np.floor(rows).astype(np.int64)
+    c0 = np.floor(cols).astype(np.int64)
+    ii = np.arange(H)[:, None] % 2
+    jj = np.arange(W)[None, :] % 2
+    probe = {}
+    for a in (0, 1):
+        for b in (0, 1):
+            img = ((ii == a) & (jj == b)).astype(np.float64)
+            out = np.zeros(len(rows))
+            map_coordinates(img, (rows, cols), order=1, output=out, cval=0)
+            probe[a, b] = out
+    idx = np.full((len(rows), 4), -1, dtype=np.int32)
+    w = np.zeros((len(rows), 4))
+    for k, (di, dj) in enumerate(((0, 0), (0, 1), (1, 0), (1, 1))):
+        pr, pc = r0 + di, c0 + dj
+        ok = (pr >= 0) & (pr < H) & (pc >= 0) & (pc < W)
+        for a in (0, 1):
+            for b in (0, 1):
+                sel = ok & (pr % 2 == a) & (pc % 2 == b)
+                w[sel, k] = probe[a, b][sel]
+        use = ok & (w[:, k] != 0)
+        idx[use, k] = (pr * W + pc)[use]
+        w[~use, k] = 0.0
+    return idx, w
+
+
+def shift_peak_maps(det_h, det_v, shape, pad_width_qspace, pad_range_qspace):
+    """The fixed parts of shift_peak (comparison.py:566-592) for a trimmed
+    image of `shape` on the (det_v, det_h) grid: the polar warp of
+    linear_polar (:469-499; centre at the pixel nearest q = 0, radius the
+    image diagonal, output round(2 pi radius) x round(radius)), the column
+    map of add_pad (:540-563) and the inverse warp of polar_linear
+    (:501-538).  Returns dict(n_t, n_r, p_idx, p_w, col_src, q_idx, q_w)."""
+    from scipy.ndimage import map_coordinates
+    det_h, det_v = np.asarray(det_h), np.asarray(det_v)
+    rows, cols = shape
+    radius = float(np.sqrt(rows ** 2 + cols ** 2))
+    ctr = np.array([int(np.argmin(np.abs(det_v))), int(np.argmin(np.abs(det_h)))])
+    n_t, n_r = int(round(radius * 2 * np.pi)), int(round(radius))
+    rr = np.linspace(0, radius, n_r)
+    tt = np.linspace(0, 2 * np.pi, n_t)
+    pc = rr * np.cos(tt[:, None]) + ctr[1]
+    pr = rr * np.sin(tt[:, None]) + ctr[0]
+    p_idx, p_w = _bilinear_map((rows, cols), pr, pc)
+    # r axis: row 0 of the polar warp of |q|
+    hh, vv = np.meshgrid(det_h, det_v)
+    r_axis = np.zeros(n_r)
+    map_coordinates(np.hypot(hh, vv), (pr[0], pc[0]), order=1, output=r_axis, cval=0)
+    col_src = np.arange(n_r)
+    steps = np.diff(r_axis)
+    px = np.mean(steps[steps > 0])
+    n_pad = int(np.round(pad_width_qspace / px))
+    if n_pad:
+        lo, hi = pad_range_qspace
+        i0 = int(np.argmin(np.abs(r_axis - lo)))
+        i1 = int(np.argmin(np.abs(r_axis - hi)))
+        gap = int((i1 - i0 - 1) / n_pad - 1)
+        assert gap >= 0, "pad_range is too small for desired pad_width"
+        for k in range(n_pad):
+            at = i0 + 2 * k + gap * k
+            col_src = np.insert(col_src, at + 1, col_src[at])
+        col_src = col_src[:-n_pad]
+    yy, xx = np.mgrid[:rows, :cols] - ctr[:, None, None]
+    rad = np.sqrt(yy ** 2 + xx ** 2)
+    ang = np.arctan2(yy, xx)
+    ang[ang < 0] += 2 * np.pi
+    rad = (rad / n_r) * (n_r - 1)
+    ang = (ang / (2 * np.pi)) * (n_t - 1)
+    q_idx, q_w = _bilinear_map((n_t, n_r), ang, rad)
+    return dict(n_t=n_t, n_r=n_r, p_idx=p_idx, p_w=p_w,
+                col_src=np.ascontiguousarray(col_src, dtype=np.int32),
+                q_idx=q_idx, q_w=q_w)
+
+
+class Warp:
+    """shift_peak of one trimmed-image geometry on the device (gw_warp)."""
+
+    def __init__(self, det_h, det_v, shape, pad_width_qspace, pad_range_qspace,
+                 ctx=None):
+        import ctypes
+        from .. import _native as N
+        self._N = N
+        self.ctx = ctx or N.default_context()
+        self.shape = tuple(int(v) for v in shape)
+        m = shift_peak_maps(det_h, det_v, self.shape, pad_width_qspace,
+                            pad_range_qspace)
+        h = ctypes.c_void_p()
+        N.check(N.lib().gw_warp_create(
+            self.ctx.handle, self.shape[0], self.shape[1], m["n_t"], m["n_r"],
+            N.ptr(m["p_idx"]), N.ptr(m["p_w"]), N.ptr(m["col_src"]),
+            N.ptr(m["q_idx"]), N.ptr(m["q_w"]), ctypes.byref(h)))
+        self.handle = h
+
+    def apply(self, image):
+        N = self._N
+        img = np.ascontiguousarray(image, dtype=np.float64)
+        if img.shape != self.shape:
+            raise ValueError("image shape differs from the warp's")
+        out = np.empty_like(img)
+        N.check(N.lib().gw_warp_apply(self.handle, N.ptr(img), 0, N.ptr(out), 0))
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._N.lib().gw_warp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_WARPS = {}
+
+
+def shift_peak(image, det_h, det_v, pad_width_qspace, pad_range_qspace, *,
+               ctx=None):
+    """Drop-in for comparison.py:566-592 on the device; the maps of a
+    geometry are made once and kept."""
+    det_h, det_v = np.asarray(det_h, np.float64), np.asarray(det_v, np.float64)
+    key = (det_h.tobytes(), det_v.tobytes(), np.shape(image),
+           float(pad_width_qspace), tuple(float(v) for v in pad_range_qspace),
+           id(ctx))
+    w = _WARPS.get(key)
+    if w is None:
+        if len(_WARPS) > 8:
+            for old in _WARPS.values():
+                old.close()
+            _WARPS.clear()
+        w = _WARPS[key] = Warp(det_h, det_v, np.shape(image), pad_width_qspace,
+                               pad_range_qspace, ctx=ctx)
+    return w.apply(image)
+
+
 class Comparison:
     """Device plan of the experimental comparison: the experiment rebinned
     once onto the trimmed simulation grid, then per simulated image the
@@ -173,7 +320,9 @@ class Comparison:
     (comparison.py:161-191, :406-445, :873-882; fit_slabsize.py:43-44)."""
 
     def __init__(self, det_h, det_v, exp_img, exp_qxy, exp_qz, exp_mask,
-                 weights=None, ctx=None):
+                 weights=None, shift=None, ctx=None):
+        """shift: (pad_width, pad_range) to apply shift_peak to the trimmed
+        simulated image first, as fit_slabsize.py:36 does; None: no warp."""
         import ctypes
         from .. import _native as N
         self._N = N
@@ -198,6 +347,12 @@ class Comparison:
             self.cols, N.ptr(idx), N.ptr(w), N.ptr(vals), N.ptr(mvals),
             len(vals), ctypes.byref(h)))
         self.handle = h
+        self.warp = None
+        if shift is not None:
+            self.warp = Warp(self.det_h_trim, self.det_v_trim,
+                             (self.rows, self.cols), shift[0], shift[1],
+                             ctx=self.ctx)
+            N.check(N.lib().gw_compare_set_warp(self.handle, self.warp.handle))
 
     def target(self):
         """(rebinned map, rebinned mask) on the trimmed grid."""
@@ -230,6 +385,9 @@ class Comparison:
         if getattr(self, "handle", None):
             self._N.lib().gw_compare_destroy(self.handle)
             self.handle = None
+        if getattr(self, "warp", None) is not None:
+            self.warp.close()
+            self.warp = None
 
     def __del__(self):
         try:

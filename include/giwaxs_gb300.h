@@ -366,6 +366,27 @@ int gw_compare_target(gw_compare *cmp, double *target, uint8_t *mask);
 int gw_compare_eval(gw_compare *cmp, const double *sim, int32_t sim_on_device,
                     double *out, double *residual);
 
+/* shift_peak (tools/comparison.py:566-592: linear_polar, add_pad, the zero
+ * mask, polar_linear) on a rows x cols trimmed image, as fixed maps:
+ *   polar[j] = sum_k p_w[4j+k] image[p_idx[4j+k]]       (n_t x n_r polar)
+ *   z[t][c]  = polar[t][c] == 0 ? 0 : polar[t][col_src[c]]
+ *   out[i]   = sum_k q_w[4i+k] z[q_idx[4i+k]]
+ * indices flat (row-major), -1 = unused.  The maps come from the host
+ * (giwaxsim_gb300.tools.comparison.shift_peak_maps). */
+typedef struct gw_warp gw_warp;
+int gw_warp_create(gw_ctx *ctx, int32_t rows, int32_t cols, int32_t n_t,
+                   int32_t n_r, const int32_t *p_idx, const double *p_w,
+                   const int32_t *col_src, const int32_t *q_idx,
+                   const double *q_w, gw_warp **out);
+int gw_warp_destroy(gw_warp *warp);
+/* out = shift_peak(in), both rows x cols, host or device (flags). */
+int gw_warp_apply(gw_warp *warp, const double *in, int32_t in_on_device,
+                  double *out, int32_t out_on_device);
+/* Apply `warp` (borrowed, same context and trimmed shape; NULL: none) to the
+ * trimmed simulated image before every gw_compare_eval, as fit_slabsize.py
+ * fullfit_model does (:36). */
+int gw_compare_set_warp(gw_compare *cmp, gw_warp *warp);
+
 /* ---- per-slice and helper entry points (device, synchronous) ---------- */
 /* Gather I(q) at points (x,y,z) after applying n_R 3x3 rotations in order
  * (BLAS fused order), with the reference's floor division by dq and clip:

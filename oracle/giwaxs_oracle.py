@@ -25,6 +25,11 @@ It restates, in float64/complex128 numpy, the reference's forward path:
   tools/detector.py:278-300    generate_detector_ints
   tools/comparison.py:790-870  detectormaker_fitting
   old_modules/voxelgridmaker.py:56-61  averaging of I(q) over input files
+  tools/comparison.py:595-671  slabmaker_fitting
+  tools/comparison.py:469-592  linear_polar, polar_linear, add_pad, shift_peak
+  tools/voxelgrids.py:535-722  generate_voxel_grid_low_mem, aff_num_qs > 1
+  tools/utilities.py:318-340   get_element_f0_dict
+  fit_slabsize.py:19-46        fullfit_model
 
 Differences from the reference, all deliberate:
   * BLAS products are evaluated by oracle_fma.c as the explicit fused chain
@@ -48,7 +53,7 @@ import os
 
 import numpy as np
 from numpy.fft import fft2, fftshift
-from scipy.ndimage import gaussian_filter1d
+from scipy.ndimage import gaussian_filter1d, map_coordinates
 
 _LIB = None
 
@@ -369,6 +374,69 @@ def voxelgrid(structures, r_voxel_size, q_voxel_size, max_q, phis=None,
 
 
 # --------------------------------------------------------------------------
+# shift_peak (comparison.py:469-592): polar warp, pi-pi peak padding, back
+
+def to_polar(img, centre, radius):
+    """comparison.py:469-499 (linear_polar, order 1, cval 0) with the output
+    shape (round(2 pi radius), round(radius))."""
+    n_t, n_r = int(round(radius * 2 * np.pi)), int(round(radius))
+    rr = np.linspace(0, radius, n_r)
+    tt = np.linspace(0, 2 * np.pi, n_t)
+    cols = rr * np.cos(tt[:, None]) + centre[1]
+    rows = rr * np.sin(tt[:, None]) + centre[0]
+    out = np.zeros((n_t, n_r), dtype=img.dtype)
+    map_coordinates(img, (rows, cols), order=1, output=out, cval=0)
+    return out
+
+
+def from_polar(polar, centre, shape):
+    """comparison.py:501-538 (polar_linear, r = polar width, order 1)."""
+    n_t, n_r = polar.shape
+    o = np.array(centre)
+    yy, xx = np.mgrid[:shape[0], :shape[1]] - o[:, None, None]
+    rad = np.sqrt(yy ** 2 + xx ** 2)
+    ang = np.arctan2(yy, xx)
+    ang[ang < 0] += 2 * np.pi
+    rad = (rad / n_r) * (n_r - 1)
+    ang = (ang / (2 * np.pi)) * (n_t - 1)
+    out = np.zeros(shape, dtype=polar.dtype)
+    map_coordinates(polar, (ang, rad), order=1, output=out, cval=0)
+    return out
+
+
+def pad_columns(polar, r_axis, pad_width, pad_range):
+    """comparison.py:540-563 (add_pad): duplicate round(pad_width/pixel)
+    columns evenly spread from pad_range[0] on, then drop as many columns at
+    the far end."""
+    steps = np.diff(r_axis)
+    px = np.mean(steps[steps > 0])
+    n_pad = int(np.round(pad_width / px))
+    if n_pad == 0:
+        return polar
+    i0 = int(np.argmin(np.abs(r_axis - pad_range[0])))
+    i1 = int(np.argmin(np.abs(r_axis - pad_range[1])))
+    gap = int((i1 - i0 - 1) / n_pad - 1)
+    assert gap >= 0, "pad_range is too small for desired pad_width"
+    for k in range(n_pad):
+        at = i0 + 2 * k + gap * k
+        polar = np.insert(polar, at + 1, polar[:, at], axis=1)
+    return polar[:, :-n_pad]
+
+
+def shift_peak(image, det_h, det_v, pad_width, pad_range):
+    """comparison.py:566-592."""
+    hh, vv = np.meshgrid(det_h, det_v)
+    qr = np.hypot(hh, vv)
+    radius = float(np.sqrt(image.shape[0] ** 2 + image.shape[1] ** 2))
+    centre = (int(np.argmin(np.abs(det_v))), int(np.argmin(np.abs(det_h))))
+    polar = to_polar(image, centre, radius)
+    r_axis = to_polar(qr, centre, radius)[0, :]
+    padded = pad_columns(polar.copy(), r_axis, pad_width, pad_range)
+    padded[polar == 0] = 0
+    return from_polar(padded, centre, image.shape)
+
+
+# --------------------------------------------------------------------------
 # multi-q form factors (generate_voxel_grid_low_mem with aff_num_qs > 1)
 
 def element_f0_at(q_val, element):
@@ -633,3 +701,31 @@ def slabmaker(cell_xyz, cell_elements, vecs, size):
     for k in range(3):
         coords[:, k] -= np.min(coords[:, k])
     return coords, elements
+
+
+# ------------------------------------------------------------------ fit model
+def fullfit_residuals(cell_xyz, cell_elements, vecs, size, r_voxel_size,
+                      q_voxel_size, max_q, f_of_element, num_pixels,
+                      angle_init_vals, angle_init_axs, psis, psi_w, phis, phi_w,
+                      thetas, theta_w, rebin_map, rebin_mask, exp_qxy, exp_qz,
+                      pad_width, pad_range, fill_bkg=False, smooth=0):
+    """fit_slabsize.py:19-46 fullfit_model: slab, I(q) with the carbon f0,
+    detector image (mirror=True), trim_sim_data (comparison.py:161-191),
+    shift_peak, optimize_scale_offset (comparison.py:873-882, lstsq) and the
+    residuals where the mask is 0, flattened."""
+    coords, els = slabmaker(cell_xyz, cell_elements, vecs, size)
+    fv = np.array([f_of_element[e] for e in els], dtype=complex)
+    vg = voxelgrid([(coords, fv)], r_voxel_size, q_voxel_size, max_q, None,
+                   fill_bkg, smooth)
+    det, h, v = detector(vg["iq"], vg["qx"], vg["qy"], vg["qz"], num_pixels,
+                         max_q, angle_init_vals, angle_init_axs, psis, psi_w,
+                         phis, phi_w, thetas, theta_w, mirror=True)
+    hm = (h >= np.min(exp_qxy)) & (h <= np.max(exp_qxy))
+    vm = (v >= np.min(exp_qz)) & (v <= np.max(exp_qz))
+    sim = det[vm, :][:, hm]
+    sim = shift_peak(sim.copy(), h[hm], v[vm], pad_width, pad_range)
+    keep = rebin_mask == 0
+    A = np.vstack([sim[keep].ravel(), np.ones(int(keep.sum()))]).T
+    (scale, offset), _, _, _ = np.linalg.lstsq(A, rebin_map[keep].ravel(), rcond=None)
+    res = (rebin_map - (scale * sim + offset)) * keep
+    return res.ravel(), scale, offset

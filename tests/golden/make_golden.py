@@ -4,7 +4,7 @@ GIWAXSim code itself (a Python package, imported from its checkout).
 Run in a container that has the reference checkout:
     python tests/golden/make_golden.py [/path/to/reference]
     python tests/golden/make_golden.py /path/to/reference pm6   # PM6 example
-    (other fixture groups: slab, compare, multiq)
+    (other fixture groups: slab, compare, multiq, shift)
 
 The reference imports matplotlib, mpl_toolkits, fabio, lmfit and xraydb and
 scipy.signal.tukey at module level; none of these is on the computation path
@@ -386,6 +386,35 @@ def multiq():
     print("multi-q fixture written")
 
 
+SHIFT_CASES = [
+    # (name, pad_width, pad_range (q))
+    ("pad", 0.05, (1.2, 1.9)),
+    ("nopad", 0.0, (1.2, 1.9)),
+]
+
+
+def shift():
+    """The reference's shift_peak (comparison.py:566-592: linear_polar,
+    add_pad, the zero mask, polar_linear) on a synthetic trimmed detector
+    image with rings, on a positive-qxy grid like trim_sim_data leaves."""
+    comparison, detector, utilities, voxelgrids = _import_reference()
+    rng = np.random.default_rng(33)
+    det_h = np.linspace(0.0, 2.4, 97)
+    det_v = np.linspace(-0.1, 2.2, 83)
+    hx, vz = np.meshgrid(det_h, det_v)
+    q = np.hypot(hx, vz)
+    img = (np.exp(-((q - 1.45) / 0.05) ** 2) + 0.5 * np.exp(-((q - 0.9) / 0.08) ** 2)
+           + 0.05 + 0.01 * rng.random(q.shape))
+    img[:3, :] = 0.0  # a zero band (the reference's mask keeps zeros zero)
+    out = dict(det_h=det_h, det_v=det_v, img=img)
+    for name, pw, pr in SHIFT_CASES:
+        out[name + "_out"] = comparison.shift_peak(img.copy(), det_h, det_v, pw, pr)
+        out[name + "_pw"] = pw
+        out[name + "_pr"] = np.array(pr)
+    np.savez_compressed(os.path.join(HERE, "golden_shift.npz"), **out)
+    print("shift_peak fixture written")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "pm6":
         pm6()
@@ -395,5 +424,7 @@ if __name__ == "__main__":
         compare()
     elif len(sys.argv) > 2 and sys.argv[2] == "multiq":
         multiq()
+    elif len(sys.argv) > 2 and sys.argv[2] == "shift":
+        shift()
     else:
         main()
