@@ -262,15 +262,19 @@ __global__ void k_profile(SliceArgs a, int slice0) {
   const gw_phi ph = a.ph[p];
   const int4 e = a.ext[sl];
   if (e.y < 0) {  // no valid atom: np.min of an empty array raises
-    if (threadIdx.x == 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
+    if (threadIdx.x == 0 && blockIdx.y == 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
     return;
   }
   const double cre = GW_DMUL(s.avg_f_re, s.max_voxels);
   const double cim = GW_DMUL(s.avg_f_im, s.max_voxels);
   const bool bg = !a.plain && (a.fill || a.smooth_on);
+  // blockIdx.y-th part of the columns / rows
+  const int i0 = blockIdx.y * blockDim.x + threadIdx.x;
+  const int di = gridDim.y * blockDim.x;
+  const bool lead = blockIdx.y == 0 && threadIdx.x == 0;
   if (a.fill) {
     const double base = a.clbase[sl];
-    for (int yy = threadIdx.x; yy < a.Ly; yy += blockDim.x) {
+    for (int yy = i0; yy < a.Ly; yy += di) {
       int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
       const double x = GW_DMUL((double)yi, a.r);
       const double len = collapse_length(ph, s.y_bound, s.x_bound, base, x);
@@ -285,23 +289,23 @@ __global__ void k_profile(SliceArgs a, int slice0) {
   if (a.smooth_on) {
     int ys, ye, zs, ze;
     plateau(a, e, ys, ye, zs, ze);
-    for (int yy = threadIdx.x; yy < a.Ly; yy += blockDim.x) {
+    for (int yy = i0; yy < a.Ly; yy += di) {
       int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
       a.my[(size_t)blockIdx.x * a.Ly + yy] = smooth_at(yi, ys, ye, a.g, a.radius, a.gw);
     }
-    for (int zz = threadIdx.x; zz < a.Lz; zz += blockDim.x) {
+    for (int zz = i0; zz < a.Lz; zz += di) {
       int zi = a.z_lo + zz; if (zi < 0) zi += a.g; if (zi >= a.g) zi -= a.g;
       a.mz[(size_t)blockIdx.x * a.Lz + zz] = smooth_at(zi, zs, ze, a.g, a.radius, a.gw);
     }
     // the smoothing support must lie inside the transformed window
-    if (threadIdx.x == 0 && a.Ly < a.g) {
+    if (lead && a.Ly < a.g) {
       int l = a.y_lo - 1; if (l < 0) l += a.g;
       int r = a.y_lo + a.Ly; r %= a.g; if (r < 0) r += a.g;
       if (smooth_at(l, ys, ye, a.g, a.radius, a.gw) != 0.f ||
           smooth_at(r, ys, ye, a.g, a.radius, a.gw) != 0.f)
         dev_error(a.err, GW_DEVERR_MASK_WRAP);
     }
-    if (threadIdx.x == 0 && a.Lz < a.g) {
+    if (lead && a.Lz < a.g) {
       const int rows = a.roff ? a.roff[sl + 1] - a.roff[sl] : a.Lz;
       int l = a.z_lo - 1; if (l < 0) l += a.g;
       int r = a.z_lo + rows; r %= a.g; if (r < 0) r += a.g;
@@ -377,25 +381,28 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   for (int t = threadIdx.x; t < NB * LDM; t += NT) buf[t] = make_float2(0.f, 0.f);
   const int row0 = blockIdx.x * NB;
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int f = 0; f < NB; ++f) {
-      const int row = row0 + f;
-      int lo = 0, mid = 0, hi = 0, slot = 0, zz = 0;
-      if (row < n_rows) {
-        row_slot(a, slice0, n_sl, row, slot, zz);
-        const int sl = slice0 + slot, t = sl / a.n_phi;
-        if (a.ext[sl].y < 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
-        row_atoms(a, t, zz, lo, mid, hi);
-      }
-      r_lo[f] = lo;
-      r_mid[f] = mid;
-      r_cnt[f] = acc;
-      r_slot[f] = slot;
-      r_zz[f] = zz;
-      acc += hi - lo;
+  // the block's rows: slot, window row and atom range, one thread per row
+  // (independent loads), then a scan of the atom counts
+  static_assert(NB <= 32, "one warp sets the rows up");
+  if (threadIdx.x < NB) {
+    const int f = threadIdx.x, row = row0 + f;
+    int lo = 0, mid = 0, hi = 0, slot = 0, zz = 0;
+    if (row < n_rows) {
+      row_slot(a, slice0, n_sl, row, slot, zz);
+      const int sl = slice0 + slot, t = sl / a.n_phi;
+      if (a.ext[sl].y < 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
+      row_atoms(a, t, zz, lo, mid, hi);
     }
-    r_cnt[NB] = acc;
+    r_lo[f] = lo;
+    r_mid[f] = mid;
+    r_cnt[f + 1] = hi - lo;
+    r_slot[f] = slot;
+    r_zz[f] = zz;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    r_cnt[0] = 0;
+    for (int f = 0; f < NB; ++f) r_cnt[f + 1] += r_cnt[f];
   }
   __syncthreads();
   const int total = r_cnt[NB];
@@ -547,49 +554,60 @@ __global__ void k_col_tables(const gw_phi *ph, int g, int k0, int nc,
 
 // I = sum / count (0 where count == 0), crop, f0 factor (comparison.py:765-786,
 // voxelgrids.py:16-48, :828-857).  Output in crop coordinates (qy,qx,qz).
-// One block row per (qy, qx) line; threads run along qz, the contiguous
-// axis.  The count and the f0 factor are exact integers / float32 (the
-// factor's 1e-7 relative error is far inside the tolerance); the sum keeps
-// float64 and takes one float64 multiply.
-__global__ void k_finalize(const double *sum, const float2 *sumk, int kahan,
-                           const unsigned int *C2, const int *C1, int W,
-                           int off, int Qc, float inv_nstruct,
-                           const float *f0tab, int use_f0, float f0_c,
-                           float f0_invz, double *out64, float *out32) {
-  const int line = blockIdx.x;  // iy * Qc + ix
-  const int iy = line / Qc, ix = line - iy * Qc;
-  const int wy = iy + off, wx = ix + off;
-  const unsigned c2 = C2[(size_t)wy * W + wx];
-  const size_t wbase = ((size_t)wy * W + wx) * W + off;
-  const size_t obase = (size_t)line * Qc;
-  float fxy[4];
-  if (use_f0) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float *t = f0tab + i * 3 * Qc;
-      fxy[i] = t[ix] * t[Qc + iy];
-    }
-  }
-  for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
-    const unsigned cnt = c2 * (unsigned)C1[iz + off];
-    double s;
-    if (kahan) {
-      const float2 sc = sumk[wbase + iz];
-      s = (double)sc.x - (double)sc.y;
-    } else {
-      s = sum[wbase + iz];
-    }
-    float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
+// One warp per (qy, qx) line, lanes along qz (the contiguous axis), lines
+// in a grid-stride loop: per line the count factor C2 and the (qx, qy) part
+// of the separable f0 sum stay in registers; per qz the four z factors come
+// as one float4 (zf0) and C1 from L1.  The count and the f0 factor are exact
+// integers / float32 (the factor's 1e-7 relative error is far inside the
+// tolerance); the sum keeps float64 and takes one float64 multiply.
+__global__ void __launch_bounds__(256)
+k_finalize(const double *sum, const float2 *sumk, int kahan,
+           const unsigned int *C2, const int *C1, int W, int off, int Qc,
+           float inv_nstruct, const float *f0tab, const float4 *zf0,
+           int use_f0, float f0_c, float f0_invz, double *out64, float *out32) {
+  const int lane = threadIdx.x & 31;
+  const int n_lines = Qc * Qc;
+  const int stride = gridDim.x * (blockDim.x >> 5);
+  for (int line = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       line < n_lines; line += stride) {
+    const int iy = line / Qc, ix = line - iy * Qc;
+    const int wy = iy + off, wx = ix + off;
+    const unsigned c2 = C2[(size_t)wy * W + wx];
+    const size_t wbase = ((size_t)wy * W + wx) * W + off;
+    const size_t obase = (size_t)line * Qc;
+    float fxy[4];
     if (use_f0) {
-      float acc = f0_c;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) acc += fxy[i] * f0tab[(i * 3 + 2) * Qc + iz];
-      const float fq = acc * f0_invz;
-      scale *= fq * fq;
+      for (int i = 0; i < 4; ++i) {
+        const float *t = f0tab + i * 3 * Qc;
+        fxy[i] = t[ix] * t[Qc + iy];
+      }
     }
-    const double I = s * (double)scale;
-    out64[obase + iz] = I;
-    out32[obase + iz] = (float)I;
+#pragma unroll 4
+    for (int iz = lane; iz < Qc; iz += 32) {
+      const unsigned cnt = c2 * (unsigned)__ldg(C1 + iz + off);
+      double s;
+      if (kahan) {
+        const float2 sc = sumk[wbase + iz];
+        s = (double)sc.x - (double)sc.y;
+      } else {
+        s = sum[wbase + iz];
+      }
+      float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
+      if (use_f0) {
+        const float4 z = __ldg(zf0 + iz);
+        float acc = f0_c;
+        acc += fxy[0] * z.x;
+        acc += fxy[1] * z.y;
+        acc += fxy[2] * z.z;
+        acc += fxy[3] * z.w;
+        const float fq = acc * f0_invz;
+        scale *= fq * fq;
+      }
+      const double I = s * (double)scale;
+      out64[obase + iz] = I;
+      out32[obase + iz] = (float)I;
+    }
   }
 }
 
@@ -599,8 +617,8 @@ __global__ void k_finalize(const double *sum, const float2 *sumk, int kahan,
 __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan,
                                 const unsigned int *C2, const int *C1, int Qc,
                                 float inv_nstruct, const float *f0tab,
-                                int use_f0, float f0_c, float f0_invz,
-                                double *out64, float *out32) {
+                                const float4 *zf0, int use_f0, float f0_c,
+                                float f0_invz, double *out64, float *out32) {
   const int n = Qc * Qc * Qc;  // < 2^31 (checked by the caller)
   const int npair = (n + 1) / 2;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npair;
@@ -628,16 +646,16 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
       if (e == 1 && !two) break;
       int line = line0, iz = iz0 + e;
       if (iz == Qc) { iz = 0; ++line; }
-      const unsigned cnt = C2[line] * (unsigned)C1[iz];
+      const unsigned cnt = C2[line] * (unsigned)__ldg(C1 + iz);
       float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
       if (use_f0) {
         const int iy = line / Qc, ix = line - iy * Qc;
+        const float4 z = __ldg(zf0 + iz);
         float acc = f0_c;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const float *t = f0tab + k * 3 * Qc;
-          acc += (t[ix] * t[Qc + iy]) * t[2 * Qc + iz];
-        }
+        acc += (__ldg(f0tab + ix) * __ldg(f0tab + Qc + iy)) * z.x;
+        acc += (__ldg(f0tab + 3 * Qc + ix) * __ldg(f0tab + 4 * Qc + iy)) * z.y;
+        acc += (__ldg(f0tab + 6 * Qc + ix) * __ldg(f0tab + 7 * Qc + iy)) * z.z;
+        acc += (__ldg(f0tab + 9 * Qc + ix) * __ldg(f0tab + 10 * Qc + iy)) * z.w;
         const float fq = acc * f0_invz;
         scale *= fq * fq;
       }
@@ -998,6 +1016,16 @@ int enqueue_prep(gw_voxel_plan *P) {
   return GW_OK;
 }
 
+// Slice arguments whose fill/smoothing profile arrays start at slice s0
+// (the setup kernels and the row stage index them by batch slot).
+SliceArgs profile_view(const SliceArgs &a, int s0) {
+  SliceArgs v = a;
+  v.amo = a.amo + (size_t)s0 * a.Ly;
+  v.my = a.my + (size_t)s0 * a.Ly;
+  v.mz = a.mz + (size_t)s0 * a.Lz;
+  return v;
+}
+
 int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
   gw_ctx *ctx = P->ctx;
   cudaStream_t st = ctx->stream;
@@ -1024,11 +1052,16 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
   }
   if (a.fill || a.smooth_on) {
     gw::KTimer tm(ctx, GW_K_PROFILE);
-    k_profile<<<n, 256, 0, st>>>(a, s0);
+    // several blocks per slice when the slices alone would not fill the GPU
+    const int parts = std::max(1, std::min(8, (2 * ctx->sm_count + n - 1) / n));
+    k_profile<<<dim3(n, parts), 256, 0, st>>>(a, s0);
     GW_LAUNCHED(ctx);
   }
   return GW_OK;
 }
+
+// Slices per launch of the setup kernels (their grids index slices in y).
+constexpr int kSetupChunk = 32768;
 
 // Enqueue the whole chain (no synchronisation).
 int enqueue(gw_voxel_plan *P) {
@@ -1063,14 +1096,21 @@ int enqueue(gw_voxel_plan *P) {
       bn.shell_k = k;
     }
     GW_TRY(enqueue_prep(P));
+    // Batched: the per-slice setup of every slice at once (fuller grids,
+    // fewer launches); the profile arrays hold every slice and each batch
+    // sees its part.  Plain mode keeps the reference's per-rotation order.
+    if (!P->plain)
+      for (int c0 = 0; c0 < P->n_slices; c0 += kSetupChunk)
+        GW_TRY(enqueue_slice_setup(P, profile_view(a, c0), c0,
+                                   std::min(kSetupChunk, P->n_slices - c0)));
     for (int s0 = 0; s0 < P->n_slices; s0 += P->S) {
       const int n = std::min(P->S, P->n_slices - s0);
-      GW_TRY(enqueue_slice_setup(P, a, s0, n));
-      GW_TRY(row_dispatch(P, a, cy, s0, n));
-      GW_TRY(col_dispatch(P, a, cz, bn, s0, n));
+      const SliceArgs ab = profile_view(a, s0);
+      if (P->plain) GW_TRY(enqueue_slice_setup(P, ab, s0, n));
+      GW_TRY(row_dispatch(P, ab, cy, s0, n));
+      GW_TRY(col_dispatch(P, ab, cz, bn, s0, n));
     }
   }
-  const int fin_blocks = P->Qc * P->Qc;
   const float f0c = (float)P->p.f0_coef[8];
   const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
   const float inv_ns = P->p.average == GW_STRUCTS_AVERAGE ? 1.0f / (float)P->n_struct : 1.0f;
@@ -1086,15 +1126,15 @@ int enqueue(gw_voxel_plan *P) {
       const int64_t pairs = ((int64_t)Qc3 + 1) / 2;
       const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
       k_finalize_flat<<<blocks, 256, 0, st>>>(
-          sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0,
+          sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
           P->p.f0_z > 0, f0c, f0iz, o64, o32);
       GW_LAUNCHED(ctx);
     } else {
       gw::KTimer tm(ctx, GW_K_FINALIZE);
-      const int fin_threads = P->Qc >= 256 ? 256 : ((P->Qc + 31) / 32) * 32;
-      k_finalize<<<fin_blocks, fin_threads, 0, st>>>(
+      const int blocks = std::min((P->Qc * P->Qc + 7) / 8, 16 * ctx->sm_count);
+      k_finalize<<<blocks, 256, 0, st>>>(
           sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
-          inv_ns, P->d_f0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
+          inv_ns, P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
       GW_LAUNCHED(ctx);
     }
     if (K > 0 && P->shell_mode == GW_SHELLS_REFERENCE) {
@@ -1304,6 +1344,12 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
           f0tab[(i * 3 + ax) * P->Qc + k] = (float)e;
         }
   }
+  // the z factors of the four terms, packed per qz
+  std::vector<float4> zf0;
+  if (p->f0_z > 0)
+    for (int k = 0; k < P->Qc; ++k)
+      zf0.push_back(make_float4(f0tab[2 * P->Qc + k], f0tab[5 * P->Qc + k],
+                                f0tab[8 * P->Qc + k], f0tab[11 * P->Qc + k]));
   CztTables ty = make_czt(g, P->y_lo, P->Ly, P->k0, P->Nc, P->My);
   CztTables tz = make_czt(g, P->z_lo, P->Lz, P->kz0, P->Nr, P->Mz);
   const size_t W3 = (size_t)P->W * P->W * P->W;
@@ -1314,6 +1360,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = upload(&P->d_phis, P->phis, &B)) ||
       (st = upload(&P->d_clbase, clbase, &B)) ||
       (st = upload(&P->d_gw, gwv, &B)) || (st = upload(&P->d_f0, f0tab, &B)) ||
+      (st = upload(&P->d_zf0, zf0, &B)) ||
       (st = upload(&P->d_rowofs, rowofs, &B)) ||
       (st = upload(&P->d_C1, P->C1host, &B)) ||
       (st = upload(&P->d_Ay, ty.A, &B)) || (st = upload(&P->d_Hy, ty.H, &B)) ||
@@ -1338,9 +1385,9 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_cursor, (size_t)n_struct * (g + 1), &B)) ||
       (st = alloc(&P->d_zstat, n_struct, &B)) ||
       (st = alloc(&P->d_F1, (size_t)P->S * P->Lz * P->Nc, &B)) ||
-      (st = alloc(&P->d_amo, (size_t)P->S * P->Ly, &B)) ||
-      (st = alloc(&P->d_my, (size_t)P->S * P->Ly, &B)) ||
-      (st = alloc(&P->d_mz, (size_t)P->S * P->Lz, &B)) ||
+      (st = alloc(&P->d_amo, (size_t)P->n_slices * P->Ly, &B)) ||
+      (st = alloc(&P->d_my, (size_t)P->n_slices * P->Ly, &B)) ||
+      (st = alloc(&P->d_mz, (size_t)P->n_slices * P->Lz, &B)) ||
       (st = upload(&P->d_roff, P->roff_host, &B))) {
     gw_voxel_plan_destroy(P);
     return st;
@@ -1381,7 +1428,7 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_fz_s,
                   P->d_perm, P->d_cand, P->d_cand_off, P->d_roff, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
-                  P->d_shell, P->d_f_shells, P->d_structs_shells};
+                  P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;

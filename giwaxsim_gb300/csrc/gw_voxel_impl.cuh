@@ -346,6 +346,7 @@ struct gw_voxel_plan {
   double *d_sum = nullptr;
   float2 *d_sumk = nullptr;
   float *d_f0 = nullptr;
+  float4 *d_zf0 = nullptr;  // f0 z factors of the four terms per qz (or null)
   double *d_iq64 = nullptr;
   float *d_iq32 = nullptr;
   float2 *d_F1 = nullptr, *d_amo = nullptr;
