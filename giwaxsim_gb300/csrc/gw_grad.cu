@@ -337,7 +337,8 @@ k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_sl, int n_rows) {
     const int sl = slice0 + slot;
     const float mz = a.smooth_on ? a.mz[(size_t)slot * a.Lz + zz] : 1.f;
     const float dmz = a.smooth_on ? gr.dmz[(size_t)slot * a.Lz + zz] : 0.f;
-    const float2 fs = a.f_s[at];
+    const float4 q = a.xyf_s[at];
+    const float2 fs = make_float2(q.z, q.w);
     if constexpr (!BIL) {
       int yy;
       if (!deposit_column(a, at, sl, yy) || yy >= a.Ly) continue;

@@ -133,8 +133,8 @@ k_zscan(const gw_structure *st, int g, const int *hist, int *rowstart,
 __global__ void k_zscatter(const double *xyz, const float2 *f,
                            const gw_structure *st, const int *zidx, int g,
                            const unsigned long long *zmin_ord, double inv_r,
-                           int *cursor, double *xyz_s, float2 *f_s,
-                           float2 *xy32_s, int *perm, float *fz_s) {
+                           int *cursor, double *xyz_s, float4 *xyf_s,
+                           int *perm, float *fz_s) {
   const gw_structure s = st[blockIdx.y];
   int *cur = cursor + (size_t)blockIdx.y * (g + 1);
   const double zmin = ord_dbl(zmin_ord[blockIdx.y]);
@@ -146,8 +146,8 @@ __global__ void k_zscatter(const double *xyz, const float2 *f,
     xyz_s[3 * (size_t)pos] = xyz[3 * a];
     xyz_s[3 * (size_t)pos + 1] = xyz[3 * a + 1];
     xyz_s[3 * (size_t)pos + 2] = xyz[3 * a + 2];
-    f_s[pos] = f[a];
-    xy32_s[pos] = make_float2((float)xyz[3 * a], (float)xyz[3 * a + 1]);
+    const float2 fa = f[a];
+    xyf_s[pos] = make_float4((float)xyz[3 * a], (float)xyz[3 * a + 1], fa.x, fa.y);
     perm[pos] = (int)a;
     if (fz_s) {
       const double v = GW_DMUL(GW_DSUB(xyz[3 * a + 2], zmin), inv_r);
@@ -330,18 +330,14 @@ template <int M>
 struct RowLoad {
   const SliceArgs *a;
   const CztArgs *cz;
-  const float2 *rows;  // row f at rows + f * LDM
-  const int *r_slot, *r_zz;  // per block row: slot and window row
-  int slice0, row0, n_rows;
+  const float2 *rows;     // row f at rows + f * LDM
+  const RowConst *rc;     // per block row (shared memory)
+  int row0, n_rows;
   __device__ float2 operator()(int f, int n) const {
     const int row = row0 + f;
     if (row >= n_rows || n >= cz->L) return make_float2(0.f, 0.f);
-    const int slot = r_slot[f], zz = r_zz[f];
-    const int sl = slice0 + slot;
-    const SliceConst k = slice_const(*a, sl);
     const float2 dep = rows[f * FftPlan<M>::LDM + n];
-    return cmul(d_value(*a, slot, sl, zz, n, dep, k.cd, k.cbg, a->ext[sl]),
-                __ldg(cz->A + n));
+    return cmul(d_value_row(*a, rc[f], n, dep), __ldg(cz->A + n));
   }
 };
 
@@ -377,9 +373,13 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   extern __shared__ float2 smem[];
   float2 *tw = smem;
   float2 *buf = smem + TWL;
-  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1], r_slot[NB], r_zz[NB];
+  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1], r_slot[NB];
+  __shared__ RowConst r_k[NB];
+  __shared__ DepRow r_d[NB];
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
-  for (int t = threadIdx.x; t < NB * LDM; t += NT) buf[t] = make_float2(0.f, 0.f);
+  // only the window columns [0, L) are deposited into and read back
+  for (int f = 0; f < NB; ++f)
+    for (int n = threadIdx.x; n < cz.L; n += NT) buf[f * LDM + n] = make_float2(0.f, 0.f);
   const int row0 = blockIdx.x * NB;
   // the block's rows: slot, window row and atom range, one thread per row
   // (independent loads), then a scan of the atom counts
@@ -397,7 +397,10 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
     r_mid[f] = mid;
     r_cnt[f + 1] = hi - lo;
     r_slot[f] = slot;
-    r_zz[f] = zz;
+    if (row < n_rows) {
+      r_k[f] = row_const(a, slot, slice0 + slot, zz);
+      r_d[f] = dep_row(a, slice0 + slot);
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -413,11 +416,11 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
     const int sl = slice0 + r_slot[f];
     if constexpr (!BIL) {
       int yy;
-      if (deposit_column(a, at, sl, yy)) {
+      const float4 q = a.xyf_s[at];
+      if (deposit_column(a, r_d[f], make_float2(q.x, q.y), at, yy)) {
         if (yy < a.Ly) {
-          const float2 fv = a.f_s[at];
-          atomicAdd(&buf[f * LDM + yy].x, fv.x);
-          atomicAdd(&buf[f * LDM + yy].y, fv.y);
+          atomicAdd(&buf[f * LDM + yy].x, q.z);
+          atomicAdd(&buf[f * LDM + yy].y, q.w);
         } else {
           dev_error(a.err, GW_DEVERR_BOX);
         }
@@ -428,14 +431,15 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
       if (bilinear_column(a, at, sl, i0, fu)) {
         const float fz = a.fz_s[at];
         const float wz = at >= r_mid[f] ? 1.f - fz : fz;
-        const float2 fv = a.f_s[at];
+        const float4 q = a.xyf_s[at];
+        const float2 fv = make_float2(q.z, q.w);
         deposit_at(a, buf + f * LDM, i0, fv, wz * (1.f - fu));
         if (i0 + 1 < a.g) deposit_at(a, buf + f * LDM, i0 + 1, fv, wz * fu);
       }
     }
   }
   __syncthreads();
-  RowLoad<M> ld{&a, &cz, buf, r_slot, r_zz, slice0, row0, n_rows};
+  RowLoad<M> ld{&a, &cz, buf, r_k, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false>(buf, tw, nullptr, ld, NoStore());
   RowStore stv{cz.B, F1, row0, n_rows, nc_out};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), stv);
@@ -728,15 +732,15 @@ __global__ void k_debug_window(SliceArgs a, int sl, float2 *win) {
       if (!a.bil) {
         int yy;
         if (deposit_column(a, at, sl, yy) && yy < a.Ly) {
-          atomicAdd(&row[yy].x, a.f_s[at].x);
-          atomicAdd(&row[yy].y, a.f_s[at].y);
+          atomicAdd(&row[yy].x, a.xyf_s[at].z);
+          atomicAdd(&row[yy].y, a.xyf_s[at].w);
         }
       } else {
         int i0;
         float fu;
         if (bilinear_column(a, at, sl, i0, fu)) {
           const float wz = at >= mid ? 1.f - a.fz_s[at] : a.fz_s[at];
-          const float2 fv = a.f_s[at];
+          const float2 fv = make_float2(a.xyf_s[at].z, a.xyf_s[at].w);
           for (int c = 0; c < 2; ++c) {
             const int i = i0 + c;
             const int yy = window_col(a, i);
@@ -902,8 +906,8 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.fill = P->p.fill_bkg != 0; a.smooth_on = P->p.smooth != 0.0;
   a.sigma = (float)P->p.smooth; a.radius = P->radius; a.plain = P->plain;
   a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
-  a.xyz_s = P->d_xyz_s; a.f_s = P->d_f_s; a.rowstart = P->d_rowstart;
-  a.xy32_s = P->d_xy32_s; a.fz_s = P->d_fz_s; a.bil = P->bil;
+  a.xyz_s = P->d_xyz_s; a.xyf_s = P->d_xyf_s; a.rowstart = P->d_rowstart;
+  a.fz_s = P->d_fz_s; a.bil = P->bil;
   a.cand = P->d_cand;
   a.cand_off = P->d_cand_off;
   a.roff = P->d_roff;
@@ -1010,7 +1014,7 @@ int enqueue_prep(gw_voxel_plan *P) {
     gw::KTimer tm(ctx, GW_K_PREP);
     k_zscatter<<<dim3(nblk_at, P->n_struct), 256, 0, st>>>(
         P->d_xyz, P->d_f, P->d_structs, P->d_zidx, P->g, P->d_zmin, P->inv_r,
-        P->d_cursor, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_perm, P->d_fz_s);
+        P->d_cursor, P->d_xyz_s, P->d_xyf_s, P->d_perm, P->d_fz_s);
     GW_LAUNCHED(ctx);
   }
   return GW_OK;
@@ -1425,7 +1429,7 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_twz, P->d_gw, P->d_colofs, P->d_rowofs, P->d_C1,
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
                   P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
-                  P->d_sconst, P->d_xyz_s, P->d_f_s, P->d_xy32_s, P->d_fz_s,
+                  P->d_sconst, P->d_xyz_s, P->d_xyf_s, P->d_fz_s,
                   P->d_perm, P->d_cand, P->d_cand_off, P->d_roff, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
                   P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0};
@@ -1498,11 +1502,11 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
     if (s.atom_begin < 0 || s.atom_count < 1 || s.atom_begin + s.atom_count > n)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: structure atom range outside the atom arrays");
   if (n != P->n_atoms) {
-    void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_f_s,
-                   P->d_xy32_s, P->d_perm, P->d_fz_s, P->d_cand};
+    void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_xyf_s,
+                   P->d_perm, P->d_fz_s, P->d_cand};
     for (void *q : old) gw::dev_free(q);
     P->d_xyz = nullptr; P->d_f = nullptr; P->d_zidx = nullptr;
-    P->d_xyz_s = nullptr; P->d_f_s = nullptr; P->d_xy32_s = nullptr;
+    P->d_xyz_s = nullptr; P->d_xyf_s = nullptr;
     P->d_perm = nullptr; P->d_fz_s = nullptr; P->d_cand = nullptr;
     P->n_atoms = -1;
     if (n > INT_MAX / 4)
@@ -1511,8 +1515,7 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
     GW_CUDA(gw::dev_malloc((void **)&P->d_f, (size_t)n * sizeof(float2)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_zidx, (size_t)n * sizeof(int)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_xyz_s, (size_t)n * 3 * sizeof(double)));
-    GW_CUDA(gw::dev_malloc((void **)&P->d_xy32_s, (size_t)n * sizeof(float2)));
-    GW_CUDA(gw::dev_malloc((void **)&P->d_f_s, (size_t)n * sizeof(float2)));
+    GW_CUDA(gw::dev_malloc((void **)&P->d_xyf_s, (size_t)n * sizeof(float4)));
     GW_CUDA(gw::dev_malloc((void **)&P->d_perm, (size_t)n * sizeof(int)));
     if (P->bil)
       GW_CUDA(gw::dev_malloc((void **)&P->d_fz_s, (size_t)n * sizeof(float)));

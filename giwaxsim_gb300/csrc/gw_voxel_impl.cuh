@@ -34,8 +34,7 @@ struct SliceArgs {
   const float2 *f;
   const int *zidx;
   const double *xyz_s; // atoms sorted by z index within each structure
-  const float2 *f_s;
-  const float2 *xy32_s; // float32 (x, y) of the sorted atoms
+  const float4 *xyf_s; // sorted atoms: float32 (x, y) and f (re, im)
   const float *fz_s;   // bilinear: fractional z position of the sorted atoms
   const int *cand;     // atoms (input order) near each structure's (x,y) hull
   const int2 *cand_off; // per structure (begin, count); count < 0: all atoms
@@ -203,6 +202,50 @@ __device__ __forceinline__ float2 d_value(const SliceArgs &a, int slot, int sl,
   return v;
 }
 
+// The per-row part of d_value, hoisted: a block that transforms whole rows
+// evaluates it once per row.
+struct RowConst {
+  float2 cd, cbg;  // slice constants (sconst)
+  int4 e;          // slice extents
+  float mz;        // z smoothing factor of the row (1 when smoothing is off)
+  int zin;         // the row's z lies inside [e.z, e.w)
+  int slot;
+};
+
+__device__ __forceinline__ RowConst row_const(const SliceArgs &a, int slot,
+                                              int sl, int zz) {
+  RowConst k;
+  const SliceConst c = slice_const(a, sl);
+  k.cd = c.cd;
+  k.cbg = c.cbg;
+  k.e = a.ext[sl];
+  k.mz = a.smooth_on ? a.mz[(size_t)slot * a.Lz + zz] : 1.f;
+  const int zi = window_row_to_z(a, zz);
+  k.zin = zi >= k.e.z && zi < k.e.w;
+  k.slot = slot;
+  return k;
+}
+
+// d_value of element yy of a row with constants k: the same operations in
+// the same order.
+__device__ __forceinline__ float2 d_value_row(const SliceArgs &a,
+                                              const RowConst &k, int yy,
+                                              float2 dep) {
+  float2 v;
+  if (a.fill) {
+    int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
+    const bool inside = k.zin && yi > k.e.x && yi < k.e.y;
+    v = inside ? cadd(dep, a.amo[(size_t)k.slot * a.Ly + yy]) : k.cd;
+  } else {
+    v = csub(dep, k.cbg);
+  }
+  if (a.smooth_on) {
+    const float m = k.mz * a.my[(size_t)k.slot * a.Ly + yy];
+    v = make_float2(v.x * m + k.cd.x * (1.f - m), v.y * m + k.cd.y * (1.f - m));
+  }
+  return v;
+}
+
 // Window column of sorted atom `at` in slice `sl` (nearest-bin deposit):
 // false when the valid mask drops it (y index outside [0, g)); yy >= Ly
 // flags a window overflow.
@@ -211,30 +254,51 @@ __device__ __forceinline__ float2 d_value(const SliceArgs &a, int slot, int sl,
 // input roundings, four arithmetic roundings and those of t -+ d total at
 // most 7 u times that sum).  Only when [t-d, t+d] contains an integer is the
 // exact float64 chain replayed.
-__device__ __forceinline__ bool deposit_column(const SliceArgs &a, int at,
-                                               int sl, int &yy) {
-  const int p = sl % a.n_phi;
-  const gw_phi &ph = a.ph[p];
-  const double ymin = ord_dbl(a.ymin_ord[sl]);
-  const float2 xy = a.xy32_s[at];
-  const float cs = (float)ph.cos_phi, sn = (float)ph.sin_phi;
-  const float ym = (float)ymin, ir = (float)a.inv_r;
-  const float t = (fmaf(xy.y, cs, xy.x * sn) - ym) * ir;
+// The per-slice constants of the deposit (a block evaluates them once per
+// row).
+struct DepRow {
+  double ymin, cphi, sphi;
+  float cs, sn, ym;
+};
+
+__device__ __forceinline__ DepRow dep_row(const SliceArgs &a, int sl) {
+  const gw_phi &ph = a.ph[sl % a.n_phi];
+  DepRow k;
+  k.ymin = ord_dbl(a.ymin_ord[sl]);
+  k.cphi = ph.cos_phi;
+  k.sphi = ph.sin_phi;
+  k.cs = (float)ph.cos_phi;
+  k.sn = (float)ph.sin_phi;
+  k.ym = (float)k.ymin;
+  return k;
+}
+
+// xy: the atom's float32 (x, y) (xyf_s[at].x, .y).
+__device__ __forceinline__ bool deposit_column(const SliceArgs &a,
+                                               const DepRow &k, float2 xy,
+                                               int at, int &yy) {
+  const float ir = (float)a.inv_r;
+  const float t = (fmaf(xy.y, k.cs, xy.x * k.sn) - k.ym) * ir;
   const float d = 10.f * 5.9604645e-8f *
-                      (fabsf(xy.x * sn) + fabsf(xy.y * cs) + fabsf(ym)) * ir +
+                      (fabsf(xy.x * k.sn) + fabsf(xy.y * k.cs) + fabsf(k.ym)) * ir +
                   1e-6f;
   const float klo = floorf(t - d), khi = floorf(t + d);
   int yi;
   if (klo == khi) {
     yi = (int)klo;
   } else {
-    const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, ph.cos_phi,
-                                   ph.sin_phi), ymin);
+    const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, k.cphi, k.sphi), k.ymin);
     yi = (int)floor_div_exact(y, a.r, a.inv_r);
   }
   if (yi < 0 || yi >= a.g) return false;
   yy = window_col(a, yi);
   return true;
+}
+
+__device__ __forceinline__ bool deposit_column(const SliceArgs &a, int at,
+                                               int sl, int &yy) {
+  const float4 q = a.xyf_s[at];
+  return deposit_column(a, dep_row(a, sl), make_float2(q.x, q.y), at, yy);
 }
 
 // Bilinear deposit of sorted atom `at` in slice `sl`: the atom's shifted
@@ -351,8 +415,7 @@ struct gw_voxel_plan {
   float *d_iq32 = nullptr;
   float2 *d_F1 = nullptr, *d_amo = nullptr;
   double *d_xyz_s = nullptr;
-  float2 *d_xy32_s = nullptr;
-  float2 *d_f_s = nullptr;
+  float4 *d_xyf_s = nullptr;
   float *d_fz_s = nullptr;
   int *d_perm = nullptr;   // sorted position -> input atom index
   int *d_cand = nullptr;   // hull-near atoms of every structure (capacity n)
