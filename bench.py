@@ -35,8 +35,11 @@ L2_BYTES = 129 * 1024 * 1024
 # shape (workload, kernel, fft_y, fft_z, batch); the summaries with their
 # commands are profiles/k_row_czt_1280_si-100A.md and
 # profiles/k_col_czt_bin_1024_si-100A.md.
-NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024, 51): (1.49 + 38.11) * 1e6,
-               ("si-100A", "col_czt_bin", 1280, 1024, 51): (148.56 + 39.38) * 1e6}
+# DRAM bytes (read + write) per slice from one ncu capture of a 51-slice
+# launch (profiles/); a launch's traffic is this times its slices (both
+# kernels move per-slice data only).
+NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024): (1.49 + 38.11) * 1e6 / 51,
+               ("si-100A", "col_czt_bin", 1280, 1024): (148.56 + 39.38) * 1e6 / 51}
 
 
 def parse():
@@ -349,21 +352,24 @@ def run_gb300(args, world, rank, local, pg):
     if top:
         name, (ms_tot, nl) = top
         avg_ms = ms_tot / max(nl, 1)
-        algo = algorithmic_bytes(name, info, w, n_slices, dargs, plan.Qc)
+        # slices per launch of the batched kernels: the batches' average
+        spl = n_slices / nl if name in ("row_czt", "col_czt_bin") else None
+        algo = algorithmic_bytes(name, info, w, spl, dargs, plan.Qc)
         achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
-        tkey = (args.workload, name, info["My"], info["Mz"], info["batch"])
+        tkey = (args.workload, name, info["My"], info["Mz"])
+        traffic = NCU_TRAFFIC[tkey] * spl if tkey in NCU_TRAFFIC else None
         roof = {"kernel": name, "bound": "hbm", "achieved": achieved,
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": NCU_TRAFFIC.get(tkey),
-                "traffic_source": "ncu capture (profiles/)"
-                if tkey in NCU_TRAFFIC else None,
-                "avg_launch_ms": avg_ms,
+                "traffic": traffic,
+                "traffic_source": "ncu capture of a 51-slice launch (profiles/), "
+                "scaled by slices per launch" if traffic else None,
+                "avg_launch_ms": avg_ms, "slices_per_launch": spl,
                 "algorithmic_bytes_per_launch": algo}
         if name in ("row_czt", "col_czt_bin"):
             # the transforms' own limiter: shared-memory passes
             m = info["My"] if name == "row_czt" else info["Mz"]
-            units = info["batch"] * (info["Lz"] if name == "row_czt" else info["Nc"])
+            units = spl * (info["Lz"] if name == "row_czt" else info["Nc"])
             sb = units * 2 * fft_passes(m) * m * 16
             speak = 152 * 128 * 2070e6 / 1e12
             roof["shared"] = {"achieved": sb / (avg_ms / 1e3) / 1e12,
@@ -571,10 +577,9 @@ def run_profile(args, w, geom, phis, items, ctx):
     plan.close()
 
 
-def algorithmic_bytes(name, info, w, n_slices, dargs, Qc):
+def algorithmic_bytes(name, info, w, S, dargs, Qc):
     """Bytes a launch of `name` must move at minimum (its inputs read once,
-    outputs written once), per the plan's sizes."""
-    S = info["batch"]
+    outputs written once), per the plan's sizes; S = slices per launch."""
     if name == "row_czt":
         return S * info["Lz"] * (info["Ly"] + info["Nc"]) * 8
     if name == "col_czt_bin":

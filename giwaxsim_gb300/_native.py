@@ -27,7 +27,7 @@ EXPORTS = [
     "gw_ctx_launch_count", "gw_ctx_set_timing", "gw_ctx_kernel_times",
     "gw_kernel_category_name", "gw_rotate_points", "gw_collapse_base",
     "gw_voxel_plan_create", "gw_voxel_plan_destroy", "gw_voxel_set_atoms",
-    "gw_voxel_set_shells",
+    "gw_voxel_set_shells", "gw_voxel_get_iq32", "gw_debug_convert",
     "gw_voxel_execute", "gw_voxel_capture_graph", "gw_voxel_get_iq",
     "gw_voxel_device_iq32", "gw_voxel_get_counts", "gw_voxel_get_sums",
     "gw_voxel_info", "gw_voxel_debug_deposit", "gw_voxel_debug_window",
@@ -126,6 +126,8 @@ def _declare(lib):
         "gw_voxel_plan_destroy": ([P], ctypes.c_int),
         "gw_voxel_set_atoms": ([P, P, P, i64, i32], ctypes.c_int),
         "gw_voxel_set_shells": ([P, i32, i32, P, P, P, P, P], ctypes.c_int),
+        "gw_voxel_get_iq32": ([P, P], ctypes.c_int),
+        "gw_debug_convert": ([P, P, i64, P, P, P, P], ctypes.c_int),
         "gw_voxel_execute": ([P], ctypes.c_int),
         "gw_voxel_capture_graph": ([P], ctypes.c_int),
         "gw_voxel_get_iq": ([P, P, i32], ctypes.c_int),

@@ -96,6 +96,62 @@ GW_HD double ord_dbl(unsigned long long u) {
 #endif
 }
 
+// ------------------------------------------------- conversion-free helpers
+// On this GPU float rounding (floorf), float <-> int and float <-> double
+// conversions share the narrow float64 pipe.  Hot loops use these instead:
+// plain float adds on the FMA pipe and integer bit operations.
+// k = floor(t) for |t| < 2^21, by magic-number rounding: adding 1.5 * 2^23
+// rounds t to the nearest integer (ties to even) and leaves that integer in
+// the low mantissa bits; subtracting the magic number's bit pattern gives
+// it as an int, and one comparison turns nearest into floor.  Returns false
+// (k undefined) for |t| >= 2^21, infinities and NaN.
+__device__ __forceinline__ bool floor_to_int(float t, int &k) {
+  if (!(fabsf(t) < 2097152.0f)) return false;
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  const float r = __fadd_rn(t, kMagic);
+  const int n = __float_as_int(r) - 0x4B400000;
+  k = n - (__fsub_rn(r, kMagic) > t ? 1 : 0);
+  return true;
+}
+
+// (double)x by IEEE 754 bit manipulation on 32-bit halves (exact); the
+// hardware conversion only for subnormal, infinite and NaN inputs.
+__device__ __forceinline__ double f2d_exact(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned sign = u & 0x80000000u;
+  if (e == 0u || e == 0xffu) {
+    if ((u << 1) == 0u) return __hiloint2double((int)sign, 0);
+    return (double)x;
+  }
+  const unsigned m = u & 0x7fffffu;
+  const unsigned hi = sign | ((e + 896u) << 20) | (m >> 3);
+  return __hiloint2double((int)hi, (int)(m << 29));
+}
+
+// (float)x, IEEE 754 round to nearest even, by bit manipulation on 32-bit
+// halves; the hardware conversion only where the result is subnormal, zero
+// from a nonzero input, infinite or NaN.  A mantissa carry into the
+// exponent field is the correctly rounded result.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  if (((hi << 1) | lo) == 0u) return __uint_as_float(sign);
+  const int fe = (int)((hi >> 20) & 0x7ffu) - 896;  // float exponent field
+  if (fe <= 0 || fe >= 255) return (float)x;
+  unsigned r = ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1fffffffu;  // the 29 dropped bits
+  if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ++r;
+  return __uint_as_float(sign | r);
+}
+
+// (float)n, exact for n < 2^23 (n in the mantissa of 2^23); the hardware
+// conversion above that.
+__device__ __forceinline__ float small_u2f(unsigned n) {
+  if (n >= 8388608u) return (float)n;
+  return __fsub_rn(__uint_as_float(0x4B000000u + n), 8388608.0f);
+}
+
 // ---------------------------------------------------------------- context
 #include <vector>
 

@@ -154,9 +154,15 @@ constexpr int kOrientFloats = sizeof(OrientFast) / 4;
 constexpr int kDetThreads = 256, kDetPix = 2, kDetChunk = 128, kDetFlush = 16;
 
 __device__ __forceinline__ bool fast_axis(float t, float d, int n, int &k) {
-  const float lo = fminf(fmaxf(floorf(t - d), 0.f), (float)(n - 1));
-  const float hi = fminf(fmaxf(floorf(t + d), 0.f), (float)(n - 1));
-  k = (int)lo;
+  // floor, then clamp to [0, n-1]; pre-clamping to +-2^20 (n <= 2^20)
+  // changes no clamped result and keeps floor_to_int in range (NaN clamps
+  // to the lower bound, as fmaxf does)
+  constexpr float B = 1048576.f;
+  int a = 0, b = 0;
+  floor_to_int(fminf(fmaxf(t - d, -B), B), a);
+  floor_to_int(fminf(fmaxf(t + d, -B), B), b);
+  const int lo = min(max(a, 0), n - 1), hi = min(max(b, 0), n - 1);
+  k = lo;
   return lo == hi;
 }
 
@@ -246,15 +252,15 @@ k_detector_fast(DetArgs a, const OrientFast *ot, double *acc_out, int2 *wl,
       // float32 partial sums of kDetFlush orientations, float64 across them
       if (!a.kahan && ((o + 1) % kDetFlush == 0)) {
 #pragma unroll
-        for (int k = 0; k < kDetPix; ++k) { acc[k] += (double)part[k]; part[k] = 0.f; }
+        for (int k = 0; k < kDetPix; ++k) { acc[k] += f2d_exact(part[k]); part[k] = 0.f; }
       }
     }
   }
 #pragma unroll
   for (int k = 0; k < kDetPix; ++k) {
     if (!valid[k]) continue;
-    acc_out[pix[k]] = a.kahan ? (double)part[k] - (double)kc[k]
-                              : acc[k] + (double)part[k];
+    acc_out[pix[k]] = a.kahan ? f2d_exact(part[k]) - f2d_exact(kc[k])
+                              : acc[k] + f2d_exact(part[k]);
   }
 }
 
@@ -376,13 +382,13 @@ k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
       }
       if ((o + 1) % kDetFlush == 0) {
 #pragma unroll
-        for (int k = 0; k < KP; ++k) { acc[k] += (double)part[k]; part[k] = 0.f; }
+        for (int k = 0; k < KP; ++k) { acc[k] += f2d_exact(part[k]); part[k] = 0.f; }
       }
     }
   }
 #pragma unroll
   for (int k = 0; k < KP; ++k)
-    if (valid[k]) acc_out[pix[k]] = acc[k] + (double)part[k];
+    if (valid[k]) acc_out[pix[k]] = acc[k] + f2d_exact(part[k]);
 }
 
 // Exact float64 replay of the worklist's (pixel, orientation) pairs.

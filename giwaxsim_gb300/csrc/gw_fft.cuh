@@ -251,11 +251,14 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
     if (BF % NT == 0 || b < BF) {
       const int f = FFAST ? b % NB : b / Q;
       const int j = FFAST ? b / NB : b % Q;
+      // with Q a multiple of 16, fft_pad(j + r Q) = fft_pad(j) + r (Q + Q/16):
+      // one address per butterfly and compile-time offsets
+      const float2 *src = buf + f * LDM + fft_pad(j);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int n = j + r * Q;
         if (SRC == 0) {
-          float2 x = buf[f * LDM + fft_pad(n)];
+          float2 x = Q % 16 == 0 ? src[r * (Q + Q / 16)] : buf[f * LDM + fft_pad(n)];
           if (PREMUL) x = cmul(x, __ldg(pre + n));
           v[e][r] = x;
         } else {
@@ -287,12 +290,21 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
       const int j = FFAST ? b / NB : b % Q;
       const int k = j % NS;
       const int base = (j / NS) * NS * R + k;
+      // NS a multiple of 16: fft_pad(base + r NS) = fft_pad(base) + r (NS + NS/16);
+      // NS = 1 and R <= 16 with base = j R a multiple of 16 (R = 16): + r
+      constexpr bool kStride = NS % 16 == 0 || (NS == 1 && R == 16);
+      constexpr int kStep = NS == 1 ? 1 : NS + NS / 16;
+      float2 *dst = buf + f * LDM + fft_pad(base);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int m = base + r * NS;
         const float2 val = v[e][out_slot<R>(r)];
-        if (DST == 0) buf[f * LDM + fft_pad(m)] = val;
-        else store(f, m, val);
+        if (DST == 0) {
+          if (kStride) dst[r * kStep] = val;
+          else buf[f * LDM + fft_pad(m)] = val;
+        } else {
+          store(f, m, val);
+        }
       }
     }
   }

@@ -259,6 +259,46 @@ extern "C" int gw_f0_scale(gw_ctx *ctx, const double *iq, const int32_t *shape,
   return GW_OK;
 }
 
+__global__ void k_debug_convert(const double *in, int64_t n, float *f32,
+                                double *f64, int *fl, int *fl_ok) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    f32[i] = d2f_rn(in[i]);
+    const float x = (float)in[i];
+    f64[i] = f2d_exact(x);
+    int k = 0;
+    fl_ok[i] = floor_to_int(x, k) ? 1 : 0;
+    fl[i] = k;
+  }
+}
+
+extern "C" int gw_debug_convert(gw_ctx *ctx, const double *in, int64_t n,
+                                float *f32, double *f64, int32_t *fl,
+                                int32_t *fl_ok) {
+  if (!ctx || !in || !f32 || !f64 || !fl || !fl_ok || n < 1)
+    return gw::fail(GW_ERR_ARG, "gw_debug_convert: invalid argument");
+  GW_CUDA(cudaSetDevice(ctx->device));
+  DevBuf di, d32, d64, dfl, dok;
+  GW_TRY(up_bytes(ctx, di, in, n * 8));
+  GW_CUDA(gw::dev_malloc(&d32.p, n * 4));
+  GW_CUDA(gw::dev_malloc(&d64.p, n * 8));
+  GW_CUDA(gw::dev_malloc(&dfl.p, n * 4));
+  GW_CUDA(gw::dev_malloc(&dok.p, n * 4));
+  {
+    gw::KTimer tm(ctx, GW_K_MISC);
+    k_debug_convert<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(
+        (const double *)di.p, n, (float *)d32.p, (double *)d64.p, (int *)dfl.p,
+        (int *)dok.p);
+    GW_LAUNCHED(ctx);
+  }
+  GW_CUDA(cudaMemcpyAsync(f32, d32.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  GW_CUDA(cudaMemcpyAsync(f64, d64.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  GW_CUDA(cudaMemcpyAsync(fl, dfl.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  GW_CUDA(cudaMemcpyAsync(fl_ok, dok.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  GW_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GW_OK;
+}
+
 extern "C" int gw_collapse_lengths(gw_ctx *ctx, const double *x_vals, int64_t n,
                                    double hor, double ver, const gw_phi *ph,
                                    double *out) {

@@ -495,7 +495,7 @@ struct ColBin {
     }
     const float I = X.x * X.x + X.y * X.y;
     if (bn->kahan) kahan_add(bn->sumk + soff + co + ro, I);
-    else atomicAdd(bn->sum + soff + co + ro, (double)I);
+    else atomicAdd(bn->sum + soff + co + ro, f2d_exact(I));
   }
 };
 
@@ -593,11 +593,11 @@ k_finalize(const double *sum, const float2 *sumk, int kahan,
       double s;
       if (kahan) {
         const float2 sc = sumk[wbase + iz];
-        s = (double)sc.x - (double)sc.y;
+        s = f2d_exact(sc.x) - f2d_exact(sc.y);
       } else {
         s = sum[wbase + iz];
       }
-      float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
+      float scale = cnt ? inv_nstruct / small_u2f(cnt) : 0.f;
       if (use_f0) {
         const float4 z = __ldg(zf0 + iz);
         float acc = f0_c;
@@ -608,9 +608,9 @@ k_finalize(const double *sum, const float2 *sumk, int kahan,
         const float fq = acc * f0_invz;
         scale *= fq * fq;
       }
-      const double I = s * (double)scale;
+      const double I = s * f2d_exact(scale);
       out64[obase + iz] = I;
-      out32[obase + iz] = (float)I;
+      out32[obase + iz] = d2f_rn(I);
     }
   }
 }
@@ -636,7 +636,7 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
       for (int e = 0; e < 2; ++e)
         if (e == 0 || two) {
           const float2 sc = sumk[i0 + e];
-          s[e] = (double)sc.x - (double)sc.y;
+          s[e] = f2d_exact(sc.x) - f2d_exact(sc.y);
         }
     } else if (two) {
       const double2 v = reinterpret_cast<const double2 *>(sum)[p];
@@ -651,7 +651,7 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
       int line = line0, iz = iz0 + e;
       if (iz == Qc) { iz = 0; ++line; }
       const unsigned cnt = C2[line] * (unsigned)__ldg(C1 + iz);
-      float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
+      float scale = cnt ? inv_nstruct / small_u2f(cnt) : 0.f;
       if (use_f0) {
         const int iy = line / Qc, ix = line - iy * Qc;
         const float4 z = __ldg(zf0 + iz);
@@ -663,14 +663,14 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
         const float fq = acc * f0_invz;
         scale *= fq * fq;
       }
-      I[e] = s[e] * (double)scale;
+      I[e] = s[e] * f2d_exact(scale);
     }
     if (two) {
       reinterpret_cast<double2 *>(out64)[p] = make_double2(I[0], I[1]);
-      reinterpret_cast<float2 *>(out32)[p] = make_float2((float)I[0], (float)I[1]);
+      reinterpret_cast<float2 *>(out32)[p] = make_float2(d2f_rn(I[0]), d2f_rn(I[1]));
     } else {
       out64[i0] = I[0];
-      out32[i0] = (float)I[0];
+      out32[i0] = d2f_rn(I[0]);
     }
   }
 }
@@ -1704,6 +1704,16 @@ extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) 
                             P->n_out,
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                             P->ctx->stream));
+  return gw::check_device_error(P->ctx, "voxel stage");
+}
+
+extern "C" int gw_voxel_get_iq32(gw_voxel_plan *P, float *iq32) {
+  if (!P || !iq32) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq32: null argument");
+  if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq32: plan not executed");
+  const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
+  GW_CUDA(cudaMemcpy2DAsync(iq32, n * sizeof(float), P->d_iq32,
+                            P->iq_stride * sizeof(float), n * sizeof(float),
+                            P->n_out, cudaMemcpyDeviceToHost, P->ctx->stream));
   return gw::check_device_error(P->ctx, "voxel stage");
 }
 

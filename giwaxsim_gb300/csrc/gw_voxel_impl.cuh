@@ -282,10 +282,9 @@ __device__ __forceinline__ bool deposit_column(const SliceArgs &a,
   const float d = 10.f * 5.9604645e-8f *
                       (fabsf(xy.x * k.sn) + fabsf(xy.y * k.cs) + fabsf(k.ym)) * ir +
                   1e-6f;
-  const float klo = floorf(t - d), khi = floorf(t + d);
-  int yi;
-  if (klo == khi) {
-    yi = (int)klo;
+  int klo, khi, yi;
+  if (floor_to_int(t - d, klo) && floor_to_int(t + d, khi) && klo == khi) {
+    yi = klo;
   } else {
     const double y = GW_DSUB(rot_y(a.xyz_s + 3 * (size_t)at, k.cphi, k.sphi), k.ymin);
     yi = (int)floor_div_exact(y, a.r, a.inv_r);

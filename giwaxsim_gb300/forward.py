@@ -273,6 +273,13 @@ class VoxelPlan:
         N.check(N.lib().gw_voxel_get_iq(self.handle, N.ptr(out), 0))
         return out
 
+    def iq32(self):
+        """The float32 I(q) the detector gathers from (host copy)."""
+        shape = (self.Qc,) * 3 if self.n_out == 1 else (self.n_out,) + (self.Qc,) * 3
+        out = np.empty(shape, dtype=np.float32)
+        N.check(N.lib().gw_voxel_get_iq32(self.handle, N.ptr(out)))
+        return out
+
     def iq_to_device(self, dev_ptr):
         N.check(N.lib().gw_voxel_get_iq(self.handle, ctypes.c_void_p(dev_ptr), 1))
 

@@ -208,6 +208,8 @@ int gw_voxel_debug_deposit(gw_voxel_plan *plan, int32_t slice, int32_t *y_idx,
  * complex64 (Lz, Ly) (row z_lo+zz, column y_lo+yy of the grid, cyclic):
  * np.add.at(grid[z, y], f) of voxelgrids.py:341 restricted to the window. */
 int gw_voxel_debug_window(gw_voxel_plan *plan, int32_t slice, float *window);
+/* The float32 I(q) the detector gathers from (crop^3 per structure, host). */
+int gw_voxel_get_iq32(gw_voxel_plan *plan, float *iq32);
 /* One-shot: plan, upload, execute, download, destroy (host buffers). */
 int gw_voxelgrid(gw_ctx *ctx, const gw_voxel_params *p,
                  const gw_structure *structs, int32_t n_struct,
@@ -417,6 +419,12 @@ int gw_f0_scale(gw_ctx *ctx, const double *iq, const int32_t *shape,
  * slice scalars in ph (hor, ver before the phi > 90 swap). */
 int gw_collapse_lengths(gw_ctx *ctx, const double *x_vals, int64_t n,
                         double hor, double ver, const gw_phi *ph, double *out);
+/* Test hook for the conversion helpers hot kernels use instead of hardware
+ * conversions: f32[i] = in[i] rounded to float (nearest even), f64[i] =
+ * (double)(float)in[i], fl[i] = floor((float)in[i]) where fl_ok[i] = 1
+ * (|x| < 2^21). */
+int gw_debug_convert(gw_ctx *ctx, const double *in, int64_t n, float *f32,
+                     double *f64, int32_t *fl, int32_t *fl_ok);
 
 #ifdef __cplusplus
 }
