@@ -5,8 +5,36 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
+#include <vector>
+
+#include <unistd.h>
 
 #include "gw_common.cuh"
+
+namespace gw {
+
+void prefault_host(void *p, size_t bytes) {
+  if (!p || bytes < ((size_t)64 << 20)) return;
+  long pg = sysconf(_SC_PAGESIZE);
+  const size_t page = pg > 0 ? (size_t)pg : 4096;
+  const unsigned hw = std::thread::hardware_concurrency();
+  const unsigned nt = std::min(16u, std::max(1u, hw));
+  const size_t chunk = ((bytes / nt) / page + 1) * page;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nt; ++t) {
+    const size_t lo = (size_t)t * chunk;
+    if (lo >= bytes) break;
+    const size_t hi = std::min(bytes, lo + chunk);
+    th.emplace_back([p, lo, hi, page] {
+      volatile char *b = static_cast<volatile char *>(p);
+      for (size_t o = lo; o < hi; o += page) b[o] = 0;
+    });
+  }
+  for (auto &x : th) x.join();
+}
+
+}  // namespace gw
 
 namespace gw {
 

@@ -202,6 +202,12 @@ void dev_free(void *p);
 // checks the device error word of ctx (synchronizes the stream)
 int check_device_error(gw_ctx *ctx, const char *where);
 
+// Fault in the pages of a large host destination with several threads
+// (one byte written per page) before a device-to-host copy into it.  For a
+// fresh buffer the operating system's zeroing of every new page on first
+// touch costs several times the copy itself, and it scales with threads.
+void prefault_host(void *p, size_t bytes);
+
 }  // namespace gw
 
 #define GW_CUDA(call)                                                    \

@@ -159,6 +159,73 @@ __global__ void k_zscatter(const double *xyz, const float2 *f,
 // ------------------------------------------------------------ per slice
 // Per slice: min and max of the rotated y over all atoms (the shift to the
 // minimum, voxelgrids.py:323), and the slice's background constants.
+// Per-slice extremes of the rotated y' = x sin(phi) + y cos(phi) over all
+// atoms of the structure (voxelgrids.py:325-330: np.min / np.max of
+// rot[:, 1]), exact in float64, in two passes over the z-sorted atoms.
+// Pass 1 (k_ybound) evaluates y' in float32 with a rigorous error bound d
+// (10 u (|x s| + |y c|), u = 2^-24: input, product and fma roundings total
+// about 4.1 u of that sum) and keeps lo = min(y' + d) and hi = max(y' - d),
+// rounded outward.  Pass 2 (k_yminmax) evaluates the float64 chain only for
+// the atoms whose interval reaches below lo or above hi: every other atom's
+// exact value is above lo >= the exact minimum (below hi <= the maximum).
+__device__ __forceinline__ unsigned flt_ord(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord_flt(unsigned o) {
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+__device__ __forceinline__ void y_interval(const SliceArgs &a, int64_t at,
+                                           float cs, float sn, float &lo,
+                                           float &hi) {
+  const float4 q = a.xyf_s[at];
+  const float xs = q.x * sn, yc = q.y * cs;
+  const float t = fmaf(q.y, cs, xs);
+  const float d = 10.f * 5.9604645e-8f * (fabsf(xs) + fabsf(yc));
+  lo = __fsub_rd(t, d);
+  hi = __fadd_ru(t, d);
+}
+
+// lo bounds to the largest ordered value, hi bounds to the smallest
+__global__ void k_yreset(unsigned *ybnd, int s0, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    ybnd[2 * (size_t)(s0 + i)] = ~0u;
+    ybnd[2 * (size_t)(s0 + i) + 1] = 0u;
+  }
+}
+
+__global__ void k_ybound(SliceArgs a, int slice0) {
+  const int sl = slice0 + blockIdx.y;
+  const int t = sl / a.n_phi, p = sl % a.n_phi;
+  const gw_structure s = a.st[t];
+  const float cs = (float)a.ph[p].cos_phi, sn = (float)a.ph[p].sin_phi;
+  unsigned lo = ~0u, hi = 0u;  // ordered: min of (y'+d), max of (y'-d)
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    float l, h;
+    y_interval(a, s.atom_begin + i, cs, sn, l, h);
+    lo = min(lo, flt_ord(h));
+    hi = max(hi, flt_ord(l));
+  }
+  // block reduction, then one atomic per block and bound
+  __shared__ unsigned s_lo[32], s_hi[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) { s_lo[w] = lo; s_hi[w] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < nw; ++k) { lo = min(lo, s_lo[k]); hi = max(hi, s_hi[k]); }
+    if (lo != ~0u) {
+      atomicMin(a.ybnd + 2 * (size_t)sl, lo);
+      atomicMax(a.ybnd + 2 * (size_t)sl + 1, hi);
+    }
+  }
+}
+
 __global__ void k_yminmax(SliceArgs a, int slice0) {
   const int sl = slice0 + blockIdx.y;
   const int t = sl / a.n_phi, p = sl % a.n_phi;
@@ -174,31 +241,34 @@ __global__ void k_yminmax(SliceArgs a, int slice0) {
                       : make_float4(0.f, 0.f, c.x, c.y);
   }
   const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
+  const float csf = (float)c, snf = (float)sn;
+  const float blo = ord_flt(a.ybnd[2 * (size_t)sl]);
+  const float bhi = ord_flt(a.ybnd[2 * (size_t)sl + 1]);
   unsigned long long lo = ~0ULL, hi = 0ULL;
-  const int2 co = a.cand_off ? a.cand_off[t] : make_int2(0, -1);
-  if (co.y >= 0) {
-    // only the atoms near the (x, y) hull can hold the extremes
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < co.y;
-         i += gridDim.x * blockDim.x) {
-      const unsigned long long v = dbl_ord(rot_y(a.xyz + 3 * (size_t)a.cand[co.x + i], c, sn));
-      lo = min(lo, v);
-      hi = max(hi, v);
-    }
-  } else {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-         i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+    float l, h;
+    y_interval(a, s.atom_begin + i, csf, snf, l, h);
+    if (l <= blo || h >= bhi) {
       const unsigned long long v = dbl_ord(rot_y(a.xyz_s + 3 * (s.atom_begin + i), c, sn));
       lo = min(lo, v);
       hi = max(hi, v);
     }
   }
+  __shared__ unsigned long long s_lo[32], s_hi[32];
   for (int o = 16; o > 0; o >>= 1) {
     lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
     hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
   }
-  if ((threadIdx.x & 31) == 0 && lo != ~0ULL) {
-    atomicMin(a.ymin_ord + sl, lo);
-    atomicMax(a.ymax_ord + sl, hi);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) { s_lo[w] = lo; s_hi[w] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < nw; ++k) { lo = min(lo, s_lo[k]); hi = max(hi, s_hi[k]); }
+    if (lo != ~0ULL) {
+      atomicMin(a.ymin_ord + sl, lo);
+      atomicMax(a.ymax_ord + sl, hi);
+    }
   }
 }
 
@@ -908,8 +978,7 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.xyz = P->d_xyz; a.f = P->d_f; a.zidx = P->d_zidx; a.st = P->d_structs;
   a.xyz_s = P->d_xyz_s; a.xyf_s = P->d_xyf_s; a.rowstart = P->d_rowstart;
   a.fz_s = P->d_fz_s; a.bil = P->bil;
-  a.cand = P->d_cand;
-  a.cand_off = P->d_cand_off;
+  a.ybnd = P->d_ybnd;
   a.roff = P->d_roff;
   a.zstat = P->d_zstat; a.ymax_ord = P->d_ymax; a.extflag = P->d_extflag;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
@@ -1036,10 +1105,15 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
   const int nblk_at = atom_blocks(P);
   {
     gw::KTimer tm(ctx, GW_K_DEPOSIT);
-    const int nblk_mm = P->cand_max >= 0
-        ? (int)std::min<int64_t>(std::max<int64_t>(1, (P->cand_max + 255) / 256), nblk_at)
-        : nblk_at;
-    k_yminmax<<<dim3(nblk_mm, n), 256, 0, st>>>(a, s0);
+    // bounds of slice s live at ybnd[2s], ybnd[2s+1]: reset this range
+    k_yreset<<<(n + 255) / 256, 256, 0, st>>>(P->d_ybnd, s0, n);
+    GW_LAUNCHED(ctx);
+    // a few blocks per slice (grid-stride over the atoms), one atomic per
+    // block: the slice's two words are the only targets
+    const int nblk_y = std::min(nblk_at, 8);
+    k_ybound<<<dim3(nblk_y, n), 256, 0, st>>>(a, s0);
+    GW_LAUNCHED(ctx);
+    k_yminmax<<<dim3(nblk_y, n), 256, 0, st>>>(a, s0);
     GW_LAUNCHED(ctx);
   }
   {
@@ -1383,6 +1457,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_iq64, P->iq_stride * P->n_out, &B)) ||
       (st = alloc(&P->d_iq32, P->iq_stride * P->n_out, &B)) ||
       (st = alloc(&P->d_ymax, P->n_slices, &B)) ||
+      (st = alloc(&P->d_ybnd, 2 * (size_t)P->n_slices, &B)) ||
       (st = alloc(&P->d_extflag, P->n_slices, &B)) ||
       (st = alloc(&P->d_zhist, (size_t)n_struct * (g + 1), &B)) ||
       (st = alloc(&P->d_rowstart, (size_t)n_struct * (g + 2), &B)) ||
@@ -1430,68 +1505,12 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_C2, P->d_sum, P->d_sumk, P->d_f0, P->d_iq64,
                   P->d_iq32, P->d_F1, P->d_amo, P->d_my, P->d_mz,
                   P->d_sconst, P->d_xyz_s, P->d_xyf_s, P->d_fz_s,
-                  P->d_perm, P->d_cand, P->d_cand_off, P->d_roff, P->d_zhist, P->d_rowstart,
+                  P->d_perm, P->d_ybnd, P->d_roff, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
                   P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
-}
-
-// Atoms of one structure that can hold the minimum or maximum of the
-// rotated y = x sin(phi) + y cos(phi) for some phi: the minimum of a linear
-// function over the atoms is attained on the convex hull of their (x, y)
-// projection, and an atom farther than D inside the hull exceeds the
-// minimum by more than D for every direction.  D = 1e-9 (1 + max|x|,|y|)
-// is far above the float64 rounding of the rotated coordinate (a few ulp of
-// |x| + |y|), so the exact float64 minimum over the candidates equals the
-// minimum over all atoms.  Points on or outside the computed hull (rounding
-// in the hull itself) are candidates too.  Appends input indices to out.
-static void hull_candidates(const double *xyz, int64_t begin, int64_t count,
-                            std::vector<int> &out) {
-  std::vector<int64_t> id(count);
-  for (int64_t i = 0; i < count; ++i) id[i] = begin + i;
-  auto X = [&](int64_t a) { return xyz[3 * a]; };
-  auto Y = [&](int64_t a) { return xyz[3 * a + 1]; };
-  std::sort(id.begin(), id.end(), [&](int64_t a, int64_t b) {
-    return X(a) < X(b) || (X(a) == X(b) && Y(a) < Y(b));
-  });
-  auto cross = [&](int64_t o, int64_t a, int64_t b) {
-    return (X(a) - X(o)) * (Y(b) - Y(o)) - (Y(a) - Y(o)) * (X(b) - X(o));
-  };
-  std::vector<int64_t> h(2 * count + 1);
-  int64_t k = 0;
-  for (int64_t i = 0; i < count; ++i) {  // lower hull
-    while (k >= 2 && cross(h[k - 2], h[k - 1], id[i]) <= 0) --k;
-    h[k++] = id[i];
-  }
-  for (int64_t i = count - 2, lo = k + 1; i >= 0; --i) {  // upper hull
-    while (k >= lo && cross(h[k - 2], h[k - 1], id[i]) <= 0) --k;
-    h[k++] = id[i];
-  }
-  const int64_t nh = k - 1;  // counter-clockwise, last == first
-  if (nh < 3) {
-    for (int64_t i = 0; i < count; ++i) out.push_back((int)(begin + i));
-    return;
-  }
-  double scale = 0.0;
-  for (int64_t i = 0; i < count; ++i)
-    scale = std::max(scale, std::max(std::fabs(X(begin + i)), std::fabs(Y(begin + i))));
-  const double D = 1e-9 * (1.0 + scale);
-  std::vector<double> ex(nh), ey(nh), nx(nh), ny(nh);
-  for (int64_t e = 0; e < nh; ++e) {
-    const double dx = X(h[e + 1]) - X(h[e]), dy = Y(h[e + 1]) - Y(h[e]);
-    const double len = std::sqrt(dx * dx + dy * dy);
-    ex[e] = X(h[e]); ey[e] = Y(h[e]);
-    nx[e] = -dy / len; ny[e] = dx / len;  // inward unit normal
-  }
-  for (int64_t i = 0; i < count; ++i) {
-    const double px = X(begin + i), py = Y(begin + i);
-    double d = HUGE_VAL;
-    for (int64_t e = 0; e < nh && d > D; ++e)
-      d = std::min(d, (px - ex[e]) * nx[e] + (py - ey[e]) * ny[e]);
-    if (d <= D) out.push_back((int)(begin + i));
-  }
 }
 
 extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
@@ -1503,11 +1522,11 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: structure atom range outside the atom arrays");
   if (n != P->n_atoms) {
     void *old[] = {P->d_xyz, P->d_f, P->d_zidx, P->d_xyz_s, P->d_xyf_s,
-                   P->d_perm, P->d_fz_s, P->d_cand};
+                   P->d_perm, P->d_fz_s};
     for (void *q : old) gw::dev_free(q);
     P->d_xyz = nullptr; P->d_f = nullptr; P->d_zidx = nullptr;
     P->d_xyz_s = nullptr; P->d_xyf_s = nullptr;
-    P->d_perm = nullptr; P->d_fz_s = nullptr; P->d_cand = nullptr;
+    P->d_perm = nullptr; P->d_fz_s = nullptr;
     P->n_atoms = -1;
     if (n > INT_MAX / 4)
       return gw::fail(GW_ERR_ARG, "gw_voxel_set_atoms: more than 2^29 atoms");
@@ -1527,34 +1546,6 @@ extern "C" int gw_voxel_set_atoms(gw_voxel_plan *P, const double *xyz,
   GW_CUDA(cudaMemcpyAsync(P->d_xyz, xyz, (size_t)n * 3 * sizeof(double), kind, P->ctx->stream));
   GW_CUDA(cudaMemcpyAsync(P->d_f, f, (size_t)n * sizeof(float2), kind, P->ctx->stream));
   P->f_stale = false;
-  // hull-near atoms per structure (host coordinates only; device-resident
-  // atoms keep the full scan).  The arrays keep their addresses, so a
-  // captured graph stays valid.
-  if (!P->d_cand) GW_CUDA(gw::dev_malloc((void **)&P->d_cand, (size_t)n * sizeof(int)));
-  if (!P->d_cand_off)
-    GW_CUDA(gw::dev_malloc((void **)&P->d_cand_off, P->n_struct * sizeof(int2)));
-  P->cand_host.clear();
-  P->cand_off_host.assign(P->n_struct, make_int2(0, -1));
-  P->cand_max = -1;
-  if (!on_device) {
-    int64_t mx = 0;
-    for (int t = 0; t < P->n_struct; ++t) {
-      const int begin = (int)P->cand_host.size();
-      hull_candidates(xyz, P->structs[t].atom_begin, P->structs[t].atom_count,
-                      P->cand_host);
-      const int cnt = (int)P->cand_host.size() - begin;
-      P->cand_off_host[t] = make_int2(begin, cnt);
-      mx = std::max<int64_t>(mx, cnt);
-    }
-    P->cand_max = mx;
-    if (!P->cand_host.empty())
-      GW_CUDA(cudaMemcpyAsync(P->d_cand, P->cand_host.data(),
-                              P->cand_host.size() * sizeof(int),
-                              cudaMemcpyHostToDevice, P->ctx->stream));
-  }
-  GW_CUDA(cudaMemcpyAsync(P->d_cand_off, P->cand_off_host.data(),
-                          P->n_struct * sizeof(int2), cudaMemcpyHostToDevice,
-                          P->ctx->stream));
   return GW_OK;
 }
 
@@ -1698,6 +1689,7 @@ extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) 
   if (!P || !iq) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq: plan not executed");
   const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
+  if (!on_device) gw::prefault_host(iq, n * P->n_out * sizeof(double));
   // one 2-D copy packs the structures' padded grids back to back
   GW_CUDA(cudaMemcpy2DAsync(iq, n * sizeof(double), P->d_iq64,
                             P->iq_stride * sizeof(double), n * sizeof(double),
@@ -1711,6 +1703,7 @@ extern "C" int gw_voxel_get_iq32(gw_voxel_plan *P, float *iq32) {
   if (!P || !iq32) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq32: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq32: plan not executed");
   const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
+  gw::prefault_host(iq32, n * P->n_out * sizeof(float));
   GW_CUDA(cudaMemcpy2DAsync(iq32, n * sizeof(float), P->d_iq32,
                             P->iq_stride * sizeof(float), n * sizeof(float),
                             P->n_out, cudaMemcpyDeviceToHost, P->ctx->stream));

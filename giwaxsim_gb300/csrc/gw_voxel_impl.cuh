@@ -36,8 +36,7 @@ struct SliceArgs {
   const double *xyz_s; // atoms sorted by z index within each structure
   const float4 *xyf_s; // sorted atoms: float32 (x, y) and f (re, im)
   const float *fz_s;   // bilinear: fractional z position of the sorted atoms
-  const int *cand;     // atoms (input order) near each structure's (x,y) hull
-  const int2 *cand_off; // per structure (begin, count); count < 0: all atoms
+  unsigned *ybnd;      // per slice: float32 bounds on the y extremes (ordered)
   const int *roff;     // per slice: first window row (n_slices+1 entries),
                        // when structures have their own z windows; else null
   const int *rowstart; // per structure: g+2 offsets into the sorted arrays
@@ -417,11 +416,7 @@ struct gw_voxel_plan {
   float4 *d_xyf_s = nullptr;
   float *d_fz_s = nullptr;
   int *d_perm = nullptr;   // sorted position -> input atom index
-  int *d_cand = nullptr;   // hull-near atoms of every structure (capacity n)
-  int2 *d_cand_off = nullptr;
-  int64_t cand_max = -1;   // largest per-structure count; < 0: none
-  std::vector<int> cand_host;
-  std::vector<int2> cand_off_host;
+  unsigned *d_ybnd = nullptr;  // 2 per slice (see k_ybound)
   std::vector<int> roff_host;  // per-slice first window row (n_slices+1)
   int *d_roff = nullptr;       // null when every slice has Lz rows
   int *d_zhist = nullptr, *d_rowstart = nullptr, *d_cursor = nullptr;
