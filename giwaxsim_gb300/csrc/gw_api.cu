@@ -1,5 +1,8 @@
 // Context, error reporting, allocation and host helpers of the C ABI.
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <unordered_map>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -8,6 +11,7 @@
 #include <thread>
 #include <vector>
 
+#include <sys/mman.h>
 #include <unistd.h>
 
 #include "gw_common.cuh"
@@ -15,9 +19,14 @@
 namespace gw {
 
 void prefault_host(void *p, size_t bytes) {
-  if (!p || bytes < ((size_t)64 << 20)) return;
+  if (!p || bytes < ((size_t)16 << 20)) return;
   long pg = sysconf(_SC_PAGESIZE);
   const size_t page = pg > 0 ? (size_t)pg : 4096;
+  // transparent huge pages where the system allows them: far fewer faults
+  // (a no-op elsewhere)
+  const uintptr_t a0 = ((uintptr_t)p + page - 1) / page * page;
+  const uintptr_t a1 = ((uintptr_t)p + bytes) / page * page;
+  if (a1 > a0) madvise((void *)a0, a1 - a0, MADV_HUGEPAGE);
   const unsigned hw = std::thread::hardware_concurrency();
   const unsigned nt = std::min(16u, std::max(1u, hw));
   const size_t chunk = ((bytes / nt) / page + 1) * page;
@@ -32,6 +41,49 @@ void prefault_host(void *p, size_t bytes) {
     });
   }
   for (auto &x : th) x.join();
+}
+
+int copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+  // Pipelined: worker threads fault in 32 MB chunks in order while this
+  // thread copies each chunk as soon as it is ready.
+  constexpr size_t kChunk = (size_t)32 << 20;
+  if (bytes < 2 * kChunk) {
+    prefault_host(dst, bytes);
+    GW_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    return GW_OK;
+  }
+  long pg = sysconf(_SC_PAGESIZE);
+  const size_t page = pg > 0 ? (size_t)pg : 4096;
+  const uintptr_t a0 = ((uintptr_t)dst + page - 1) / page * page;
+  const uintptr_t a1 = ((uintptr_t)dst + bytes) / page * page;
+  if (a1 > a0) madvise((void *)a0, a1 - a0, MADV_HUGEPAGE);
+  const size_t nc = (bytes + kChunk - 1) / kChunk;
+  std::vector<std::atomic<int>> done(nc);
+  for (auto &d : done) d.store(0);
+  std::atomic<size_t> next{0};
+  const unsigned hw = std::thread::hardware_concurrency();
+  const unsigned nt = std::min(15u, std::max(1u, hw > 1 ? hw - 1 : 1u));
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nt; ++t)
+    th.emplace_back([&, page] {
+      for (size_t c; (c = next.fetch_add(1)) < nc;) {
+        volatile char *b = static_cast<volatile char *>(dst);
+        const size_t lo = c * kChunk, hi = std::min(bytes, lo + kChunk);
+        for (size_t o = lo; o < hi; o += page) b[o] = 0;
+        done[c].store(1, std::memory_order_release);
+      }
+    });
+  cudaError_t e = cudaSuccess;
+  for (size_t c = 0; c < nc; ++c) {
+    while (!done[c].load(std::memory_order_acquire)) std::this_thread::yield();
+    const size_t lo = c * kChunk, len = std::min(bytes - lo, kChunk);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((char *)dst + lo, (const char *)src + lo, len,
+                          cudaMemcpyDeviceToHost, st);
+  }
+  for (auto &x : th) x.join();
+  if (e != cudaSuccess) return cuda_fail(e, "copy to host", __FILE__, __LINE__);
+  return GW_OK;
 }
 
 }  // namespace gw
@@ -57,6 +109,48 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
 
 static std::atomic<long long> g_alloc_count{0};
 
+// Device blocks freed by the library are kept for reuse by an allocation of
+// the same device and size (plans of one shape made again and again: the
+// drop-in calls in a loop, fit candidates), up to GW_ALLOC_CACHE_MB
+// (default 4096; 0 disables).  A failed cudaMalloc releases the cache and
+// retries; gw_ctx_destroy releases it.
+namespace {
+std::mutex g_cache_mu;
+std::multimap<std::pair<int, size_t>, void *> g_cache;   // free blocks
+std::unordered_map<void *, std::pair<int, size_t>> g_live;  // our blocks
+size_t g_cached = 0;
+
+size_t cache_cap() {
+  static const size_t cap = [] {
+    const char *s = getenv("GW_ALLOC_CACHE_MB");
+    const long long mb = s ? atoll(s) : 4096;
+    return mb > 0 ? (size_t)mb << 20 : (size_t)0;
+  }();
+  return cap;
+}
+
+void release_cache_locked(int device) {
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (auto it = g_cache.begin(); it != g_cache.end();) {
+    if (device < 0 || it->first.first == device) {
+      cudaSetDevice(it->first.first);
+      cudaFree(it->second);
+      g_cached -= it->first.second;
+      it = g_cache.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  cudaSetDevice(cur);
+}
+}  // namespace
+
+void release_alloc_cache(int device) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  release_cache_locked(device);
+}
+
 cudaError_t dev_malloc(void **p, size_t bytes) {
   static const long long fail_after = [] {
     const char *s = getenv("GW_FAIL_ALLOC_AFTER");
@@ -67,11 +161,51 @@ cudaError_t dev_malloc(void **p, size_t bytes) {
     *p = nullptr;
     return cudaErrorMemoryAllocation;
   }
-  return cudaMalloc(p, bytes);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const std::pair<int, size_t> key(dev, bytes);
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  auto it = g_cache.find(key);
+  if (it != g_cache.end()) {
+    *p = it->second;
+    g_cache.erase(it);
+    g_cached -= bytes;
+    g_live[*p] = key;
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaErrorMemoryAllocation && g_cached > 0) {
+    cudaGetLastError();
+    release_cache_locked(-1);
+    e = cudaMalloc(p, bytes);
+  }
+  if (e == cudaSuccess) g_live[*p] = key;
+  return e;
 }
 
 void dev_free(void *p) {
-  if (p) cudaFree(p);
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  auto it = g_live.find(p);
+  if (it == g_live.end()) {
+    cudaFree(p);
+    return;
+  }
+  const std::pair<int, size_t> key = it->second;
+  g_live.erase(it);
+  if (key.second > cache_cap() - std::min(cache_cap(), g_cached)) {
+    cudaFree(p);
+    return;
+  }
+  // work queued on any stream may still use the block: wait, as cudaFree
+  // would, before it can be handed out again
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(key.first);
+  cudaDeviceSynchronize();
+  cudaSetDevice(cur);
+  g_cache.emplace(key, p);
+  g_cached += key.second;
 }
 
 int check_device_error(gw_ctx *ctx, const char *where) {
@@ -232,6 +366,7 @@ int gw_ctx_destroy(gw_ctx *c) {
     if (e) cudaEventDestroy(e);
   gw::dev_free(c->d_err);
   if (c->stream) cudaStreamDestroy(c->stream);
+  gw::release_alloc_cache(c->device);
   delete c;
   return GW_OK;
 }

@@ -198,6 +198,8 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 // (n+1)-th device allocation of the process fail with GW_ERR_OOM.
 cudaError_t dev_malloc(void **p, size_t bytes);
 void dev_free(void *p);
+// Free the cached device blocks of one device (-1: all devices).
+void release_alloc_cache(int device);
 
 // checks the device error word of ctx (synchronizes the stream)
 int check_device_error(gw_ctx *ctx, const char *where);
@@ -207,6 +209,10 @@ int check_device_error(gw_ctx *ctx, const char *where);
 // fresh buffer the operating system's zeroing of every new page on first
 // touch costs several times the copy itself, and it scales with threads.
 void prefault_host(void *p, size_t bytes);
+// Device-to-host copy of `bytes` into host memory dst on stream st (returns
+// after the copy is enqueued; pageable destinations complete before), with
+// the destination's page faulting pipelined ahead of the copy.
+int copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t st);
 
 }  // namespace gw
 

@@ -1689,6 +1689,10 @@ extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) 
   if (!P || !iq) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq: plan not executed");
   const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
+  if (!on_device && P->n_out == 1) {
+    GW_TRY(gw::copy_to_host(iq, P->d_iq64, n * sizeof(double), P->ctx->stream));
+    return gw::check_device_error(P->ctx, "voxel stage");
+  }
   if (!on_device) gw::prefault_host(iq, n * P->n_out * sizeof(double));
   // one 2-D copy packs the structures' padded grids back to back
   GW_CUDA(cudaMemcpy2DAsync(iq, n * sizeof(double), P->d_iq64,
