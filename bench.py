@@ -38,8 +38,8 @@ L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) per slice from one ncu capture of a 51-slice
 # launch (profiles/); a launch's traffic is this times its slices (both
 # kernels move per-slice data only).
-NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024): (1.49 + 38.11) * 1e6 / 51,
-               ("si-100A", "col_czt_bin", 1280, 1024): (148.56 + 39.38) * 1e6 / 51}
+NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024): (1.48 + 38.03) * 1e6 / 51,
+               ("si-100A", "col_czt_bin", 1280, 1024): (148.55 + 30.01) * 1e6 / 51}
 
 
 def parse():
