@@ -131,6 +131,51 @@ def f0_params(element):
     return list(aff_dict[element]), float(ptable[element])
 
 
+class HostPool:
+    """Recycled host buffers for large results.  A fresh multi-hundred-MB
+    numpy array costs the operating system a first-touch zeroing of every
+    page several times longer than the device-to-host copy into it; a
+    buffer whose previous result the caller has dropped (only the pool
+    still references it) is handed out again instead.  Arrays given out are
+    ordinary float64 arrays owned by the caller for as long as it keeps
+    them; the pool keeps at most `per_shape` buffers per shape and
+    `max_bytes` in all."""
+
+    def __init__(self, min_bytes=64 << 20, per_shape=2, max_bytes=4 << 30):
+        import sys
+        import threading
+        self._refs = sys.getrefcount
+        self._lock = threading.Lock()
+        self.min_bytes, self.per_shape, self.max_bytes = min_bytes, per_shape, max_bytes
+        self._bufs = {}
+
+    def empty(self, shape, dtype=np.float64):
+        shape, dtype = tuple(int(v) for v in shape), np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        if nbytes < self.min_bytes:
+            return np.empty(shape, dtype)
+        key = (shape, dtype.str)
+        with self._lock:
+            bufs = self._bufs.setdefault(key, [])
+            for b in bufs:
+                # referenced by the list, the loop variable and getrefcount's
+                # argument only: no result array uses it any more
+                if self._refs(b) <= 3:
+                    return b.view()
+            held = sum(x.nbytes for v in self._bufs.values() for x in v)
+            b = np.empty(shape, dtype)
+            if len(bufs) < self.per_shape and held + nbytes <= self.max_bytes:
+                bufs.append(b)
+            return b.view()
+
+    def clear(self):
+        with self._lock:
+            self._bufs.clear()
+
+
+HOST_POOL = HostPool()
+
+
 class VoxelPlan:
     """Owner of a gw_voxel_plan for one geometry, a list of structures and
     a list of phis.  structures: list of (coords (N,3), f_values (N,)
@@ -267,9 +312,11 @@ class VoxelPlan:
         N.check(N.lib().gw_voxel_capture_graph(self.handle))
 
     def iq(self, out=None):
-        """I(q) (Qc, Qc, Qc); (n_struct, Qc, Qc, Qc) for separate structures."""
+        """I(q) (Qc, Qc, Qc); (n_struct, Qc, Qc, Qc) for separate structures.
+        Without `out`, a fresh array (large ones from the recycled host
+        buffers of HostPool)."""
         shape = (self.Qc,) * 3 if self.n_out == 1 else (self.n_out,) + (self.Qc,) * 3
-        out = np.empty(shape) if out is None else out
+        out = HOST_POOL.empty(shape) if out is None else out
         N.check(N.lib().gw_voxel_get_iq(self.handle, N.ptr(out), 0))
         return out
 
