@@ -318,7 +318,9 @@ def run_gb300(args, world, rank, local, pg):
     if len(items) == 1:
         xyz, el, wt = structs[0]
         t_e = []
-        for k in range(1 + max(1, min(args.steps, 3))):
+        # two untimed calls first: the host result buffers the API recycles
+        # (forward.HOST_POOL) exist from then on
+        for k in range(2 + max(3, min(args.steps, 5))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             iq, qx, qy, qz = comparison.voxelgridmaker_fitting(
@@ -326,7 +328,7 @@ def run_gb300(args, world, rank, local, pg):
                 fill_bkg=w["fill_bkg"], smooth=w["smooth"], phis=phis,
                 weights=wt, ctx=ctx)
             t_e.append(time.perf_counter() - t0)
-        te = float(np.mean(t_e[1:]))
+        te = float(np.mean(t_e[2:]))
         # where the e2e time goes: the same call split into its phases
         fv = F.element_f_values(el, w["energy"])
         ph = {}

@@ -11,7 +11,6 @@
 #include <thread>
 #include <vector>
 
-#include <sys/mman.h>
 #include <unistd.h>
 
 #include "gw_common.cuh"
@@ -22,11 +21,6 @@ void prefault_host(void *p, size_t bytes) {
   if (!p || bytes < ((size_t)16 << 20)) return;
   long pg = sysconf(_SC_PAGESIZE);
   const size_t page = pg > 0 ? (size_t)pg : 4096;
-  // transparent huge pages where the system allows them: far fewer faults
-  // (a no-op elsewhere)
-  const uintptr_t a0 = ((uintptr_t)p + page - 1) / page * page;
-  const uintptr_t a1 = ((uintptr_t)p + bytes) / page * page;
-  if (a1 > a0) madvise((void *)a0, a1 - a0, MADV_HUGEPAGE);
   const unsigned hw = std::thread::hardware_concurrency();
   const unsigned nt = std::min(16u, std::max(1u, hw));
   const size_t chunk = ((bytes / nt) / page + 1) * page;
@@ -54,9 +48,6 @@ int copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t st) {
   }
   long pg = sysconf(_SC_PAGESIZE);
   const size_t page = pg > 0 ? (size_t)pg : 4096;
-  const uintptr_t a0 = ((uintptr_t)dst + page - 1) / page * page;
-  const uintptr_t a1 = ((uintptr_t)dst + bytes) / page * page;
-  if (a1 > a0) madvise((void *)a0, a1 - a0, MADV_HUGEPAGE);
   const size_t nc = (bytes + kChunk - 1) / kChunk;
   std::vector<std::atomic<int>> done(nc);
   for (auto &d : done) d.store(0);

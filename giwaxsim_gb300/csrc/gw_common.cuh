@@ -114,6 +114,15 @@ __device__ __forceinline__ bool floor_to_int(float t, int &k) {
   return true;
 }
 
+// floor(min(max(t, 0), n - 1)) for 1 <= n < 2^21 (NaN gives 0, as fmaxf
+// does): the clamped value is in range for the magic-number rounding.
+__device__ __forceinline__ int floor_clamped(float t, int n) {
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  const float c = fminf(fmaxf(t, 0.f), (float)(n - 1));
+  const float r = __fadd_rn(c, kMagic);
+  return __float_as_int(r) - 0x4B400000 - (__fsub_rn(r, kMagic) > c ? 1 : 0);
+}
+
 // (double)x by IEEE 754 bit manipulation on 32-bit halves (exact); the
 // hardware conversion only for subnormal, infinite and NaN inputs.
 __device__ __forceinline__ double f2d_exact(float x) {

@@ -154,14 +154,8 @@ constexpr int kOrientFloats = sizeof(OrientFast) / 4;
 constexpr int kDetThreads = 256, kDetPix = 2, kDetChunk = 128, kDetFlush = 16;
 
 __device__ __forceinline__ bool fast_axis(float t, float d, int n, int &k) {
-  // floor, then clamp to [0, n-1]; pre-clamping to +-2^20 (n <= 2^20)
-  // changes no clamped result and keeps floor_to_int in range (NaN clamps
-  // to the lower bound, as fmaxf does)
-  constexpr float B = 1048576.f;
-  int a = 0, b = 0;
-  floor_to_int(fminf(fmaxf(t - d, -B), B), a);
-  floor_to_int(fminf(fmaxf(t + d, -B), B), b);
-  const int lo = min(max(a, 0), n - 1), hi = min(max(b, 0), n - 1);
+  // clamp(floor(x), 0, n-1) == floor(clamp(x, 0, n-1)); NaN clamps to 0
+  const int lo = floor_clamped(t - d, n), hi = floor_clamped(t + d, n);
   k = lo;
   return lo == hi;
 }
