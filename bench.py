@@ -488,7 +488,45 @@ def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8, tune=True):
     ctx.synchronize()
     det_ms = _event_ms(ts, det.execute, reps)
     info = plan.info()
+    det_ref = det.result() if len(items) > 1 else None
     det.close()
+    # the Kahan-compensated float32 accumulation beside float64 (the
+    # multi-structure workload compares them): time and normwise difference
+    kahan = None
+    if len(items) > 1:
+        dk = F.DetectorPlan((plan.Qc,) * 3, q, q, q, dargs["num_pixels"],
+                            dargs["max_q"], dargs["angle_init_vals"],
+                            dargs["angle_init_axs"], dargs["psis"],
+                            dargs["psi_weights"], dargs["phis"],
+                            dargs["phi_weights"], dargs["thetas"],
+                            dargs["theta_weights"], mirror=True,
+                            accum="kahan32", ctx=ctx)
+        dk.set_iq_device32(plan.device_iq32())
+        dk.execute()
+        ctx.synchronize()
+        dk_ms = _event_ms(ts, dk.execute, reps)
+        dimg = dk.result()
+        dk.close()
+        ref = plan.iq()
+        pk = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
+                         smooth=w["smooth"], accum="kahan32",
+                         fft_y=plan.params.fft_y, fft_z=plan.params.fft_z,
+                         batch_slices=plan.params.batch_slices, ctx=ctx)
+        pk.set_atoms()
+        pk.execute()
+        ctx.synchronize()
+        pk.capture_graph()
+        pk.execute()
+        ctx.synchronize()
+        k_ms = _event_ms(ts, pk.execute, reps, flush)
+        ik = pk.iq()
+        kahan = {"voxel_ms": round(k_ms, 4),
+                 "rel_l2_vs_fp64": float(np.linalg.norm(ik - ref) / np.linalg.norm(ref)),
+                 "detector_ms": round(dk_ms, 4),
+                 "detector_rel_l2_vs_fp64":
+                     float(np.linalg.norm(dimg - det_ref) / np.linalg.norm(det_ref))}
+        del ik, ref
+        pk.close()
     plan.close()
     # plain: per-slice cost from two sample sizes (the difference removes the
     # per-execute memset, structure preparation and finalize), plus one
@@ -518,7 +556,8 @@ def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8, tune=True):
             "s_per_image_batched": batched, "s_per_image_plain": plain,
             "plain_ms_per_slice": round(per_slice, 4),
             "plain_fixed_ms": round(fixed, 4),
-            "plain_sample_slices": [n1, n], "batched_vs_plain": plain / batched}
+            "plain_sample_slices": [n1, n], "batched_vs_plain": plain / batched,
+            "kahan32": kahan}
 
 
 def grad_timing(ctx, steps=3):
