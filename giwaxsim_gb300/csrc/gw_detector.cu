@@ -154,10 +154,16 @@ constexpr int kOrientFloats = sizeof(OrientFast) / 4;
 constexpr int kDetThreads = 256, kDetPix = 2, kDetChunk = 128, kDetFlush = 16;
 
 __device__ __forceinline__ bool fast_axis(float t, float d, int n, int &k) {
-  // clamp(floor(x), 0, n-1) == floor(clamp(x, 0, n-1)); NaN clamps to 0
-  const int lo = floor_clamped(t - d, n), hi = floor_clamped(t + d, n);
-  k = lo;
-  return lo == hi;
+  // k = clamp(floor(t + d), 0, n-1) (clamping first is the same: NaN and
+  // -inf give 0, +inf n-1), by magic-number rounding; clamp(floor(t - d))
+  // equals it exactly when max(t - d, 0) >= k
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  const float c = fminf(fmaxf(t + d, 0.f), (float)(n - 1));
+  const float r = __fadd_rn(c, kMagic);
+  const float fr = __fsub_rn(r, kMagic);
+  const bool down = fr > c;
+  k = __float_as_int(r) - 0x4B400000 - (down ? 1 : 0);
+  return fmaxf(t - d, 0.f) >= (down ? fr - 1.f : fr);
 }
 
 __device__ __forceinline__ bool fast_index(const OrientFast &T, const DetArgs &a,
