@@ -220,6 +220,9 @@ int check_device_error(gw_ctx *ctx, const char *where) {
       what = "zero-size array to reduction operation minimum which has no "
              "identity (no atom inside the real-space grid)";
       break;
+    case GW_DEVERR_TIMEOUT:
+      return fail(GW_ERR_TIMEOUT, std::string(where) +
+                                      ": a bounded wait for an asynchronous tile load ran out");
   }
   return fail(GW_ERR_BOUNDS, std::string(where) + ": " + what);
 }

@@ -259,7 +259,7 @@ struct KTimer {
 
 // device error codes written to ctx->d_err
 enum { GW_DEVERR_NONE = 0, GW_DEVERR_BOX = 1, GW_DEVERR_MASK_WRAP = 2,
-       GW_DEVERR_NO_ATOMS = 3 };
+       GW_DEVERR_NO_ATOMS = 3, GW_DEVERR_TIMEOUT = 4 };
 
 __device__ __forceinline__ void dev_error(int *err, int code) {
   atomicCAS(err, 0, code);

@@ -28,6 +28,7 @@
 #include <cstring>
 #include <vector>
 
+#include "gw_tma.cuh"
 #include "gw_voxel_impl.cuh"
 
 using namespace gwv;
@@ -545,6 +546,30 @@ struct ColLoad {
   }
 };
 
+// The same columns from a shared-memory tile (row n, column f at
+// tile[n * NB + f]) that a TMA load brought in.
+template <int NB>
+struct ColTileLoad {
+  const float2 *tile, *A;
+  int L, nc, m0;
+  __device__ float2 operator()(int f, int n) const {
+    if (n >= L || m0 + f >= nc) return make_float2(0.f, 0.f);
+    return cmul(tile[n * NB + f], __ldg(A + n));
+  }
+};
+
+// Rows per TMA box for transform length M: a divisor of M of at most 256,
+// so the boxes covering a slice's rows (at most M) fit the FFT buffer.
+__host__ __device__ constexpr int tma_box_rows(int M) {
+  return M % 256 == 0 ? 256 : M % 192 == 0 ? 192 : M % 160 == 0 ? 160
+                                                                 : M % 128 == 0 ? 128 : 64;
+}
+// The box's inner extent (NB complex values) must be a multiple of 16 bytes.
+template <int M>
+__host__ __device__ constexpr bool col_tma_ok() {
+  return (FftShape<M>::NB * (int)sizeof(float2)) % 16 == 0;
+}
+
 struct ColBin {
   const BinArgs *bn;
   const int *cofs;
@@ -569,13 +594,18 @@ struct ColBin {
   }
 };
 
-template <int M>
+// TMA: the slice's F1 rows of the block's NB columns come in as boxes of a
+// 2-D tensor map of F1 (one thread issues them, an mbarrier counts their
+// bytes) into the FFT buffer, which the first pass reads completely before
+// it writes; otherwise each thread loads its elements.
+template <int M, bool TMA>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
 k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
-              const float2 *F1) {
+              const float2 *F1, const __grid_constant__ CUtensorMap f1map) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   constexpr int TWL = FftPlan<M>::tw_len();
-  extern __shared__ float2 smem[];
+  extern __shared__ __align__(128) float2 smem[];
+  __shared__ uint64_t tile_bar;
   float2 *tw = smem;
   float2 *buf = smem + TWL;
   const int slot = blockIdx.y, sl = slice0 + slot;
@@ -587,15 +617,40 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
   for (int f = 0; f < NB; ++f)
     if (m0 + f < nc && cofs[m0 + f] >= 0) any = true;
   if (!any) return;
-  for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
-  __syncthreads();
   int first, rows;
   slice_rows(a, slice0, sl, first, rows);
-  ColLoad ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
-  fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
+  // 128-byte aligned tile inside the FFT buffer: the boxes cover at most M
+  // rows of NB values, the buffer holds NB (M + M/16 + 4), and the
+  // alignment skips at most 15 values
+  constexpr int BR = tma_box_rows(M);
+  static_assert(M % BR == 0 && NB * (FftPlan<M>::LDM - M) >= 16, "tile fits");
+  float2 *tile = buf + ((128u - (smem_u32(buf) & 127u)) & 127u) / sizeof(float2);
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      const int nload = (rows + BR - 1) / BR;
+      mbar_init(&tile_bar, 1);
+      mbar_arrive_expect_tx(&tile_bar, (unsigned)(nload * BR * NB * sizeof(float2)));
+      for (int i = 0; i < nload; ++i)
+        tma_load_2d(tile + (size_t)i * BR * NB, &f1map, m0, first + i * BR, &tile_bar);
+    }
+  }
+  for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
+  __syncthreads();
+  bool tile_ok = true;
+  if constexpr (TMA) {
+    tile_ok = mbar_wait_bounded(&tile_bar, 0, 1u << 22);
+    if (!tile_ok && threadIdx.x == 0) dev_error(a.err, GW_DEVERR_TIMEOUT);
+    ColTileLoad<NB> ld{tile, cz.A, rows, nc, m0};
+    fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
+  } else {
+    ColLoad ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
+    fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
+  }
   ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0,
             bn.sstride * (int64_t)(sl / a.n_phi)};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), st);
+  // a load that ran out of time must not land after the block has gone
+  if (TMA && !tile_ok) mbar_wait_bounded(&tile_bar, 0, 1u << 22);
 }
 
 // ---------------------------------------------------------- geometry tables
@@ -1022,18 +1077,80 @@ int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
   static bool attr = false;
   if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M>,
+    GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, false>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
+    if constexpr (col_tma_ok<M>())
+      GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
     attr = true;
   }
   dim3 grid((P->Nc + NB - 1) / NB, n_sl);
   gw::KTimer tm(P->ctx, GW_K_COLBIN);
-  k_col_czt_bin<M><<<grid, NT, smem, P->ctx->stream>>>(a, cz, bn, slice0,
-                                                       P->Nc, P->d_F1);
+  if constexpr (col_tma_ok<M>()) {
+    if (P->f1_tma) {
+      k_col_czt_bin<M, true><<<grid, NT, smem, P->ctx->stream>>>(
+          a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
+      GW_LAUNCHED(P->ctx);
+      return GW_OK;
+    }
+  }
+  k_col_czt_bin<M, false><<<grid, NT, smem, P->ctx->stream>>>(
+      a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
 }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
+                                   void *, const cuuint64_t *, const cuuint64_t *,
+                                   const cuuint32_t *, const cuuint32_t *,
+                                   CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of F1 (S*Lz rows of Nc complex values) with NB x BR boxes;
+// leaves f1_tma false where the rules of tiled loads are not met (odd
+// band: row pitch not a multiple of 16 bytes; NB * 8 bytes not a multiple
+// of 16) or the encoder is unavailable.  Rows and columns past the map
+// read as zeros.
+template <int M>
+int col_map_create(gw_voxel_plan *P) {
+  P->f1_tma = false;
+  if constexpr (col_tma_ok<M>()) {
+    constexpr int NB = FftShape<M>::NB, BR = tma_box_rows(M);
+    const size_t pitch = (size_t)P->Nc * sizeof(float2);
+    EncodeTiledFn enc = encode_tiled();
+    if (P->plain || !enc || pitch % 16 != 0 ||
+        reinterpret_cast<uintptr_t>(P->d_F1) % 16 != 0)
+      return GW_OK;
+    const cuuint64_t dims[2] = {(cuuint64_t)P->Nc, (cuuint64_t)P->S * P->Lz};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch};
+    const cuuint32_t box[2] = {(cuuint32_t)NB, (cuuint32_t)BR};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(&P->f1map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, P->d_F1,
+                           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    P->f1_tma = r == CUDA_SUCCESS;
+  }
+  return GW_OK;
+}
+
+int col_map_dispatch(gw_voxel_plan *P) { GW_DISPATCH_M(P->Mz, col_map_create, P) }
 
 int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  int s0, int n) {
@@ -1317,6 +1434,9 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     const int K = (int)std::ceil(hcap / dh) + 2;
     int c_lo = std::max(0, (g - 1) / 2 - K);
     int c_hi = std::min(g - 1, g / 2 + K);
+    // an even band keeps F1's rows 16-byte aligned for tensor-map loads; a
+    // column past the grid (c_hi = g) is marked unbinned by k_col_tables
+    if ((c_hi - c_lo + 1) % 2) ++c_hi;
     P->k0 = c_lo - g / 2;
     P->Nc = c_hi - c_lo + 1;
   }
@@ -1467,7 +1587,8 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_amo, (size_t)P->n_slices * P->Ly, &B)) ||
       (st = alloc(&P->d_my, (size_t)P->n_slices * P->Ly, &B)) ||
       (st = alloc(&P->d_mz, (size_t)P->n_slices * P->Lz, &B)) ||
-      (st = upload(&P->d_roff, P->roff_host, &B))) {
+      (st = upload(&P->d_roff, P->roff_host, &B)) ||
+      (st = col_map_dispatch(P))) {
     gw_voxel_plan_destroy(P);
     return st;
   }

@@ -10,6 +10,8 @@
 #include <complex>
 #include <vector>
 
+#include <cuda.h>
+
 #include "gw_common.cuh"
 #include "gw_fft.cuh"
 #include "gw_slice.cuh"
@@ -412,6 +414,10 @@ struct gw_voxel_plan {
   double *d_iq64 = nullptr;
   float *d_iq32 = nullptr;
   float2 *d_F1 = nullptr, *d_amo = nullptr;
+  // 2-D tensor map of d_F1 (columns inner) for the column kernel's tile
+  // loads; f1_tma false when the band or the block width does not allow them
+  CUtensorMap f1map{};
+  bool f1_tma = false;
   double *d_xyz_s = nullptr;
   float4 *d_xyf_s = nullptr;
   float *d_fz_s = nullptr;
