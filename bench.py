@@ -39,7 +39,7 @@ L2_BYTES = 129 * 1024 * 1024
 # launch (profiles/); a launch's traffic is this times its slices (both
 # kernels move per-slice data only).
 NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024): (1.48 + 38.03) * 1e6 / 51,
-               ("si-100A", "col_czt_bin", 1280, 1024): (148.55 + 30.01) * 1e6 / 51}
+               ("si-100A", "col_czt_bin", 1280, 1024): (148.42 + 28.70) * 1e6 / 51}
 
 
 def parse():
@@ -329,27 +329,38 @@ def run_gb300(args, world, rank, local, pg):
                 weights=wt, ctx=ctx)
             t_e.append(time.perf_counter() - t0)
         te = float(np.mean(t_e[2:]))
-        # where the e2e time goes: the same call split into its phases
-        fv = F.element_f_values(el, w["energy"])
-        ph = {}
-        t0 = time.perf_counter()
-        pl = F.VoxelPlan(geom, [(xyz, fv, wt)], phis=phis,
-                         fill_bkg=w["fill_bkg"], smooth=w["smooth"], ctx=ctx)
-        ph["plan_s"] = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        pl.set_atoms()
-        pl.execute()
-        ctx.synchronize()
-        ph["upload_execute_s"] = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        out = pl.iq()  # the result array as the API returns it (HostPool)
-        ph["d2h_s"] = time.perf_counter() - t0
-        del out
-        pl.close()
+        # where the e2e time goes: the same steps as the call, each timed,
+        # averaged over as many calls
+        ph = {k: [] for k in ("inputs_s", "plan_s", "upload_execute_s",
+                              "d2h_s", "close_s")}
+        for k in range(len(t_e) - 2):
+            out = None
+            t0 = time.perf_counter()
+            g2 = F.VoxelGeometry(w["r"], w["dq"], w["max_q"])
+            c2 = np.asarray(xyz, dtype=np.float64)
+            g2.check_bounds(c2)
+            fv = F.element_f_values(el, w["energy"])
+            t1 = time.perf_counter()
+            pl = F.VoxelPlan(g2, [(c2, fv, wt)], phis=phis,
+                             fill_bkg=w["fill_bkg"], smooth=w["smooth"], ctx=ctx)
+            t2 = time.perf_counter()
+            pl.set_atoms()
+            pl.execute()
+            ctx.synchronize()
+            t3 = time.perf_counter()
+            out = pl.iq()  # the result array as the API returns it (HostPool)
+            t4 = time.perf_counter()
+            pl.close()
+            t5 = time.perf_counter()
+            for key, v in zip(ph, (t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4)):
+                ph[key].append(v)
+            del out
+        ph = {k: float(np.mean(v)) for k, v in ph.items()}
         e2e = {"value": world * n_slices / te, "unit": "slices/s",
                "h2d_bytes_per_step": int(xyz.size * 8 + len(xyz) * 8),
                "d2h_bytes_per_step": int(iq.size * 8),
-               "s_per_step": te, "phases": ph}
+               "s_per_step": te, "s_per_call": [round(v, 6) for v in t_e],
+               "phases": ph}
 
     # roofline of the dominant kernel
     peak, peak_kind = measured_peaks()

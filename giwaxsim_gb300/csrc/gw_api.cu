@@ -11,14 +11,30 @@
 #include <thread>
 #include <vector>
 
+#include <sys/mman.h>
 #include <unistd.h>
 
 #include "gw_common.cuh"
 
 namespace gw {
 
+// True when every page of [p, p + bytes) is resident (a recycled result
+// buffer): such a destination needs no faulting in before a copy.  False
+// when the query fails (not a mapping the kernel reports on).
+static bool host_resident(const void *p, size_t bytes) {
+  long pg = sysconf(_SC_PAGESIZE);
+  const size_t page = pg > 0 ? (size_t)pg : 4096;
+  const uintptr_t lo = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)(page - 1);
+  const uintptr_t hi = reinterpret_cast<uintptr_t>(p) + bytes;
+  std::vector<unsigned char> v((hi - lo + page - 1) / page);
+  if (mincore(reinterpret_cast<void *>(lo), hi - lo, v.data()) != 0) return false;
+  for (unsigned char c : v)
+    if (!(c & 1)) return false;
+  return true;
+}
+
 void prefault_host(void *p, size_t bytes) {
-  if (!p || bytes < ((size_t)16 << 20)) return;
+  if (!p || bytes < ((size_t)16 << 20) || host_resident(p, bytes)) return;
   long pg = sysconf(_SC_PAGESIZE);
   const size_t page = pg > 0 ? (size_t)pg : 4096;
   const unsigned hw = std::thread::hardware_concurrency();
@@ -41,7 +57,7 @@ int copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t st) {
   // Pipelined: worker threads fault in 32 MB chunks in order while this
   // thread copies each chunk as soon as it is ready.
   constexpr size_t kChunk = (size_t)32 << 20;
-  if (bytes < 2 * kChunk) {
+  if (bytes < 2 * kChunk || host_resident(dst, bytes)) {
     prefault_host(dst, bytes);
     GW_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
     return GW_OK;
