@@ -16,6 +16,7 @@ same float64 arithmetic per atom and per pixel:
   tools/detector.py:33-162      axis of each plane rotation from the
                                 current plane's corners
 """
+import atexit
 import ctypes
 import warnings
 
@@ -184,8 +185,9 @@ class VoxelPlan:
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
                  batch_slices=0, constants=None, deposit="nearest", fft_y=0,
-                 fft_z=0, tune=False, ctx=None):
+                 fft_z=0, tune=False, ctx=None, create=True):
         self.geom = geom
+        self.handle = None
         self.ctx = ctx or N.default_context()
         self.tuned = None
         if tune and mode == "batched":
@@ -256,13 +258,25 @@ class VoxelPlan:
                      "bilinear": N.GW_DEPOSIT_BILINEAR}[deposit]
         p.fft_y, p.fft_z = int(fft_y), int(fft_z)
         self.params = p
+        self.Qc = geom.crop_hi - geom.crop_lo + 1
+        if create:
+            self.create()
+
+    def create(self):
+        """Make the native plan (VoxelPlan(..., create=False) leaves it to
+        this call)."""
         h = ctypes.c_void_p()
         N.check(N.lib().gw_voxel_plan_create(
-            self.ctx.handle, ctypes.byref(p), N.ptr(self.structs),
+            self.ctx.handle, ctypes.byref(self.params), N.ptr(self.structs),
             len(self.structs), N.ptr(self.phi_tab), len(self.phi_tab),
             ctypes.byref(h)))
         self.handle = h
-        self.Qc = geom.crop_hi - geom.crop_lo + 1
+
+    def key(self):
+        """Everything gw_voxel_plan_create receives: two plans with equal
+        keys are the same plan (the atoms themselves come with set_atoms)."""
+        return (self.ctx.handle.value, bytes(self.params),
+                self.structs.tobytes(), self.phi_tab.tobytes(), self.n_out)
 
     def set_atoms(self, xyz=None, f=None, on_device=False):
         if xyz is None:
@@ -415,6 +429,63 @@ class VoxelPlan:
             self.close()
         except Exception:
             pass
+
+
+class PlanCache:
+    """Voxel plans kept after a call for the next call with the same plan
+    inputs (geometry, options, phis, structure constants and atom count),
+    as FFT libraries keep plans: such a call skips the plan's table set-up
+    and allocations; the atoms are uploaded and every slice is computed
+    again.  A plan is checked out for the duration of a call (concurrent
+    callers never share one), returned afterwards, and the least recently
+    returned plans beyond `size` are destroyed.  size 0 disables keeping;
+    clear() destroys every kept plan (their device memory is released)."""
+
+    def __init__(self, size=1):
+        import collections
+        import threading
+        self.size = size
+        self._lock = threading.Lock()
+        self._plans = collections.OrderedDict()
+
+    def checkout(self, geom, structures, **kw):
+        spec = VoxelPlan(geom, structures, create=False, **kw)
+        key = spec.key()
+        with self._lock:
+            plan = self._plans.pop(key, None)
+        if plan is None:
+            spec.create()
+            return spec
+        plan.xyz, plan.f = spec.xyz, spec.f
+        return plan
+
+    def give_back(self, plan, ok=True):
+        """Return a checked-out plan; ok False (the call failed) destroys it."""
+        if not ok or self.size <= 0 or not plan.handle:
+            plan.close()
+            return
+        drop = []
+        with self._lock:
+            key = plan.key()
+            old = self._plans.pop(key, None)
+            if old is not None and old is not plan:
+                drop.append(old)
+            self._plans[key] = plan
+            while len(self._plans) > self.size:
+                drop.append(self._plans.popitem(last=False)[1])
+        for p in drop:
+            p.close()
+
+    def clear(self):
+        with self._lock:
+            plans = list(self._plans.values())
+            self._plans.clear()
+        for p in plans:
+            p.close()
+
+
+PLAN_CACHE = PlanCache()
+atexit.register(PLAN_CACHE.clear)  # kept plans go before the interpreter tears down
 
 
 # ------------------------------------------------------------------ slab

@@ -17,7 +17,7 @@ Keyword-only extensions (all default to the reference's behaviour):
 """
 import numpy as np
 
-from ..forward import (DetectorPlan, Slab, VoxelGeometry, VoxelPlan,
+from ..forward import (PLAN_CACHE, DetectorPlan, Slab, VoxelGeometry, VoxelPlan,
                        element_f_values)
 from .utilities import calc_real_space_abc, load_pdb, load_xyz
 
@@ -33,15 +33,17 @@ def voxelgridmaker_fitting(coords, elements, r_voxel_size, q_voxel_size, max_q,
     coords = np.asarray(coords, dtype=np.float64)
     geom.check_bounds(coords)
     fv = element_f_values(elements, energy, f1f2)
-    plan = VoxelPlan(geom, [(coords, fv, weights)], phis=phis,
-                     fill_bkg=fill_bkg, smooth=smooth, mode=mode, accum=accum,
-                     batch_slices=batch_slices, ctx=ctx)
+    plan = PLAN_CACHE.checkout(geom, [(coords, fv, weights)], phis=phis,
+                               fill_bkg=fill_bkg, smooth=smooth, mode=mode,
+                               accum=accum, batch_slices=batch_slices, ctx=ctx)
+    ok = False
     try:
         plan.set_atoms()
         plan.execute()
         iq = plan.iq()
+        ok = True
     finally:
-        plan.close()
+        PLAN_CACHE.give_back(plan, ok)
     q = geom.q_crop
     return iq, q.copy(), q.copy(), q.copy()
 
