@@ -78,8 +78,8 @@ class VoxelGeometry:
         g.h_max = np.max(q_h)
         return g
 
-    def check_bounds(self, coords):
-        b = [np.max(coords[:, i]) - np.min(coords[:, i]) for i in range(3)]
+    def check_bounds(self, coords, ranges=None):
+        b = coord_ranges(coords) if ranges is None else ranges
         if self.grid_size * self.r_voxel_size < np.min(b):
             raise Exception("Calculated real-space bounds smaller than "
                             "simulation. Please lower delta_q value")
@@ -87,7 +87,7 @@ class VoxelGeometry:
     def phi_table(self, phis):
         """Per-slice scalars as numpy computes them in the reference."""
         phis = np.asarray(phis, dtype=np.float64)
-        t = np.zeros(len(phis), dtype=np.dtype(N.Phi))
+        t = np.zeros(len(phis), dtype=_dtype_of(N.Phi))
         pr = np.radians(phis)
         t["cos_phi"] = np.cos(pr)
         t["sin_phi"] = np.sin(pr)
@@ -104,23 +104,57 @@ class VoxelGeometry:
         return t
 
 
+_DTYPES = {}
+
+
+def _dtype_of(ctype):
+    """numpy dtype of a ctypes structure, made once per type."""
+    d = _DTYPES.get(ctype)
+    if d is None:
+        d = _DTYPES[ctype] = np.dtype(ctype)
+    return d
+
+
+def element_kinds(elements):
+    """Distinct element symbols and every atom's index into them.  Symbols
+    of up to two characters (numpy's fixed-width strings) are compared as
+    64-bit integers: no string sort, and one vector compare when all atoms
+    are of one element."""
+    a = np.asarray(elements)
+    if a.ndim == 1 and len(a) and a.dtype.kind == "U" and a.dtype.itemsize <= 8:
+        cp = np.ascontiguousarray(a).view(np.uint32).reshape(len(a), -1)
+        key = cp[:, 0].astype(np.uint64)
+        if cp.shape[1] == 2:
+            key |= cp[:, 1].astype(np.uint64) << np.uint64(32)
+        if (key == key[0]).all():
+            return [str(a[0])], np.zeros(len(a), np.intp)
+        _, first, inv = np.unique(key, return_index=True, return_inverse=True)
+        return [str(a[i]) for i in first], inv.reshape(-1)
+    uniq, inv = np.unique(a, return_inverse=True)
+    return [str(e) for e in uniq], inv.reshape(-1)
+
+
 def element_f_values(elements, energy, f1f2=None):
     """f = Z + f' + i f'' per atom (comparison.py:735-739)."""
     from .tools.utilities import get_element_f1_f2_dict
-    elements = np.asarray(elements)
-    uniq, inv = np.unique(elements, return_inverse=True)
+    uniq, inv = element_kinds(elements)
     d = f1f2 if f1f2 is not None else get_element_f1_f2_dict(energy, uniq)
     vals = np.array([complex(d[e]) for e in uniq], dtype=complex)
     vals += np.array([ptable[e] for e in uniq])
     return vals[inv]
 
 
-def structure_constants(coords, f_values, r_voxel_size):
+def coord_ranges(coords):
+    """max - min of x, y and z (comparison.py:712-717), from a transposed
+    copy (contiguous reductions)."""
+    t = np.ascontiguousarray(np.asarray(coords, dtype=np.float64).T)
+    return [t[i].max() - t[i].min() for i in range(3)]
+
+
+def structure_constants(coords, f_values, r_voxel_size, ranges=None):
     """x/y/z bounds, avg_voxel_f (comparison.py:712-744) and max_voxels
     (voxelgrids.py:344)."""
-    xb = np.max(coords[:, 0]) - np.min(coords[:, 0])
-    yb = np.max(coords[:, 1]) - np.min(coords[:, 1])
-    zb = np.max(coords[:, 2]) - np.min(coords[:, 2])
+    xb, yb, zb = coord_ranges(coords) if ranges is None else ranges
     avg = (np.sum(f_values) / (xb * yb * zb)) * r_voxel_size ** 3
     max_voxels = np.sqrt(xb ** 2 + yb ** 2) // r_voxel_size
     return xb, yb, zb, complex(avg), float(max_voxels)
@@ -208,7 +242,7 @@ class VoxelPlan:
         if len(self.phis) < 1:
             raise ValueError("at least one phi is required")
         r = geom.r_voxel_size
-        st = np.zeros(len(structures), dtype=np.dtype(N.Structure))
+        st = np.zeros(len(structures), dtype=_dtype_of(N.Structure))
         xyz, fs = [], []
         begin = 0
         for i, (coords, fv, w) in enumerate(structures):
@@ -224,8 +258,9 @@ class VoxelPlan:
                 avg = complex(avg)
                 mv = float(np.sqrt(xb ** 2 + yb ** 2) // r)
             else:
-                geom.check_bounds(coords)
-                xb, yb, zb, avg, mv = structure_constants(coords, fv, r)
+                rg = coord_ranges(coords)
+                geom.check_bounds(coords, rg)
+                xb, yb, zb, avg, mv = structure_constants(coords, fv, r, rg)
             st[i] = (begin, len(coords), xb, yb, zb, avg.real, avg.imag, mv)
             begin += len(coords)
             xyz.append(coords)

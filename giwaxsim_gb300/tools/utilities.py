@@ -169,14 +169,28 @@ def get_element_f0_dict(q_val, elements):
 _warned_xraydb = False
 
 
+_XRAYDB = []
+
+
+def _xraydb():
+    """The xraydb module or None, looked up once (a failed import is not
+    cached by Python and costs a path search on every call)."""
+    if not _XRAYDB:
+        try:
+            import xraydb
+        except ImportError:
+            xraydb = None
+        _XRAYDB.append(xraydb)
+    return _XRAYDB[0]
+
+
 def get_element_f1_f2_dict(energy, elements):
     """f' + i f'' per element at `energy` eV from xraydb's Chantler tables
     when xraydb is installed; otherwise 0 (a warning is issued once), so the
     scattering factor is Z."""
     global _warned_xraydb
-    try:
-        import xraydb
-    except ImportError:
+    xraydb = _xraydb()
+    if xraydb is None:
         if not _warned_xraydb:
             warnings.warn("xraydb is not installed: using f' = f'' = 0")
             _warned_xraydb = True
