@@ -61,6 +61,24 @@ def test_structure_constants_match_oracle():
         assert mv == np.sqrt(xb ** 2 + yb ** 2) // 0.3
 
 
+@pytest.mark.parametrize("elements", [
+    np.array(["Si"] * 50),
+    np.array(["C", "H", "O", "C", "N", "H", "C"] * 9),
+    ["S", "O", "O", "Si", "C"] * 4,
+    np.array(["C", "Si", "Cl"], dtype="<U3"),
+    np.array(["H"])])
+def test_element_kinds_match_numpy_unique(elements):
+    uniq, inv = F.element_kinds(elements)
+    ref_u, ref_inv = np.unique(np.asarray(elements), return_inverse=True)
+    assert np.array_equal(np.asarray(uniq)[inv], ref_u[ref_inv.reshape(-1)])
+    assert sorted(uniq) == list(ref_u)
+    if all(e in ("Si", "C", "H", "O", "N", "S") for e in uniq):
+        fv = F.element_f_values(elements, 10000.0)
+        z = {"Si": 14, "C": 6, "H": 1, "O": 8, "N": 7, "S": 16}
+        assert np.array_equal(fv, np.array([z[str(e)] for e in np.asarray(elements)],
+                                           dtype=complex))
+
+
 def test_detector_corner_matrices_match_full_plane():
     """Rotation matrices from the tracked corners equal the ones the
     reference builds from the full rotated plane."""
