@@ -309,8 +309,10 @@ class VoxelPlan:
 
     def key(self):
         """Everything gw_voxel_plan_create receives: two plans with equal
-        keys are the same plan (the atoms themselves come with set_atoms)."""
-        return (self.ctx.handle.value, bytes(self.params),
+        keys are the same plan (the atoms themselves come with set_atoms).
+        The context enters by identity: a plan keeps its context object
+        alive, so a context made after another was closed never matches."""
+        return (id(self.ctx), bytes(self.params),
                 self.structs.tobytes(), self.phi_tab.tobytes(), self.n_out)
 
     def set_atoms(self, xyz=None, f=None, on_device=False):
