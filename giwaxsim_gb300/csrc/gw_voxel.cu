@@ -756,6 +756,27 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
     const bool two = i0 + 1 < n;
     // (line, iz) of the pair's first voxel; the second is the next voxel
     const int line0 = i0 / Qc, iz0 = i0 - line0 * Qc;
+    unsigned cnt[2] = {0u, 0u};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      if (e == 1 && !two) break;
+      int line = line0, iz = iz0 + e;
+      if (iz == Qc) { iz = 0; ++line; }
+      cnt[e] = C2[line] * (unsigned)__ldg(C1 + iz);
+    }
+    // voxels no pixel was binned into hold a zero sum and I = 0: a pair
+    // of them (whole warps where a (qy, qx) line is never hit) skips the
+    // sum load and the float64 multiply
+    if ((cnt[0] | cnt[1]) == 0u) {
+      if (two) {
+        reinterpret_cast<double2 *>(out64)[p] = make_double2(0.0, 0.0);
+        reinterpret_cast<float2 *>(out32)[p] = make_float2(0.f, 0.f);
+      } else {
+        out64[i0] = 0.0;
+        out32[i0] = 0.f;
+      }
+      continue;
+    }
     double s[2] = {0.0, 0.0};
     if (kahan) {
       for (int e = 0; e < 2; ++e)
@@ -775,8 +796,7 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
       if (e == 1 && !two) break;
       int line = line0, iz = iz0 + e;
       if (iz == Qc) { iz = 0; ++line; }
-      const unsigned cnt = C2[line] * (unsigned)__ldg(C1 + iz);
-      float scale = cnt ? inv_nstruct / small_u2f(cnt) : 0.f;
+      float scale = cnt[e] ? inv_nstruct / small_u2f(cnt[e]) : 0.f;
       if (use_f0) {
         const int iy = line / Qc, ix = line - iy * Qc;
         const float4 z = __ldg(zf0 + iz);
