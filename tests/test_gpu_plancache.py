@@ -74,3 +74,33 @@ def test_failed_call_drops_its_plan():
         C.voxelgridmaker_fitting(a, ["Xx"] * len(a), phis=[0.0, 90.0], **kw)
     assert len(C.PLAN_CACHE._plans) == 1
     C.PLAN_CACHE.clear()
+
+
+def test_result_copy_into_resident_buffer_fills_every_line():
+    """A resident host destination gets the lines with binned pixels from
+    the device and the others zeroed on the host: prefilled with NaN, it
+    must come back equal to a fresh copy, on repeated calls."""
+    rng = np.random.default_rng(13)
+    xyz, _ = W.graphite_slab((12.0, 10.0, 9.0), rng, disp_sigma=0.05)
+    geom = F.VoxelGeometry(0.5, 0.1, 1.5)
+    fv = F.element_f_values(["C"] * len(xyz), 10000.0)
+    plan = F.VoxelPlan(geom, [(xyz, fv, None)], phis=np.linspace(0, 170, 8),
+                       smooth=1.0)
+    try:
+        plan.set_atoms()
+        plan.execute()
+        ref32 = plan.iq32()   # copied by the copy engine, one float32 per voxel
+        counts = plan.counts()
+        empty_lines = (counts.reshape(plan.Qc * plan.Qc, plan.Qc) == 0).all(1)
+        assert 0.05 < empty_lines.mean() < 0.95   # both kinds of line exist
+        out = np.full((plan.Qc,) * 3, np.nan)
+        for _ in range(2):
+            out[:] = np.nan
+            plan.iq(out=out)
+            assert not np.isnan(out).any()
+            # the float32 result is the float64 one rounded to nearest
+            assert np.array_equal(out.astype(np.float32), ref32)
+        assert np.all(out.reshape(-1, plan.Qc)[empty_lines] == 0)
+        assert np.any(out.reshape(-1, plan.Qc)[~empty_lines] != 0)
+    finally:
+        plan.close()
