@@ -21,7 +21,7 @@ namespace gw {
 // True when every page of [p, p + bytes) is resident (a recycled result
 // buffer): such a destination needs no faulting in before a copy.  False
 // when the query fails (not a mapping the kernel reports on).
-bool host_resident(const void *p, size_t bytes) {
+static bool host_resident(const void *p, size_t bytes) {
   long pg = sysconf(_SC_PAGESIZE);
   const size_t page = pg > 0 ? (size_t)pg : 4096;
   const uintptr_t lo = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)(page - 1);
@@ -31,47 +31,6 @@ bool host_resident(const void *p, size_t bytes) {
   for (unsigned char c : v)
     if (!(c & 1)) return false;
   return true;
-}
-
-bool device_writes_pageable(int device) {
-  static std::mutex mu;
-  static std::map<int, bool> known;
-  std::lock_guard<std::mutex> lk(mu);
-  auto it = known.find(device);
-  if (it != known.end()) return it->second;
-  int pma = 0, hpt = 0;
-  const bool ok =
-      cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess &&
-      cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
-                             device) == cudaSuccess &&
-      pma == 1 && hpt == 1;
-  known[device] = ok;
-  return ok;
-}
-
-void zero_ranges(char *base, const std::vector<std::pair<size_t, size_t>> &ranges) {
-  size_t total = 0;
-  for (const auto &r : ranges) total += r.second;
-  if (!total) return;
-  const unsigned hw = std::thread::hardware_concurrency();
-  const unsigned nt = (unsigned)std::min<size_t>(
-      std::min(12u, std::max(1u, hw)), std::max<size_t>(1, total >> 22));
-  // thread t zeroes bytes [t total / nt, (t+1) total / nt) of the ranges
-  // taken back to back
-  auto work = [&](unsigned t) {
-    const size_t lo = total * t / nt, hi = total * (t + 1) / nt;
-    size_t at = 0;
-    for (const auto &r : ranges) {
-      const size_t a = std::max(lo, at), b = std::min(hi, at + r.second);
-      if (a < b) memset(base + r.first + (a - at), 0, b - a);
-      at += r.second;
-      if (at >= hi) break;
-    }
-  };
-  std::vector<std::thread> th;
-  for (unsigned t = 1; t < nt; ++t) th.emplace_back(work, t);
-  work(0);
-  for (auto &x : th) x.join();
 }
 
 void prefault_host(void *p, size_t bytes) {

@@ -17,8 +17,6 @@
 #include <stdint.h>
 
 #include <string>
-#include <utility>
-#include <vector>
 
 #include "giwaxs_gb300.h"
 
@@ -224,14 +222,6 @@ void prefault_host(void *p, size_t bytes);
 // after the copy is enqueued; pageable destinations complete before), with
 // the destination's page faulting pipelined ahead of the copy.
 int copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t st);
-// True when every page of [p, p + bytes) is resident.
-bool host_resident(const void *p, size_t bytes);
-// True when kernels on `device` can store to ordinary (pageable) host
-// memory through the host's page tables (address translation services:
-// no page migration), so a kernel may write a result straight into it.
-bool device_writes_pageable(int device);
-// Zero the byte ranges (offset, length) of base with several threads.
-void zero_ranges(char *base, const std::vector<std::pair<size_t, size_t>> &ranges);
 
 }  // namespace gw
 

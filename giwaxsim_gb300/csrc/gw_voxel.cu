@@ -1648,8 +1648,7 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_sconst, P->d_xyz_s, P->d_xyf_s, P->d_fz_s,
                   P->d_perm, P->d_ybnd, P->d_roff, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
-                  P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0,
-                  P->d_nz_lines};
+                  P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -1827,75 +1826,10 @@ extern "C" int gw_voxel_capture_graph(gw_voxel_plan *P) {
   return GW_OK;
 }
 
-namespace {
-
-// Lines (qy, qx) of the float64 I(q) that hold a binned pixel, stored by
-// the kernel straight into the caller's host array (memory the device
-// addresses through the host page tables); one block per line at a time.
-__global__ void k_lines_to_host(const double *__restrict__ src, double *dst,
-                                const int *__restrict__ lines, int n_lines, int Qc) {
-  for (int li = blockIdx.x; li < n_lines; li += gridDim.x) {
-    const size_t base = (size_t)lines[li] * Qc;
-    for (int e = threadIdx.x; e < Qc; e += blockDim.x) dst[base + e] = src[base + e];
-  }
-}
-
-// The line lists from the count factor C2 (geometry only: made once).
-int make_line_lists(gw_voxel_plan *P) {
-  const int nl = P->Qc * P->Qc;
-  std::vector<unsigned> c2(nl);
-  GW_CUDA(cudaMemcpyAsync(c2.data(), P->d_C2, nl * sizeof(unsigned),
-                          cudaMemcpyDeviceToHost, P->ctx->stream));
-  GW_CUDA(cudaStreamSynchronize(P->ctx->stream));
-  std::vector<int> nz;
-  nz.reserve(nl);
-  P->zero_line_bytes.clear();
-  const size_t lb = (size_t)P->Qc * sizeof(double);
-  for (int l = 0; l < nl; ++l) {
-    if (c2[l]) {
-      nz.push_back(l);
-    } else if (!P->zero_line_bytes.empty() &&
-               P->zero_line_bytes.back().first + P->zero_line_bytes.back().second == l * lb) {
-      P->zero_line_bytes.back().second += lb;
-    } else {
-      P->zero_line_bytes.emplace_back(l * lb, lb);
-    }
-  }
-  P->n_nz_lines = (int)nz.size();
-  if (!nz.empty()) {
-    GW_CUDA(gw::dev_malloc((void **)&P->d_nz_lines, nz.size() * sizeof(int)));
-    GW_CUDA(cudaMemcpy(P->d_nz_lines, nz.data(), nz.size() * sizeof(int),
-                       cudaMemcpyHostToDevice));
-  }
-  P->lines_ready = true;
-  return GW_OK;
-}
-
-}  // namespace
-
 extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) {
   if (!P || !iq) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq: plan not executed");
   const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
-  // One result whose lines partly hold no binned pixel, into resident host
-  // memory the device can store to: only the other lines cross the link
-  // (a kernel writes them), while host threads zero the empty lines.
-  if (!on_device && P->n_out == 1 && P->W == P->Qc &&
-      reinterpret_cast<uintptr_t>(iq) % sizeof(double) == 0 &&
-      gw::device_writes_pageable(P->ctx->device) &&
-      gw::host_resident(iq, n * sizeof(double))) {
-    if (!P->lines_ready) GW_TRY(make_line_lists(P));
-    if (!P->zero_line_bytes.empty()) {
-      if (P->n_nz_lines > 0) {
-        gw::KTimer tm(P->ctx, GW_K_MISC);
-        k_lines_to_host<<<152 * 8, 128, 0, P->ctx->stream>>>(P->d_iq64, iq, P->d_nz_lines,
-                                                           P->n_nz_lines, P->Qc);
-        GW_LAUNCHED(P->ctx);
-      }
-      gw::zero_ranges(reinterpret_cast<char *>(iq), P->zero_line_bytes);
-      return gw::check_device_error(P->ctx, "voxel stage");
-    }
-  }
   if (!on_device && P->n_out == 1) {
     GW_TRY(gw::copy_to_host(iq, P->d_iq64, n * sizeof(double), P->ctx->stream));
     return gw::check_device_error(P->ctx, "voxel stage");

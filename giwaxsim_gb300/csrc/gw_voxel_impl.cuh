@@ -431,13 +431,6 @@ struct gw_voxel_plan {
   int *d_extflag = nullptr;
   float *d_my = nullptr, *d_mz = nullptr;
   float4 *d_sconst = nullptr;
-  // lines (qy, qx) of the crop without a binned pixel (C2 == 0) as byte
-  // ranges of the float64 result, and the other lines' indices on the
-  // device: the host result copy sends only the latter (made on first use)
-  bool lines_ready = false;
-  std::vector<std::pair<size_t, size_t>> zero_line_bytes;
-  int *d_nz_lines = nullptr;
-  int n_nz_lines = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int64_t graph_kernels = 0;

@@ -77,9 +77,9 @@ def test_failed_call_drops_its_plan():
 
 
 def test_result_copy_into_resident_buffer_fills_every_line():
-    """A resident host destination gets the lines with binned pixels from
-    the device and the others zeroed on the host: prefilled with NaN, it
-    must come back equal to a fresh copy, on repeated calls."""
+    """A resident host destination (copied in one call): prefilled with
+    NaN, every voxel is overwritten, lines without a binned pixel with
+    zeros, on repeated calls."""
     rng = np.random.default_rng(13)
     xyz, _ = W.graphite_slab((12.0, 10.0, 9.0), rng, disp_sigma=0.05)
     geom = F.VoxelGeometry(0.5, 0.1, 1.5)
