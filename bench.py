@@ -11,8 +11,8 @@ kernel, the CPU baseline (the float64 numpy oracle on the host cores), the
 SM clocks sampled during the timed region, and e2e (the public drop-in API
 voxelgridmaker_fitting on host numpy arrays, copies included).
 
-Multi-GPU: the path has no exchange step that this build performs; each rank
-runs an independent replica of the workload (weak scaling), rank 0 prints.
+Multi-GPU: the path has no exchange step; each rank runs an independent
+replica of the workload (weak scaling), rank 0 prints.
 """
 import argparse
 import json
