@@ -222,6 +222,8 @@ class VoxelPlan:
                  fft_z=0, tune=False, ctx=None, create=True):
         self.geom = geom
         self.handle = None
+        self.reused = False          # handed out again by PlanCache
+        self.graph_captured = False
         self.ctx = ctx or N.default_context()
         self.tuned = None
         if tune and mode == "batched":
@@ -361,6 +363,7 @@ class VoxelPlan:
 
     def capture_graph(self):
         N.check(N.lib().gw_voxel_capture_graph(self.handle))
+        self.graph_captured = True
 
     def iq(self, out=None):
         """I(q) (Qc, Qc, Qc); (n_struct, Qc, Qc, Qc) for separate structures.
@@ -494,6 +497,7 @@ class PlanCache:
             spec.create()
             return spec
         plan.xyz, plan.f = spec.xyz, spec.f
+        plan.reused = True
         return plan
 
     def give_back(self, plan, ok=True):

@@ -39,6 +39,11 @@ def voxelgridmaker_fitting(coords, elements, r_voxel_size, q_voxel_size, max_q,
     ok = False
     try:
         plan.set_atoms()
+        # a plan used a second time is recorded as one CUDA graph (its
+        # launches depend on the plan only; the atoms are in its buffers)
+        # and replayed from then on
+        if plan.reused and not plan.graph_captured:
+            plan.capture_graph()
         plan.execute()
         iq = plan.iq()
         ok = True

@@ -46,17 +46,22 @@ def test_repeated_and_interleaved_calls():
            for k, (x, e) in {"a": (a, el_a), "b": (b, el_b), "a2": (a2, el_a)}.items()}
     seq = ["a", "a", "b", "a", "a2", "a", "b", "b"]
     inputs = {"a": (a, el_a), "b": (b, el_b), "a2": (a2, el_a)}
-    handles = []
+    handles, graphs = [], []
     for k in seq:
         x, e = inputs[k]
         iq, qx, qy, qz = C.voxelgridmaker_fitting(x, e, smooth=1.0, phis=phis, **kw)
         assert rel_l2(iq, ref[k]) <= 1e-9, k
         assert len(C.PLAN_CACHE._plans) == 1
-        handles.append(next(iter(C.PLAN_CACHE._plans.values())).handle.value)
+        kept = next(iter(C.PLAN_CACHE._plans.values()))
+        handles.append(kept.handle.value)
+        graphs.append(kept.graph_captured)
     # the second call of a reused the first call's plan, and a2 (other
     # atoms, equal plan inputs) the plan of the call before it
     assert handles[1] == handles[0]
     assert handles[4] == handles[3]
+    # a reused plan runs as a recorded graph: a2 and the a after it were
+    # replays of the graph recorded with other atoms in the buffers
+    assert graphs == [False, True, False, False, True, True, False, True]
     assert rel_l2(ref["a2"], ref["a"]) > 1e-3
     C.PLAN_CACHE.clear()
     assert len(C.PLAN_CACHE._plans) == 0
