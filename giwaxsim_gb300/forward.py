@@ -223,7 +223,8 @@ class VoxelPlan:
         self.geom = geom
         self.handle = None
         self.reused = False          # handed out again by PlanCache
-        self.graph_captured = False
+        self.graph_captured = False  # the library drops the graph when the
+        self._atoms_n = None         # atom count or the shells change
         self.ctx = ctx or N.default_context()
         self.tuned = None
         if tune and mode == "batched":
@@ -320,13 +321,17 @@ class VoxelPlan:
     def set_atoms(self, xyz=None, f=None, on_device=False):
         if xyz is None:
             xyz, f = self.xyz, self.f
+        n = len(self.xyz) if on_device else len(xyz)
+        if n != self._atoms_n:
+            self.graph_captured = False
+            self._atoms_n = None
         if on_device:
             N.check(N.lib().gw_voxel_set_atoms(self.handle, ctypes.c_void_p(xyz),
-                                               ctypes.c_void_p(f),
-                                               len(self.xyz), 1))
+                                               ctypes.c_void_p(f), n, 1))
         else:
             N.check(N.lib().gw_voxel_set_atoms(self.handle, N.ptr(xyz), N.ptr(f),
-                                               len(xyz), 0))
+                                               n, 0))
+        self._atoms_n = n
 
     def set_shells(self, q_axis, lower, upper, f_shells, avg_shells,
                    mode="per_shell"):
@@ -337,6 +342,7 @@ class VoxelPlan:
         "reference" (the reference's own output, see gw_voxel_set_shells).
         Call after set_atoms; set_shells(None) clears them (set the atoms
         again afterwards)."""
+        self.graph_captured = False
         if q_axis is None:
             N.check(N.lib().gw_voxel_set_shells(self.handle, 0, 0, None, None,
                                                 None, None, None))

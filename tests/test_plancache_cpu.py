@@ -36,3 +36,52 @@ def test_size_zero_keeps_nothing():
     p = FakePlan("a")
     c.give_back(p)
     assert p.closed and not c._plans
+
+
+class FakeVoxelLib:
+    """Stand-in for the native library's set-atoms/shells calls: records
+    the atom counts and fails on request."""
+
+    def __init__(self):
+        self.counts, self.fail = [], False
+
+    def gw_voxel_set_atoms(self, handle, xyz, f, n, on_device):
+        self.counts.append(n)
+        return 1 if self.fail else 0
+
+    def gw_voxel_set_shells(self, *args):
+        return 0
+
+
+def test_graph_flag_follows_atom_count_and_shells(monkeypatch):
+    """The library drops a plan's recorded graph when the atom count or
+    the shells change; the host flag that says a graph is recorded follows."""
+    import numpy as np
+    from giwaxsim_gb300 import _native as N
+    from giwaxsim_gb300.forward import VoxelPlan
+    fake = FakeVoxelLib()
+    monkeypatch.setattr(N, "lib", lambda: fake)
+    monkeypatch.setattr(N, "last_error", lambda: "fake failure")
+    plan = VoxelPlan.__new__(VoxelPlan)
+    plan.handle, plan.graph_captured, plan._atoms_n = object(), False, None
+    x4, x5 = np.zeros((4, 3)), np.zeros((5, 3))
+    f4, f5 = np.zeros(8, np.float32), np.zeros(10, np.float32)
+    plan.set_atoms(x4, f4)
+    plan.graph_captured = True           # as capture_graph() leaves it
+    plan.set_atoms(x4, f4)               # same count: the graph stays
+    assert plan.graph_captured
+    plan.set_atoms(x5, f5)               # new count: the library drops it
+    assert not plan.graph_captured
+    plan.graph_captured = True
+    fake.fail = True                     # a failed upload leaves no count
+    try:
+        plan.set_atoms(x4, f4)
+    except N.GwError:
+        pass
+    assert not plan.graph_captured and plan._atoms_n is None
+    fake.fail = False
+    plan.set_atoms(x4, f4)
+    plan.graph_captured = True
+    plan.set_shells(None, None, None, None, None)
+    assert not plan.graph_captured
+    assert fake.counts == [4, 4, 5, 4, 4]
