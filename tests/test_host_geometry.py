@@ -34,6 +34,20 @@ def test_geometry_errors():
         g.check_bounds(np.array([[0, 0, 0], [100.0, 100.0, 100.0]]))
 
 
+def test_empty_atom_list_raises_before_device_work(monkeypatch):
+    """An empty structure fails as the reference's bounds reduction fails
+    (numpy max of an empty array, comparison.py:712-714), on the host,
+    before any plan or device call."""
+    from giwaxsim_gb300 import _native as N
+
+    def no_device():
+        raise AssertionError("device library reached")
+    monkeypatch.setattr(N, "lib", no_device)
+    with pytest.raises(ValueError, match="zero-size array"):
+        comparison.voxelgridmaker_fitting(np.zeros((0, 3)), np.array([], "<U2"),
+                                          0.3, 0.03, 3.0, 10000)
+
+
 def test_phi_table_matches_reference_scalars():
     g = F.VoxelGeometry(0.3, 0.03, 3.0)
     phis = np.concatenate([g.auto_phis[:50], [0.0, 45.0, 90.0, 91.0, 135.0,
