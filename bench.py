@@ -342,12 +342,14 @@ def run_gb300(args, world, rank, local, pg):
             t0 = time.perf_counter()
             g2 = F.VoxelGeometry(w["r"], w["dq"], w["max_q"])
             c2 = np.asarray(xyz, dtype=np.float64)
-            g2.check_bounds(c2)
+            rg = F.coord_ranges(c2)
+            g2.check_bounds(c2, rg)
             fv = F.element_f_values(el, w["energy"])
             t1 = time.perf_counter()
             pl = F.PLAN_CACHE.checkout(g2, [(c2, fv, wt)], phis=phis,
                                        fill_bkg=w["fill_bkg"],
-                                       smooth=w["smooth"], ctx=ctx)
+                                       smooth=w["smooth"], ctx=ctx,
+                                       ranges=[rg])
             t2 = time.perf_counter()
             pl.set_atoms()
             pl.execute()

@@ -219,7 +219,7 @@ class VoxelPlan:
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
                  batch_slices=0, constants=None, deposit="nearest", fft_y=0,
-                 fft_z=0, tune=False, ctx=None, create=True):
+                 fft_z=0, tune=False, ctx=None, create=True, ranges=None):
         self.geom = geom
         self.handle = None
         self.reused = False          # handed out again by PlanCache
@@ -261,7 +261,8 @@ class VoxelPlan:
                 avg = complex(avg)
                 mv = float(np.sqrt(xb ** 2 + yb ** 2) // r)
             else:
-                rg = coord_ranges(coords)
+                # ranges: per-structure coord_ranges the caller already has
+                rg = coord_ranges(coords) if ranges is None else ranges[i]
                 geom.check_bounds(coords, rg)
                 xb, yb, zb, avg, mv = structure_constants(coords, fv, r, rg)
             st[i] = (begin, len(coords), xb, yb, zb, avg.real, avg.imag, mv)

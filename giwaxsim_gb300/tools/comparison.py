@@ -18,7 +18,7 @@ Keyword-only extensions (all default to the reference's behaviour):
 import numpy as np
 
 from ..forward import (PLAN_CACHE, DetectorPlan, Slab, VoxelGeometry, VoxelPlan,
-                       element_f_values)
+                       coord_ranges, element_f_values)
 from .utilities import calc_real_space_abc, load_pdb, load_xyz
 
 
@@ -31,11 +31,13 @@ def voxelgridmaker_fitting(coords, elements, r_voxel_size, q_voxel_size, max_q,
     reference.  num_cpus is accepted and ignored (one GPU)."""
     geom = VoxelGeometry(r_voxel_size, q_voxel_size, max_q)
     coords = np.asarray(coords, dtype=np.float64)
-    geom.check_bounds(coords)
+    rg = coord_ranges(coords)
+    geom.check_bounds(coords, rg)
     fv = element_f_values(elements, energy, f1f2)
     plan = PLAN_CACHE.checkout(geom, [(coords, fv, weights)], phis=phis,
                                fill_bkg=fill_bkg, smooth=smooth, mode=mode,
-                               accum=accum, batch_slices=batch_slices, ctx=ctx)
+                               accum=accum, batch_slices=batch_slices, ctx=ctx,
+                               ranges=[rg])
     ok = False
     try:
         plan.set_atoms()

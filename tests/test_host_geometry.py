@@ -132,3 +132,20 @@ def test_trim_and_rebin_weights_vs_reference():
     out = ((w[:, 0] * val[idx[:, 0]]) + w[:, 1] * val[idx[:, 1]]) + w[:, 2] * val[idx[:, 2]]
     out[idx[:, 0] < 0] = np.nan
     assert np.array_equal(out.reshape(s.shape), d["rebin_raw"], equal_nan=True)
+
+
+def test_plan_inputs_equal_with_ranges_given():
+    """The drop-in computes each structure's coordinate ranges once and hands
+    them to the plan; the plan's structure table is the same either way."""
+    xyz, el, wt = W.structures("graphite-50A")[0]
+    g = F.VoxelGeometry(0.3, 0.03, 3.0)
+    fv = F.element_f_values(el, 10000.0)
+
+    class NoContext:
+        handle = None
+    kw = dict(phis=np.arange(7.0), fill_bkg=True, smooth=1.0, ctx=NoContext(),
+              create=False)
+    a = F.VoxelPlan(g, [(xyz, fv, wt)], **kw)
+    b = F.VoxelPlan(g, [(xyz, fv, wt)], ranges=[F.coord_ranges(xyz)], **kw)
+    assert a.structs.tobytes() == b.structs.tobytes()
+    assert a.key()[1:] == b.key()[1:]
