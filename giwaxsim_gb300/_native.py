@@ -282,16 +282,24 @@ class Context:
             pass
 
 
-_contexts = {}
-_ctx_lock = threading.Lock()
+_thread_contexts = threading.local()
 
 
 def default_context(device=0):
-    with _ctx_lock:
-        c = _contexts.get(device)
-        if c is None:
-            c = _contexts[device] = Context(device)
-        return c
+    """The calling thread's context on `device`, made on first use.  Each
+    thread has its own (own stream, own device error word): calls from
+    several threads, as the reference's drivers make from a thread pool,
+    run concurrently on the GPU and never land in each other's stream or
+    graph capture.  A context passed explicitly is for one thread at a
+    time.  A thread's context is destroyed when the thread ends and no
+    plan holds it."""
+    ctxs = getattr(_thread_contexts, "by_device", None)
+    if ctxs is None:
+        ctxs = _thread_contexts.by_device = {}
+    c = ctxs.get(device)
+    if c is None:
+        c = ctxs[device] = Context(device)
+    return c
 
 
 def rotate_points(R, pts):

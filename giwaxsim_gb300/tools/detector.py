@@ -13,6 +13,7 @@
 The orientation-summed fast path is detectormaker_fitting in
 tools/comparison.py.
 """
+import threading
 from multiprocessing import shared_memory
 
 import numpy as np
@@ -54,6 +55,10 @@ def rotate_psi_phi_theta(det_x, det_y, det_z, psi, phi, theta):
     x, y, z = rotate_about_normal(det_x, det_y, det_z, psi)
     x, y, z = rotate_about_vertical(x, y, z, phi)
     return rotate_about_horizontal(x, y, z, theta)
+
+
+# held while an orientation's image is added into the named image
+_IMAGE_ADD_LOCK = threading.Lock()
 
 
 def _gather(iq, qx, qy, qz, x, y, z, mats=(), weight=None, ctx=None):
@@ -107,7 +112,10 @@ def generate_detector_ints(args, ctx=None):
     try:
         det_ints = np.ndarray(np.shape(det_int), dtype=np.float64,
                               buffer=shm.buf)
-        det_ints += det_int
+        # the reference's thread pool adds orientations concurrently and
+        # loses updates; here the additions are serialised
+        with _IMAGE_ADD_LOCK:
+            det_ints += det_int
         del det_ints
     finally:
         shm.close()

@@ -11,10 +11,15 @@
 
 The per-slice functions keep the reference's calling convention (shared
 memory by name) for callers that drive slices one at a time; the batched
-voxelgridmaker_fitting in tools/comparison.py is the fast path.
+voxelgridmaker_fitting in tools/comparison.py is the fast path.  The
+reference calls them from a thread pool and its unguarded accumulation into
+the shared grids loses updates; here the device work of concurrent calls
+overlaps (one context per thread) and the additions into the named grids
+are serialised, so a threaded run sums what a serial run sums.
 """
 import ctypes
 import os
+import threading
 from multiprocessing import shared_memory
 
 import numpy as np
@@ -64,6 +69,10 @@ def rectangular_collapse_lengths(x_vals, hor_length, ver_length, phi,
     return out
 
 
+# held while a slice's sums and counts are added into the named grids
+_GRID_ADD_LOCK = threading.Lock()
+
+
 def _shm_grid(name, q_num):
     shm = shared_memory.SharedMemory(name=name)
     return shm, np.ndarray((q_num,) * 3, dtype=np.float64, buffer=shm.buf)
@@ -92,8 +101,9 @@ def rotate_project_fft_coords(args, ctx=None):
     s_shm, s = _shm_grid(sum_name, q_num)
     c_shm, c = _shm_grid(count_name, q_num)
     try:
-        s += sums
-        c += counts
+        with _GRID_ADD_LOCK:
+            s += sums
+            c += counts
     finally:
         del s, c
         s_shm.close()
@@ -114,10 +124,12 @@ def process_file2(iq_2d, det_h_qx, det_h_qy, det_v_qz, qx, qy, qz,
     s_shm, s = _shm_grid(voxel_grid_shm_name, q_num)
     c_shm, c = _shm_grid(voxel_grid_count_shm_name, q_num)
     try:
-        N.check(N.lib().gw_bin_slice(
-            ctx.handle, N.ptr(iq_2d), iq_2d.shape[0], iq_2d.shape[1],
-            N.ptr(hx), N.ptr(hy), N.ptr(vz), q_num, float(np.min(qx)),
-            float(np.max(qx)), float(np.diff(qz)[0]), N.ptr(s), N.ptr(c)))
+        # gw_bin_slice adds into the grids on the host after its device pass
+        with _GRID_ADD_LOCK:
+            N.check(N.lib().gw_bin_slice(
+                ctx.handle, N.ptr(iq_2d), iq_2d.shape[0], iq_2d.shape[1],
+                N.ptr(hx), N.ptr(hy), N.ptr(vz), q_num, float(np.min(qx)),
+                float(np.max(qx)), float(np.diff(qz)[0]), N.ptr(s), N.ptr(c)))
     finally:
         del s, c
         s_shm.close()
