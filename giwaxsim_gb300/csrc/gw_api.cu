@@ -120,7 +120,7 @@ static std::atomic<long long> g_alloc_count{0};
 // the same device and size (plans of one shape made again and again: the
 // drop-in calls in a loop, fit candidates), up to GW_ALLOC_CACHE_MB
 // (default 4096; 0 disables).  A failed cudaMalloc releases the cache and
-// retries; gw_ctx_destroy releases it.
+// retries; destroying the last context of a device releases its blocks.
 namespace {
 std::mutex g_cache_mu;
 std::multimap<std::pair<int, size_t>, void *> g_cache;   // free blocks
@@ -340,6 +340,14 @@ size_t gw_last_error(char *buf, size_t len) {
   return m.size();
 }
 
+namespace {
+// Live contexts per device.  The device block cache is shared by every
+// context of a device; it is released when the last of them is destroyed
+// (a thread pool's per-thread contexts ending leaves it to the others).
+std::mutex g_ctx_mu;
+std::map<int, int> g_ctx_live;
+}  // namespace
+
 int gw_ctx_create(int device, gw_ctx **out) {
   if (!out) return gw::fail(GW_ERR_ARG, "gw_ctx_create: out is null");
   int n = 0;
@@ -355,6 +363,10 @@ int gw_ctx_create(int device, gw_ctx **out) {
   auto *c = new gw_ctx();
   c->device = device;
   c->sm_count = prop.multiProcessorCount;
+  {
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    ++g_ctx_live[device];
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = gw::dev_malloc((void **)&c->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
@@ -376,7 +388,13 @@ int gw_ctx_destroy(gw_ctx *c) {
     if (e) cudaEventDestroy(e);
   gw::dev_free(c->d_err);
   if (c->stream) cudaStreamDestroy(c->stream);
-  gw::release_alloc_cache(c->device);
+  {
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    if (--g_ctx_live[c->device] <= 0) {
+      g_ctx_live.erase(c->device);
+      gw::release_alloc_cache(c->device);
+    }
+  }
   delete c;
   return GW_OK;
 }
