@@ -85,3 +85,30 @@ def test_graph_flag_follows_atom_count_and_shells(monkeypatch):
     plan.set_shells(None, None, None, None, None)
     assert not plan.graph_captured
     assert fake.counts == [4, 4, 5, 4, 4]
+
+
+def test_default_context_is_per_thread(monkeypatch):
+    """default_context() gives each thread its own context (own stream and
+    error word) and the same one on every call within a thread."""
+    import threading
+    from giwaxsim_gb300 import _native as N
+
+    class FakeContext:
+        def __init__(self, device=0):
+            self.device = device
+    monkeypatch.setattr(N, "Context", FakeContext)
+    monkeypatch.setattr(N, "_thread_contexts", threading.local())
+    main = N.default_context()
+    assert N.default_context() is main and N.default_context(1) is not main
+    got = []
+
+    def worker():
+        got.append((N.default_context(), N.default_context()))
+    ts = [threading.Thread(target=worker) for _ in range(3)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert all(a is b for a, b in got)
+    ids = {id(a) for a, _ in got}
+    assert len(ids) == 3 and id(main) not in ids
