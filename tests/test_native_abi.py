@@ -72,3 +72,22 @@ def test_error_reporting_without_gpu(lib):
     assert "null argument" in N.last_error()
     with pytest.raises(N.GwError, match="GW_ERR_ARG"):
         N.check(st)
+
+
+def test_product_imports_no_oracle_or_tests():
+    """The package never imports the oracle or the tests: the oracle is only
+    the checker, never a fallback of the product path."""
+    import ast
+    import pathlib
+    root = pathlib.Path(__file__).resolve().parents[1] / "giwaxsim_gb300"
+    for path in root.rglob("*.py"):
+        tree = ast.parse(path.read_text(), str(path))
+        for node in ast.walk(tree):
+            names = []
+            if isinstance(node, ast.Import):
+                names = [a.name for a in node.names]
+            elif isinstance(node, ast.ImportFrom) and node.module:
+                names = [node.module]
+            for n in names:
+                top = n.split(".")[0]
+                assert top not in ("oracle", "tests"), (path, n)
