@@ -32,6 +32,7 @@ through libgiwaxs_gb300.so.
 import numpy as np
 import torch
 
+from . import _native as N
 from .forward import (DetectorPlan, VoxelGeometry, VoxelPlan, element_f_values,
                       structure_constants)
 
@@ -57,7 +58,11 @@ class DetectorModel:
         self.deposit = deposit
         self.checkpoint_every = int(checkpoint_every)
         self.f0_element = f0_element
-        self.ctx = ctx
+        # every plan of the model (the detector plan made here, the voxel
+        # plans of each forward) works on one context, so that the I(q) a
+        # voxel plan leaves on the device is ordered before the detector
+        # reads it, whichever thread calls forward
+        self.ctx = ctx or N.default_context()
 
         def w(a, ws):
             a = np.atleast_1d(np.asarray(a, dtype=np.float64))
@@ -71,7 +76,7 @@ class DetectorModel:
         Qc = len(q)
         self.det = DetectorPlan((Qc, Qc, Qc), q, q, q, num_pixels, max_q,
                                 angle_init_vals, angle_init_axs, psis, pw,
-                                dphis, hw, thetas, tw, mirror=mirror, ctx=ctx)
+                                dphis, hw, thetas, tw, mirror=mirror, ctx=self.ctx)
         self._det_state = None
 
     @property

@@ -112,3 +112,32 @@ def test_default_context_is_per_thread(monkeypatch):
     assert all(a is b for a, b in got)
     ids = {id(a) for a, _ in got}
     assert len(ids) == 3 and id(main) not in ids
+
+
+def test_detector_model_keeps_one_context(monkeypatch):
+    """A DetectorModel made without ctx takes the constructing thread's
+    context and hands the same one to its detector plan (its forward's
+    voxel plans use self.ctx too), so a forward called from another thread
+    stays on one stream."""
+    import threading
+    from giwaxsim_gb300 import _native as N
+    from giwaxsim_gb300 import autograd as A
+
+    class FakeContext:
+        def __init__(self, device=0):
+            self.device = device
+    got = {}
+
+    class FakeDetectorPlan:
+        def __init__(self, *args, ctx=None, **kw):
+            got["det_ctx"] = ctx
+    monkeypatch.setattr(N, "Context", FakeContext)
+    monkeypatch.setattr(N, "_thread_contexts", threading.local())
+    monkeypatch.setattr(A, "DetectorPlan", FakeDetectorPlan)
+    m = A.DetectorModel(["C"] * 4, 10000.0, 0.5, 0.15, 1.5, 16)
+    assert m.ctx is N.default_context() and got["det_ctx"] is m.ctx
+    seen = []
+    t = threading.Thread(target=lambda: seen.append(N.default_context()))
+    t.start()
+    t.join()
+    assert seen[0] is not m.ctx
