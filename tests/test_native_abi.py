@@ -74,6 +74,25 @@ def test_error_reporting_without_gpu(lib):
         N.check(st)
 
 
+def test_noalloc_limits_checked_before_any_device_call(lib):
+    """The allocation-free detector call rejects null pointers and images
+    beyond its fixed scratch (1024 x 1024 pixels) on the host, before it
+    touches a device: the pointers below are never dereferenced."""
+    p = N.DetectorParams()
+    p.n_h, p.n_v = 1025, 1024
+    p.iq_shape[:] = [4, 4, 4]
+    p.dq = 0.1
+    fake = ctypes.c_void_p(16)
+    n_rot = ctypes.c_void_p(32)
+    args = [ctypes.byref(p), fake, fake, fake, None, 0, n_rot, fake, fake, 1,
+            fake, None]
+    assert lib.gw_detector_noalloc(*args) == N.GW_ERR_ARG
+    assert "1048576" in N.last_error()
+    args[1] = None
+    assert lib.gw_detector_noalloc(*args) == N.GW_ERR_ARG
+    assert "null argument" in N.last_error()
+
+
 def test_product_imports_no_oracle_or_tests():
     """The package never imports the oracle or the tests: the oracle is only
     the checker, never a fallback of the product path."""
