@@ -15,7 +15,8 @@ voxelgridmaker_fitting in tools/comparison.py is the fast path.  The
 reference calls them from a thread pool and its unguarded accumulation into
 the shared grids loses updates; here the device work of concurrent calls
 overlaps (one context per thread) and the additions into the named grids
-are serialised, so a threaded run sums what a serial run sums.
+are serialised within the process, so a threaded run sums what a serial
+run sums.
 """
 import ctypes
 import os
