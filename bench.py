@@ -30,14 +30,11 @@ sys.path.insert(0, ROOT)
 METRIC = "slices/s & s/detector image: batched vs plain on 1 GB300 at <=1e-5 rel err vs FP64"
 L2_BYTES = 129 * 1024 * 1024
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# one ncu --set full capture of the kernel on the same workload and plan
-# shape (workload, kernel, fft_y, fft_z, batch); the summaries with their
-# commands are profiles/k_row_czt_1280_si-100A.md and
-# profiles/k_col_czt_bin_1024_si-100A.md.
-# DRAM bytes (read + write) per slice from one ncu capture of a 51-slice
-# launch (profiles/); a launch's traffic is this times its slices (both
-# kernels move per-slice data only).
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per slice of the
+# two transform kernels, keyed by (workload, kernel, fft_y, fft_z), from one
+# ncu --set full capture of a 51-slice launch of that kernel on the same
+# workload and plan shape; a launch's traffic is this times its slices
+# (both kernels move per-slice data only).
 NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024): (1.48 + 38.03) * 1e6 / 51,
                ("si-100A", "col_czt_bin", 1280, 1024): (148.42 + 28.70) * 1e6 / 51}
 
@@ -63,6 +60,9 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="one eager voxel pass and one detector pass, no "
                          "timing (for ncu)")
+    ap.add_argument("--transform", default="auto",
+                    choices=["auto", "stockham", "fused"],
+                    help="chirp-z kernel family of --profile's plan")
     return ap.parse_args()
 
 
@@ -293,25 +293,12 @@ def run_gb300(args, world, rank, local, pg):
     ctx.set_timing(False)
     eager.close()
 
-    # plain per-rotation path: one slice per launch sequence, full grid
-    # (per-slice cost from 8- and 24-slice plans; their difference removes
-    # the per-execute memset, preparation and finalize, counted once)
+    # plain per-rotation path: one slice per launch sequence, full grid,
+    # timed over every slice of the workload
     plain = None
     if not args.no_plain:
-        t = {}
-        for k in (min(len(phis), 8), min(len(phis), 24)):
-            pp = F.VoxelPlan(geom, items[:1], phis=phis[:k],
-                             fill_bkg=w["fill_bkg"], smooth=w["smooth"],
-                             mode="plain", ctx=ctx)
-            pp.set_atoms()
-            pp.execute()
-            ctx.synchronize()
-            t[k] = _event_ms(ts, pp.execute, 2)
-            pp.close()
-        (k1, t1), (k2, t2) = sorted(t.items())
-        per_slice = (t2 - t1) / (k2 - k1) if k2 > k1 else t2 / k2
-        fixed = max(0.0, t1 - k1 * per_slice)
-        plain = n_slices / ((fixed + per_slice * n_slices) / 1e3)
+        plain_ms = plain_path_ms(geom, w, items, phis, ctx, ts)
+        plain = n_slices / (plain_ms / 1e3)
 
     # e2e through the public API with host arrays
     e2e = None
@@ -376,38 +363,38 @@ def run_gb300(args, world, rank, local, pg):
                "s_per_step": te, "s_per_call": [round(v, 6) for v in t_e],
                "phases": ph}
 
-    # roofline of the dominant kernel
+    # rooflines: the dominant kernel (`roofline`) and every stage kernel
+    # (`rooflines`: row and column transforms with the binning, finalize,
+    # detector), from the eager per-kernel event times
     peak, peak_kind = measured_peaks()
-    top = max(kt.items(), key=lambda kv: kv[1][0]) if kt else None
-    roof = None
-    if top:
-        name, (ms_tot, nl) = top
+
+    def kernel_roof(name):
+        ms_tot, nl = kt[name]
         avg_ms = ms_tot / max(nl, 1)
         # slices per launch of the batched kernels: the batches' average
         spl = n_slices / nl if name in ("row_czt", "col_czt_bin") else None
         algo = algorithmic_bytes(name, info, w, spl, dargs, plan.Qc)
-        achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
+        if not algo:
+            return None
+        achieved = algo / (avg_ms / 1e3) / 1e9
         tkey = (args.workload, name, info["My"], info["Mz"])
         traffic = NCU_TRAFFIC[tkey] * spl if tkey in NCU_TRAFFIC else None
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved,
-                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None,
-                "traffic": traffic,
-                "traffic_source": "ncu capture of a 51-slice launch (profiles/), "
-                "scaled by slices per launch" if traffic else None,
-                "avg_launch_ms": avg_ms, "slices_per_launch": spl,
-                "algorithmic_bytes_per_launch": algo}
+        r = {"kernel": name, "bound": "hbm", "achieved": achieved,
+             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+             "frac": achieved / peak, "traffic": traffic,
+             "traffic_source": "ncu capture of a 51-slice launch, scaled by "
+                               "slices per launch" if traffic else None,
+             "avg_launch_ms": avg_ms, "launches": nl,
+             "slices_per_launch": spl, "algorithmic_bytes_per_launch": algo}
         if name in ("row_czt", "col_czt_bin"):
             # the transforms' own limiter: shared-memory passes
-            m = info["My"] if name == "row_czt" else info["Mz"]
-            units = spl * (info["Lz"] if name == "row_czt" else info["Nc"])
-            sb = units * 2 * fft_passes(m) * m * 16
-            speak = 152 * 128 * 2070e6 / 1e12
-            roof["shared"] = {"achieved": sb / (avg_ms / 1e3) / 1e12,
-                              "peak": speak, "unit": "TB/s",
-                              "frac": sb / (avg_ms / 1e3) / 1e12 / speak,
-                              "peak_kind": "nominal: 152 SMs x 128 B/clk x 2070 MHz",
-                              "bytes_per_launch": sb}
+            r["shared"] = shared_roof(name, info, spl, avg_ms)
+        return r
+
+    rooflines = {k: kernel_roof(k) for k in ("row_czt", "col_czt_bin",
+                                             "finalize", "detector") if k in kt}
+    top = max(kt.items(), key=lambda kv: kv[1][0])[0] if kt else None
+    roof = rooflines.get(top) if top else None
     kernel_share = {k: {"ms": round(v[0], 4), "launches": v[1]}
                     for k, v in kt.items()}
 
@@ -420,16 +407,39 @@ def run_gb300(args, world, rank, local, pg):
                                            tune=not args.no_tune)
     grad = None if args.no_grad else grad_timing(ctx)
 
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, w, geom, phis, items)
+    # CPU baseline and accuracy: one pass of the float64 oracle over every
+    # slice (timed), then its detector image; the GPU's I(q), counts and
+    # image are compared with them outside every timed region
+    cpu = accuracy = None
+    if rank == 0 and not args.no_cpu_baseline and len(items) == 1:
+        ref = oracle_voxel(w, geom, phis, items)
+        cpu = {"value": ref["slices"] / ref["seconds"], "unit": "slices/s",
+               "cores": ref["cores"], "threads": ref["threads"], "kind": "port",
+               "sample": "all %d slices of %s, one pass (float64 numpy oracle, "
+                         "%d threads), %.1f s" % (ref["slices"], args.workload,
+                                                  ref["threads"], ref["seconds"])}
+        t0 = time.perf_counter()
+        dref = oracle_detector(ref["iq"], ref["q"], dargs, ref["threads"])
+        t_det = time.perf_counter() - t0
+        accuracy = {
+            "reference": "float64 numpy oracle, all %d slices, %d px x %d "
+                         "orientations" % (n_slices, dargs["num_pixels"],
+                                           int(det.n_orient)),
+            "iq": compare(plan.iq(), ref["iq"]),
+            "counts_bit_exact": bool(np.array_equal(plan.counts(), ref["count"])),
+            "detector": compare(det.result(), dref),
+            "oracle_detector_s": round(t_det, 2)}
+        accuracy["meets_1e-5"] = (accuracy["iq"]["rel_l2"] <= 1e-5 and
+                                  accuracy["detector"]["rel_l2"] <= 1e-5 and
+                                  accuracy["counts_bit_exact"])
+        del ref, dref
 
     out = {
         "metric": METRIC, "value": value, "unit": "slices/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 accum)",
-        "data": "synthetic (seeded structure generator)",
+        "data": "synthetic (seeded structure generator, f = Z)",
         "config": {"workload": args.workload, "atoms": int(len(plan.xyz)),
                    "grid_size": geom.grid_size, "crop": plan.Qc,
                    "slices_per_step": n_slices,
@@ -444,8 +454,9 @@ def run_gb300(args, world, rank, local, pg):
         "plain_slices_per_s": plain,
         "batched_vs_plain": (value / world / plain) if plain else None,
         "gpu_launches": int(launches),
-        "e2e": e2e, "roofline": roof, "kernel_ms": kernel_share,
-        "cpu_baseline": cpu, "clocks": clk,
+        "e2e": e2e, "roofline": roof, "rooflines": rooflines,
+        "kernel_ms": kernel_share,
+        "cpu_baseline": cpu, "accuracy": accuracy, "clocks": clk,
         "workloads": table, "gradient": grad,
     }
     if rank == 0:
@@ -468,6 +479,20 @@ def fft_passes(m):
     return l2 // 4 + (1 if l2 % 4 else 0) + (1 if odd > 1 else 0)
 
 
+def shared_roof(name, info, spl, avg_ms):
+    """Shared-memory traffic of a transform kernel's Stockham passes (one
+    read and one write of every point per pass, forward and inverse) per
+    launch, against the nominal shared bandwidth."""
+    m = info["My"] if name == "row_czt" else info["Mz"]
+    units = spl * (info["Lz"] if name == "row_czt" else info["Nc"])
+    sb = units * 2 * fft_passes(m) * m * 16
+    speak = 152 * 128 * 2070e6 / 1e12
+    return {"achieved": sb / (avg_ms / 1e3) / 1e12, "peak": speak,
+            "unit": "TB/s", "frac": sb / (avg_ms / 1e3) / 1e12 / speak,
+            "peak_kind": "nominal: 152 SMs x 128 B/clk x 2070 MHz",
+            "bytes_per_launch": sb}
+
+
 def _event_ms(ts, fn, reps, flush=None):
     import torch
     tot = 0.0
@@ -484,10 +509,25 @@ def _event_ms(ts, fn, reps, flush=None):
     return tot / reps
 
 
-def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8, tune=True):
+def plain_path_ms(geom, w, items, phis, ctx, ts, reps=2):
+    """Device time of the plain per-rotation path (one slice per launch
+    sequence, full grid and transform, binning into the whole cube) over
+    every slice of every structure, ms (mean of `reps` executions)."""
+    from giwaxsim_gb300 import forward as F
+    pp = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
+                     smooth=w["smooth"], mode="plain", ctx=ctx)
+    pp.set_atoms()
+    pp.execute()
+    ctx.synchronize()
+    t = _event_ms(ts, pp.execute, reps)
+    pp.close()
+    return t
+
+
+def workload_summary(name, ctx, ts, flush, reps=3, tune=True):
     """Seconds per detector image of one workload: batched (graph replay of
     the voxel stage over all slices + detector) and plain (the per-rotation
-    path, timed on n_plain slices and scaled to all slices, + detector)."""
+    path over all slices + detector)."""
     from giwaxsim_gb300 import forward as F
     w, structs, geom, phis, items = load_workload(name)
     n_slices = len(items) * len(phis)
@@ -553,23 +593,8 @@ def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8, tune=True):
         del ik, ref
         pk.close()
     plan.close()
-    # plain: per-slice cost from two sample sizes (the difference removes the
-    # per-execute memset, structure preparation and finalize), plus one
-    # fixed cost
-    n = min(n_plain, len(phis))
-    n1 = max(1, n // 3)
-    t = {}
-    for k in (n1, n):
-        pp = F.VoxelPlan(geom, items[:1], phis=phis[:k], fill_bkg=w["fill_bkg"],
-                         smooth=w["smooth"], mode="plain", ctx=ctx)
-        pp.set_atoms()
-        pp.execute()
-        ctx.synchronize()
-        t[k] = _event_ms(ts, pp.execute, 2)
-        pp.close()
-    per_slice = (t[n] - t[n1]) / (n - n1) if n > n1 else t[n] / n
-    fixed = max(0.0, t[n1] - n1 * per_slice)
-    plain_ms = fixed + per_slice * n_slices
+    # plain: the per-rotation path over every slice of every structure
+    plain_ms = plain_path_ms(geom, w, items, phis, ctx, ts)
     batched = (vox_ms + det_ms) / 1e3
     plain = (plain_ms + det_ms) / 1e3
     return {"slices": n_slices, "atoms": int(sum(len(x[0]) for x in items)),
@@ -579,9 +604,8 @@ def workload_summary(name, ctx, ts, flush, reps=3, n_plain=8, tune=True):
             "voxel_ms": round(vox_ms, 4), "detector_ms": round(det_ms, 4),
             "slices_per_s": n_slices / (vox_ms / 1e3),
             "s_per_image_batched": batched, "s_per_image_plain": plain,
-            "plain_ms_per_slice": round(per_slice, 4),
-            "plain_fixed_ms": round(fixed, 4),
-            "plain_sample_slices": [n1, n], "batched_vs_plain": plain / batched,
+            "plain_ms": round(plain_ms, 4),
+            "plain_sample_slices": n_slices, "batched_vs_plain": plain / batched,
             "kahan32": kahan}
 
 
@@ -626,7 +650,7 @@ def run_profile(args, w, geom, phis, items, ctx):
     """One eager pass of the voxel stage and one detector image."""
     from giwaxsim_gb300 import forward as F
     plan = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
-                       smooth=w["smooth"], ctx=ctx)
+                       smooth=w["smooth"], transform=args.transform, ctx=ctx)
     plan.set_atoms()
     plan.execute()
     ctx.synchronize()
@@ -664,76 +688,80 @@ def algorithmic_bytes(name, info, w, S, dargs, Qc):
 
 
 # ------------------------------------------------------------------ CPU
-def _cpu_slices(payload):
+def oracle_voxel(w, geom, phis, items, workers=None):
+    """The float64 numpy oracle over every slice of a single-structure
+    workload, threaded over slices like the reference's ThreadPoolExecutor
+    (comparison.py:759-763).  Returns the cropped I(q) with the f0 factor,
+    the count grid and the wall time of the whole pass."""
     from oracle import giwaxs_oracle as O
-    (xyz, fv, phis, g, r, fill, smooth, q, consts, vs, vc) = payload
-    xb, yb, zb, avg = consts
-    t0 = time.perf_counter()
-    for phi in phis:
-        grid, _ = O.project_slice(xyz, fv, phi, g, r, avg, xb, yb, zb, fill,
-                                  smooth)
-        hx, hy, vz = O.slice_axes(g, r, phi)
-        O.bin_slice(O.slice_intensity(grid), hx, hy, vz, q, q, q, vs, vc)
-    return time.perf_counter() - t0, len(phis)
-
-
-def cpu_baseline(args, w, geom, phis, items, budget=None):
-    """The float64 numpy oracle on a bounded sample of the workload's slices,
-    threaded over slices like the reference's ThreadPoolExecutor."""
-    from concurrent.futures import ThreadPoolExecutor
-    from oracle import giwaxs_oracle as O
-    budget = budget or args.cpu_seconds
     xyz, fv, wt = items[0]
     fvw = fv if wt is None else fv * wt
-    consts = O.structure_constants(xyz, fvw, w["r"])
     cores = os.cpu_count() or 1
-    workers = min(32, cores + 4)
-    # one shared (sum, count) grid, as the reference's threads share one
-    qn = len(geom.q)
-    vs = np.zeros((qn, qn, qn))
-    vc = np.zeros((qn, qn, qn))
-    # one slice first to size the sample
-    t1, _ = _cpu_slices((xyz, fvw, phis[:1], geom.grid_size, w["r"],
-                         w["fill_bkg"], w["smooth"], geom.q, consts, vs, vc))
-    per_batch = workers
-    n_target = max(1, int(budget / max(t1, 1e-3) * min(workers, cores) * 0.5))
-    n_target = min(n_target, len(phis))
-    sample = phis[np.linspace(0, len(phis) - 1, n_target).astype(int)]
-    chunks = [sample[i::per_batch] for i in range(per_batch)]
-    chunks = [c for c in chunks if len(c)]
+    workers = workers or min(32, cores + 4)
     t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=workers) as ex:
-        list(ex.map(_cpu_slices, [(xyz, fvw, c, geom.grid_size, w["r"],
-                                   w["fill_bkg"], w["smooth"], geom.q, consts,
-                                   vs, vc) for c in chunks]))
-    dt = time.perf_counter() - t0
-    return {"value": len(sample) / dt, "unit": "slices/s", "cores": cores,
-            "threads": workers, "kind": "port",
-            "sample": "%d of %d slices of %s (float64 numpy oracle, %d "
-                      "threads), %.1f s" % (len(sample), len(phis),
-                                             args.workload, workers, dt)}
+    out = O.voxelgrid_crop_threaded(xyz, fvw, w["r"], w["dq"], w["max_q"],
+                                    phis, w["fill_bkg"], w["smooth"], workers)
+    out.update(seconds=time.perf_counter() - t0, threads=workers, cores=cores,
+               slices=len(phis))
+    return out
+
+
+def oracle_detector(iq, qc, dargs, workers):
+    """The oracle's detector image (comparison.py:790-870) of a float64
+    I(q), its orientations summed on `workers` threads."""
+    from oracle import giwaxs_oracle as O
+    return O.detector_threaded(iq, qc, qc, qc, dargs["num_pixels"],
+                               dargs["max_q"], dargs["angle_init_vals"],
+                               dargs["angle_init_axs"], dargs["psis"],
+                               dargs["psi_weights"], dargs["phis"],
+                               dargs["phi_weights"], dargs["thetas"],
+                               dargs["theta_weights"], True, workers)[0]
+
+
+def compare(gpu, ref):
+    """Per-output error of a GPU result against the float64 oracle:
+    normwise relative L2, max |diff| / max |ref|, and the p50/p99 of the
+    elementwise relative error over the nonzero reference values."""
+    gpu = np.asarray(gpu, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    d = np.abs(gpu - ref)
+    nz = ref != 0
+    rel = d[nz] / np.abs(ref[nz])
+    return {"rel_l2": float(np.linalg.norm(gpu - ref) / np.linalg.norm(ref)),
+            "max_abs_over_max": float(d.max() / np.abs(ref).max()),
+            "p50_rel": float(np.percentile(rel, 50)),
+            "p99_rel": float(np.percentile(rel, 99)),
+            "zero_where_ref_zero": bool(np.all(gpu[~nz] == 0))}
 
 
 def run_reference(args, world, rank, local, pg):
+    """The reference arm: the float64 numpy oracle (the reference's path
+    restated) on the host cores, every step the whole workload (all slices
+    of the voxel stage), threaded like the reference."""
     if rank != 0:
         return
     w, structs, geom, phis, items = load_workload(args.workload, args.phis)
-    vals = []
-    for _ in range(max(1, args.warmup > 0) + args.steps):
-        vals.append(cpu_baseline(args, w, geom, phis, items,
-                                 budget=max(2.0, args.cpu_seconds / max(1, args.steps))))
-    v = vals[-args.steps:]
-    value = float(np.mean([x["value"] for x in v]))
-    cb = dict(v[-1])
-    cb["value"] = value
+    for _ in range(args.warmup):
+        oracle_voxel(w, geom, phis, items)
+    secs = []
+    for _ in range(args.steps):
+        r = oracle_voxel(w, geom, phis, items)
+        secs.append(r["seconds"])
+    n = len(phis) * len(items)
+    t = float(np.sum(secs))
+    value = n * args.steps / t
+    cb = {"value": value, "unit": "slices/s", "cores": r["cores"],
+          "threads": r["threads"], "kind": "port",
+          "sample": "%d full steps of %d slices of %s (float64 numpy oracle, "
+                    "%d threads), %.1f s timed" % (args.steps, n,
+                                                    args.workload,
+                                                    r["threads"], t)}
     out = {"metric": METRIC, "impl": "reference", "value": value,
            "unit": "slices/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup,
-           "ms_per_step": 1e3 * len(phis) * len(items) / value,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64", "data": "synthetic (seeded structure generator)",
-           "config": {"workload": args.workload,
-                      "slices_per_step": len(phis) * len(items)},
+           "dtype": "f64", "data": "synthetic (seeded structure generator, f = Z)",
+           "config": {"workload": args.workload, "slices_per_step": n},
            "cpu_baseline": cb,
            "e2e": {"value": value, "unit": "slices/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
@@ -742,6 +770,10 @@ def run_reference(args, world, rank, local, pg):
 
 def main():
     args = parse()
+    # synthetic workloads: f = Z for every atom (f' = f'' = 0), as stated
+    # in the line's "data"; xraydb is not installed on the GPU machine
+    from giwaxsim_gb300.tools import utilities
+    utilities.use_zero_f1f2()
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank, local, pg)

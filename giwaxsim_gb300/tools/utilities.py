@@ -14,6 +14,7 @@ behaviour (tools/utilities.py of the reference):
                          q instead of q**2 in the exponent)
   get_element_f1_f2_dict utilities.py:342-366
 """
+import os
 import re
 import warnings
 from collections import Counter
@@ -168,8 +169,20 @@ def get_element_f0_dict(q_val, elements):
 
 _warned_xraydb = False
 
+# f' = f'' = 0 (f = Z) when xraydb is missing: off unless the caller opts in
+# (use_zero_f1f2(), or GIWAXSIM_F1F2=zero in the environment)
+_ZERO_F1F2 = [os.environ.get("GIWAXSIM_F1F2", "").lower() == "zero"]
 
 _XRAYDB = []
+
+
+def use_zero_f1f2(on=True):
+    """Opt in (or out) to f' = f'' = 0 when xraydb is not installed.  The
+    reference imports xraydb at module level (tools/utilities.py:3) and
+    cannot run without it; by default this drop-in refuses as well rather
+    than change the intensities silently.  Callers that pass their own
+    f' + i f'' table (the f1f2= keyword of the drivers) need neither."""
+    _ZERO_F1F2[0] = bool(on)
 
 
 def _xraydb():
@@ -186,13 +199,22 @@ def _xraydb():
 
 def get_element_f1_f2_dict(energy, elements):
     """f' + i f'' per element at `energy` eV from xraydb's Chantler tables
-    when xraydb is installed; otherwise 0 (a warning is issued once), so the
-    scattering factor is Z."""
+    (utilities.py:342-366).  Without xraydb: ImportError, unless the caller
+    opted in to f' = f'' = 0 with use_zero_f1f2() (then a warning is issued
+    once and the scattering factor is Z)."""
     global _warned_xraydb
     xraydb = _xraydb()
     if xraydb is None:
+        if not _ZERO_F1F2[0]:
+            raise ImportError(
+                "xraydb is not installed: the f', f'' lookup needs it "
+                "(tools/utilities.py:342-366).  Install xraydb, pass an "
+                "f' + i f'' table (f1f2=...), or opt in to f' = f'' = 0 with "
+                "giwaxsim_gb300.tools.utilities.use_zero_f1f2() or "
+                "GIWAXSIM_F1F2=zero")
         if not _warned_xraydb:
-            warnings.warn("xraydb is not installed: using f' = f'' = 0")
+            warnings.warn("xraydb is not installed: using f' = f'' = 0 "
+                          "(opted in)")
             _warned_xraydb = True
         return {el: 0j for el in set(np.asarray(elements).tolist())}
     out = {}

@@ -7,6 +7,7 @@ host it runs on (x86_64 here, aarch64 on the GPU host).
 """
 import os
 import subprocess
+import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "oracle_fma.c")
@@ -14,7 +15,15 @@ OUT_DIR = os.path.join(HERE, "_build")
 OUT = os.path.join(OUT_DIR, "liboracle_fma.so")
 
 
+_LOCK = threading.Lock()
+
+
 def build(force: bool = False) -> str:
+    with _LOCK:  # threads of one process share the temporary file name
+        return _build(force)
+
+
+def _build(force):
     if (not force and os.path.exists(OUT)
             and os.path.getmtime(OUT) >= os.path.getmtime(SRC)):
         return OUT

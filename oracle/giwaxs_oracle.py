@@ -36,7 +36,9 @@ Differences from the reference, all deliberate:
     that OpenBLAS uses on x86_64 (pinned in tests/golden), so the oracle is
     bit-reproducible on any host.
   * phis may be passed explicitly (the reference always derives them).
-  * the count grid is returned alongside I(q); accumulation is serial.
+  * the count grid is returned alongside I(q); accumulation is serial
+    (voxelgrid_crop_threaded and detector_threaded spread slices and
+    orientations over threads, with the additions guarded).
   * detectormaker copies the summed image before releasing it (the reference
     reads a closed shared-memory buffer when mirror=False).
   * smoothing accepts a non-integer sigma; mask edges are ceil(lo+sigma) and
@@ -50,15 +52,25 @@ not installed); f values are an input to both the oracle and the product.
 import ctypes
 import math
 import os
+import threading
 
 import numpy as np
 from numpy.fft import fft2, fftshift
 from scipy.ndimage import gaussian_filter1d, map_coordinates
 
 _LIB = None
+_LIB_LOCK = threading.Lock()
 
 
 def _lib():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LIB_LOCK:
+        return _load_lib()
+
+
+def _load_lib():
     global _LIB
     if _LIB is None:
         from . import build_oracle
@@ -261,6 +273,25 @@ def bin_indices(det_h_qx, det_h_qy, det_v_qz, qx, qy, qz):
     return vm, hm, iy, ix, iz
 
 
+def crop_pairs(iq_2d, det_h_qx, det_h_qy, det_v_qz, q, lo, Qc):
+    """The pixels of one slice that process_file2 (voxelgrids.py:464-506)
+    bins into the cropped cube q[lo:lo+Qc]^3, as flat crop indices
+    ((iy*Qc + ix)*Qc + iz) and intensities."""
+    vm, hm, iy, ix, iz = bin_indices(det_h_qx, det_h_qy, det_v_qz, q, q, q)
+    ky, kx, kz = iy - lo, ix - lo, iz - lo
+    oh = (ky >= 0) & (ky < Qc) & (kx >= 0) & (kx < Qc)
+    ov = (kz >= 0) & (kz < Qc)
+    sub = iq_2d[vm, :][:, hm][ov, :][:, oh]
+    flat = (ky[oh] * Qc + kx[oh])[None, :] * Qc + kz[ov][:, None]
+    return flat.ravel().astype(np.int64), sub.ravel()
+
+
+def crop_window(q, max_q):
+    """First index and length of downselect_voxelgrid's crop of axis q."""
+    idx = np.where(np.abs(q) < max_q + np.abs(q[1] - q[0]))[0]
+    return int(idx[0]), int(idx[-1] - idx[0] + 1)
+
+
 def bin_slice(iq_2d, det_h_qx, det_h_qy, det_v_qz, qx, qy, qz, vsum, vcount):
     """voxelgrids.py:464-506 (process_file2) into plain arrays."""
     vm, hm, iy, ix, iz = bin_indices(det_h_qx, det_h_qy, det_v_qz, qx, qy, qz)
@@ -371,6 +402,50 @@ def voxelgrid(structures, r_voxel_size, q_voxel_size, max_q, phis=None,
     if keep_full:
         out["full_sum"], out["full_count"] = vsum, vcnt
     return out
+
+
+def _crop_chunk(payload):
+    (coords, fv, phis, g, r, fill, smooth, q, consts, lo, Qc, vsum, vcnt,
+     lock) = payload
+    xb, yb, zb, avg = consts
+    for phi in phis:
+        grid, _ = project_slice(coords, fv, phi, g, r, avg, xb, yb, zb, fill,
+                                smooth)
+        hx, hy, vz = slice_axes(g, r, phi)
+        i, v = crop_pairs(slice_intensity(grid), hx, hy, vz, q, lo, Qc)
+        with lock:  # process_file2's np.add.at, one slice at a time
+            np.add.at(vsum, i, v)
+            np.add.at(vcnt, i, 1.0)
+
+
+def voxelgrid_crop_threaded(coords, f_values, r_voxel_size, q_voxel_size,
+                            max_q, phis, fill_bkg=False, smooth=0, workers=8):
+    """voxelgrid() for one structure, with the slices spread over `workers`
+    threads as the reference's driver does (comparison.py:759-763) and only
+    the cropped cube accumulated (downselect_voxelgrid keeps nothing else).
+    Threads add their slices into one shared pair of grids under a lock:
+    the reference's unguarded np.add.at from threads loses updates.  Sums
+    are added in another order than the serial voxelgrid() (differences at
+    the float64 rounding level); counts are identical.
+    Returns dict(iq, count, q) over the crop."""
+    from concurrent.futures import ThreadPoolExecutor
+    grid_size, q, _ = voxel_geometry(r_voxel_size, q_voxel_size, max_q, coords)
+    lo, Qc = crop_window(q, max_q)
+    phis = np.asarray(phis)
+    chunks = [c for c in (phis[i::workers] for i in range(workers)) if len(c)]
+    consts = structure_constants(coords, f_values, r_voxel_size)
+    vsum = np.zeros(Qc ** 3)
+    vcnt = np.zeros(Qc ** 3)
+    lock = threading.Lock()
+    _lib()  # build/load the helper before the threads use it
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        list(ex.map(_crop_chunk, [
+            (coords, f_values, c, grid_size, r_voxel_size, fill_bkg, smooth,
+             q, consts, lo, Qc, vsum, vcnt, lock) for c in chunks]))
+    iq = np.divide(vsum, vcnt, out=np.zeros_like(vsum), where=vcnt != 0)
+    qc = q[lo:lo + Qc]
+    iq = add_f0_q_3d(iq.reshape(Qc, Qc, Qc), qc, qc, qc, "C")
+    return dict(iq=iq, count=vcnt.reshape(Qc, Qc, Qc), q=qc)
 
 
 # --------------------------------------------------------------------------
@@ -648,20 +723,56 @@ def detector(iq, qx, qy, qz, num_pixels, max_q, angle_init_vals,
                    else np.asarray(phi_weights))
     theta_weights = (np.ones_like(thetas) / len(thetas) if theta_weights is None
                      else np.asarray(theta_weights))
-    acc = np.zeros((num_pixels, num_pixels))
-    for ps, pw, ph, hw, th, tw in orientation_list(
-            psis, psi_weights, phis, phi_weights, thetas, theta_weights):
+    acc = detector_partial(iq, qx, qy, qz, x0, y0, z0, orientation_list(
+        psis, psi_weights, phis, phi_weights, thetas, theta_weights))
+    return detector_epilogue(acc, mirror), h, v
+
+
+def detector_threaded(iq, qx, qy, qz, num_pixels, max_q, angle_init_vals,
+                      angle_init_axs, psis, psi_weights, phis, phi_weights,
+                      thetas, theta_weights, mirror=True, workers=8):
+    """detector() with the orientation list split over `workers` threads
+    (the reference's driver sums orientations from a thread pool,
+    comparison.py:850-853); the partial images are added at the end."""
+    from concurrent.futures import ThreadPoolExecutor
+    x0, y0, z0, h, v = init_detector(num_pixels, max_q, angle_init_vals,
+                                     angle_init_axs)
+    psis, phis, thetas = map(np.asarray, (psis, phis, thetas))
+    w = [np.ones_like(a) / len(a) if wa is None else np.asarray(wa)
+         for a, wa in ((psis, psi_weights), (phis, phi_weights),
+                       (thetas, theta_weights))]
+    orients = orientation_list(psis, w[0], phis, w[1], thetas, w[2])
+    chunks = [c for c in (orients[i::workers] for i in range(workers)) if c]
+    _lib()
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        parts = list(ex.map(lambda c: detector_partial(iq, qx, qy, qz, x0, y0,
+                                                       z0, c), chunks))
+    return detector_epilogue(sum(parts), mirror), h, v
+
+
+def detector_partial(iq, qx, qy, qz, x0, y0, z0, orients):
+    """detector.py:278-300: the weighted sum over `orients` (a slice of
+    orientation_list) of the gathered images, in list order.  Independent
+    parts of the list may be summed on separate threads and added."""
+    acc = np.zeros(x0.shape)
+    for ps, pw, ph, hw, th, tw in orients:
         x, y, z = rotate_psi_phi_theta(x0, y0, z0, ps, ph, th)
         d = intersect_detector(iq, qx, qy, qz, x, y, z)
         d = d * (pw * hw * tw)
         acc += d
+    return acc
+
+
+def detector_epilogue(acc, mirror=True):
+    """comparison.py:857-868: optional mirror, NaN/non-positive -> 1e-6,
+    scale by 1e-6 (on a copy of the summed image)."""
     det = acc.copy()
     if mirror:
         det = mirror_vertical_horizontal(det)
     det[det != det] = 1e-6
     det[det <= 0] = 1e-6
     det *= 1e-6
-    return det, h, v
+    return det
 
 
 # ------------------------------------------------------------------ slab

@@ -9,6 +9,10 @@ if ROOT not in sys.path:
 
 
 def pytest_configure(config):
+    # the synthetic structures and fixtures use f = Z (xraydb is not
+    # installed here, and the fixtures were made with f' = f'' = 0)
+    from giwaxsim_gb300.tools import utilities
+    utilities.use_zero_f1f2()
     config.addinivalue_line(
         "markers", "gpu: needs a CUDA device (GB300, sm_103a) and the built "
         "native library")

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in tests/golden/ by running the reference
 GIWAXSim code itself (a Python package, imported from its checkout).
 
-Run in a container that has the reference checkout:
-    python tests/golden/make_golden.py [/path/to/reference]
+Run in a container that has the reference checkout, giving its path as the
+first argument or in the environment variable GIWAXSIM_REFERENCE:
+    python tests/golden/make_golden.py /path/to/reference
     python tests/golden/make_golden.py /path/to/reference pm6   # PM6 example
     (other fixture groups: slab, compare, multiq, shift)
 
@@ -22,7 +23,7 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GIWAXSIM_REFERENCE")
 
 
 class _Stub(types.ModuleType):
@@ -33,6 +34,9 @@ class _Stub(types.ModuleType):
 
 
 def _import_reference():
+    if not REF or not os.path.isdir(REF):
+        raise SystemExit("usage: make_golden.py /path/to/reference [group] "
+                         "(or set GIWAXSIM_REFERENCE)")
     import scipy.signal
     import scipy.signal.windows
     for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.cm",

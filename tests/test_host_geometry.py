@@ -149,3 +149,24 @@ def test_plan_inputs_equal_with_ranges_given():
     b = F.VoxelPlan(g, [(xyz, fv, wt)], ranges=[F.coord_ranges(xyz)], **kw)
     assert a.structs.tobytes() == b.structs.tobytes()
     assert a.key()[1:] == b.key()[1:]
+
+
+def test_missing_xraydb_refuses_without_opt_in(monkeypatch):
+    """Without xraydb the f', f'' lookup (utilities.py:342-366) raises, as
+    the reference's module-level `import xraydb` (utilities.py:3) does,
+    unless the caller opts in to f' = f'' = 0 or passes a table."""
+    if utilities._xraydb() is not None:
+        pytest.skip("xraydb is installed")
+    monkeypatch.setattr(utilities, "_ZERO_F1F2", [False])
+    with pytest.raises(ImportError, match="xraydb"):
+        utilities.get_element_f1_f2_dict(10000.0, ["C", "Si"])
+    with pytest.raises(ImportError, match="xraydb"):
+        F.element_f_values(["C", "Si"], 10000.0)
+    f = F.element_f_values(["C", "Si", "C"], 10000.0,
+                           {"C": 0.25 + 0.5j, "Si": -1.0 + 2.0j})
+    assert np.array_equal(f, np.array([6.25 + 0.5j, 13.0 + 2.0j, 6.25 + 0.5j]))
+    utilities.use_zero_f1f2()
+    assert utilities.get_element_f1_f2_dict(10000.0, ["C"]) == {"C": 0j}
+    utilities.use_zero_f1f2(False)
+    with pytest.raises(ImportError, match="xraydb"):
+        utilities.get_element_f1_f2_dict(10000.0, ["C"])
