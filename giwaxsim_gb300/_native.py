@@ -29,6 +29,7 @@ EXPORTS = [
     "gw_voxel_plan_create", "gw_voxel_plan_destroy", "gw_voxel_set_atoms",
     "gw_voxel_set_shells", "gw_voxel_get_iq32", "gw_debug_convert",
     "gw_voxel_execute", "gw_voxel_capture_graph", "gw_voxel_get_iq",
+    "gw_voxel_set_wait_limit", "gw_set_alloc_fault",
     "gw_voxel_device_iq32", "gw_voxel_get_counts", "gw_voxel_get_sums",
     "gw_voxel_info", "gw_voxel_debug_deposit", "gw_voxel_debug_window",
     "gw_voxelgrid",
@@ -130,6 +131,8 @@ def _declare(lib):
         "gw_debug_convert": ([P, P, i64, P, P, P, P], ctypes.c_int),
         "gw_voxel_execute": ([P], ctypes.c_int),
         "gw_voxel_capture_graph": ([P], ctypes.c_int),
+        "gw_voxel_set_wait_limit": ([P, ctypes.c_uint32], ctypes.c_int),
+        "gw_set_alloc_fault": ([i64], ctypes.c_int),
         "gw_voxel_get_iq": ([P, P, i32], ctypes.c_int),
         "gw_voxel_device_iq32": ([P, ctypes.c_int32, pp], ctypes.c_int),
         "gw_voxel_get_counts": ([P, P], ctypes.c_int),
@@ -317,3 +320,9 @@ def collapse_base(ver, cos_t):
     out = np.empty_like(ver)
     check(lib().gw_collapse_base(ptr(ver), ptr(cos_t), len(ver), ptr(out)))
     return out
+
+
+def set_alloc_fault(after):
+    """Test hook: the (after+1)-th device allocation from now on and every
+    later one fail with GW_ERR_OOM; after < 0 turns the injection off."""
+    check(lib().gw_set_alloc_fault(int(after)))

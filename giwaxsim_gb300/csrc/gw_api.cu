@@ -115,6 +115,12 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
 }
 
 static std::atomic<long long> g_alloc_count{0};
+// gw_set_alloc_fault: allocations numbered from here on fail (-1: off)
+static std::atomic<long long> g_fault_from{-1};
+
+void set_alloc_fault(long long after) {
+  g_fault_from.store(after < 0 ? -1 : g_alloc_count.load() + after);
+}
 
 // Device blocks freed by the library are kept for reuse by an allocation of
 // the same device and size (plans of one shape made again and again: the
@@ -164,7 +170,8 @@ cudaError_t dev_malloc(void **p, size_t bytes) {
     return s ? atoll(s) : -1LL;
   }();
   const long long n = g_alloc_count.fetch_add(1);
-  if (fail_after >= 0 && n >= fail_after) {
+  const long long from = g_fault_from.load();
+  if ((fail_after >= 0 && n >= fail_after) || (from >= 0 && n >= from)) {
     *p = nullptr;
     return cudaErrorMemoryAllocation;
   }
@@ -192,27 +199,33 @@ cudaError_t dev_malloc(void **p, size_t bytes) {
 
 void dev_free(void *p) {
   if (!p) return;
-  std::lock_guard<std::mutex> lk(g_cache_mu);
-  auto it = g_live.find(p);
-  if (it == g_live.end()) {
-    cudaFree(p);
-    return;
+  std::pair<int, size_t> key;
+  bool keep = false;
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_live.find(p);
+    if (it != g_live.end()) {
+      key = it->second;
+      g_live.erase(it);
+      // reserve the block's bytes in the cache before the lock is let go
+      keep = key.second <= cache_cap() - std::min(cache_cap(), g_cached);
+      if (keep) g_cached += key.second;
+    }
   }
-  const std::pair<int, size_t> key = it->second;
-  g_live.erase(it);
-  if (key.second > cache_cap() - std::min(cache_cap(), g_cached)) {
+  if (!keep) {
     cudaFree(p);
     return;
   }
   // work queued on any stream may still use the block: wait, as cudaFree
-  // would, before it can be handed out again
+  // would, before it can be handed out again; outside the lock, so that
+  // other threads' allocations and frees do not wait for this device
   int cur = 0;
   cudaGetDevice(&cur);
   cudaSetDevice(key.first);
   cudaDeviceSynchronize();
   cudaSetDevice(cur);
+  std::lock_guard<std::mutex> lk(g_cache_mu);
   g_cache.emplace(key, p);
-  g_cached += key.second;
 }
 
 int check_device_error(gw_ctx *ctx, const char *where) {
@@ -330,6 +343,11 @@ const char *gw_status_string(int s) {
   return "GW_UNKNOWN";
 }
 
+int gw_set_alloc_fault(int64_t after) {
+  gw::set_alloc_fault(after);
+  return GW_OK;
+}
+
 size_t gw_last_error(char *buf, size_t len) {
   const std::string &m = gw::g_last_error;
   if (buf && len) {
@@ -380,6 +398,10 @@ int gw_ctx_create(int device, gw_ctx **out) {
 
 int gw_ctx_destroy(gw_ctx *c) {
   if (!c) return GW_OK;
+  // contexts may be destroyed on any thread (thread exit, garbage
+  // collection): leave that thread's current device as it was
+  int prev = 0;
+  cudaGetDevice(&prev);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   gw::collect(c);
@@ -396,6 +418,7 @@ int gw_ctx_destroy(gw_ctx *c) {
     }
   }
   delete c;
+  cudaSetDevice(prev);
   return GW_OK;
 }
 

@@ -204,8 +204,11 @@ int fail(int status, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 
 // fault injection for allocation failures: GW_FAIL_ALLOC_AFTER=<n> makes the
-// (n+1)-th device allocation of the process fail with GW_ERR_OOM.
+// (n+1)-th device allocation of the process and every later one fail with
+// GW_ERR_OOM; set_alloc_fault(n) does the same counting from the call (n < 0
+// turns it off).
 cudaError_t dev_malloc(void **p, size_t bytes);
+void set_alloc_fault(long long after);
 void dev_free(void *p);
 // Free the cached device blocks of one device (-1: all devices).
 void release_alloc_cache(int device);

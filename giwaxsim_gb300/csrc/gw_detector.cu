@@ -957,7 +957,9 @@ __global__ void k_detector_noalloc(DetArgs a, const int *n_rot, double *sum) {
   float s = 0.f, c = 0.f;
   int start = 0;
   for (int o = 0; o < a.n_orient; ++o) {
-    const int n = n_rot[o];
+    // counts come from caller memory the host cannot check: clamp them to
+    // the documented 0..3, so that `start` only moves forward by at most 3
+    const int n = min(max(n_rot[o], 0), 3);
     double x = x0, y = y0, z = z0;
     for (int k = 0; k < n; ++k) rotate(a.rot_R + 9 * (start + k), x, y, z);
     start += n;

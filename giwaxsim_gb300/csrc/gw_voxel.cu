@@ -636,10 +636,15 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
   }
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   __syncthreads();
-  bool tile_ok = true;
   if constexpr (TMA) {
-    tile_ok = mbar_wait_bounded(&tile_bar, 0, 1u << 22);
-    if (!tile_ok && threadIdx.x == 0) dev_error(a.err, GW_DEVERR_TIMEOUT);
+    // one decision for the whole block: every thread goes on, or none
+    if (!__syncthreads_and(mbar_wait_bounded(&tile_bar, 0, bn.wait_polls))) {
+      if (threadIdx.x == 0) dev_error(a.err, GW_DEVERR_TIMEOUT);
+      // the loads still in flight must land before the block's shared
+      // memory is released; nothing is binned from this block
+      mbar_wait_bounded(&tile_bar, 0, kTileWaitPolls);
+      return;
+    }
     ColTileLoad<NB> ld{tile, cz.A, rows, nc, m0};
     fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
   } else {
@@ -649,8 +654,6 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
   ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0,
             bn.sstride * (int64_t)(sl / a.n_phi)};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), st);
-  // a load that ran out of time must not land after the block has gone
-  if (TMA && !tile_ok) mbar_wait_bounded(&tile_bar, 0, 1u << 22);
 }
 
 // ---------------------------------------------------------- geometry tables
@@ -1292,7 +1295,8 @@ int enqueue(gw_voxel_plan *P) {
   BinArgs bn{P->d_colofs, P->d_rowofs, P->d_sum, P->d_sumk,
              P->p.accum == GW_ACCUM_KAHAN32, P->k0, P->kz0,
              (float)((double)P->g * (double)P->g),
-             P->n_out > 1 ? (int64_t)P->sum_stride : 0, nullptr, 0};
+             P->n_out > 1 ? (int64_t)P->sum_stride : 0, nullptr, 0,
+             P->wait_polls};
   // Multi-q form factors: one pass per shell with that shell's atom f
   // values and average voxel f, binning only the shell's voxels into the
   // common sums (GW_SHELLS_PER_SHELL); or the reference's single pass with
@@ -1803,6 +1807,17 @@ extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
   return GW_OK;
 }
 
+extern "C" int gw_voxel_set_wait_limit(gw_voxel_plan *P, uint32_t polls) {
+  if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_set_wait_limit: null plan");
+  P->wait_polls = polls;
+  // a captured graph holds the old limit in its kernel arguments
+  if (P->gexec) cudaGraphExecDestroy(P->gexec);
+  if (P->graph) cudaGraphDestroy(P->graph);
+  P->gexec = nullptr;
+  P->graph = nullptr;
+  return GW_OK;
+}
+
 extern "C" int gw_voxel_capture_graph(gw_voxel_plan *P) {
   if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_capture_graph: null plan");
   if (P->n_atoms < 0) return gw::fail(GW_ERR_STATE, "gw_voxel_capture_graph: atoms not set");
@@ -1912,7 +1927,8 @@ extern "C" int gw_voxel_info(gw_voxel_plan *P, int64_t *info, int32_t n) {
   if (!P || !info) return gw::fail(GW_ERR_ARG, "gw_voxel_info: null argument");
   const int64_t v[] = {P->Qc, P->S, P->Ly, P->Lz, P->Nc, P->Nr, P->My, P->Mz,
                        P->y_lo, P->z_lo, P->k0, P->kz0, P->n_slices,
-                       (int64_t)P->bytes, P->graph_kernels};
+                       (int64_t)P->bytes, P->graph_kernels,
+                       (int64_t)P->f1_tma};
   const int k = std::min<int>(n, (int)(sizeof v / sizeof v[0]));
   for (int i = 0; i < k; ++i) info[i] = v[i];
   return k;

@@ -75,7 +75,13 @@ struct BinArgs {
   // shell_k; null = every voxel
   const unsigned short *shell;
   int shell_k;
+  // polls of the column kernel's bounded wait for its tile load
+  unsigned wait_polls;
 };
+
+// Default poll limit of a bounded wait for an asynchronous tile load: far
+// beyond any load's latency (a few microseconds), short of a hang.
+constexpr unsigned kTileWaitPolls = 1u << 22;
 
 // Shell code of a voxel: 2 k + 1 if it lies in shells k and k + 1 (a
 // boundary rounding case), 2 k if in shell k only, kNoShell if in none.
@@ -418,6 +424,7 @@ struct gw_voxel_plan {
   // loads; f1_tma false when the band or the block width does not allow them
   CUtensorMap f1map{};
   bool f1_tma = false;
+  unsigned wait_polls = gwv::kTileWaitPolls;  // gw_voxel_set_wait_limit
   double *d_xyz_s = nullptr;
   float4 *d_xyf_s = nullptr;
   float *d_fz_s = nullptr;

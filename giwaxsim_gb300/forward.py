@@ -372,6 +372,13 @@ class VoxelPlan:
         N.check(N.lib().gw_voxel_capture_graph(self.handle))
         self.graph_captured = True
 
+    def set_wait_limit(self, polls):
+        """Poll limit of the column kernel's bounded tile-load wait (0 makes
+        every wait run out: a test hook for the timeout path).  Drops a
+        captured graph."""
+        N.check(N.lib().gw_voxel_set_wait_limit(self.handle, int(polls)))
+        self.graph_captured = False
+
     def iq(self, out=None):
         """I(q) (Qc, Qc, Qc); (n_struct, Qc, Qc, Qc) for separate structures.
         Without `out`, a fresh array (large ones from the recycled host
@@ -414,7 +421,7 @@ class VoxelPlan:
         n = N.lib().gw_voxel_info(self.handle, N.ptr(v), 16)
         keys = ["crop", "batch", "Ly", "Lz", "Nc", "Nr", "My", "Mz", "y_lo",
                 "z_lo", "k0", "kz0", "n_slices", "device_bytes",
-                "graph_kernels"]
+                "graph_kernels", "col_tma"]
         return dict(zip(keys, (int(x) for x in v[:n])))
 
     def debug_deposit(self, slice_index):

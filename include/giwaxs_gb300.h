@@ -11,10 +11,10 @@
  *   tools/detector.py:278    generate_detector_ints(args)     (per orientation)
  *   tools/detector.py:194    intersect_detector(...)
  *
- * A reference-side binding is plain ctypes; the
- * package giwaxsim_gb300.tools.* is that binding, with the reference's
- * signatures.  All entry points return a gw_status; gw_last_error() gives
- * the message of the last failure on the calling thread.  Pointers are plain
+ * A reference-side binding is plain ctypes; the package
+ * giwaxsim_gb300.tools.* is that binding, with the reference's signatures.
+ * All entry points return a gw_status; gw_last_error() gives the message of
+ * the last failure on the calling thread.  Pointers are plain
  * host or device addresses; a flag says which.  No call allocates pinned
  * host memory or keeps host pointers after it returns.
  *
@@ -47,6 +47,12 @@ const char *gw_status_string(int status);
 /* Copies the calling thread's last error message (NUL-terminated, truncated
  * to len-1).  Returns the full message length. */
 size_t gw_last_error(char *buf, size_t len);
+/* Allocation-failure injection, a test hook with no counterpart in the
+ * reference: from this call on, the (after+1)-th device allocation the
+ * library makes and every later one fail with GW_ERR_OOM, as if the device
+ * were out of memory (after < 0 turns it off).  The environment variable
+ * GW_FAIL_ALLOC_AFTER=n does the same counting from process start. */
+int gw_set_alloc_fault(int64_t after);
 
 /* ---- context ----------------------------------------------------------- */
 typedef struct gw_ctx gw_ctx;
@@ -183,6 +189,15 @@ int gw_voxel_set_shells(gw_voxel_plan *plan, int32_t n_shells, int32_t mode,
  * replay when gw_voxel_capture_graph succeeded). */
 int gw_voxel_execute(gw_voxel_plan *plan);
 int gw_voxel_capture_graph(gw_voxel_plan *plan);
+/* Poll limit of the column kernel's bounded wait for its tile load
+ * (default 4194304 polls, far beyond a load's latency).  When a wait runs
+ * out the block records GW_ERR_TIMEOUT in the context's device error word
+ * (reported by the next gw_ctx_synchronize or result call), waits again
+ * with the default limit for the load in flight, and bins nothing; the
+ * context stays usable.  0 makes every wait run out at once (a test hook
+ * for that path).  Drops a captured graph.  No counterpart in the
+ * reference (a bounded wait of this library's own). */
+int gw_voxel_set_wait_limit(gw_voxel_plan *plan, uint32_t polls);
 /* Results (synchronous).  iq: crop^3 float64, C order (qy,qx,qz); in
  * GW_STRUCTS_SEPARATE mode n_struct such grids back to back.
  * on_device: write to a device pointer instead of host memory. */
@@ -195,9 +210,10 @@ int gw_voxel_device_iq32(gw_voxel_plan *plan, int32_t structure,
 /* Parity hooks: the cropped count and sum grids (float64, crop^3). */
 int gw_voxel_get_counts(gw_voxel_plan *plan, double *counts);
 int gw_voxel_get_sums(gw_voxel_plan *plan, double *sums);
-/* Plan sizes: see GW_INFO_* in the implementation's order:
- * [crop, batch, Ly, Lz, Nc, Nr, My, Mz, y_lo, z_lo, k0, kz0, n_slices,
- *  device_bytes]. Returns the number written. */
+/* Plan sizes, in this order: [crop, batch, Ly, Lz, Nc, Nr, My, Mz, y_lo,
+ * z_lo, k0, kz0, n_slices, device_bytes, graph_kernels, col_tma (1 when
+ * the column kernel loads its tiles by TMA)].  Returns the number written
+ * (at most n). */
 int gw_voxel_info(gw_voxel_plan *plan, int64_t *info, int32_t n);
 /* Deposit indices of one slice (after execute): y,z voxel index per atom of
  * that slice's structure, -1 where the reference's valid_mask drops it
@@ -266,8 +282,10 @@ int gw_detector_debug_indices(gw_detector_plan *plan, int32_t orient,
  * memory budget is reserved up front, or a cudaMalloc/cudaFree stall or
  * failure mid-loop is not acceptable).  Every pointer is caller-owned device
  * memory: iq32 float32 (ny*nx*nz), h_axis/v_axis float64, init_R n_init
- * 3x3 matrices, n_rot int32 per orientation (0..3) with rot_R holding the
- * sum of n_rot matrices, weights float64 per orientation, out float64
+ * 3x3 matrices, n_rot int32 per orientation (0..3; the kernel reads counts
+ * outside that range as the nearest of 0 and 3) with rot_R holding at least
+ * the sum of the counts' matrices (9 doubles each; a shorter rot_R is read
+ * past its end), weights float64 per orientation, out float64
  * (n_v, n_h).  Work is enqueued on `stream` (a cudaStream_t of the current
  * device) and not waited for.  The only scratch is a fixed 8 MiB float64
  * image inside the library, so images are limited to 1024 x 1024 pixels
