@@ -691,7 +691,12 @@ __global__ void k_col_tables(const gw_phi *ph, int g, int k0, int nc,
 // of the separable f0 sum stay in registers; per qz the four z factors come
 // as one float4 (zf0) and C1 from L1.  The count and the f0 factor are exact
 // integers / float32 (the factor's 1e-7 relative error is far inside the
-// tolerance); the sum keeps float64 and takes one float64 multiply.
+// tolerance).  F64: the float64 I(q) (the sum times the factor, one float64
+// multiply); otherwise the float32 I(q) the detector gathers from, computed
+// in float32 from the sum rounded to float (no float64 arithmetic: on this
+// GPU the float64 pipe is the slow one), within about one float32 ulp of
+// the rounded float64 value.
+template <bool F64>
 __global__ void __launch_bounds__(256)
 k_finalize(const double *sum, const float2 *sumk, int kahan,
            const unsigned int *C2, const int *C1, int W, int off, int Qc,
@@ -718,12 +723,16 @@ k_finalize(const double *sum, const float2 *sumk, int kahan,
 #pragma unroll 4
     for (int iz = lane; iz < Qc; iz += 32) {
       const unsigned cnt = c2 * (unsigned)__ldg(C1 + iz + off);
-      double s;
+      double s = 0.0;
+      float s32 = 0.f;
       if (kahan) {
         const float2 sc = sumk[wbase + iz];
-        s = f2d_exact(sc.x) - f2d_exact(sc.y);
-      } else {
+        if (F64) s = f2d_exact(sc.x) - f2d_exact(sc.y);
+        else s32 = sc.x - sc.y;
+      } else if (F64) {
         s = sum[wbase + iz];
+      } else {
+        s32 = d2f_rn(sum[wbase + iz]);
       }
       float scale = cnt ? inv_nstruct / small_u2f(cnt) : 0.f;
       if (use_f0) {
@@ -736,9 +745,8 @@ k_finalize(const double *sum, const float2 *sumk, int kahan,
         const float fq = acc * f0_invz;
         scale *= fq * fq;
       }
-      const double I = s * f2d_exact(scale);
-      out64[obase + iz] = I;
-      out32[obase + iz] = d2f_rn(I);
+      if (F64) out64[obase + iz] = s * f2d_exact(scale);
+      else out32[obase + iz] = s32 * scale;
     }
   }
 }
@@ -746,6 +754,7 @@ k_finalize(const double *sum, const float2 *sumk, int kahan,
 // Batched-mode finalize: the window is the crop (W = Qc, offset 0), so sum
 // and output share the flat index; each thread takes two consecutive voxels
 // with 16-byte loads and stores.  Same per-voxel arithmetic as k_finalize.
+template <bool F64>
 __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan,
                                 const unsigned int *C2, const int *C1, int Qc,
                                 float inv_nstruct, const float *f0tab,
@@ -772,20 +781,22 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
     // sum load and the float64 multiply
     if ((cnt[0] | cnt[1]) == 0u) {
       if (two) {
-        reinterpret_cast<double2 *>(out64)[p] = make_double2(0.0, 0.0);
-        reinterpret_cast<float2 *>(out32)[p] = make_float2(0.f, 0.f);
+        if (F64) reinterpret_cast<double2 *>(out64)[p] = make_double2(0.0, 0.0);
+        else reinterpret_cast<float2 *>(out32)[p] = make_float2(0.f, 0.f);
       } else {
-        out64[i0] = 0.0;
-        out32[i0] = 0.f;
+        if (F64) out64[i0] = 0.0;
+        else out32[i0] = 0.f;
       }
       continue;
     }
     double s[2] = {0.0, 0.0};
+    float s32[2] = {0.f, 0.f};
     if (kahan) {
       for (int e = 0; e < 2; ++e)
         if (e == 0 || two) {
           const float2 sc = sumk[i0 + e];
-          s[e] = f2d_exact(sc.x) - f2d_exact(sc.y);
+          if (F64) s[e] = f2d_exact(sc.x) - f2d_exact(sc.y);
+          else s32[e] = sc.x - sc.y;
         }
     } else if (two) {
       const double2 v = reinterpret_cast<const double2 *>(sum)[p];
@@ -793,7 +804,12 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
     } else {
       s[0] = sum[i0];
     }
+    if (!F64 && !kahan) {
+      s32[0] = d2f_rn(s[0]);
+      s32[1] = d2f_rn(s[1]);
+    }
     double I[2] = {0.0, 0.0};
+    float I32[2] = {0.f, 0.f};
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       if (e == 1 && !two) break;
@@ -811,14 +827,15 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
         const float fq = acc * f0_invz;
         scale *= fq * fq;
       }
-      I[e] = s[e] * f2d_exact(scale);
+      if (F64) I[e] = s[e] * f2d_exact(scale);
+      else I32[e] = s32[e] * scale;
     }
     if (two) {
-      reinterpret_cast<double2 *>(out64)[p] = make_double2(I[0], I[1]);
-      reinterpret_cast<float2 *>(out32)[p] = make_float2(d2f_rn(I[0]), d2f_rn(I[1]));
+      if (F64) reinterpret_cast<double2 *>(out64)[p] = make_double2(I[0], I[1]);
+      else reinterpret_cast<float2 *>(out32)[p] = make_float2(I32[0], I32[1]);
     } else {
-      out64[i0] = I[0];
-      out32[i0] = d2f_rn(I[0]);
+      if (F64) out64[i0] = I[0];
+      else out32[i0] = I32[0];
     }
   }
 }
@@ -862,8 +879,8 @@ __global__ void k_shell_double(const unsigned short *codes, int W, int off,
     const int ix = (int)(line % Qc), iy = (int)(line / Qc);
     const int64_t w = ((int64_t)(iy + off) * W + (ix + off)) * W + (iz + off);
     if (shell_member(codes[w], k)) {
-      out64[i] *= 2.0;
-      out32[i] *= 2.f;
+      if (out64) out64[i] *= 2.0;
+      if (out32) out32[i] *= 2.f;
     }
   }
 }
@@ -1281,6 +1298,60 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
 // Slices per launch of the setup kernels (their grids index slices in y).
 constexpr int kSetupChunk = 32768;
 
+// Average, crop and f0 factor of every I(q) grid the plan produces: the
+// float32 grid the detector reads (f64 false; part of every execute) or the
+// float64 grid (f64 true; made when a caller asks for float64 I(q)).
+int enqueue_finalize(gw_voxel_plan *P, bool f64) {
+  gw_ctx *ctx = P->ctx;
+  cudaStream_t st = ctx->stream;
+  const int K = P->n_shells;
+  const float f0c = (float)P->p.f0_coef[8];
+  const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
+  const float inv_ns = P->p.average == GW_STRUCTS_AVERAGE ? 1.0f / (float)P->n_struct : 1.0f;
+  const int kahan = P->p.accum == GW_ACCUM_KAHAN32;
+  const size_t Qc3 = (size_t)P->Qc * P->Qc * P->Qc;
+  for (int t = 0; t < P->n_out; ++t) {  // one I(q) per structure when separate
+    double *sum = P->d_sum ? P->d_sum + t * P->sum_stride : nullptr;
+    float2 *sumk = P->d_sumk ? P->d_sumk + t * P->sum_stride : nullptr;
+    double *o64 = f64 ? P->d_iq64 + t * P->iq_stride : nullptr;
+    float *o32 = f64 ? nullptr : P->d_iq32 + t * P->iq_stride;
+    if (P->W == P->Qc && P->lo == P->wlo && (int64_t)Qc3 < ((int64_t)1 << 31) - 2) {
+      gw::KTimer tm(ctx, GW_K_FINALIZE);
+      const int64_t pairs = ((int64_t)Qc3 + 1) / 2;
+      const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
+      if (f64)
+        k_finalize_flat<true><<<blocks, 256, 0, st>>>(
+            sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
+            P->p.f0_z > 0, f0c, f0iz, o64, o32);
+      else
+        k_finalize_flat<false><<<blocks, 256, 0, st>>>(
+            sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
+            P->p.f0_z > 0, f0c, f0iz, o64, o32);
+      GW_LAUNCHED(ctx);
+    } else {
+      gw::KTimer tm(ctx, GW_K_FINALIZE);
+      const int blocks = std::min((P->Qc * P->Qc + 7) / 8, 16 * ctx->sm_count);
+      if (f64)
+        k_finalize<true><<<blocks, 256, 0, st>>>(
+            sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
+            inv_ns, P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
+      else
+        k_finalize<false><<<blocks, 256, 0, st>>>(
+            sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
+            inv_ns, P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
+      GW_LAUNCHED(ctx);
+    }
+    if (K > 0 && P->shell_mode == GW_SHELLS_REFERENCE) {
+      gw::KTimer tm(ctx, GW_K_FINALIZE);
+      const int blocks = (int)std::min<int64_t>(((int64_t)Qc3 + 255) / 256, 16 * ctx->sm_count);
+      k_shell_double<<<blocks, 256, 0, st>>>(P->d_shell, P->W, P->lo - P->wlo,
+                                             P->Qc, K - 1, o64, o32);
+      GW_LAUNCHED(ctx);
+    }
+  }
+  return GW_OK;
+}
+
 // Enqueue the whole chain (no synchronisation).
 int enqueue(gw_voxel_plan *P) {
   gw_ctx *ctx = P->ctx;
@@ -1330,41 +1401,7 @@ int enqueue(gw_voxel_plan *P) {
       GW_TRY(col_dispatch(P, ab, cz, bn, s0, n));
     }
   }
-  const float f0c = (float)P->p.f0_coef[8];
-  const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
-  const float inv_ns = P->p.average == GW_STRUCTS_AVERAGE ? 1.0f / (float)P->n_struct : 1.0f;
-  const int kahan = P->p.accum == GW_ACCUM_KAHAN32;
-  const size_t Qc3 = (size_t)P->Qc * P->Qc * P->Qc;
-  for (int t = 0; t < P->n_out; ++t) {  // one I(q) per structure when separate
-    double *sum = P->d_sum ? P->d_sum + t * P->sum_stride : nullptr;
-    float2 *sumk = P->d_sumk ? P->d_sumk + t * P->sum_stride : nullptr;
-    double *o64 = P->d_iq64 + t * P->iq_stride;
-    float *o32 = P->d_iq32 + t * P->iq_stride;
-    if (P->W == P->Qc && P->lo == P->wlo && (int64_t)Qc3 < ((int64_t)1 << 31) - 2) {
-      gw::KTimer tm(ctx, GW_K_FINALIZE);
-      const int64_t pairs = ((int64_t)Qc3 + 1) / 2;
-      const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
-      k_finalize_flat<<<blocks, 256, 0, st>>>(
-          sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
-          P->p.f0_z > 0, f0c, f0iz, o64, o32);
-      GW_LAUNCHED(ctx);
-    } else {
-      gw::KTimer tm(ctx, GW_K_FINALIZE);
-      const int blocks = std::min((P->Qc * P->Qc + 7) / 8, 16 * ctx->sm_count);
-      k_finalize<<<blocks, 256, 0, st>>>(
-          sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
-          inv_ns, P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
-      GW_LAUNCHED(ctx);
-    }
-    if (K > 0 && P->shell_mode == GW_SHELLS_REFERENCE) {
-      gw::KTimer tm(ctx, GW_K_FINALIZE);
-      const int blocks = (int)std::min<int64_t>(((int64_t)Qc3 + 255) / 256, 16 * ctx->sm_count);
-      k_shell_double<<<blocks, 256, 0, st>>>(P->d_shell, P->W, P->lo - P->wlo,
-                                             P->Qc, K - 1, o64, o32);
-      GW_LAUNCHED(ctx);
-    }
-  }
-  return GW_OK;
+  return enqueue_finalize(P, false);
 }
 
 }  // namespace
@@ -1804,6 +1841,7 @@ extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
     GW_TRY(voxel_enqueue_all(P));
   }
   P->executed = true;
+  P->iq64_valid = false;
   return GW_OK;
 }
 
@@ -1845,6 +1883,13 @@ extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) 
   if (!P || !iq) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq: plan not executed");
   const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
+  // the float64 grid is made when asked for: an execute writes only the
+  // float32 grid the detector reads
+  if (!P->iq64_valid) {
+    GW_CUDA(cudaSetDevice(P->ctx->device));
+    GW_TRY(gwv::enqueue_finalize(P, true));
+    P->iq64_valid = true;
+  }
   if (!on_device && P->n_out == 1) {
     GW_TRY(gw::copy_to_host(iq, P->d_iq64, n * sizeof(double), P->ctx->stream));
     return gw::check_device_error(P->ctx, "voxel stage");

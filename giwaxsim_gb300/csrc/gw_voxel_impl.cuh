@@ -442,6 +442,8 @@ struct gw_voxel_plan {
   cudaGraphExec_t gexec = nullptr;
   int64_t graph_kernels = 0;
   bool executed = false;
+  // d_iq64 holds the last execute's float64 I(q) (made on request)
+  bool iq64_valid = false;
   gw_grad_state *grad = nullptr;  // adjoint workspace (gw_grad.cu)
 };
 
@@ -454,6 +456,9 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n);
 // Row transforms of the window rows of slices [s0, s0+n_sl), into d_F1.
 int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  int s0, int n_sl);
+// Average, crop and f0 factor into the float32 (f64 false) or the float64
+// I(q) grids.
+int enqueue_finalize(gw_voxel_plan *P, bool f64);
 // Number of window rows of slices [s0, s0+n).
 int batch_rows(gw_voxel_plan *P, int s0, int n);
 void grad_state_destroy(gw_grad_state *g);
