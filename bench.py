@@ -446,7 +446,8 @@ def run_gb300(args, world, rank, local, pg):
                    "detector_px": w["num_pixels"],
                    "orientations": int(det.n_orient),
                    "l2": "flushed between timed iterations (2x L2 write)",
-                   "plan": info, "tuned": plan.tuned},
+                   "plan": info, "tuned": plan.tuned and dict(
+                       plan.tuned, transform=list(plan.tuned["transform"]))},
         "s_per_detector_image": {
             "batched": ms_per_step / 1e3 / len(items) + det_ms / 1e3,
             "detector_only_s": det_ms / 1e3,

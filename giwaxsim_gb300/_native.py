@@ -19,6 +19,7 @@ GW_VOXEL_BATCHED, GW_VOXEL_PLAIN = 0, 1
 GW_ACCUM_FP64, GW_ACCUM_KAHAN32 = 0, 1
 GW_DEPOSIT_NEAREST, GW_DEPOSIT_BILINEAR = 0, 1
 GW_SHELLS_PER_SHELL, GW_SHELLS_REFERENCE = 1, 2
+GW_TRANSFORM_AUTO, GW_TRANSFORM_STOCKHAM, GW_TRANSFORM_FUSED = 0, 1, 2
 
 # every symbol include/giwaxs_gb300.h declares
 EXPORTS = [
@@ -29,7 +30,7 @@ EXPORTS = [
     "gw_voxel_plan_create", "gw_voxel_plan_destroy", "gw_voxel_set_atoms",
     "gw_voxel_set_shells", "gw_voxel_get_iq32", "gw_debug_convert",
     "gw_voxel_execute", "gw_voxel_capture_graph", "gw_voxel_get_iq",
-    "gw_voxel_set_wait_limit", "gw_set_alloc_fault",
+    "gw_voxel_set_wait_limit", "gw_set_alloc_fault", "gw_voxel_block_variants",
     "gw_voxel_device_iq32", "gw_voxel_get_counts", "gw_voxel_get_sums",
     "gw_voxel_info", "gw_voxel_debug_deposit", "gw_voxel_debug_window",
     "gw_voxelgrid",
@@ -73,7 +74,8 @@ class VoxelParams(ctypes.Structure):
                 ("f0_coef", ctypes.c_double * 9), ("f0_z", ctypes.c_double),
                 ("batch_slices", ctypes.c_int32), ("deposit", ctypes.c_int32),
                 ("fft_y", ctypes.c_int32), ("fft_z", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("transform_y", ctypes.c_int32), ("transform_z", ctypes.c_int32),
+                ("block_variant", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
 
 class Structure(ctypes.Structure):
@@ -133,6 +135,7 @@ def _declare(lib):
         "gw_voxel_capture_graph": ([P], ctypes.c_int),
         "gw_voxel_set_wait_limit": ([P, ctypes.c_uint32], ctypes.c_int),
         "gw_set_alloc_fault": ([i64], ctypes.c_int),
+        "gw_voxel_block_variants": ([], ctypes.c_int32),
         "gw_voxel_get_iq": ([P, P, i32], ctypes.c_int),
         "gw_voxel_device_iq32": ([P, ctypes.c_int32, pp], ctypes.c_int),
         "gw_voxel_get_counts": ([P, P], ctypes.c_int),
@@ -326,3 +329,8 @@ def set_alloc_fault(after):
     """Test hook: the (after+1)-th device allocation from now on and every
     later one fail with GW_ERR_OOM; after < 0 turns the injection off."""
     check(lib().gw_set_alloc_fault(int(after)))
+
+
+def fused_variant_count():
+    """Block shapes of the fused chirp-z kernels (block_variant 0 .. n-1)."""
+    return int(lib().gw_voxel_block_variants())

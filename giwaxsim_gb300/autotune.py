@@ -1,19 +1,26 @@
 """Autotuner for the batched voxel plan.
 
-Three plan choices trade work against efficiency and are picked by timing
-them on the plan's own inputs (graph replays, device events):
+Plan choices that trade work against efficiency, picked by timing them on
+the plan's own inputs (graph replays, device events):
 
-  fft_y, fft_z   chirp-z convolution length per axis: the smallest supported
-                 length >= L+N-1 (2^k, 3*2^k or 5*2^k) and the next two
-                 larger ones (a power of two may run faster per point than a
-                 mixed-radix length that is a little shorter);
-  batch_slices   slices per batch: the L2-sized default, half and double.
+  fft_y, fft_z     chirp-z convolution length per axis: the smallest
+                   supported length >= L+N-1 (2^k, 3*2^k or 5*2^k) and the
+                   next larger one (a power of two may run faster per point
+                   than a mixed-radix length that is a little shorter);
+  transform        kernel family per axis: the fused chirp-z kernel (two
+                   shared-memory exchanges per convolution, where the length
+                   has a fused shape) or the Stockham kernels;
+  batch_slices     slices per batch: the L2-sized default, half and double;
+  block_variant    block shape of the fused kernels: sequences per block and
+                   register cap (occupancy against register spills).
 
-Results are cached per device and plan shape in a JSON file
-($GIWAXSIM_GB300_TUNE_CACHE, default ~/.cache/giwaxsim_gb300/tune.json), so a
-shape is tuned once.  tune() returns the keyword arguments for VoxelPlan.
+The search is staged (rows, then columns, then batch, then block shape),
+each stage keeping the best of the previous ones: the two transform kernels
+are separate launches whose times add.  Results are cached per device and
+plan shape in a JSON file ($GIWAXSIM_GB300_TUNE_CACHE, default
+~/.cache/giwaxsim_gb300/tune.json), so a shape is tuned once.  tune()
+returns the keyword arguments for VoxelPlan.
 """
-import itertools
 import json
 import os
 import threading
@@ -60,19 +67,29 @@ def length_candidates(need, count=2):
 
 def shape_key(ctx, info, n_structures, fill_bkg, smooth, deposit):
     return "|".join(str(x) for x in (
-        ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
+        "v2", ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
         info["n_slices"], n_structures, int(bool(fill_bkg)),
         int(bool(smooth)), deposit))
 
 
+def _as_kwargs(choice):
+    out = dict(choice)
+    out["transform"] = tuple(out["transform"])
+    return out
+
+
 def tune(make_plan, n_structures, fill_bkg=False, smooth=0,
          deposit="nearest", ctx=None, reps=3, use_cache=True, log=None):
-    """Best {fft_y, fft_z, batch_slices} for the plan make_plan(**choice)
-    builds (make_plan must accept those three keywords; 0 = automatic).
-    Every candidate plan gets its atoms, one warm-up, a captured graph and
-    `reps` timed replays."""
+    """Best {fft_y, fft_z, batch_slices, transform, block_variant} for the
+    plan make_plan(**choice) builds (make_plan must accept those keywords;
+    0 / "auto" = the defaults).  Every candidate plan gets its atoms, one
+    warm-up, a captured graph and `reps` timed replays; a candidate the
+    library refuses (a fused family for a length without a fused shape) is
+    skipped."""
     ctx = ctx or N.default_context()
-    base = make_plan(fft_y=0, fft_z=0, batch_slices=0)
+    default = dict(fft_y=0, fft_z=0, batch_slices=0,
+                   transform=("auto", "auto"), block_variant=0)
+    base = make_plan(**_as_kwargs(default))
     try:
         info = base.info()
     finally:
@@ -82,15 +99,21 @@ def tune(make_plan, n_structures, fill_bkg=False, smooth=0,
         with _lock:
             hit = _load().get(key)
         if hit:
-            return dict(hit["choice"])
-    ys = length_candidates(info["Ly"] + info["Nc"] - 1)
-    zs = length_candidates(info["Lz"] + info["Nr"] - 1)
-    S = info["batch"]
-    batches = sorted({S, max(1, S // 2), min(info["n_slices"], 2 * S, 4096)})
-    results = []
-    for fy, fz, b in itertools.product(ys, zs, batches):
-        choice = dict(fft_y=fy, fft_z=fz, batch_slices=b)
-        plan = make_plan(**choice)
+            return _as_kwargs(hit["choice"])
+
+    timed = {}
+
+    def time_choice(choice):
+        k = json.dumps(choice, sort_keys=True)
+        if k in timed:
+            return timed[k]
+        try:
+            plan = make_plan(**_as_kwargs(choice))
+        except N.GwError as e:
+            if e.status != N.GW_ERR_ARG:
+                raise
+            timed[k] = None
+            return None
         try:
             plan.set_atoms()
             plan.execute()
@@ -100,17 +123,41 @@ def tune(make_plan, n_structures, fill_bkg=False, smooth=0,
             ms = ctx.time_ms(plan.execute, reps)
         finally:
             plan.close()
-        results.append((ms, choice))
+        timed[k] = ms
         if log:
             log("tune %s: %.4f ms" % (choice, ms))
-    ms, best = min(results, key=lambda r: r[0])
+        return ms
+
+    def best_of(cands):
+        res = [(time_choice(c), c) for c in cands]
+        res = [r for r in res if r[0] is not None]
+        return min(res, key=lambda r: r[0])
+
+    families = ("fused", "stockham")
+    best = dict(default, fft_y=info["My"], fft_z=info["Mz"],
+                batch_slices=info["batch"])
+    default_ms = time_choice(best)
+    # rows: length x kernel family
+    ys = length_candidates(info["Ly"] + info["Nc"] - 1)
+    _, best = best_of([dict(best, fft_y=m, transform=[fam, best["transform"][1]])
+                       for m in ys for fam in families])
+    # columns
+    zs = length_candidates(info["Lz"] + info["Nr"] - 1)
+    _, best = best_of([dict(best, fft_z=m, transform=[best["transform"][0], fam])
+                       for m in zs for fam in families])
+    # slices per batch
+    S = info["batch"]
+    batches = sorted({S, max(1, S // 2), min(info["n_slices"], 2 * S, 4096)})
+    _, best = best_of([dict(best, batch_slices=b) for b in batches])
+    # block shape of the fused kernels
+    if "fused" in best["transform"]:
+        _, best = best_of([dict(best, block_variant=v)
+                           for v in range(N.fused_variant_count())])
+    ms = time_choice(best)
     if use_cache:
         with _lock:
             cache = _load()
-            cache[key] = {"choice": best, "ms": ms,
-                          "default_ms": next(m for m, c in results
-                                             if c == dict(fft_y=ys[0], fft_z=zs[0],
-                                                          batch_slices=S)),
-                          "candidates": len(results)}
+            cache[key] = {"choice": best, "ms": ms, "default_ms": default_ms,
+                          "candidates": len(timed)}
             _store(cache)
-    return dict(best)
+    return _as_kwargs(best)

@@ -269,15 +269,15 @@ __device__ __forceinline__ void dev_error(int *err, int code) {
 }
 
 // float2 complex helpers
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
   return make_float2(a.x + b.x, a.y + b.y);
 }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
   return make_float2(a.x - b.x, a.y - b.y);
 }
-__device__ __forceinline__ float2 cscale(float2 a, float s) {
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) {
   return make_float2(a.x * s, a.y * s);
 }

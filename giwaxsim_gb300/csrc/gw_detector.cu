@@ -286,7 +286,7 @@ struct PlaneArgs {
 struct PlaneOrient {
   float4 u, v, e;
 };
-constexpr int kPlTW = 32, kPlTH = 32, kPlThreads = 256;
+constexpr int kPlTW = 32, kPlTH = 32, kPlThreads = 512;
 constexpr size_t kPlaneSmemMax = 200 * 1024;
 
 __global__ void k_plane_extract(DetArgs a, PlaneArgs pa, float *P) {

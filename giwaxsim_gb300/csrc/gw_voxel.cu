@@ -422,18 +422,6 @@ struct RowStore {
   }
 };
 
-// Add w * fv at grid column i of a shared-memory row.
-__device__ __forceinline__ void deposit_at(const SliceArgs &a, float2 *row,
-                                           int i, float2 fv, float w) {
-  const int yy = window_col(a, i);
-  if (yy < a.Ly) {
-    atomicAdd(&row[yy].x, fv.x * w);
-    atomicAdd(&row[yy].y, fv.y * w);
-  } else {
-    dev_error(a.err, GW_DEVERR_BOX);
-  }
-}
-
 template <int M, bool BIL>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
 k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
@@ -444,93 +432,14 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   extern __shared__ float2 smem[];
   float2 *tw = smem;
   float2 *buf = smem + TWL;
-  __shared__ int r_lo[NB], r_mid[NB], r_cnt[NB + 1], r_slot[NB];
-  __shared__ RowConst r_k[NB];
-  __shared__ DepRow r_d[NB];
+  __shared__ RowShared<NB> rs;
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
-  // only the window columns [0, L) are deposited into and read back
-  for (int f = 0; f < NB; ++f)
-    for (int n = threadIdx.x; n < cz.L; n += NT) buf[f * LDM + n] = make_float2(0.f, 0.f);
   const int row0 = blockIdx.x * NB;
-  // the block's rows: slot, window row and atom range, one thread per row
-  // (independent loads), then a scan of the atom counts
-  static_assert(NB <= 32, "one warp sets the rows up");
-  if (threadIdx.x < NB) {
-    const int f = threadIdx.x, row = row0 + f;
-    int lo = 0, mid = 0, hi = 0, slot = 0, zz = 0;
-    if (row < n_rows) {
-      row_slot(a, slice0, n_sl, row, slot, zz);
-      const int sl = slice0 + slot, t = sl / a.n_phi;
-      if (a.ext[sl].y < 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
-      row_atoms(a, t, zz, lo, mid, hi);
-    }
-    r_lo[f] = lo;
-    r_mid[f] = mid;
-    r_cnt[f + 1] = hi - lo;
-    r_slot[f] = slot;
-    if (row < n_rows) {
-      r_k[f] = row_const(a, slot, slice0 + slot, zz);
-      r_d[f] = dep_row(a, slice0 + slot);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    r_cnt[0] = 0;
-    for (int f = 0; f < NB; ++f) r_cnt[f + 1] += r_cnt[f];
-  }
-  __syncthreads();
-  const int total = r_cnt[NB];
-  for (int i = threadIdx.x; i < total; i += NT) {
-    int f = 0;
-    while (f + 1 < NB && i >= r_cnt[f + 1]) ++f;
-    const int at = r_lo[f] + (i - r_cnt[f]);
-    const int sl = slice0 + r_slot[f];
-    if constexpr (!BIL) {
-      int yy;
-      const float4 q = a.xyf_s[at];
-      if (deposit_column(a, r_d[f], make_float2(q.x, q.y), at, yy)) {
-        if (yy < a.Ly) {
-          atomicAdd(&buf[f * LDM + yy].x, q.z);
-          atomicAdd(&buf[f * LDM + yy].y, q.w);
-        } else {
-          dev_error(a.err, GW_DEVERR_BOX);
-        }
-      }
-    } else {
-      int i0;
-      float fu;
-      if (bilinear_column(a, at, sl, i0, fu)) {
-        const float fz = a.fz_s[at];
-        const float wz = at >= r_mid[f] ? 1.f - fz : fz;
-        const float4 q = a.xyf_s[at];
-        const float2 fv = make_float2(q.z, q.w);
-        deposit_at(a, buf + f * LDM, i0, fv, wz * (1.f - fu));
-        if (i0 + 1 < a.g) deposit_at(a, buf + f * LDM, i0 + 1, fv, wz * fu);
-      }
-    }
-  }
-  __syncthreads();
-  RowLoad<M> ld{&a, &cz, buf, r_k, row0, n_rows};
+  deposit_rows<NB, NT, BIL>(a, cz.L, slice0, n_sl, n_rows, row0, buf, LDM, rs);
+  RowLoad<M> ld{&a, &cz, buf, rs.k, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false>(buf, tw, nullptr, ld, NoStore());
   RowStore stv{cz.B, F1, row0, n_rows, nc_out};
   fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), stv);
-}
-
-__device__ __forceinline__ void kahan_add(float2 *addr, float x) {
-  unsigned long long *p = reinterpret_cast<unsigned long long *>(addr);
-  unsigned long long old = *p, assumed;
-  do {
-    assumed = old;
-    float2 sc;
-    memcpy(&sc, &assumed, 8);
-    const float y = x - sc.y;
-    const float t = sc.x + y;
-    const float c = (t - sc.x) - y;
-    float2 nw = make_float2(t, c);
-    unsigned long long nv;
-    memcpy(&nv, &nw, 8);
-    old = atomicCAS(p, assumed, nv);
-  } while (old != assumed);
 }
 
 // Column stage: NB columns of one slice, transformed along z.  The forward
@@ -558,12 +467,6 @@ struct ColTileLoad {
   }
 };
 
-// Rows per TMA box for transform length M: a divisor of M of at most 256,
-// so the boxes covering a slice's rows (at most M) fit the FFT buffer.
-__host__ __device__ constexpr int tma_box_rows(int M) {
-  return M % 256 == 0 ? 256 : M % 192 == 0 ? 192 : M % 160 == 0 ? 160
-                                                                 : M % 128 == 0 ? 128 : 64;
-}
 // The box's inner extent (NB complex values) must be a multiple of 16 bytes.
 template <int M>
 __host__ __device__ constexpr bool col_tma_ok() {
@@ -838,6 +741,85 @@ __global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan
       else out32[i0] = I32[0];
     }
   }
+}
+
+// The step's float32 finalize over the flat crop (window = crop) for the
+// float64 sums: four consecutive voxels per thread and iteration, their
+// count factors, sums (two 16-byte loads) and f0 factors loaded together,
+// one 16-byte store; the same per-voxel arithmetic as
+// k_finalize_flat<false>.  n4 = Qc^3 / 4 quads; the caller handles no tail
+// (k_finalize_flat<false> covers the last Qc^3 mod 4 voxels).
+__global__ void __launch_bounds__(256)
+k_finalize32_quad(const double *__restrict__ sum, const unsigned int *__restrict__ C2,
+                  const int *__restrict__ C1, int Qc, float inv_nstruct,
+                  const float *__restrict__ f0tab, const float4 *__restrict__ zf0,
+                  int use_f0, float f0_c, float f0_invz, float *__restrict__ out32,
+                  int64_t n4) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i0 = 4 * q;
+    int line = (int)(i0 / Qc), iz = (int)(i0 - (int64_t)line * Qc);
+    int lines[4], izs[4];
+    unsigned cnt[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      lines[e] = line;
+      izs[e] = iz;
+      cnt[e] = __ldg(C2 + line) * (unsigned)__ldg(C1 + iz);
+      if (++iz == Qc) { iz = 0; ++line; }
+    }
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((cnt[0] | cnt[1] | cnt[2] | cnt[3]) != 0u) {
+      const double2 a = reinterpret_cast<const double2 *>(sum)[2 * q];
+      const double2 b = reinterpret_cast<const double2 *>(sum)[2 * q + 1];
+      const float s[4] = {d2f_rn(a.x), d2f_rn(a.y), d2f_rn(b.x), d2f_rn(b.y)};
+      float I[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        float scale = cnt[e] ? inv_nstruct / small_u2f(cnt[e]) : 0.f;
+        if (use_f0) {
+          const int iy = lines[e] / Qc, ix = lines[e] - iy * Qc;
+          const float4 z = __ldg(zf0 + izs[e]);
+          float acc = f0_c;
+          acc += (__ldg(f0tab + ix) * __ldg(f0tab + Qc + iy)) * z.x;
+          acc += (__ldg(f0tab + 3 * Qc + ix) * __ldg(f0tab + 4 * Qc + iy)) * z.y;
+          acc += (__ldg(f0tab + 6 * Qc + ix) * __ldg(f0tab + 7 * Qc + iy)) * z.z;
+          acc += (__ldg(f0tab + 9 * Qc + ix) * __ldg(f0tab + 10 * Qc + iy)) * z.w;
+          const float fq = acc * f0_invz;
+          scale *= fq * fq;
+        }
+        I[e] = s[e] * scale;
+      }
+      o = make_float4(I[0], I[1], I[2], I[3]);
+    }
+    reinterpret_cast<float4 *>(out32)[q] = o;
+  }
+}
+
+// The last (at most three) voxels of the flat float32 finalize after the
+// quads, one thread each.
+__global__ void k_finalize_tail32(const double *sum, const unsigned int *C2,
+                                  const int *C1, int Qc, float inv_nstruct,
+                                  const float *f0tab, const float4 *zf0, int use_f0,
+                                  float f0_c, float f0_invz, float *out32,
+                                  int64_t begin, int64_t end) {
+  const int64_t i = begin + threadIdx.x;
+  if (i >= end) return;
+  const int line = (int)(i / Qc), iz = (int)(i - (int64_t)line * Qc);
+  const unsigned cnt = C2[line] * (unsigned)C1[iz];
+  float scale = cnt ? inv_nstruct / small_u2f(cnt) : 0.f;
+  if (use_f0) {
+    const int iy = line / Qc, ix = line - iy * Qc;
+    const float4 z = zf0[iz];
+    float acc = f0_c;
+    acc += (f0tab[ix] * f0tab[Qc + iy]) * z.x;
+    acc += (f0tab[3 * Qc + ix] * f0tab[4 * Qc + iy]) * z.y;
+    acc += (f0tab[6 * Qc + ix] * f0tab[7 * Qc + iy]) * z.z;
+    acc += (f0tab[9 * Qc + ix] * f0tab[10 * Qc + iy]) * z.w;
+    const float fq = acc * f0_invz;
+    scale *= fq * fq;
+  }
+  out32[i] = cnt ? d2f_rn(sum[i]) * scale : 0.f;
 }
 
 // Shell code of every window voxel (voxelgrids.py:651-652, :659-664, :706):
@@ -1194,10 +1176,12 @@ int col_map_dispatch(gw_voxel_plan *P) { GW_DISPATCH_M(P->Mz, col_map_create, P)
 
 int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  int s0, int n) {
+  if (P->fused_y) return fused_row_dispatch(P, a, cz, s0, n);
   GW_DISPATCH_M(P->My, launch_row, P, a, cz, s0, n)
 }
 int col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  const BinArgs &bn, int s0, int n) {
+  if (P->fused_z) return fused_col_dispatch(P, a, cz, bn, s0, n);
   GW_DISPATCH_M(P->Mz, launch_col, P, a, cz, bn, s0, n)
 }
 
@@ -1319,15 +1303,33 @@ int enqueue_finalize(gw_voxel_plan *P, bool f64) {
       gw::KTimer tm(ctx, GW_K_FINALIZE);
       const int64_t pairs = ((int64_t)Qc3 + 1) / 2;
       const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
-      if (f64)
+      if (f64) {
         k_finalize_flat<true><<<blocks, 256, 0, st>>>(
             sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
             P->p.f0_z > 0, f0c, f0iz, o64, o32);
-      else
+        GW_LAUNCHED(ctx);
+      } else if (!kahan) {
+        // quads of voxels, then the Qc^3 mod 4 last ones by the pair kernel
+        // (it starts at an even voxel: its pairs from that one on)
+        const int64_t n4 = (int64_t)Qc3 / 4;
+        const int qb = (int)std::min<int64_t>((n4 + 255) / 256, 8 * ctx->sm_count);
+        k_finalize32_quad<<<std::max(qb, 1), 256, 0, st>>>(
+            sum, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
+            P->p.f0_z > 0, f0c, f0iz, o32, n4);
+        GW_LAUNCHED(ctx);
+        const int64_t done = 4 * n4;
+        if (done < (int64_t)Qc3) {
+          k_finalize_tail32<<<1, 32, 0, st>>>(sum, P->d_C2, P->d_C1, P->Qc, inv_ns,
+                                               P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c,
+                                               f0iz, o32, done, (int64_t)Qc3);
+          GW_LAUNCHED(ctx);
+        }
+      } else {
         k_finalize_flat<false><<<blocks, 256, 0, st>>>(
             sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
             P->p.f0_z > 0, f0c, f0iz, o64, o32);
-      GW_LAUNCHED(ctx);
+        GW_LAUNCHED(ctx);
+      }
     } else {
       gw::KTimer tm(ctx, GW_K_FINALIZE);
       const int blocks = std::min((P->Qc * P->Qc + 7) / 8, 16 * ctx->sm_count);
@@ -1420,6 +1422,9 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: invalid geometry");
   if (p->smooth < 0)
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: smooth must be >= 0");
+  if (p->block_variant < 0 || p->block_variant >= gwv::fused_variant_count())
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: block_variant must be 0.." +
+                                    std::to_string(gwv::fused_variant_count() - 1));
   if (p->deposit != GW_DEPOSIT_NEAREST && p->deposit != GW_DEPOSIT_BILINEAR)
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: unknown deposit mode");
   if (p->deposit == GW_DEPOSIT_BILINEAR && p->mode == GW_VOXEL_PLAIN)
@@ -1611,6 +1616,19 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
                                 f0tab[8 * P->Qc + k], f0tab[11 * P->Qc + k]));
   CztTables ty = make_czt(g, P->y_lo, P->Ly, P->k0, P->Nc, P->My);
   CztTables tz = make_czt(g, P->z_lo, P->Lz, P->kz0, P->Nr, P->Mz);
+  // fused chirp-z kernels where the length has a fused shape, unless the
+  // caller asks for the Stockham kernels
+  P->fused_y = p->transform_y != GW_TRANSFORM_STOCKHAM && fused_supported(P->My);
+  P->fused_z = p->transform_z != GW_TRANSFORM_STOCKHAM && fused_supported(P->Mz);
+  if ((p->transform_y == GW_TRANSFORM_FUSED && !P->fused_y) ||
+      (p->transform_z == GW_TRANSFORM_FUSED && !P->fused_z)) {
+    const int m = (p->transform_y == GW_TRANSFORM_FUSED && !P->fused_y) ? P->My : P->Mz;
+    delete P;
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: no fused transform of length " +
+                                    std::to_string(m));
+  }
+  const std::vector<float2> fty = P->fused_y ? fused_twiddles(P->My) : std::vector<float2>();
+  const std::vector<float2> ftz = P->fused_z ? fused_twiddles(P->Mz) : std::vector<float2>();
   const size_t W3 = (size_t)P->W * P->W * P->W;
   const size_t Qc3 = (size_t)P->Qc * P->Qc * P->Qc;
   P->sum_stride = (W3 + 3) & ~(size_t)3;
@@ -1626,6 +1644,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = upload(&P->d_By, ty.B, &B)) || (st = upload(&P->d_twy, ty.tw, &B)) ||
       (st = upload(&P->d_Az, tz.A, &B)) || (st = upload(&P->d_Hz, tz.H, &B)) ||
       (st = upload(&P->d_Bz, tz.B, &B)) || (st = upload(&P->d_twz, tz.tw, &B)) ||
+      (st = upload(&P->d_fty, fty, &B)) || (st = upload(&P->d_ftz, ftz, &B)) ||
       (st = alloc(&P->d_zmin, n_struct, &B)) ||
       (st = alloc(&P->d_ymin, P->n_slices, &B)) ||
       (st = alloc(&P->d_ext, P->n_slices, &B)) ||
@@ -1689,7 +1708,8 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_sconst, P->d_xyz_s, P->d_xyf_s, P->d_fz_s,
                   P->d_perm, P->d_ybnd, P->d_roff, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
-                  P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0};
+                  P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0,
+                  P->d_fty, P->d_ftz};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -1845,6 +1865,8 @@ extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
   return GW_OK;
 }
 
+extern "C" int32_t gw_voxel_block_variants(void) { return gwv::fused_variant_count(); }
+
 extern "C" int gw_voxel_set_wait_limit(gw_voxel_plan *P, uint32_t polls) {
   if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_set_wait_limit: null plan");
   P->wait_polls = polls;
@@ -1973,7 +1995,8 @@ extern "C" int gw_voxel_info(gw_voxel_plan *P, int64_t *info, int32_t n) {
   const int64_t v[] = {P->Qc, P->S, P->Ly, P->Lz, P->Nc, P->Nr, P->My, P->Mz,
                        P->y_lo, P->z_lo, P->k0, P->kz0, P->n_slices,
                        (int64_t)P->bytes, P->graph_kernels,
-                       (int64_t)P->f1_tma};
+                       (int64_t)P->f1_tma, (int64_t)P->fused_y,
+                       (int64_t)P->fused_z};
   const int k = std::min<int>(n, (int)(sizeof v / sizeof v[0]));
   for (int i = 0; i < k; ++i) info[i] = v[i];
   return k;

@@ -337,6 +337,125 @@ __device__ __forceinline__ void row_atoms(const SliceArgs &a, int t, int zz,
   lo = (a.bil && zi > 0) ? rs[zi - 1] : mid;
 }
 
+// Add w * fv at grid column i of a shared-memory row.
+__device__ __forceinline__ void deposit_at(const SliceArgs &a, float2 *row,
+                                           int i, float2 fv, float w) {
+  const int yy = window_col(a, i);
+  if (yy < a.Ly) {
+    atomicAdd(&row[yy].x, fv.x * w);
+    atomicAdd(&row[yy].y, fv.y * w);
+  } else {
+    dev_error(a.err, GW_DEVERR_BOX);
+  }
+}
+
+// Per-row state of a row-transform block (shared memory).
+template <int NB>
+struct RowShared {
+  int lo[NB], mid[NB], cnt[NB + 1], slot[NB];
+  RowConst k[NB];
+  DepRow d[NB];
+};
+
+// The deposit of a row-transform block (voxelgrids.py:319-341: shift,
+// floor division, valid mask, np.add.at): NB window rows starting at row0
+// of the batch, row f into buf[f * ldm + 0 .. L) (zeroed first), by shared
+// atomics.  Sets up rs (slot, window row, atom range and constants of every
+// row) and leaves the block synchronised.
+template <int NB, int NT, bool BIL>
+__device__ __forceinline__ void deposit_rows(const SliceArgs &a, int L,
+                                             int slice0, int n_sl, int n_rows,
+                                             int row0, float2 *buf, int ldm,
+                                             RowShared<NB> &rs) {
+  // only the window columns [0, L) are deposited into and read back
+  for (int f = 0; f < NB; ++f)
+    for (int n = threadIdx.x; n < L; n += NT) buf[f * ldm + n] = make_float2(0.f, 0.f);
+  // the block's rows: slot, window row and atom range, one thread per row
+  // (independent loads), then a scan of the atom counts
+  static_assert(NB <= 32, "one warp sets the rows up");
+  if (threadIdx.x < NB) {
+    const int f = threadIdx.x, row = row0 + f;
+    int lo = 0, mid = 0, hi = 0, slot = 0, zz = 0;
+    if (row < n_rows) {
+      row_slot(a, slice0, n_sl, row, slot, zz);
+      const int sl = slice0 + slot, t = sl / a.n_phi;
+      if (a.ext[sl].y < 0) dev_error(a.err, GW_DEVERR_NO_ATOMS);
+      row_atoms(a, t, zz, lo, mid, hi);
+    }
+    rs.lo[f] = lo;
+    rs.mid[f] = mid;
+    rs.cnt[f + 1] = hi - lo;
+    rs.slot[f] = slot;
+    if (row < n_rows) {
+      rs.k[f] = row_const(a, slot, slice0 + slot, zz);
+      rs.d[f] = dep_row(a, slice0 + slot);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    rs.cnt[0] = 0;
+    for (int f = 0; f < NB; ++f) rs.cnt[f + 1] += rs.cnt[f];
+  }
+  __syncthreads();
+  const int total = rs.cnt[NB];
+  for (int i = threadIdx.x; i < total; i += NT) {
+    int f = 0;
+    while (f + 1 < NB && i >= rs.cnt[f + 1]) ++f;
+    const int at = rs.lo[f] + (i - rs.cnt[f]);
+    const int sl = slice0 + rs.slot[f];
+    if constexpr (!BIL) {
+      int yy;
+      const float4 q = a.xyf_s[at];
+      if (deposit_column(a, rs.d[f], make_float2(q.x, q.y), at, yy)) {
+        if (yy < a.Ly) {
+          atomicAdd(&buf[f * ldm + yy].x, q.z);
+          atomicAdd(&buf[f * ldm + yy].y, q.w);
+        } else {
+          dev_error(a.err, GW_DEVERR_BOX);
+        }
+      }
+    } else {
+      int i0;
+      float fu;
+      if (bilinear_column(a, at, sl, i0, fu)) {
+        const float fz = a.fz_s[at];
+        const float wz = at >= rs.mid[f] ? 1.f - fz : fz;
+        const float4 q = a.xyf_s[at];
+        const float2 fv = make_float2(q.z, q.w);
+        deposit_at(a, buf + f * ldm, i0, fv, wz * (1.f - fu));
+        if (i0 + 1 < a.g) deposit_at(a, buf + f * ldm, i0 + 1, fv, wz * fu);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Kahan-compensated float32 accumulation into a (sum, compensation) pair,
+// as one 64-bit compare-and-swap.
+__device__ __forceinline__ void kahan_add(float2 *addr, float x) {
+  unsigned long long *p = reinterpret_cast<unsigned long long *>(addr);
+  unsigned long long old = *p, assumed;
+  do {
+    assumed = old;
+    float2 sc;
+    memcpy(&sc, &assumed, 8);
+    const float y = x - sc.y;
+    const float t = sc.x + y;
+    const float c = (t - sc.x) - y;
+    float2 nw = make_float2(t, c);
+    unsigned long long nv;
+    memcpy(&nv, &nw, 8);
+    old = atomicCAS(p, assumed, nv);
+  } while (old != assumed);
+}
+
+// Rows per TMA box for transform length M: a divisor of M of at most 256,
+// so the boxes covering a slice's rows (at most M) fit the FFT buffer.
+__host__ __device__ constexpr int tma_box_rows(int M) {
+  return M % 256 == 0 ? 256 : M % 192 == 0 ? 192 : M % 160 == 0 ? 160
+                                                                 : M % 128 == 0 ? 128 : 64;
+}
+
 // ------------------------------------------------------------ host helpers
 struct CztTables {
   std::vector<float2> A, H, B, tw;
@@ -425,6 +544,9 @@ struct gw_voxel_plan {
   CUtensorMap f1map{};
   bool f1_tma = false;
   unsigned wait_polls = gwv::kTileWaitPolls;  // gw_voxel_set_wait_limit
+  // fused chirp-z kernels (gw_czt2.cuh) along y / z, with their twiddles
+  bool fused_y = false, fused_z = false;
+  float2 *d_fty = nullptr, *d_ftz = nullptr;
   double *d_xyz_s = nullptr;
   float4 *d_xyf_s = nullptr;
   float *d_fz_s = nullptr;
@@ -456,6 +578,16 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n);
 // Row transforms of the window rows of slices [s0, s0+n_sl), into d_F1.
 int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  int s0, int n_sl);
+// Fused chirp-z kernels (gw_czt2_row.cu, gw_czt2_col.cu): lengths with a
+// fused shape, the number of block shapes, their twiddle tables, and the
+// launches for the plan's My / Mz.
+bool fused_supported(int M);
+int fused_variant_count();
+std::vector<float2> fused_twiddles(int M);
+int fused_row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                       int s0, int n);
+int fused_col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                       const BinArgs &bn, int s0, int n);
 // Average, crop and f0 factor into the float32 (f64 false) or the float64
 // I(q) grids.
 int enqueue_finalize(gw_voxel_plan *P, bool f64);

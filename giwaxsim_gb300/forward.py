@@ -219,7 +219,8 @@ class VoxelPlan:
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
                  batch_slices=0, constants=None, deposit="nearest", fft_y=0,
-                 fft_z=0, tune=False, ctx=None, create=True, ranges=None):
+                 fft_z=0, tune=False, ctx=None, create=True, ranges=None,
+                 transform="auto", block_variant=0):
         self.geom = geom
         self.handle = None
         self.reused = False          # handed out again by PlanCache
@@ -241,6 +242,8 @@ class VoxelPlan:
                                        deposit, ctx=self.ctx)
             fft_y, fft_z = self.tuned["fft_y"], self.tuned["fft_z"]
             batch_slices = self.tuned["batch_slices"]
+            transform = self.tuned["transform"]
+            block_variant = self.tuned["block_variant"]
         self.phis = geom.auto_phis if phis is None else np.asarray(phis, np.float64)
         if len(self.phis) < 1:
             raise ValueError("at least one phi is required")
@@ -296,6 +299,12 @@ class VoxelPlan:
         p.deposit = {"nearest": N.GW_DEPOSIT_NEAREST,
                      "bilinear": N.GW_DEPOSIT_BILINEAR}[deposit]
         p.fft_y, p.fft_z = int(fft_y), int(fft_z)
+        # one kernel family for both axes, or (rows, columns)
+        ty, tz = (transform, transform) if isinstance(transform, str) else transform
+        fam = {"auto": N.GW_TRANSFORM_AUTO, "stockham": N.GW_TRANSFORM_STOCKHAM,
+               "fused": N.GW_TRANSFORM_FUSED}
+        p.transform_y, p.transform_z = fam[ty], fam[tz]
+        p.block_variant = int(block_variant)
         self.params = p
         self.Qc = geom.crop_hi - geom.crop_lo + 1
         if create:
@@ -417,11 +426,11 @@ class VoxelPlan:
         return out
 
     def info(self):
-        v = np.zeros(16, dtype=np.int64)
-        n = N.lib().gw_voxel_info(self.handle, N.ptr(v), 16)
+        v = np.zeros(24, dtype=np.int64)
+        n = N.lib().gw_voxel_info(self.handle, N.ptr(v), 24)
         keys = ["crop", "batch", "Ly", "Lz", "Nc", "Nr", "My", "Mz", "y_lo",
                 "z_lo", "k0", "kz0", "n_slices", "device_bytes",
-                "graph_kernels", "col_tma"]
+                "graph_kernels", "col_tma", "fused_y", "fused_z"]
         return dict(zip(keys, (int(x) for x in v[:n])))
 
     def debug_deposit(self, slice_index):

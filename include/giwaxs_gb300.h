@@ -102,6 +102,8 @@ enum { GW_STRUCTS_SUM = 0, GW_STRUCTS_AVERAGE = 1, GW_STRUCTS_SEPARATE = 2 };
 enum { GW_DEPOSIT_NEAREST = 0, GW_DEPOSIT_BILINEAR = 1 };
 enum { GW_SHELLS_PER_SHELL = 1, GW_SHELLS_REFERENCE = 2 };
 
+enum { GW_TRANSFORM_AUTO = 0, GW_TRANSFORM_STOCKHAM = 1, GW_TRANSFORM_FUSED = 2 };
+
 typedef struct gw_voxel_params {
   int32_t grid_size;    /* g = ceil(2pi/(dq*r))          comparison.py:710 */
   double r_voxel_size;  /* r                                               */
@@ -131,7 +133,19 @@ typedef struct gw_voxel_params {
   int32_t fft_y, fft_z; /* chirp-z convolution lengths along y and z: 0 =
                            the smallest supported length >= L+N-1; else one
                            of 2^k, 3*2^k, 5*2^k in [64, 8192] and >= L+N-1 */
-  int32_t reserved[4];
+  int32_t transform_y, transform_z; /* kernel family of the row (y) and
+                           column (z) chirp-z transforms.
+                           GW_TRANSFORM_AUTO: the fused kernel where the
+                           length has a fused shape (two shared-memory
+                           exchanges per convolution), the Stockham kernels
+                           elsewhere; GW_TRANSFORM_STOCKHAM: Stockham;
+                           GW_TRANSFORM_FUSED: fused (GW_ERR_ARG if the
+                           length has no fused shape)                      */
+  int32_t block_variant; /* block shape of the fused kernels (sequences per
+                           block, register cap), 0 .. count-1 with the count
+                           from gw_voxel_block_variants(); an autotuner
+                           picks it by timing; 0 = the default shape       */
+  int32_t reserved[1];
 } gw_voxel_params;
 
 typedef struct gw_structure {
@@ -198,6 +212,9 @@ int gw_voxel_capture_graph(gw_voxel_plan *plan);
  * for that path).  Drops a captured graph.  No counterpart in the
  * reference (a bounded wait of this library's own). */
 int gw_voxel_set_wait_limit(gw_voxel_plan *plan, uint32_t polls);
+/* Number of block shapes of the fused chirp-z kernels (valid
+ * gw_voxel_params.block_variant values are 0 .. count-1). */
+int32_t gw_voxel_block_variants(void);
 /* Results (synchronous).  iq: crop^3 float64, C order (qy,qx,qz); in
  * GW_STRUCTS_SEPARATE mode n_struct such grids back to back.
  * on_device: write to a device pointer instead of host memory. */
@@ -212,7 +229,8 @@ int gw_voxel_get_counts(gw_voxel_plan *plan, double *counts);
 int gw_voxel_get_sums(gw_voxel_plan *plan, double *sums);
 /* Plan sizes, in this order: [crop, batch, Ly, Lz, Nc, Nr, My, Mz, y_lo,
  * z_lo, k0, kz0, n_slices, device_bytes, graph_kernels, col_tma (1 when
- * the column kernel loads its tiles by TMA)].  Returns the number written
+ * the column kernel loads its tiles by TMA), fused_y, fused_z (1 when the
+ * fused chirp-z kernel runs along that axis)].  Returns the number written
  * (at most n). */
 int gw_voxel_info(gw_voxel_plan *plan, int64_t *info, int32_t n);
 /* Deposit indices of one slice (after execute): y,z voxel index per atom of

@@ -47,21 +47,31 @@ class FakeCtx:
 
 class FakePlan:
     made = []
+    FUSED = (1024, 1280)  # lengths with a fused shape
 
-    def __init__(self, ctx, fft_y, fft_z, batch_slices):
-        self.ctx, self.choice = ctx, (fft_y, fft_z, batch_slices)
+    def __init__(self, ctx, fft_y, fft_z, batch_slices, transform, block_variant):
+        ty, tz = transform
+        for m, fam in ((fft_y, ty), (fft_z, tz)):
+            if fam == "fused" and m and m not in self.FUSED:
+                raise T.N.GwError(T.N.GW_ERR_ARG, "no fused transform")
+        self.ctx = ctx
+        self.choice = (fft_y, fft_z, batch_slices, ty, tz, block_variant)
         FakePlan.made.append(self.choice)
 
     def info(self):
-        return dict(Ly=293, Nc=226, Lz=211, Nr=150, batch=180, n_slices=180)
+        return dict(Ly=579, Nc=584, Lz=414, Nr=402, batch=102, n_slices=360,
+                    My=1280, Mz=1024)
 
     def set_atoms(self):
         pass
 
     def execute(self):
-        fy, fz, b = self.choice
-        # pretend the power of two along z and the half batch are fastest
-        self.ctx.last_ms = fy / 640 + (0.5 if fz == 384 else 0.4) + (0 if b == 90 else 0.1)
+        fy, fz, b, ty, tz, v = self.choice
+        # pretend: fused rows, Stockham columns, the half batch and block
+        # variant 2 are fastest
+        row = {1280: 1.4, 1536: 1.9}[fy] * (0.8 if ty == "fused" else 1.0)
+        col = {1024: 0.8, 1280: 1.0}[fz] * (1.1 if tz == "fused" else 1.0)
+        self.ctx.last_ms = row + col + (0 if b == 51 else 0.05) + (0 if v == 2 else 0.01)
 
     def capture_graph(self):
         pass
@@ -72,16 +82,20 @@ class FakePlan:
 
 def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
     monkeypatch.setenv("GIWAXSIM_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(T.N, "fused_variant_count", lambda: 4)
     ctx = FakeCtx()
     FakePlan.made = []
     make = lambda **kw: FakePlan(ctx, **kw)  # noqa: E731
     best = T.tune(make, 1, smooth=1.5, ctx=ctx)
-    assert best == dict(fft_y=640, fft_z=512, batch_slices=90)
-    # the default plan plus 2 x 2 lengths x 2 batch sizes (180 is all slices)
-    assert len(FakePlan.made) == 1 + 2 * 2 * 2
+    assert best == dict(fft_y=1280, fft_z=1024, batch_slices=51,
+                        transform=("fused", "stockham"), block_variant=2)
+    # the shape probe, the default plan, 3 row candidates (1536 has no fused
+    # shape), 4 column candidates, 2 new batch sizes, 3 new block shapes
+    assert len(FakePlan.made) == 1 + 1 + 3 + 4 + 2 + 3
     cache = json.load(open(tmp_path / "tune.json"))
     (entry,) = cache.values()
-    assert entry["choice"] == best and entry["candidates"] == 8
+    assert entry["choice"]["transform"] == ["fused", "stockham"]
+    assert entry["candidates"] == 14 and entry["ms"] < entry["default_ms"]
     FakePlan.made = []
     assert T.tune(make, 1, smooth=1.5, ctx=ctx) == best
     assert len(FakePlan.made) == 1  # only the shape probe

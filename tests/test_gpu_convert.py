@@ -54,7 +54,13 @@ def test_conversions_bit_exact():
     assert np.array_equal(fl[fin], np.floor(ref32[fin]).astype(np.int64))
 
 
-def test_float32_iq_is_float64_iq_rounded():
+def test_float32_iq_within_two_ulps_of_float64_iq():
+    """The step's float32 I(q) (the detector's input) is computed in
+    float32 from the float64 sum rounded to float, RN(RN(s) * f), so that
+    the step does no float64 arithmetic; the float64 I(q) is s * f with one
+    rounding.  The two differ by at most 1.5 float32 ulps (checked as 2 on
+    the bit patterns, which are ordered like the values for positives), and
+    are zero together."""
     geom = F.VoxelGeometry(0.5, 0.15, 1.5)
     rng = np.random.default_rng(5)
     xyz, _ = W.graphite_slab((12.0, 11.0, 13.0), rng, disp_sigma=0.05)
@@ -65,7 +71,9 @@ def test_float32_iq_is_float64_iq_rounded():
         plan.set_atoms()
         plan.execute()
         i64, i32 = plan.iq(), plan.iq32()
-        assert np.array_equal(i32.view(np.uint32),
-                              i64.astype(np.float32).view(np.uint32))
+        r32 = i64.astype(np.float32)
+        assert np.all(i32 >= 0) and np.array_equal(i32 == 0, r32 == 0)
+        ulps = np.abs(i32.view(np.int32).astype(np.int64)
+                      - r32.view(np.int32).astype(np.int64))
+        assert ulps.max() <= 2, ulps.max()
         plan.close()
-

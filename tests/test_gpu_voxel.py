@@ -256,9 +256,13 @@ def test_autotuned_plan_vs_oracle(tmp_path, monkeypatch):
     ref = O.voxelgrid([(xyz, fv)], 0.5, 0.15, 1.5, phis, False, 1.5)
     got = gpu_run(geom, [(xyz, fv, None)], phis, False, 1.5, tune=True)
     plan = got["plan"]
-    assert set(plan.tuned) == {"fft_y", "fft_z", "batch_slices"}
+    assert set(plan.tuned) == {"fft_y", "fft_z", "batch_slices", "transform",
+                               "block_variant"}
     assert (got["info"]["My"], got["info"]["Mz"]) == (plan.tuned["fft_y"],
                                                       plan.tuned["fft_z"])
+    fam = tuple("fused" if f else "stockham"
+                for f in (got["info"]["fused_y"], got["info"]["fused_z"]))
+    assert fam == plan.tuned["transform"]
     assert np.array_equal(got["counts"], ref["count"])
     assert rel_l2(got["iq"], ref["iq"]) <= RTOL
     assert (tmp_path / "t.json").exists()
