@@ -18,6 +18,10 @@ int launch_col_fused(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
+  if (TMA && P->f1_box_cols != NB)
+    return gw::fail(GW_ERR_STATE, "fused column kernel: tensor-map box of " +
+                                      std::to_string(P->f1_box_cols) +
+                                      " columns, blocks of " + std::to_string(NB));
   dim3 grid((P->Nc + NB - 1) / NB, n_sl);
   gw::KTimer tm(P->ctx, GW_K_COLBIN);
   k_col_fused<M, NB, MINB, HALF, TMA><<<grid, NT, smem, P->ctx->stream>>>(
@@ -56,6 +60,14 @@ int col_fused(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
 }  // namespace
 
 namespace gwv {
+
+int fused_col_block(const gw_voxel_plan *P) {
+  // the plan's block shape where it applies (the half-length TMA form,
+  // col_variant), else the default
+  const bool half = (P->Mz == 1024 && half_fits<1024>(P->Lz, P->Nr)) ||
+                    (P->Mz == 1280 && half_fits<1280>(P->Lz, P->Nr));
+  return half ? kFusedVariants[P->p.block_variant].nb : kFusedVariants[0].nb;
+}
 
 int fused_col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                        const BinArgs &bn, int s0, int n) {

@@ -26,6 +26,7 @@
 #pragma once
 
 #include "gw_bfly.cuh"
+#include "gw_dft.cuh"
 
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
 __host__ __device__ constexpr int fft_pad(int a) { return a + (a >> 4); }
@@ -102,11 +103,19 @@ __host__ __device__ constexpr int tw_offset(int p) {
 // 1 = load(f, n).  DST: 0 = shared memory, 1 = store(f, m, value).
 // FFAST maps the sequence index f fastest across threads (column loads from
 // global memory); otherwise the butterfly index j is fastest.
+// Pruning (the chirp-z window and band are shorter than M): HIN, in a first
+// pass (NS = 1), reads only the inputs r < R/2 of each butterfly (the
+// others, n >= M/2, are zero) and transforms them with the pruned register
+// DFT; HOUT, in a last pass, produces only the outputs r < ceil(R/2) (the
+// others, m >= M/2, are not wanted), the rest being dead code.
 template <int M, int R, int NS, int NB, int NT, bool INV, int SRC, bool PREMUL,
-          int DST, bool FFAST, class Load, class Store>
+          int DST, bool FFAST, bool HIN = false, bool HOUT = false, class Load,
+          class Store>
 __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
                                          const float2 *pre, Load load,
                                          Store store) {
+  static_assert(!HIN || NS == 1, "input pruning is for a first pass");
+  constexpr int KIN = HIN ? R / 2 : R, KOUT = HOUT ? (R + 1) / 2 : R;
   constexpr int Q = M / R;
   constexpr int BF = NB * Q;
   constexpr int PER = (BF + NT - 1) / NT;
@@ -122,7 +131,7 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
       // one address per butterfly and compile-time offsets
       const float2 *src = buf + f * LDM + fft_pad(j);
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
+      for (int r = 0; r < KIN; ++r) {
         const int n = j + r * Q;
         if (SRC == 0) {
           float2 x = Q % 16 == 0 ? src[r * (Q + Q / 16)] : buf[f * LDM + fft_pad(n)];
@@ -144,7 +153,8 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
           for (int r = 1; r < R; ++r) v[e][r] = cmul(v[e][r], conj_if<INV>(t[r]));
         }
       }
-      dft<R, INV>(v[e]);
+      if constexpr (HIN) gwd::dft_prefix<R, KIN, INV>(v[e]);
+      else dft<R, INV>(v[e]);
     }
   }
   // a first pass may read inputs that alias its shared destination
@@ -163,9 +173,10 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
       constexpr int kStep = NS == 1 ? 1 : NS + NS / 16;
       float2 *dst = buf + f * LDM + fft_pad(base);
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
+      for (int r = 0; r < KOUT; ++r) {
         const int m = base + r * NS;
-        const float2 val = v[e][out_slot<R>(r)];
+        // dft_prefix leaves natural order, dft its out_slot order
+        const float2 val = HIN ? v[e][r] : v[e][out_slot<R>(r)];
         if (DST == 0) {
           if (kStride) dst[r * kStep] = val;
           else buf[f * LDM + fft_pad(m)] = val;
@@ -189,35 +200,40 @@ struct NoStore {
 // when PREMUL) or load(f, n) (SRC=1); the last pass writes shared memory
 // (DST=0) or calls store(f, m, value) (DST=1).  Middle passes stay in shared
 // memory.  A transform ending in shared memory leaves the block synchronised.
+// HIN / HOUT: the first pass reads only the first half of its inputs / the
+// last pass produces only the first half of its outputs (fft_pass).
 template <int M, int NB, int NT, bool INV, int SRC, bool PREMUL, int DST,
-          bool FFAST_FIRST, class Load, class Store>
+          bool FFAST_FIRST, bool HIN = false, bool HOUT = false, class Load,
+          class Store>
 __device__ __forceinline__ void fft_run(float2 *buf, const float2 *tw,
                                         const float2 *pre, Load load,
                                         Store store) {
   using Pl = FftPlan<M>;
   static_assert(Pl::N16 >= 1, "M >= 16");
   if constexpr (Pl::NPASS == 1) {
-    fft_pass<M, 16, 1, NB, NT, INV, SRC, PREMUL, DST, FFAST_FIRST>(buf, tw, pre, load, store);
+    fft_pass<M, 16, 1, NB, NT, INV, SRC, PREMUL, DST, FFAST_FIRST, HIN, HOUT>(
+        buf, tw, pre, load, store);
   } else {
-    fft_pass<M, 16, 1, NB, NT, INV, SRC, PREMUL, 0, FFAST_FIRST>(buf, tw, pre, load, NoStore());
+    fft_pass<M, 16, 1, NB, NT, INV, SRC, PREMUL, 0, FFAST_FIRST, HIN, false>(
+        buf, tw, pre, load, NoStore());
     if constexpr (Pl::N16 >= 2) {
       constexpr int dst = Pl::NPASS == 2 ? DST : 0;
-      fft_pass<M, 16, 16, NB, NT, INV, 0, false, dst, false>(
-          buf, tw + tw_offset<M>(1), nullptr, NoLoad(), store);
+      fft_pass<M, 16, 16, NB, NT, INV, 0, false, dst, false, false,
+               HOUT && Pl::NPASS == 2>(buf, tw + tw_offset<M>(1), nullptr, NoLoad(), store);
     }
     if constexpr (Pl::N16 >= 3) {
       constexpr int dst = Pl::NPASS == 3 ? DST : 0;
-      fft_pass<M, 16, 256, NB, NT, INV, 0, false, dst, false>(
-          buf, tw + tw_offset<M>(2), nullptr, NoLoad(), store);
+      fft_pass<M, 16, 256, NB, NT, INV, 0, false, dst, false, false,
+               HOUT && Pl::NPASS == 3>(buf, tw + tw_offset<M>(2), nullptr, NoLoad(), store);
     }
     if constexpr (Pl::R2 > 1) {
       constexpr int NS2 = 1 << (4 * Pl::N16);
       constexpr int dst = Pl::F == 1 ? DST : 0;
-      fft_pass<M, Pl::R2, NS2, NB, NT, INV, 0, false, dst, false>(
-          buf, tw + Pl::tw_r2(), nullptr, NoLoad(), store);
+      fft_pass<M, Pl::R2, NS2, NB, NT, INV, 0, false, dst, false, false,
+               HOUT && Pl::F == 1>(buf, tw + Pl::tw_r2(), nullptr, NoLoad(), store);
     }
     if constexpr (Pl::F > 1) {
-      fft_pass<M, Pl::F, Pl::P2, NB, NT, INV, 0, false, DST, false>(
+      fft_pass<M, Pl::F, Pl::P2, NB, NT, INV, 0, false, DST, false, false, HOUT>(
           buf, tw + Pl::tw_f(), nullptr, NoLoad(), store);
     }
   }

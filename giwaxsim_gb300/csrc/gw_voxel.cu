@@ -422,7 +422,9 @@ struct RowStore {
   }
 };
 
-template <int M, bool BIL>
+// HALF: the window (L) and the band (N) both fit in M / 2, so the forward
+// transform's first pass and the inverse transform's last pass are pruned.
+template <int M, bool BIL, bool HALF>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
 k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
           int nc_out, float2 *F1) {
@@ -437,9 +439,10 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   const int row0 = blockIdx.x * NB;
   deposit_rows<NB, NT, BIL>(a, cz.L, slice0, n_sl, n_rows, row0, buf, LDM, rs);
   RowLoad<M> ld{&a, &cz, buf, rs.k, row0, n_rows};
-  fft_run<M, NB, NT, false, 1, false, 0, false>(buf, tw, nullptr, ld, NoStore());
+  fft_run<M, NB, NT, false, 1, false, 0, false, HALF, false>(buf, tw, nullptr, ld,
+                                                            NoStore());
   RowStore stv{cz.B, F1, row0, n_rows, nc_out};
-  fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), stv);
+  fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), stv);
 }
 
 // Column stage: NB columns of one slice, transformed along z.  The forward
@@ -501,7 +504,7 @@ struct ColBin {
 // 2-D tensor map of F1 (one thread issues them, an mbarrier counts their
 // bytes) into the FFT buffer, which the first pass reads completely before
 // it writes; otherwise each thread loads its elements.
-template <int M, bool TMA>
+template <int M, bool TMA, bool HALF>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
 k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
               const float2 *F1, const __grid_constant__ CUtensorMap f1map) {
@@ -549,14 +552,16 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
       return;
     }
     ColTileLoad<NB> ld{tile, cz.A, rows, nc, m0};
-    fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
+    fft_run<M, NB, NT, false, 1, false, 0, true, HALF, false>(buf, tw, nullptr, ld,
+                                                             NoStore());
   } else {
     ColLoad ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
-    fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
+    fft_run<M, NB, NT, false, 1, false, 0, true, HALF, false>(buf, tw, nullptr, ld,
+                                                             NoStore());
   }
   ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0,
             bn.sstride * (int64_t)(sl / a.n_phi)};
-  fft_run<M, NB, NT, true, 0, true, 1, false>(buf, tw, cz.H, NoLoad(), st);
+  fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), st);
 }
 
 // ---------------------------------------------------------- geometry tables
@@ -1064,7 +1069,7 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   return a;
 }
 
-template <int M, bool BIL>
+template <int M, bool BIL, bool HALF>
 int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  int slice0, int n_sl) {
   const int n_rows = batch_rows(P, slice0, n_sl);
@@ -1072,38 +1077,49 @@ int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
   static bool attr = false;
   if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_row_czt<M, BIL>,
+    GW_CUDA(cudaFuncSetAttribute(k_row_czt<M, BIL, HALF>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
     attr = true;
   }
   const int blocks = (n_rows + NB - 1) / NB;
   gw::KTimer tm(P->ctx, GW_K_ROW);
-  k_row_czt<M, BIL><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_sl,
-                                                          n_rows, P->Nc, P->d_F1);
+  k_row_czt<M, BIL, HALF><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_sl,
+                                                                n_rows, P->Nc, P->d_F1);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
+}
+
+// The pruned forms (window and band within M/2) for the batched lengths.
+template <int M>
+bool pruned(const CztArgs &cz) {
+  return M <= 2048 && cz.L <= M / 2 && cz.N <= M / 2;
 }
 
 template <int M>
 int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                int slice0, int n_sl) {
-  return a.bil ? launch_row_t<M, true>(P, a, cz, slice0, n_sl)
-               : launch_row_t<M, false>(P, a, cz, slice0, n_sl);
+  if constexpr (M <= 2048) {
+    if (pruned<M>(cz))
+      return a.bil ? launch_row_t<M, true, true>(P, a, cz, slice0, n_sl)
+                   : launch_row_t<M, false, true>(P, a, cz, slice0, n_sl);
+  }
+  return a.bil ? launch_row_t<M, true, false>(P, a, cz, slice0, n_sl)
+               : launch_row_t<M, false, false>(P, a, cz, slice0, n_sl);
 }
 
-template <int M>
-int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-               const BinArgs &bn, int slice0, int n_sl) {
+template <int M, bool HALF>
+int launch_col_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                 const BinArgs &bn, int slice0, int n_sl) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
   static bool attr = false;
   if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, false>,
+    GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, false, HALF>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
     if constexpr (col_tma_ok<M>())
-      GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, true>,
+      GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, true, HALF>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
     attr = true;
@@ -1112,16 +1128,25 @@ int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   gw::KTimer tm(P->ctx, GW_K_COLBIN);
   if constexpr (col_tma_ok<M>()) {
     if (P->f1_tma) {
-      k_col_czt_bin<M, true><<<grid, NT, smem, P->ctx->stream>>>(
+      k_col_czt_bin<M, true, HALF><<<grid, NT, smem, P->ctx->stream>>>(
           a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
       GW_LAUNCHED(P->ctx);
       return GW_OK;
     }
   }
-  k_col_czt_bin<M, false><<<grid, NT, smem, P->ctx->stream>>>(
+  k_col_czt_bin<M, false, HALF><<<grid, NT, smem, P->ctx->stream>>>(
       a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
+}
+
+template <int M>
+int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+               const BinArgs &bn, int slice0, int n_sl) {
+  if constexpr (M <= 2048) {
+    if (pruned<M>(cz)) return launch_col_t<M, true>(P, a, cz, bn, slice0, n_sl);
+  }
+  return launch_col_t<M, false>(P, a, cz, bn, slice0, n_sl);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
@@ -1152,8 +1177,12 @@ EncodeTiledFn encode_tiled() {
 template <int M>
 int col_map_create(gw_voxel_plan *P) {
   P->f1_tma = false;
-  if constexpr (col_tma_ok<M>()) {
-    constexpr int NB = FftShape<M>::NB, BR = tma_box_rows(M);
+  // the box is as wide as the column kernel's block of columns: a box of
+  // another width would deliver other than the bytes the kernel waits for
+  const int NB = P->fused_z ? fused_col_block(P) : FftShape<M>::NB;
+  P->f1_box_cols = NB;
+  if ((NB * (int)sizeof(float2)) % 16 == 0) {
+    constexpr int BR = tma_box_rows(M);
     const size_t pitch = (size_t)P->Nc * sizeof(float2);
     EncodeTiledFn enc = encode_tiled();
     if (P->plain || !enc || pitch % 16 != 0 ||

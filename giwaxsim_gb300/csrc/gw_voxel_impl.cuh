@@ -544,6 +544,7 @@ struct gw_voxel_plan {
   CUtensorMap f1map{};
   bool f1_tma = false;
   unsigned wait_polls = gwv::kTileWaitPolls;  // gw_voxel_set_wait_limit
+  int f1_box_cols = 0;  // columns per box of f1map
   // fused chirp-z kernels (gw_czt2.cuh) along y / z, with their twiddles
   bool fused_y = false, fused_z = false;
   float2 *d_fty = nullptr, *d_ftz = nullptr;
@@ -588,6 +589,9 @@ int fused_row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                        int s0, int n);
 int fused_col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                        const BinArgs &bn, int s0, int n);
+// Columns per block the fused column kernel will run with (the tensor map's
+// box width).
+int fused_col_block(const gw_voxel_plan *P);
 // Average, crop and f0 factor into the float32 (f64 false) or the float64
 // I(q) grids.
 int enqueue_finalize(gw_voxel_plan *P, bool f64);
