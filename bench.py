@@ -280,9 +280,7 @@ def run_gb300(args, world, rank, local, pg):
 
     # per-kernel device times (eager, instrumented replica of the same work)
     eager = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
-                        smooth=w["smooth"], fft_y=plan.params.fft_y,
-                        fft_z=plan.params.fft_z,
-                        batch_slices=plan.params.batch_slices, ctx=ctx)
+                        smooth=w["smooth"], **plan_choice(plan), ctx=ctx)
     eager.set_atoms()
     eager.execute()
     ctx.synchronize()
@@ -510,6 +508,16 @@ def _event_ms(ts, fn, reps, flush=None):
     return tot / reps
 
 
+def plan_choice(plan):
+    """The tuned choices of a plan (lengths, batch, kernel family per axis,
+    block shape) as VoxelPlan keywords, for a replica of it."""
+    p = plan.params
+    fam = {0: "auto", 1: "stockham", 2: "fused"}
+    return dict(fft_y=p.fft_y, fft_z=p.fft_z, batch_slices=p.batch_slices,
+                transform=(fam[p.transform_y], fam[p.transform_z]),
+                block_variant=p.block_variant)
+
+
 def plain_path_ms(geom, w, items, phis, ctx, ts, reps=2):
     """Device time of the plain per-rotation path (one slice per launch
     sequence, full grid and transform, binning into the whole cube) over
@@ -576,8 +584,7 @@ def workload_summary(name, ctx, ts, flush, reps=3, tune=True):
         ref = plan.iq()
         pk = F.VoxelPlan(geom, items, phis=phis, fill_bkg=w["fill_bkg"],
                          smooth=w["smooth"], accum="kahan32",
-                         fft_y=plan.params.fft_y, fft_z=plan.params.fft_z,
-                         batch_slices=plan.params.batch_slices, ctx=ctx)
+                         **plan_choice(plan), ctx=ctx)
         pk.set_atoms()
         pk.execute()
         ctx.synchronize()

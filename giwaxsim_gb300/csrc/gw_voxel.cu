@@ -387,183 +387,6 @@ __global__ void k_profile(SliceArgs a, int slice0) {
   }
 }
 
-// --------------------------------------------------------------- CZT stages
-// Row stage: NB rows (slice, z) per block, transformed along y; Nc outputs
-// kept.  The block first deposits the atoms of its rows (contiguous in the
-// z-sorted arrays) into shared-memory row buffers with shared atomics
-// (voxelgrids.py:328-341: shift, floor division, valid mask, np.add.at).
-// The forward FFT's first pass reads those rows with the fill/smoothing
-// transform and the chirp A; the inverse FFT's first pass multiplies by the
-// filter spectrum H, and its last pass writes F1 = B * result to global
-// memory.  The row buffers share storage with the FFT buffer: the first pass
-// reads all its inputs before it writes.
-template <int M>
-struct RowLoad {
-  const SliceArgs *a;
-  const CztArgs *cz;
-  const float2 *rows;     // row f at rows + f * LDM
-  const RowConst *rc;     // per block row (shared memory)
-  int row0, n_rows;
-  __device__ float2 operator()(int f, int n) const {
-    const int row = row0 + f;
-    if (row >= n_rows || n >= cz->L) return make_float2(0.f, 0.f);
-    const float2 dep = rows[f * FftPlan<M>::LDM + n];
-    return cmul(d_value_row(*a, rc[f], n, dep), __ldg(cz->A + n));
-  }
-};
-
-struct RowStore {
-  const float2 *B;
-  float2 *F1;
-  int row0, n_rows, nc;
-  __device__ void operator()(int f, int m, float2 v) const {
-    const int row = row0 + f;
-    if (row < n_rows && m < nc) F1[(size_t)row * nc + m] = cmul(v, __ldg(B + m));
-  }
-};
-
-// HALF: the window (L) and the band (N) both fit in M / 2, so the forward
-// transform's first pass and the inverse transform's last pass are pruned.
-template <int M, bool BIL, bool HALF>
-__global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
-k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
-          int nc_out, float2 *F1) {
-  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
-  constexpr int TWL = FftPlan<M>::tw_len();
-  constexpr int LDM = FftPlan<M>::LDM;
-  extern __shared__ float2 smem[];
-  float2 *tw = smem;
-  float2 *buf = smem + TWL;
-  __shared__ RowShared<NB> rs;
-  for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
-  const int row0 = blockIdx.x * NB;
-  deposit_rows<NB, NT, BIL>(a, cz.L, slice0, n_sl, n_rows, row0, buf, LDM, rs);
-  RowLoad<M> ld{&a, &cz, buf, rs.k, row0, n_rows};
-  fft_run<M, NB, NT, false, 1, false, 0, false, HALF, false>(buf, tw, nullptr, ld,
-                                                            NoStore());
-  RowStore stv{cz.B, F1, row0, n_rows, nc_out};
-  fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), stv);
-}
-
-// Column stage: NB columns of one slice, transformed along z.  The forward
-// FFT's first pass reads F1 columns (sequence index fastest across threads,
-// so a warp reads whole 32-byte sectors), and the inverse FFT's last pass
-// squares B * result and bins it into the float64 sum grid.
-struct ColLoad {
-  const float2 *src, *A;
-  int L, nc, m0;
-  __device__ float2 operator()(int f, int n) const {
-    if (n >= L || m0 + f >= nc) return make_float2(0.f, 0.f);
-    return cmul(src[(size_t)n * nc + m0 + f], __ldg(A + n));
-  }
-};
-
-// The same columns from a shared-memory tile (row n, column f at
-// tile[n * NB + f]) that a TMA load brought in.
-template <int NB>
-struct ColTileLoad {
-  const float2 *tile, *A;
-  int L, nc, m0;
-  __device__ float2 operator()(int f, int n) const {
-    if (n >= L || m0 + f >= nc) return make_float2(0.f, 0.f);
-    return cmul(tile[n * NB + f], __ldg(A + n));
-  }
-};
-
-// The box's inner extent (NB complex values) must be a multiple of 16 bytes.
-template <int M>
-__host__ __device__ constexpr bool col_tma_ok() {
-  return (FftShape<M>::NB * (int)sizeof(float2)) % 16 == 0;
-}
-
-struct ColBin {
-  const BinArgs *bn;
-  const int *cofs;
-  const float2 *B;
-  float2 cbg;
-  int nr, nc, m0;
-  int64_t soff;  // sum-grid offset of the slice's structure (separate mode)
-  __device__ void operator()(int f, int mr, float2 v) const {
-    const int m = m0 + f;
-    if (mr >= nr || m >= nc) return;
-    const int co = cofs[m], ro = bn->rowofs[mr];
-    if (co < 0 || ro < 0) return;
-    if (bn->shell && !shell_member(bn->shell[co + ro], bn->shell_k)) return;
-    float2 X = cmul(v, __ldg(B + mr));
-    if (bn->k0 + m == 0 && bn->kz0 + mr == 0) {
-      X.x += cbg.x * bn->dc_scale;
-      X.y += cbg.y * bn->dc_scale;
-    }
-    const float I = X.x * X.x + X.y * X.y;
-    if (bn->kahan) kahan_add(bn->sumk + soff + co + ro, I);
-    else atomicAdd(bn->sum + soff + co + ro, f2d_exact(I));
-  }
-};
-
-// TMA: the slice's F1 rows of the block's NB columns come in as boxes of a
-// 2-D tensor map of F1 (one thread issues them, an mbarrier counts their
-// bytes) into the FFT buffer, which the first pass reads completely before
-// it writes; otherwise each thread loads its elements.
-template <int M, bool TMA, bool HALF>
-__global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
-k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
-              const float2 *F1, const __grid_constant__ CUtensorMap f1map) {
-  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
-  constexpr int TWL = FftPlan<M>::tw_len();
-  extern __shared__ __align__(128) float2 smem[];
-  __shared__ uint64_t tile_bar;
-  float2 *tw = smem;
-  float2 *buf = smem + TWL;
-  const int slot = blockIdx.y, sl = slice0 + slot;
-  const int p = sl % a.n_phi;
-  const int m0 = blockIdx.x * NB;
-  const int *cofs = bn.colofs + (size_t)p * nc;
-  // skip column groups none of whose pixels lands in the binned window
-  bool any = false;
-  for (int f = 0; f < NB; ++f)
-    if (m0 + f < nc && cofs[m0 + f] >= 0) any = true;
-  if (!any) return;
-  int first, rows;
-  slice_rows(a, slice0, sl, first, rows);
-  // 128-byte aligned tile inside the FFT buffer: the boxes cover at most M
-  // rows of NB values, the buffer holds NB (M + M/16 + 4), and the
-  // alignment skips at most 15 values
-  constexpr int BR = tma_box_rows(M);
-  static_assert(M % BR == 0 && NB * (FftPlan<M>::LDM - M) >= 16, "tile fits");
-  float2 *tile = buf + ((128u - (smem_u32(buf) & 127u)) & 127u) / sizeof(float2);
-  if constexpr (TMA) {
-    if (threadIdx.x == 0) {
-      const int nload = (rows + BR - 1) / BR;
-      mbar_init(&tile_bar, 1);
-      mbar_arrive_expect_tx(&tile_bar, (unsigned)(nload * BR * NB * sizeof(float2)));
-      for (int i = 0; i < nload; ++i)
-        tma_load_2d(tile + (size_t)i * BR * NB, &f1map, m0, first + i * BR, &tile_bar);
-    }
-  }
-  for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
-  __syncthreads();
-  if constexpr (TMA) {
-    // one decision for the whole block: every thread goes on, or none
-    if (!__syncthreads_and(mbar_wait_bounded(&tile_bar, 0, bn.wait_polls))) {
-      if (threadIdx.x == 0) dev_error(a.err, GW_DEVERR_TIMEOUT);
-      // the loads still in flight must land before the block's shared
-      // memory is released; nothing is binned from this block
-      mbar_wait_bounded(&tile_bar, 0, kTileWaitPolls);
-      return;
-    }
-    ColTileLoad<NB> ld{tile, cz.A, rows, nc, m0};
-    fft_run<M, NB, NT, false, 1, false, 0, true, HALF, false>(buf, tw, nullptr, ld,
-                                                             NoStore());
-  } else {
-    ColLoad ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
-    fft_run<M, NB, NT, false, 1, false, 0, true, HALF, false>(buf, tw, nullptr, ld,
-                                                             NoStore());
-  }
-  ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0,
-            bn.sstride * (int64_t)(sl / a.n_phi)};
-  fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), st);
-}
-
 // ---------------------------------------------------------- geometry tables
 // Column tables per phi (voxelgrids.py:396-401 slice axes, :475-498 mask and
 // indices): window offset ((iy-wlo)*W + (ix-wlo))*W, or -1.
@@ -1069,151 +892,6 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   return a;
 }
 
-template <int M, bool BIL, bool HALF>
-int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-                 int slice0, int n_sl) {
-  const int n_rows = batch_rows(P, slice0, n_sl);
-  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
-  const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_row_czt<M, BIL, HALF>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
-  const int blocks = (n_rows + NB - 1) / NB;
-  gw::KTimer tm(P->ctx, GW_K_ROW);
-  k_row_czt<M, BIL, HALF><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_sl,
-                                                                n_rows, P->Nc, P->d_F1);
-  GW_LAUNCHED(P->ctx);
-  return GW_OK;
-}
-
-// The pruned forms (window and band within M/2) for the batched lengths.
-template <int M>
-bool pruned(const CztArgs &cz) {
-  return M <= 2048 && cz.L <= M / 2 && cz.N <= M / 2;
-}
-
-template <int M>
-int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-               int slice0, int n_sl) {
-  if constexpr (M <= 2048) {
-    if (pruned<M>(cz))
-      return a.bil ? launch_row_t<M, true, true>(P, a, cz, slice0, n_sl)
-                   : launch_row_t<M, false, true>(P, a, cz, slice0, n_sl);
-  }
-  return a.bil ? launch_row_t<M, true, false>(P, a, cz, slice0, n_sl)
-               : launch_row_t<M, false, false>(P, a, cz, slice0, n_sl);
-}
-
-template <int M, bool HALF>
-int launch_col_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-                 const BinArgs &bn, int slice0, int n_sl) {
-  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
-  const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, false, HALF>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    if constexpr (col_tma_ok<M>())
-      GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, true, HALF>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-    attr = true;
-  }
-  dim3 grid((P->Nc + NB - 1) / NB, n_sl);
-  gw::KTimer tm(P->ctx, GW_K_COLBIN);
-  if constexpr (col_tma_ok<M>()) {
-    if (P->f1_tma) {
-      k_col_czt_bin<M, true, HALF><<<grid, NT, smem, P->ctx->stream>>>(
-          a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
-      GW_LAUNCHED(P->ctx);
-      return GW_OK;
-    }
-  }
-  k_col_czt_bin<M, false, HALF><<<grid, NT, smem, P->ctx->stream>>>(
-      a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
-  GW_LAUNCHED(P->ctx);
-  return GW_OK;
-}
-
-template <int M>
-int launch_col(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-               const BinArgs &bn, int slice0, int n_sl) {
-  if constexpr (M <= 2048) {
-    if (pruned<M>(cz)) return launch_col_t<M, true>(P, a, cz, bn, slice0, n_sl);
-  }
-  return launch_col_t<M, false>(P, a, cz, bn, slice0, n_sl);
-}
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
-// against the driver library).
-using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
-                                   void *, const cuuint64_t *, const cuuint64_t *,
-                                   const cuuint32_t *, const cuuint32_t *,
-                                   CUtensorMapInterleave, CUtensorMapSwizzle,
-                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_tiled() {
-  static EncodeTiledFn fn = [] {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
-                                         cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      p = nullptr;
-    return reinterpret_cast<EncodeTiledFn>(p);
-  }();
-  return fn;
-}
-
-// Tensor map of F1 (S*Lz rows of Nc complex values) with NB x BR boxes;
-// leaves f1_tma false where the rules of tiled loads are not met (odd
-// band: row pitch not a multiple of 16 bytes; NB * 8 bytes not a multiple
-// of 16) or the encoder is unavailable.  Rows and columns past the map
-// read as zeros.
-template <int M>
-int col_map_create(gw_voxel_plan *P) {
-  P->f1_tma = false;
-  // the box is as wide as the column kernel's block of columns: a box of
-  // another width would deliver other than the bytes the kernel waits for
-  const int NB = P->fused_z ? fused_col_block(P) : FftShape<M>::NB;
-  P->f1_box_cols = NB;
-  if ((NB * (int)sizeof(float2)) % 16 == 0) {
-    constexpr int BR = tma_box_rows(M);
-    const size_t pitch = (size_t)P->Nc * sizeof(float2);
-    EncodeTiledFn enc = encode_tiled();
-    if (P->plain || !enc || pitch % 16 != 0 ||
-        reinterpret_cast<uintptr_t>(P->d_F1) % 16 != 0)
-      return GW_OK;
-    const cuuint64_t dims[2] = {(cuuint64_t)P->Nc, (cuuint64_t)P->S * P->Lz};
-    const cuuint64_t strides[1] = {(cuuint64_t)pitch};
-    const cuuint32_t box[2] = {(cuuint32_t)NB, (cuuint32_t)BR};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = enc(&P->f1map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, P->d_F1,
-                           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    P->f1_tma = r == CUDA_SUCCESS;
-  }
-  return GW_OK;
-}
-
-int col_map_dispatch(gw_voxel_plan *P) { GW_DISPATCH_M(P->Mz, col_map_create, P) }
-
-int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-                 int s0, int n) {
-  if (P->fused_y) return fused_row_dispatch(P, a, cz, s0, n);
-  GW_DISPATCH_M(P->My, launch_row, P, a, cz, s0, n)
-}
-int col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
-                 const BinArgs &bn, int s0, int n) {
-  if (P->fused_z) return fused_col_dispatch(P, a, cz, bn, s0, n);
-  GW_DISPATCH_M(P->Mz, launch_col, P, a, cz, bn, s0, n)
-}
-
 int atom_blocks(gw_voxel_plan *P) {
   int64_t max_atoms = 0;
   for (auto &s : P->structs) max_atoms = std::max(max_atoms, s.atom_count);
@@ -1645,10 +1323,12 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
                                 f0tab[8 * P->Qc + k], f0tab[11 * P->Qc + k]));
   CztTables ty = make_czt(g, P->y_lo, P->Ly, P->k0, P->Nc, P->My);
   CztTables tz = make_czt(g, P->z_lo, P->Lz, P->kz0, P->Nr, P->Mz);
-  // fused chirp-z kernels where the length has a fused shape, unless the
-  // caller asks for the Stockham kernels
-  P->fused_y = p->transform_y != GW_TRANSFORM_STOCKHAM && fused_supported(P->My);
-  P->fused_z = p->transform_z != GW_TRANSFORM_STOCKHAM && fused_supported(P->Mz);
+  // fused chirp-z kernels where the caller asks for them (and the length
+  // has a fused shape); the Stockham kernels otherwise (measured faster on
+  // GB300 for every length with a fused shape; an autotuner may still pick
+  // the fused ones)
+  P->fused_y = p->transform_y == GW_TRANSFORM_FUSED && fused_supported(P->My);
+  P->fused_z = p->transform_z == GW_TRANSFORM_FUSED && fused_supported(P->Mz);
   if ((p->transform_y == GW_TRANSFORM_FUSED && !P->fused_y) ||
       (p->transform_z == GW_TRANSFORM_FUSED && !P->fused_z)) {
     const int m = (p->transform_y == GW_TRANSFORM_FUSED && !P->fused_y) ? P->My : P->Mz;

@@ -579,6 +579,17 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n);
 // Row transforms of the window rows of slices [s0, s0+n_sl), into d_F1.
 int row_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  int s0, int n_sl);
+// The pruned Stockham forms (window and band within M/2) for the batched
+// lengths.
+template <int M>
+bool pruned(const CztArgs &cz) {
+  return M <= 2048 && cz.L <= M / 2 && cz.N <= M / 2;
+}
+// Column transforms and binning of slices [s0, s0+n_sl) (gw_stockham_col.cu).
+int col_dispatch(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                 const BinArgs &bn, int s0, int n_sl);
+// The F1 tensor map for the column kernels' tile loads (gw_stockham_col.cu).
+int col_map_dispatch(gw_voxel_plan *P);
 // Fused chirp-z kernels (gw_czt2_row.cu, gw_czt2_col.cu): lengths with a
 // fused shape, the number of block shapes, their twiddle tables, and the
 // launches for the plan's My / Mz.

@@ -135,12 +135,11 @@ typedef struct gw_voxel_params {
                            of 2^k, 3*2^k, 5*2^k in [64, 8192] and >= L+N-1 */
   int32_t transform_y, transform_z; /* kernel family of the row (y) and
                            column (z) chirp-z transforms.
-                           GW_TRANSFORM_AUTO: the fused kernel where the
-                           length has a fused shape (two shared-memory
-                           exchanges per convolution), the Stockham kernels
-                           elsewhere; GW_TRANSFORM_STOCKHAM: Stockham;
-                           GW_TRANSFORM_FUSED: fused (GW_ERR_ARG if the
-                           length has no fused shape)                      */
+                           GW_TRANSFORM_AUTO and GW_TRANSFORM_STOCKHAM: the
+                           Stockham kernels (measured the faster family on
+                           GB300); GW_TRANSFORM_FUSED: the fused kernel (two
+                           shared-memory exchanges per convolution;
+                           GW_ERR_ARG if the length has no fused shape)    */
   int32_t block_variant; /* block shape of the fused kernels (sequences per
                            block, register cap), 0 .. count-1 with the count
                            from gw_voxel_block_variants(); an autotuner

@@ -103,8 +103,13 @@ def test_result_copy_into_resident_buffer_fills_every_line():
             out[:] = np.nan
             plan.iq(out=out)
             assert not np.isnan(out).any()
-            # the float32 result is the float64 one rounded to nearest
-            assert np.array_equal(out.astype(np.float32), ref32)
+            # the float32 result (float32 arithmetic) is within 2 ulps of
+            # the float64 one rounded, and zero where it is
+            r32 = out.astype(np.float32)
+            assert np.array_equal(r32 == 0, ref32 == 0)
+            ulps = np.abs(r32.view(np.int32).astype(np.int64)
+                          - ref32.view(np.int32).astype(np.int64))
+            assert ulps.max() <= 2
         assert np.all(out.reshape(-1, plan.Qc)[empty_lines] == 0)
         assert np.any(out.reshape(-1, plan.Qc)[~empty_lines] != 0)
     finally:
