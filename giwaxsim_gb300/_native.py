@@ -75,7 +75,7 @@ class VoxelParams(ctypes.Structure):
                 ("batch_slices", ctypes.c_int32), ("deposit", ctypes.c_int32),
                 ("fft_y", ctypes.c_int32), ("fft_z", ctypes.c_int32),
                 ("transform_y", ctypes.c_int32), ("transform_z", ctypes.c_int32),
-                ("block_variant", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
+                ("block_variant", ctypes.c_int32), ("real_grids", ctypes.c_int32)]
 
 
 class Structure(ctypes.Structure):

@@ -96,7 +96,7 @@ class DetectorModel:
         plan = VoxelPlan(self.geom, [(coords, f, None)], phis=self.phis,
                          smooth=sigma, f0_element=self.f0_element,
                          batch_slices=self.checkpoint_every,
-                         deposit=self.deposit, ctx=self.ctx)
+                         deposit=self.deposit, real=False, ctx=self.ctx)
         plan.set_atoms()
         plan.execute()
         self.det.set_iq_device32(plan.device_iq32())

@@ -67,7 +67,8 @@ def length_candidates(need, count=2):
 
 def shape_key(ctx, info, n_structures, fill_bkg, smooth, deposit):
     return "|".join(str(x) for x in (
-        "v2", ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
+        "v3", ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
+        info.get("real", 0),
         info["n_slices"], n_structures, int(bool(fill_bkg)),
         int(bool(smooth)), deposit))
 

@@ -30,6 +30,8 @@
 
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
 __host__ __device__ constexpr int fft_pad(int a) { return a + (a >> 4); }
+// Values per sequence in the shared-memory FFT buffer of length m.
+__host__ __device__ constexpr int fft_ldm(int m) { return fft_pad(m) + 4; }
 // odd factor of a supported length (1, 3 or 5)
 __host__ __device__ constexpr int fft_odd(int m) { return (m & 1) ? m : fft_odd(m >> 1); }
 
@@ -43,7 +45,7 @@ struct FftPlan {
   static constexpr int N16 = L2 / 4;                 // radix-16 passes
   static constexpr int R2 = 1 << (L2 - 4 * N16);    // 1 if none
   static constexpr int NPASS = N16 + (R2 > 1) + (F > 1);
-  static constexpr int LDM = fft_pad(M) + 4;  // floats2 per sequence (+4: see f-fastest maps)
+  static constexpr int LDM = fft_ldm(M);  // floats2 per sequence (+4: see f-fastest maps)
   // twiddle table length (passes with Ns > 1)
   __host__ __device__ static constexpr int tw_len() {
     int t = 0, ns = 16;

@@ -564,6 +564,9 @@ extern "C" int gw_voxel_grad_buffer(gw_voxel_plan *P, double **g_iq_dev) {
 extern "C" int gw_voxel_backward(gw_voxel_plan *P, const double *g_iq,
                                  int32_t iq_on_device, double *g_f,
                                  double *g_xyz, double *g_sigma, double *g_c) {
+  if (P && P->real)
+    return gw::fail(GW_ERR_STATE, "gw_voxel_backward: the plan was made with "
+                                  "real_grids; the adjoint needs real_grids 0");
   if (!P || !g_iq || !g_f)
     return gw::fail(GW_ERR_ARG, "gw_voxel_backward: null argument");
   if (P->plain)

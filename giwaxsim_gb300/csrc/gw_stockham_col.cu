@@ -13,12 +13,13 @@ using namespace gwv;
 
 namespace {
 
+// F1 columns j0 + f (nf per row) of the slice's rows.
 struct ColLoad {
   const float2 *src, *A;
-  int L, nc, m0;
+  int L, nf, j0;
   __device__ float2 operator()(int f, int n) const {
-    if (n >= L || m0 + f >= nc) return make_float2(0.f, 0.f);
-    return cmul(src[(size_t)n * nc + m0 + f], __ldg(A + n));
+    if (n >= L || j0 + f >= nf) return make_float2(0.f, 0.f);
+    return cmul(src[(size_t)n * nf + j0 + f], __ldg(A + n));
   }
 };
 
@@ -27,9 +28,9 @@ struct ColLoad {
 template <int NB>
 struct ColTileLoad {
   const float2 *tile, *A;
-  int L, nc, m0;
+  int L, nf, j0;
   __device__ float2 operator()(int f, int n) const {
-    if (n >= L || m0 + f >= nc) return make_float2(0.f, 0.f);
+    if (n >= L || j0 + f >= nf) return make_float2(0.f, 0.f);
     return cmul(tile[n * NB + f], __ldg(A + n));
   }
 };
@@ -40,27 +41,39 @@ __host__ __device__ constexpr bool col_tma_ok() {
   return (FftShape<M>::NB * (int)sizeof(float2)) % 16 == 0;
 }
 
+// |B y|^2 (plus the background's DC term at q = 0) of output row mr of F1
+// column j0 + f (table column m = moff + j0 + f) binned into the float64
+// sums; with mirrored binning (real grids) also at (2 m_zero - m,
+// 2 r_zero - mr) for m > m_zero.
 struct ColBin {
   const BinArgs *bn;
   const int *cofs;
   const float2 *B;
   float2 cbg;
-  int nr, nc, m0;
+  int nr, nc, j0, moff;
   int64_t soff;  // sum-grid offset of the slice's structure (separate mode)
-  __device__ void operator()(int f, int mr, float2 v) const {
-    const int m = m0 + f;
-    if (mr >= nr || m >= nc) return;
-    const int co = cofs[m], ro = bn->rowofs[mr];
+  __device__ void add(int co, int ro, float I) const {
     if (co < 0 || ro < 0) return;
     if (bn->shell && !shell_member(bn->shell[co + ro], bn->shell_k)) return;
+    if (bn->kahan) kahan_add(bn->sumk + soff + co + ro, I);
+    else atomicAdd(bn->sum + soff + co + ro, f2d_exact(I));
+  }
+  __device__ void operator()(int f, int mr, float2 v) const {
+    const int m = moff + j0 + f;
+    if (mr >= nr || m >= nc) return;
+    const int co = cofs[m], ro = bn->rowofs[mr];
+    const bool mir = bn->mirror && m > bn->m_zero;
+    const int cm = mir ? cofs[2 * bn->m_zero - m] : -1;
+    const int rm = mir ? bn->rowofs[2 * bn->r_zero - mr] : -1;
+    if ((co < 0 || ro < 0) && (cm < 0 || rm < 0)) return;
     float2 X = cmul(v, __ldg(B + mr));
     if (bn->k0 + m == 0 && bn->kz0 + mr == 0) {
       X.x += cbg.x * bn->dc_scale;
       X.y += cbg.y * bn->dc_scale;
     }
     const float I = X.x * X.x + X.y * X.y;
-    if (bn->kahan) kahan_add(bn->sumk + soff + co + ro, I);
-    else atomicAdd(bn->sum + soff + co + ro, f2d_exact(I));
+    add(co, ro, I);
+    if (mir) add(cm, rm, I);
   }
 };
 
@@ -70,7 +83,7 @@ struct ColBin {
 // it writes; otherwise each thread loads its elements.
 template <int M, bool TMA, bool HALF>
 __global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
-k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
+k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc, int nf,
               const float2 *F1, const __grid_constant__ CUtensorMap f1map) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   constexpr int TWL = FftPlan<M>::tw_len();
@@ -80,12 +93,18 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
   float2 *buf = smem + TWL;
   const int slot = blockIdx.y, sl = slice0 + slot;
   const int p = sl % a.n_phi;
-  const int m0 = blockIdx.x * NB;
+  // F1 columns j0 .. j0 + NB - 1 (table columns moff + j)
+  const int j0 = blockIdx.x * NB, moff = bn.mirror ? bn.m_zero : 0;
   const int *cofs = bn.colofs + (size_t)p * nc;
-  // skip column groups none of whose pixels lands in the binned window
+  // skip column groups none of whose pixels (nor their mirrors) lands in
+  // the binned window
   bool any = false;
-  for (int f = 0; f < NB; ++f)
-    if (m0 + f < nc && cofs[m0 + f] >= 0) any = true;
+  for (int f = 0; f < NB; ++f) {
+    const int m = moff + j0 + f;
+    if (j0 + f < nf && m < nc &&
+        (cofs[m] >= 0 || (bn.mirror && m > bn.m_zero && cofs[2 * bn.m_zero - m] >= 0)))
+      any = true;
+  }
   if (!any) return;
   int first, rows;
   slice_rows(a, slice0, sl, first, rows);
@@ -101,7 +120,7 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
       mbar_init(&tile_bar, 1);
       mbar_arrive_expect_tx(&tile_bar, (unsigned)(nload * BR * NB * sizeof(float2)));
       for (int i = 0; i < nload; ++i)
-        tma_load_2d(tile + (size_t)i * BR * NB, &f1map, m0, first + i * BR, &tile_bar);
+        tma_load_2d(tile + (size_t)i * BR * NB, &f1map, j0, first + i * BR, &tile_bar);
     }
   }
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
@@ -115,15 +134,15 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc,
       mbar_wait_bounded(&tile_bar, 0, kTileWaitPolls);
       return;
     }
-    ColTileLoad<NB> ld{tile, cz.A, rows, nc, m0};
+    ColTileLoad<NB> ld{tile, cz.A, rows, nf, j0};
     fft_run<M, NB, NT, false, 1, false, 0, true, HALF, false>(buf, tw, nullptr, ld,
                                                              NoStore());
   } else {
-    ColLoad ld{F1 + (size_t)first * nc, cz.A, rows, nc, m0};
+    ColLoad ld{F1 + (size_t)first * nf, cz.A, rows, nf, j0};
     fft_run<M, NB, NT, false, 1, false, 0, true, HALF, false>(buf, tw, nullptr, ld,
                                                              NoStore());
   }
-  ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, m0,
+  ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, j0, moff,
             bn.sstride * (int64_t)(sl / a.n_phi)};
   fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), st);
 }
@@ -148,18 +167,18 @@ int launch_col_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                                    (int)smem));
     attr = true;
   }
-  dim3 grid((P->Nc + NB - 1) / NB, n_sl);
+  dim3 grid((P->Nf + NB - 1) / NB, n_sl);
   gw::KTimer tm(P->ctx, GW_K_COLBIN);
   if constexpr (col_tma_ok<M>()) {
     if (P->f1_tma) {
       k_col_czt_bin<M, true, HALF><<<grid, NT, smem, P->ctx->stream>>>(
-          a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
+          a, cz, bn, slice0, P->Nc, P->Nf, P->d_F1, P->f1map);
       GW_LAUNCHED(P->ctx);
       return GW_OK;
     }
   }
   k_col_czt_bin<M, false, HALF><<<grid, NT, smem, P->ctx->stream>>>(
-      a, cz, bn, slice0, P->Nc, P->d_F1, P->f1map);
+      a, cz, bn, slice0, P->Nc, P->Nf, P->d_F1, P->f1map);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
 }
@@ -207,12 +226,12 @@ int col_map_create(gw_voxel_plan *P) {
   P->f1_box_cols = NB;
   if ((NB * (int)sizeof(float2)) % 16 == 0) {
     constexpr int BR = tma_box_rows(M);
-    const size_t pitch = (size_t)P->Nc * sizeof(float2);
+    const size_t pitch = (size_t)P->Nf * sizeof(float2);
     EncodeTiledFn enc = encode_tiled();
     if (P->plain || !enc || pitch % 16 != 0 ||
         reinterpret_cast<uintptr_t>(P->d_F1) % 16 != 0)
       return GW_OK;
-    const cuuint64_t dims[2] = {(cuuint64_t)P->Nc, (cuuint64_t)P->S * P->Lz};
+    const cuuint64_t dims[2] = {(cuuint64_t)P->Nf, (cuuint64_t)P->S * P->Lz};
     const cuuint64_t strides[1] = {(cuuint64_t)pitch};
     const cuuint32_t box[2] = {(cuuint32_t)NB, (cuuint32_t)BR};
     const cuuint32_t estr[2] = {1, 1};

@@ -71,10 +71,80 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), stv);
 }
 
-// Column stage: NB columns of one slice, transformed along z.  The forward
-// FFT's first pass reads F1 columns (sequence index fastest across threads,
-// so a warp reads whole 32-byte sectors), and the inverse FFT's last pass
-// squares B * result and bins it into the float64 sum grid.
+// Real grids: when every atom's f is a real multiple of one complex value,
+// a slice's grid is u R with R real and u the unit phase of the
+// structure's average voxel f (fill and smoothing values are multiples of
+// it too).  The DFT of a real row is Hermitian, Y[-k] = conj(Y[k]), so two
+// window rows A and B share one transform: x = R_A + i R_B gives
+// Z = Y_A + i Y_B, and Y_A[k] = (Z[k] + conj(Z[-k])) / 2,
+// Y_B[k] = (Z[k] - conj(Z[-k])) / (2 i).  The block deposits its 2 NB rows
+// into the halves of its NB transform buffers (row 2f at f LDM, row 2f+1 at
+// f LDM + LDM/2; the window fits: L <= LDM/2), transforms the NB packed
+// rows, leaves the inverse transform in shared memory, and writes F1 for
+// the columns ky >= 0 only (the column stage needs no others):
+// F1[row][j] = u_row Y_row[m_zero + j], j < nf.
+template <int M>
+struct RowLoadPair {
+  const SliceArgs *a;
+  const CztArgs *cz;
+  const float2 *rows;     // block row r at rows + r * (LDM / 2)
+  const RowConst *rc;     // per block row (shared memory)
+  int row0, n_rows;       // row0: the block's first window row
+  __device__ float2 operator()(int f, int n) const {
+    if (n >= cz->L) return make_float2(0.f, 0.f);
+    constexpr int HL = FftPlan<M>::LDM / 2;
+    float re = 0.f, im = 0.f;
+    const int ra = 2 * f, rb = 2 * f + 1;
+    if (row0 + ra < n_rows) {
+      const float2 d = d_value_row(*a, rc[ra], n, rows[ra * HL + n]);
+      re = d.x * rc[ra].u.x + d.y * rc[ra].u.y;  // Re(d conj(u))
+    }
+    if (row0 + rb < n_rows) {
+      const float2 d = d_value_row(*a, rc[rb], n, rows[rb * HL + n]);
+      im = d.x * rc[rb].u.x + d.y * rc[rb].u.y;
+    }
+    return cmul(make_float2(re, im), __ldg(cz->A + n));
+  }
+};
+
+template <int M, bool HALF>
+__global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
+k_row_czt_real(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
+               int m_zero, int nf, float2 *F1) {
+  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  constexpr int TWL = FftPlan<M>::tw_len();
+  constexpr int LDM = FftPlan<M>::LDM;
+  static_assert(LDM % 2 == 0, "two rows per transform buffer");
+  extern __shared__ float2 smem[];
+  float2 *tw = smem;
+  float2 *buf = smem + TWL;
+  __shared__ RowShared<2 * NB> rs;
+  for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
+  const int row0 = blockIdx.x * 2 * NB;
+  deposit_rows<2 * NB, NT, false>(a, cz.L, slice0, n_sl, n_rows, row0, buf, LDM / 2, rs);
+  RowLoadPair<M> ld{&a, &cz, buf, rs.k, row0, n_rows};
+  fft_run<M, NB, NT, false, 1, false, 0, false, HALF, false>(buf, tw, nullptr, ld,
+                                                            NoStore());
+  // the inverse transform stays in shared memory (natural order; with HALF
+  // only the outputs below M/2, which hold the band); the block is
+  // synchronised afterwards
+  fft_run<M, NB, NT, true, 0, true, 0, false, false, HALF>(buf, tw, cz.H, NoLoad(),
+                                                          NoStore());
+  for (int i = threadIdx.x; i < NB * nf; i += NT) {
+    const int f = i / nf, j = i - f * nf;
+    const int m = m_zero + j, mm = m_zero - j;  // k and -k
+    float2 X = make_float2(0.f, 0.f), Xm = make_float2(0.f, 0.f);
+    if (m < cz.N) X = cmul(buf[f * LDM + fft_pad(m)], __ldg(cz.B + m));
+    if (mm >= 0) Xm = cmul(buf[f * LDM + fft_pad(mm)], __ldg(cz.B + mm));
+    // Y_A = (X + conj(Xm)) / 2, Y_B = -i (X - conj(Xm)) / 2
+    const float2 ya = make_float2(0.5f * (X.x + Xm.x), 0.5f * (X.y - Xm.y));
+    const float2 yb = make_float2(0.5f * (X.y + Xm.y), -0.5f * (X.x - Xm.x));
+    const int ra = row0 + 2 * f, rb = ra + 1;
+    if (ra < n_rows) F1[(size_t)ra * nf + j] = cmul(rs.k[2 * f].u, ya);
+    if (rb < n_rows) F1[(size_t)rb * nf + j] = cmul(rs.k[2 * f + 1].u, yb);
+  }
+}
+
 }  // namespace
 
 namespace gwv {
@@ -95,7 +165,28 @@ int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   const int blocks = (n_rows + NB - 1) / NB;
   gw::KTimer tm(P->ctx, GW_K_ROW);
   k_row_czt<M, BIL, HALF><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_sl,
-                                                                n_rows, P->Nc, P->d_F1);
+                                                                n_rows, P->Nf, P->d_F1);
+  GW_LAUNCHED(P->ctx);
+  return GW_OK;
+}
+
+template <int M, bool HALF>
+int launch_row_real(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
+                    int slice0, int n_sl) {
+  const int n_rows = batch_rows(P, slice0, n_sl);
+  constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
+  const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
+  static bool attr = false;
+  if (!attr) {
+    GW_CUDA(cudaFuncSetAttribute(k_row_czt_real<M, HALF>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = true;
+  }
+  const int blocks = (n_rows + 2 * NB - 1) / (2 * NB);
+  gw::KTimer tm(P->ctx, GW_K_ROW);
+  k_row_czt_real<M, HALF><<<blocks, NT, smem, P->ctx->stream>>>(
+      a, cz, slice0, n_sl, n_rows, P->m_zero, P->Nf, P->d_F1);
   GW_LAUNCHED(P->ctx);
   return GW_OK;
 }
@@ -103,11 +194,15 @@ int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
 template <int M>
 int launch_row(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                int slice0, int n_sl) {
-  if constexpr (M <= 2048) {
+  if constexpr (M <= 2048 && FftShape<M>::NB <= 16) {
+    if (P->real)
+      return pruned<M>(cz) ? launch_row_real<M, true>(P, a, cz, slice0, n_sl)
+                           : launch_row_real<M, false>(P, a, cz, slice0, n_sl);
     if (pruned<M>(cz))
       return a.bil ? launch_row_t<M, true, true>(P, a, cz, slice0, n_sl)
                    : launch_row_t<M, false, true>(P, a, cz, slice0, n_sl);
   }
+  if (P->real) return gw::fail(GW_ERR_ARG, "real-grid rows need a length up to 2048");
   return a.bil ? launch_row_t<M, true, false>(P, a, cz, slice0, n_sl)
                : launch_row_t<M, false, false>(P, a, cz, slice0, n_sl);
 }

@@ -1076,7 +1076,7 @@ int enqueue(gw_voxel_plan *P) {
              P->p.accum == GW_ACCUM_KAHAN32, P->k0, P->kz0,
              (float)((double)P->g * (double)P->g),
              P->n_out > 1 ? (int64_t)P->sum_stride : 0, nullptr, 0,
-             P->wait_polls};
+             P->wait_polls, P->real ? 1 : 0, P->m_zero, P->r_zero};
   // Multi-q form factors: one pass per shell with that shell's atom f
   // values and average voxel f, binning only the shell's voxels into the
   // common sums (GW_SHELLS_PER_SHELL); or the reference's single pass with
@@ -1185,6 +1185,19 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       if (rowofs_all[i] >= 0) { if (r0 < 0) r0 = i; r1 = i; }
     if (r0 < 0) { delete P; return gw::fail(GW_ERR_ARG, "no slice row lands in the cropped cube"); }
   }
+  // real grids: bands symmetric around q = 0 (kz from -Kz to Kz), so that
+  // every output row has its mirror
+  const bool want_real = p->real_grids != 0 && !P->plain && !P->bil;
+  if (want_real) {
+    const int Kz = std::max(g / 2 - r0, r1 - g / 2);
+    if (g / 2 - Kz < 0 || g / 2 + Kz > g - 1) {
+      delete P;
+      return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: real-grid band wider than the grid");
+    }
+    r0 = g / 2 - Kz;
+    r1 = g / 2 + Kz;
+    P->r_zero = Kz;
+  }
   P->kz0 = r0 - g / 2;
   P->Nr = r1 - r0 + 1;
   std::vector<int> rowofs(P->Nr);
@@ -1207,9 +1220,24 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     const int K = (int)std::ceil(hcap / dh) + 2;
     int c_lo = std::max(0, (g - 1) / 2 - K);
     int c_hi = std::min(g - 1, g / 2 + K);
-    // an even band keeps F1's rows 16-byte aligned for tensor-map loads; a
-    // column past the grid (c_hi = g) is marked unbinned by k_col_tables
-    if ((c_hi - c_lo + 1) % 2) ++c_hi;
+    if (want_real) {
+      // symmetric: ky from -K to K, m_zero = K; F1 keeps the columns
+      // ky >= 0, an even number of them (one past K if needed: beyond the
+      // margin of K, so unbinned)
+      c_lo = g / 2 - K;
+      c_hi = g / 2 + K;
+      if (c_lo < 0 || c_hi > g - 1) {
+        delete P;
+        return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: real-grid band wider than the grid");
+      }
+      P->m_zero = K;
+      if ((K + 1) % 2) ++c_hi;
+    } else if ((c_hi - c_lo + 1) % 2) {
+      // an even band keeps F1's rows 16-byte aligned for tensor-map loads;
+      // a column past the grid (c_hi = g) is marked unbinned by
+      // k_col_tables
+      ++c_hi;
+    }
     P->k0 = c_lo - g / 2;
     P->Nc = c_hi - c_lo + 1;
   }
@@ -1266,9 +1294,15 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     delete P;
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: fft_y/fft_z must be a supported length >= L+N-1");
   }
+  // real grids: two window rows share one row transform buffer (a window
+  // of at most half the buffer) and the Stockham kernels run both axes (a
+  // fused kernel asked for by name keeps the general path)
+  P->real = want_real && 2 * P->Ly <= fft_ldm(P->My) && P->My <= 2048 &&
+            p->transform_y != GW_TRANSFORM_FUSED && p->transform_z != GW_TRANSFORM_FUSED;
+  P->Nf = P->real ? P->Nc - P->m_zero : P->Nc;
   // batch size: keep the per-batch intermediates near L2 size
   {
-    const size_t per = (size_t)P->Lz * P->Nc * sizeof(float2) +
+    const size_t per = (size_t)P->Lz * P->Nf * sizeof(float2) +
                        (P->Ly + P->Lz) * 12;
     int S = p->batch_slices > 0 ? p->batch_slices
                                 : (int)std::max<size_t>(1, (96u << 20) / per);
@@ -1327,8 +1361,8 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
   // has a fused shape); the Stockham kernels otherwise (measured faster on
   // GB300 for every length with a fused shape; an autotuner may still pick
   // the fused ones)
-  P->fused_y = p->transform_y == GW_TRANSFORM_FUSED && fused_supported(P->My);
-  P->fused_z = p->transform_z == GW_TRANSFORM_FUSED && fused_supported(P->Mz);
+  P->fused_y = !P->real && p->transform_y == GW_TRANSFORM_FUSED && fused_supported(P->My);
+  P->fused_z = !P->real && p->transform_z == GW_TRANSFORM_FUSED && fused_supported(P->Mz);
   if ((p->transform_y == GW_TRANSFORM_FUSED && !P->fused_y) ||
       (p->transform_z == GW_TRANSFORM_FUSED && !P->fused_z)) {
     const int m = (p->transform_y == GW_TRANSFORM_FUSED && !P->fused_y) ? P->My : P->Mz;
@@ -1372,7 +1406,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_rowstart, (size_t)n_struct * (g + 2), &B)) ||
       (st = alloc(&P->d_cursor, (size_t)n_struct * (g + 1), &B)) ||
       (st = alloc(&P->d_zstat, n_struct, &B)) ||
-      (st = alloc(&P->d_F1, (size_t)P->S * P->Lz * P->Nc, &B)) ||
+      (st = alloc(&P->d_F1, (size_t)P->S * P->Lz * P->Nf, &B)) ||
       (st = alloc(&P->d_amo, (size_t)P->n_slices * P->Ly, &B)) ||
       (st = alloc(&P->d_my, (size_t)P->n_slices * P->Ly, &B)) ||
       (st = alloc(&P->d_mz, (size_t)P->n_slices * P->Lz, &B)) ||
@@ -1464,6 +1498,9 @@ extern "C" int gw_voxel_set_shells(gw_voxel_plan *P, int32_t n_shells,
                                    int32_t mode, const double *q_axis,
                                    const double *lower, const double *upper,
                                    const float *f, const double *avg_f) {
+  if (P && P->real)
+    return gw::fail(GW_ERR_STATE, "gw_voxel_set_shells: the plan was made with "
+                                  "real_grids (per-shell f values): make it with real_grids 0");
   if (!P) return gw::fail(GW_ERR_ARG, "gw_voxel_set_shells: null plan");
   auto drop = [P]() {
     gw::dev_free(P->d_shell); gw::dev_free(P->d_f_shells);
@@ -1705,7 +1742,7 @@ extern "C" int gw_voxel_info(gw_voxel_plan *P, int64_t *info, int32_t n) {
                        P->y_lo, P->z_lo, P->k0, P->kz0, P->n_slices,
                        (int64_t)P->bytes, P->graph_kernels,
                        (int64_t)P->f1_tma, (int64_t)P->fused_y,
-                       (int64_t)P->fused_z};
+                       (int64_t)P->fused_z, (int64_t)P->real};
   const int k = std::min<int>(n, (int)(sizeof v / sizeof v[0]));
   for (int i = 0; i < k; ++i) info[i] = v[i];
   return k;

@@ -77,6 +77,11 @@ struct BinArgs {
   int shell_k;
   // polls of the column kernel's bounded wait for its tile load
   unsigned wait_polls;
+  // real grids (only the columns ky >= 0 are transformed): F1 column j is
+  // table column m_zero + j, and every pixel (m, mr) with m > m_zero is
+  // binned again at its mirror (2 m_zero - m, 2 r_zero - mr), where
+  // |F(-ky, -kz)|^2 = |F(ky, kz)|^2
+  int mirror, m_zero, r_zero;
 };
 
 // Default poll limit of a bounded wait for an asynchronous tile load: far
@@ -217,6 +222,8 @@ struct RowConst {
   float mz;        // z smoothing factor of the row (1 when smoothing is off)
   int zin;         // the row's z lies inside [e.z, e.w)
   int slot;
+  float2 u;        // unit phase of the structure's average voxel f (real
+                   // grids: the row is u times a real row)
 };
 
 __device__ __forceinline__ RowConst row_const(const SliceArgs &a, int slot,
@@ -230,6 +237,10 @@ __device__ __forceinline__ RowConst row_const(const SliceArgs &a, int slot,
   const int zi = window_row_to_z(a, zz);
   k.zin = zi >= k.e.z && zi < k.e.w;
   k.slot = slot;
+  const gw_structure &st = a.st[sl / a.n_phi];
+  const double mag = sqrt(st.avg_f_re * st.avg_f_re + st.avg_f_im * st.avg_f_im);
+  k.u = mag > 0.0 ? make_float2((float)(st.avg_f_re / mag), (float)(st.avg_f_im / mag))
+                  : make_float2(1.f, 0.f);
   return k;
 }
 
@@ -545,6 +556,13 @@ struct gw_voxel_plan {
   bool f1_tma = false;
   unsigned wait_polls = gwv::kTileWaitPolls;  // gw_voxel_set_wait_limit
   int f1_box_cols = 0;  // columns per box of f1map
+  // real grids (gw_voxel_params.real_grids and the shape allows it): two
+  // window rows per row transform, only the columns ky >= 0 in F1 (Nf of
+  // them, table columns m_zero ..), mirrored binning; the bands are
+  // symmetric around ky = 0 (m_zero) and kz = 0 (r_zero)
+  bool real = false;
+  int m_zero = 0, r_zero = 0;
+  int Nf = 0;  // F1 row pitch (columns stored): Nc, or Nc - m_zero
   // fused chirp-z kernels (gw_czt2.cuh) along y / z, with their twiddles
   bool fused_y = false, fused_z = false;
   float2 *d_fty = nullptr, *d_ftz = nullptr;

@@ -144,6 +144,23 @@ def element_f_values(elements, energy, f1f2=None):
     return vals[inv]
 
 
+def real_multiples(fv):
+    """True when every f value is a real multiple of one complex value (to
+    the float32 precision the device keeps them in) and their sum does not
+    cancel: the slice grids are then that value's phase times real grids
+    (gw_voxel_params.real_grids)."""
+    f = np.asarray(fv, dtype=complex).ravel()
+    if f.size == 0:
+        return False
+    ref = f[np.argmax(np.abs(f))]
+    if ref == 0:
+        return False
+    cross = f.imag * ref.real - f.real * ref.imag  # Im(f conj(ref))
+    if np.max(np.abs(cross)) > 1e-6 * abs(ref) * np.max(np.abs(f)):
+        return False
+    return abs(np.sum(f)) > 1e-3 * np.sum(np.abs(f))
+
+
 def coord_ranges(coords):
     """max - min of x, y and z (comparison.py:712-717), from a transposed
     copy (contiguous reductions)."""
@@ -214,13 +231,18 @@ HOST_POOL = HostPool()
 class VoxelPlan:
     """Owner of a gw_voxel_plan for one geometry, a list of structures and
     a list of phis.  structures: list of (coords (N,3), f_values (N,)
-    complex, weights (N,) or None)."""
+    complex, weights (N,) or None).  real: None runs the real-grid path
+    (gw_voxel_params.real_grids) when every structure's weighted f values
+    are real multiples of one complex value in a batched, nearest-bin plan
+    without a fused kernel asked for; False keeps the general path (needed
+    for set_shells and backward); True asks for it and refuses f values
+    that do not allow it."""
 
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
                  batch_slices=0, constants=None, deposit="nearest", fft_y=0,
                  fft_z=0, tune=False, ctx=None, create=True, ranges=None,
-                 transform="auto", block_variant=0):
+                 transform="auto", block_variant=0, real=None):
         self.geom = geom
         self.handle = None
         self.reused = False          # handed out again by PlanCache
@@ -236,7 +258,7 @@ class VoxelPlan:
                                  smooth=smooth, mode=mode, accum=accum,
                                  average=average, f0_element=f0_element,
                                  constants=constants, deposit=deposit,
-                                 ctx=self.ctx, **choice)
+                                 real=real, ctx=self.ctx, **choice)
 
             self.tuned = autotune.tune(make, len(structures), fill_bkg, smooth,
                                        deposit, ctx=self.ctx)
@@ -250,6 +272,7 @@ class VoxelPlan:
         r = geom.r_voxel_size
         st = np.zeros(len(structures), dtype=_dtype_of(N.Structure))
         xyz, fs = [], []
+        all_real = True
         begin = 0
         for i, (coords, fv, w) in enumerate(structures):
             coords = np.ascontiguousarray(coords, dtype=np.float64)
@@ -258,6 +281,7 @@ class VoxelPlan:
             fv = np.asarray(fv, dtype=complex)
             if w is not None:
                 fv = fv * np.asarray(w, dtype=np.float64)
+            all_real = all_real and real_multiples(fv)
             if constants is not None:
                 # the per-slice worker receives the driver's constants
                 xb, yb, zb, avg = constants[i]
@@ -305,6 +329,16 @@ class VoxelPlan:
                "fused": N.GW_TRANSFORM_FUSED}
         p.transform_y, p.transform_z = fam[ty], fam[tz]
         p.block_variant = int(block_variant)
+        # real grids (every structure's f values real multiples of one
+        # value): None decides from the f values, False keeps the general
+        # path (the adjoint and multi-q shells need it)
+        if real is None:
+            real = (all_real and mode == "batched" and deposit == "nearest"
+                    and "fused" not in (ty, tz))
+        elif real and not all_real:
+            raise ValueError("real=True needs every structure's f values to be "
+                             "real multiples of one complex value")
+        p.real_grids = int(bool(real))
         self.params = p
         self.Qc = geom.crop_hi - geom.crop_lo + 1
         if create:
@@ -331,6 +365,8 @@ class VoxelPlan:
     def set_atoms(self, xyz=None, f=None, on_device=False):
         if xyz is None:
             xyz, f = self.xyz, self.f
+        elif not on_device and getattr(getattr(self, "params", None), "real_grids", 0):
+            self._check_real(f)
         n = len(self.xyz) if on_device else len(xyz)
         if n != self._atoms_n:
             self.graph_captured = False
@@ -342,6 +378,24 @@ class VoxelPlan:
             N.check(N.lib().gw_voxel_set_atoms(self.handle, N.ptr(xyz), N.ptr(f),
                                                n, 0))
         self._atoms_n = n
+
+    def _check_real(self, f):
+        """A real-grid plan takes each structure's grid as the phase of its
+        average voxel f times a real grid: atoms whose f values are not
+        real multiples of that phase would give wrong intensities, so they
+        are refused (make the plan with real=False for them)."""
+        fc = np.asarray(f)
+        fc = (np.ascontiguousarray(fc).view(np.complex64) if fc.dtype == np.float32
+              else fc.astype(complex)).ravel()
+        for s in self.structs:
+            b, n = int(s["atom_begin"]), int(s["atom_count"])
+            part = fc[b:b + n].astype(complex)
+            avg = complex(s["avg_f_re"], s["avg_f_im"])
+            cross = part.imag * avg.real - part.real * avg.imag
+            if len(part) != n or np.max(np.abs(cross), initial=0.0) > (
+                    1e-6 * abs(avg) * np.max(np.abs(part), initial=0.0)):
+                raise ValueError("set_atoms: f values that are not real multiples "
+                                 "of the structure's average f, on a real-grid plan")
 
     def set_shells(self, q_axis, lower, upper, f_shells, avg_shells,
                    mode="per_shell"):
@@ -430,7 +484,7 @@ class VoxelPlan:
         n = N.lib().gw_voxel_info(self.handle, N.ptr(v), 24)
         keys = ["crop", "batch", "Ly", "Lz", "Nc", "Nr", "My", "Mz", "y_lo",
                 "z_lo", "k0", "kz0", "n_slices", "device_bytes",
-                "graph_kernels", "col_tma", "fused_y", "fused_z"]
+                "graph_kernels", "col_tma", "fused_y", "fused_z", "real"]
         return dict(zip(keys, (int(x) for x in v[:n])))
 
     def debug_deposit(self, slice_index):

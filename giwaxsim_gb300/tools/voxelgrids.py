@@ -205,7 +205,8 @@ def generate_voxel_grid_low_mem(input_path, r_voxel_size, q_voxel_size, max_q,
     fv = element_f_values(elements, energy, f1f2)
     plan = VoxelPlan(full, [(coords, fv, None)],
                      phis=geom.auto_phis if phis is None else phis,
-                     fill_bkg=fill_bkg, smooth=smooth, f0_element=None, ctx=ctx)
+                     fill_bkg=fill_bkg, smooth=smooth, f0_element=None,
+                     real=False if int(aff_num_qs) > 1 else None, ctx=ctx)
     try:
         plan.set_atoms()
         if int(aff_num_qs) > 1:

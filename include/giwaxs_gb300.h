@@ -144,7 +144,19 @@ typedef struct gw_voxel_params {
                            block, register cap), 0 .. count-1 with the count
                            from gw_voxel_block_variants(); an autotuner
                            picks it by timing; 0 = the default shape       */
-  int32_t reserved[1];
+  int32_t real_grids;   /* 1: the caller states that every structure's
+                           atom f values are real multiples of one complex
+                           value (one element; real occupancies), so each
+                           slice grid is that phase times a real grid: two
+                           window rows share one row transform and only the
+                           columns ky >= 0 are transformed (|F|^2 has the
+                           symmetry F(-k) = conj F(k) of a real grid); the
+                           bands are made symmetric.  Used in batched,
+                           nearest-bin plans with the Stockham kernels (not
+                           with GW_TRANSFORM_FUSED) when the window fits
+                           half a transform buffer; no shells, no backward.
+                           gw_voxel_info reports whether it runs.  0: the
+                           general path.                                   */
 } gw_voxel_params;
 
 typedef struct gw_structure {
@@ -229,8 +241,8 @@ int gw_voxel_get_sums(gw_voxel_plan *plan, double *sums);
 /* Plan sizes, in this order: [crop, batch, Ly, Lz, Nc, Nr, My, Mz, y_lo,
  * z_lo, k0, kz0, n_slices, device_bytes, graph_kernels, col_tma (1 when
  * the column kernel loads its tiles by TMA), fused_y, fused_z (1 when the
- * fused chirp-z kernel runs along that axis)].  Returns the number written
- * (at most n). */
+ * fused chirp-z kernel runs along that axis), real (1 when the real-grid
+ * path runs)].  Returns the number written (at most n). */
 int gw_voxel_info(gw_voxel_plan *plan, int64_t *info, int32_t n);
 /* Deposit indices of one slice (after execute): y,z voxel index per atom of
  * that slice's structure, -1 where the reference's valid_mask drops it

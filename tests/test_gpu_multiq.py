@@ -72,7 +72,8 @@ def test_shell_state_errors():
     full = F.VoxelGeometry.from_axes(geom.grid_size, geom.r_voxel_size, geom.q)
     xyz = d["coords"]
     fv = np.full(len(xyz), 6.0 + 0j)
-    plan = F.VoxelPlan(full, [(xyz, fv, None)], phis=[0.0, 30.0], f0_element=None)
+    plan = F.VoxelPlan(full, [(xyz, fv, None)], phis=[0.0, 30.0], f0_element=None,
+                       real=False)  # shells need the general path
     lower, upper, fk = V.aff_shell_tables(geom.q, 3, d["elements"], 1e4, F1F2)
     avg = np.ones((3, 1), dtype=complex)
     with pytest.raises(N.GwError) as e:  # before set_atoms
