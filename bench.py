@@ -31,12 +31,12 @@ METRIC = "slices/s & s/detector image: batched vs plain on 1 GB300 at <=1e-5 rel
 L2_BYTES = 129 * 1024 * 1024
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per slice of the
-# two transform kernels, keyed by (workload, kernel, fft_y, fft_z), from one
-# ncu --set full capture of a 51-slice launch of that kernel on the same
-# workload and plan shape; a launch's traffic is this times its slices
-# (both kernels move per-slice data only).
-NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024): (1.48 + 38.03) * 1e6 / 51,
-               ("si-100A", "col_czt_bin", 1280, 1024): (148.42 + 28.70) * 1e6 / 51}
+# two transform kernels, keyed by (workload, kernel, fft_y, fft_z, real
+# grids), from one ncu --set full capture of a 51-slice launch of that
+# kernel on the same workload and plan shape; a launch's traffic is this
+# times its slices (both kernels move per-slice data only).
+NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024, 0): (1.48 + 38.03) * 1e6 / 51,
+               ("si-100A", "col_czt_bin", 1280, 1024, 0): (148.42 + 28.70) * 1e6 / 51}
 
 
 def parse():
@@ -366,16 +366,19 @@ def run_gb300(args, world, rank, local, pg):
     # detector), from the eager per-kernel event times
     peak, peak_kind = measured_peaks()
 
+    # voxels with a count (the finalize reads their sums only)
+    counted = int(np.count_nonzero(plan.counts()))
+
     def kernel_roof(name):
         ms_tot, nl = kt[name]
         avg_ms = ms_tot / max(nl, 1)
         # slices per launch of the batched kernels: the batches' average
         spl = n_slices / nl if name in ("row_czt", "col_czt_bin") else None
-        algo = algorithmic_bytes(name, info, w, spl, dargs, plan.Qc)
+        algo = algorithmic_bytes(name, info, w, spl, dargs, plan.Qc, counted)
         if not algo:
             return None
         achieved = algo / (avg_ms / 1e3) / 1e9
-        tkey = (args.workload, name, info["My"], info["Mz"])
+        tkey = (args.workload, name, info["My"], info["Mz"], info.get("real", 0))
         traffic = NCU_TRAFFIC[tkey] * spl if tkey in NCU_TRAFFIC else None
         r = {"kernel": name, "bound": "hbm", "achieved": achieved,
              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
@@ -483,7 +486,9 @@ def shared_roof(name, info, spl, avg_ms):
     read and one write of every point per pass, forward and inverse) per
     launch, against the nominal shared bandwidth."""
     m = info["My"] if name == "row_czt" else info["Mz"]
-    units = spl * (info["Lz"] if name == "row_czt" else info["Nc"])
+    # real grids: two window rows per row transform, columns ky >= 0 only
+    rows = info["Lz"] / 2 if info.get("real") else info["Lz"]
+    units = spl * (rows if name == "row_czt" else f1_columns(info))
     sb = units * 2 * fft_passes(m) * m * 16
     speak = 152 * 128 * 2070e6 / 1e12
     return {"achieved": sb / (avg_ms / 1e3) / 1e12, "peak": speak,
@@ -679,19 +684,30 @@ def run_profile(args, w, geom, phis, items, ctx):
     plan.close()
 
 
-def algorithmic_bytes(name, info, w, S, dargs, Qc):
+def f1_columns(info):
+    """Columns of the row stage's output F1: the band's Nc, or with real
+    grids the columns ky >= 0 (from m_zero = -k0 on)."""
+    return info["Nc"] + info["k0"] if info.get("real") else info["Nc"]
+
+
+def algorithmic_bytes(name, info, w, S, dargs, Qc, counted=None):
     """Bytes a launch of `name` must move at minimum (its inputs read once,
-    outputs written once), per the plan's sizes; S = slices per launch."""
+    outputs written once), per the plan's sizes; S = slices per launch.
+    The row stage's input is the window grid (complex; real with real
+    grids), its output F1; the column stage reads F1 and read-modify-writes
+    a float64 sum of every band pixel."""
+    nf = f1_columns(info)
     if name == "row_czt":
-        return S * info["Lz"] * (info["Ly"] + info["Nc"]) * 8
+        return S * info["Lz"] * (info["Ly"] * (4 if info.get("real") else 8) + nf * 8)
     if name == "col_czt_bin":
-        # F1 read + float64 read-modify-write of every binned pixel
-        return S * (info["Lz"] * info["Nc"] * 8 + info["Nr"] * info["Nc"] * 16)
+        return S * (info["Lz"] * nf * 8 + info["Nr"] * info["Nc"] * 16)
     if name == "detector":
         npx = dargs["num_pixels"] ** 2
         return len(dargs["psis"]) * npx * 4 + npx * 8
     if name == "finalize":
-        return Qc ** 3 * (8 + 8 + 4)
+        # the float64 sum of every voxel with a count, the float32 I(q) of
+        # every voxel (the count factor tables are a few KB)
+        return (Qc ** 3 if counted is None else counted) * 8 + Qc ** 3 * 4
     return None
 
 

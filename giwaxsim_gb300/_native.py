@@ -31,6 +31,7 @@ EXPORTS = [
     "gw_voxel_set_shells", "gw_voxel_get_iq32", "gw_debug_convert",
     "gw_voxel_execute", "gw_voxel_capture_graph", "gw_voxel_get_iq",
     "gw_voxel_set_wait_limit", "gw_set_alloc_fault", "gw_voxel_block_variants",
+    "gw_host_pin", "gw_host_unpin",
     "gw_voxel_device_iq32", "gw_voxel_get_counts", "gw_voxel_get_sums",
     "gw_voxel_info", "gw_voxel_debug_deposit", "gw_voxel_debug_window",
     "gw_voxelgrid",
@@ -135,6 +136,8 @@ def _declare(lib):
         "gw_voxel_capture_graph": ([P], ctypes.c_int),
         "gw_voxel_set_wait_limit": ([P, ctypes.c_uint32], ctypes.c_int),
         "gw_set_alloc_fault": ([i64], ctypes.c_int),
+        "gw_host_pin": ([P, ctypes.c_uint64], ctypes.c_int),
+        "gw_host_unpin": ([P], ctypes.c_int),
         "gw_voxel_block_variants": ([], ctypes.c_int32),
         "gw_voxel_get_iq": ([P, P, i32], ctypes.c_int),
         "gw_voxel_device_iq32": ([P, ctypes.c_int32, pp], ctypes.c_int),

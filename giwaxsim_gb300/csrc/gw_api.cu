@@ -348,6 +348,26 @@ int gw_set_alloc_fault(int64_t after) {
   return GW_OK;
 }
 
+int gw_host_pin(void *ptr, uint64_t bytes) {
+  if (!ptr || bytes == 0) return gw::fail(GW_ERR_ARG, "gw_host_pin: null or empty buffer");
+  const cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return gw::fail(GW_ERR_CUDA, std::string("gw_host_pin: ") + cudaGetErrorString(e));
+  }
+  return GW_OK;
+}
+
+int gw_host_unpin(void *ptr) {
+  if (!ptr) return gw::fail(GW_ERR_ARG, "gw_host_unpin: null buffer");
+  const cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return gw::fail(GW_ERR_CUDA, std::string("gw_host_unpin: ") + cudaGetErrorString(e));
+  }
+  return GW_OK;
+}
+
 size_t gw_last_error(char *buf, size_t len) {
   const std::string &m = gw::g_last_error;
   if (buf && len) {

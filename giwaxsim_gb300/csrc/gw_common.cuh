@@ -138,20 +138,21 @@ __device__ __forceinline__ double f2d_exact(float x) {
   return __hiloint2double((int)hi, (int)(m << 29));
 }
 
-// (float)x, IEEE 754 round to nearest even, by bit manipulation on 32-bit
-// halves; the hardware conversion only where the result is subnormal, zero
-// from a nonzero input, infinite or NaN.  A mantissa carry into the
-// exponent field is the correctly rounded result.
+// (float)x, IEEE 754 round to nearest even, by integer operations on the
+// bit pattern; the hardware conversion (the float64 pipe) only where the
+// result is zero from any input, subnormal, infinite or NaN (|x| below
+// 2^-126 or from 2^128 on).  In range, the float's exponent and mantissa
+// are bits 29..58 of the double's pattern re-biased by 896 << 23: adding
+// 2^28 - 1 plus the kept lowest bit rounds to nearest even, and a mantissa
+// carry into the exponent field is the correctly rounded result (up to
+// infinity at the top).
 __device__ __forceinline__ float d2f_rn(double x) {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned sign = hi & 0x80000000u;
-  if (((hi << 1) | lo) == 0u) return __uint_as_float(sign);
-  const int fe = (int)((hi >> 20) & 0x7ffu) - 896;  // float exponent field
-  if (fe <= 0 || fe >= 255) return (float)x;
-  unsigned r = ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const unsigned rem = lo & 0x1fffffffu;  // the 29 dropped bits
-  if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ++r;
-  return __uint_as_float(sign | r);
+  const unsigned ah = hi & 0x7fffffffu;
+  if (ah - 0x38100000u >= 0x47F00000u - 0x38100000u) return (float)x;
+  const unsigned long long u =
+      (((unsigned long long)ah << 32) | lo) + (0x0FFFFFFFull + ((lo >> 29) & 1u));
+  return __uint_as_float(((unsigned)(u >> 29) - (896u << 23)) | (hi & 0x80000000u));
 }
 
 // (float)n, exact for n < 2^23 (n in the mantissa of 2^23); the hardware
@@ -159,6 +160,18 @@ __device__ __forceinline__ float d2f_rn(double x) {
 __device__ __forceinline__ float small_u2f(unsigned n) {
   if (n >= 8388608u) return (float)n;
   return __fsub_rn(__uint_as_float(0x4B000000u + n), 8388608.0f);
+}
+
+// The count grid factorises, count = C2[(y, x) line] * C1[z]: a voxel's
+// 1 / count (times the structure average's inv_nstruct) is the product of
+// a line factor and a z factor, each correctly rounded (within about one
+// float32 ulp of inv_nstruct / count); 0 where either count is 0.  The
+// finalize and its adjoint use the same two factors.
+__device__ __forceinline__ float line_count_factor(unsigned c2, float inv_nstruct) {
+  return c2 ? inv_nstruct / small_u2f(c2) : 0.f;
+}
+__device__ __forceinline__ float z_count_factor(unsigned c1) {
+  return c1 ? 1.f / small_u2f(c1) : 0.f;
 }
 
 // ---------------------------------------------------------------- context

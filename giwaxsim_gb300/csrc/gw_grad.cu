@@ -99,9 +99,9 @@ __global__ void k_fin_adj(const double *g_iq, const unsigned int *C2,
       fxy[i] = t[ix] * t[Qc + iy];
     }
   }
+  const float r2 = line_count_factor(c2, inv_nstruct);
   for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
-    const unsigned cnt = c2 * (unsigned)C1[iz + off];
-    float scale = cnt ? inv_nstruct / (float)cnt : 0.f;
+    float scale = r2 * z_count_factor((unsigned)C1[iz + off]);
     if (use_f0) {
       float acc = f0_c;
 #pragma unroll

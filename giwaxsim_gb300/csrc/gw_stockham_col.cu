@@ -62,7 +62,8 @@ struct ColBin {
     const int m = moff + j0 + f;
     if (mr >= nr || m >= nc) return;
     const int co = cofs[m], ro = bn->rowofs[mr];
-    const bool mir = bn->mirror && m > bn->m_zero;
+    // the band's extra even-width column (m = 2 m_zero + 1) has no mirror
+    const bool mir = bn->mirror && m > bn->m_zero && m <= 2 * bn->m_zero;
     const int cm = mir ? cofs[2 * bn->m_zero - m] : -1;
     const int rm = mir ? bn->rowofs[2 * bn->r_zero - mr] : -1;
     if ((co < 0 || ro < 0) && (cm < 0 || rm < 0)) return;
@@ -102,7 +103,8 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc, int nf,
   for (int f = 0; f < NB; ++f) {
     const int m = moff + j0 + f;
     if (j0 + f < nf && m < nc &&
-        (cofs[m] >= 0 || (bn.mirror && m > bn.m_zero && cofs[2 * bn.m_zero - m] >= 0)))
+        (cofs[m] >= 0 || (bn.mirror && m > bn.m_zero && m <= 2 * bn.m_zero &&
+                          cofs[2 * bn.m_zero - m] >= 0)))
       any = true;
   }
   if (!any) return;

@@ -95,13 +95,19 @@ struct RowLoadPair {
     constexpr int HL = FftPlan<M>::LDM / 2;
     float re = 0.f, im = 0.f;
     const int ra = 2 * f, rb = 2 * f + 1;
+    // the deposit holds the real row's atom sum r (deposit_rows<.., REAL>):
+    // the grid value there is d_value_row of r u, projected back on u
     if (row0 + ra < n_rows) {
-      const float2 d = d_value_row(*a, rc[ra], n, rows[ra * HL + n]);
-      re = d.x * rc[ra].u.x + d.y * rc[ra].u.y;  // Re(d conj(u))
+      const float2 u = rc[ra].u;
+      const float r = rows[ra * HL + n].x;
+      const float2 d = d_value_row(*a, rc[ra], n, make_float2(r * u.x, r * u.y));
+      re = d.x * u.x + d.y * u.y;  // Re(d conj(u))
     }
     if (row0 + rb < n_rows) {
-      const float2 d = d_value_row(*a, rc[rb], n, rows[rb * HL + n]);
-      im = d.x * rc[rb].u.x + d.y * rc[rb].u.y;
+      const float2 u = rc[rb].u;
+      const float r = rows[rb * HL + n].x;
+      const float2 d = d_value_row(*a, rc[rb], n, make_float2(r * u.x, r * u.y));
+      im = d.x * u.x + d.y * u.y;
     }
     return cmul(make_float2(re, im), __ldg(cz->A + n));
   }
@@ -121,7 +127,8 @@ k_row_czt_real(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   __shared__ RowShared<2 * NB> rs;
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   const int row0 = blockIdx.x * 2 * NB;
-  deposit_rows<2 * NB, NT, false>(a, cz.L, slice0, n_sl, n_rows, row0, buf, LDM / 2, rs);
+  deposit_rows<2 * NB, NT, false, true>(a, cz.L, slice0, n_sl, n_rows, row0, buf,
+                                        LDM / 2, rs);
   RowLoadPair<M> ld{&a, &cz, buf, rs.k, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false, HALF, false>(buf, tw, nullptr, ld,
                                                             NoStore());

@@ -418,21 +418,32 @@ __global__ void k_col_tables(const gw_phi *ph, int g, int k0, int nc,
 // I = sum / count (0 where count == 0), crop, f0 factor (comparison.py:765-786,
 // voxelgrids.py:16-48, :828-857).  Output in crop coordinates (qy,qx,qz).
 // One warp per (qy, qx) line, lanes along qz (the contiguous axis), lines
-// in a grid-stride loop: per line the count factor C2 and the (qx, qy) part
-// of the separable f0 sum stay in registers; per qz the four z factors come
-// as one float4 (zf0) and C1 from L1.  The count and the f0 factor are exact
-// integers / float32 (the factor's 1e-7 relative error is far inside the
-// tolerance).  F64: the float64 I(q) (the sum times the factor, one float64
-// multiply); otherwise the float32 I(q) the detector gathers from, computed
-// in float32 from the sum rounded to float (no float64 arithmetic: on this
-// GPU the float64 pipe is the slow one), within about one float32 ulp of
-// the rounded float64 value.
+// in a grid-stride loop.  The count grid factorises, count = C2[line] *
+// C1[z]; a voxel's factor is (inv_nstruct / C2) (1 / C1) (count_factors),
+// with the z reciprocals and the four f0 z factors staged in shared memory
+// per block and, per line, C2's factor and the (qx, qy) part of the
+// separable f0 sum in registers.  A line with C2 = 0 holds no binned pixel:
+// zeros, no sum read; so does a voxel with C1 = 0.  F64: the float64 I(q)
+// (the sum times the float32 factor, one float64 multiply); otherwise the
+// float32 I(q) the detector gathers from, computed in float32 from the sum
+// rounded to float (no float64 arithmetic: on this GPU the float64 pipe is
+// the slow one), within 1.5 float32 ulps of the float64 I(q) rounded (both
+// use the same factor).  Dynamic shared memory: Qc float4 (use_f0) + Qc
+// floats.
 template <bool F64>
 __global__ void __launch_bounds__(256)
-k_finalize(const double *sum, const float2 *sumk, int kahan,
-           const unsigned int *C2, const int *C1, int W, int off, int Qc,
-           float inv_nstruct, const float *f0tab, const float4 *zf0,
-           int use_f0, float f0_c, float f0_invz, double *out64, float *out32) {
+k_finalize(const double *__restrict__ sum, const float2 *__restrict__ sumk, int kahan,
+           const unsigned int *__restrict__ C2, const int *__restrict__ C1, int W,
+           int off, int Qc, float inv_nstruct, const float *__restrict__ f0tab,
+           const float4 *__restrict__ zf0, int use_f0, float f0_c, float f0_invz,
+           double *__restrict__ out64, float *__restrict__ out32) {
+  extern __shared__ float4 s_zf0[];
+  float *s_rc1 = reinterpret_cast<float *>(s_zf0 + (use_f0 ? Qc : 0));
+  for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
+    s_rc1[iz] = z_count_factor((unsigned)C1[iz + off]);
+    if (use_f0) s_zf0[iz] = zf0[iz];
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int n_lines = Qc * Qc;
   const int stride = gridDim.x * (blockDim.x >> 5);
@@ -441,33 +452,43 @@ k_finalize(const double *sum, const float2 *sumk, int kahan,
     const int iy = line / Qc, ix = line - iy * Qc;
     const int wy = iy + off, wx = ix + off;
     const unsigned c2 = C2[(size_t)wy * W + wx];
-    const size_t wbase = ((size_t)wy * W + wx) * W + off;
     const size_t obase = (size_t)line * Qc;
-    float fxy[4];
+    if (c2 == 0u) {
+      for (int iz = lane; iz < Qc; iz += 32) {
+        if (F64) out64[obase + iz] = 0.0;
+        else out32[obase + iz] = 0.f;
+      }
+      continue;
+    }
+    const size_t wbase = ((size_t)wy * W + wx) * W + off;
+    const float r2 = line_count_factor(c2, inv_nstruct);
+    float fxy[4] = {0.f, 0.f, 0.f, 0.f};
     if (use_f0) {
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const float *t = f0tab + i * 3 * Qc;
-        fxy[i] = t[ix] * t[Qc + iy];
+        fxy[i] = __ldg(t + ix) * __ldg(t + Qc + iy);
       }
     }
 #pragma unroll 4
     for (int iz = lane; iz < Qc; iz += 32) {
-      const unsigned cnt = c2 * (unsigned)__ldg(C1 + iz + off);
+      const float rz = s_rc1[iz];
       double s = 0.0;
       float s32 = 0.f;
-      if (kahan) {
-        const float2 sc = sumk[wbase + iz];
-        if (F64) s = f2d_exact(sc.x) - f2d_exact(sc.y);
-        else s32 = sc.x - sc.y;
-      } else if (F64) {
-        s = sum[wbase + iz];
-      } else {
-        s32 = d2f_rn(sum[wbase + iz]);
+      if (rz != 0.f) {
+        if (kahan) {
+          const float2 sc = sumk[wbase + iz];
+          if (F64) s = f2d_exact(sc.x) - f2d_exact(sc.y);
+          else s32 = sc.x - sc.y;
+        } else if (F64) {
+          s = sum[wbase + iz];
+        } else {
+          s32 = d2f_rn(sum[wbase + iz]);
+        }
       }
-      float scale = cnt ? inv_nstruct / small_u2f(cnt) : 0.f;
+      float scale = r2 * rz;
       if (use_f0) {
-        const float4 z = __ldg(zf0 + iz);
+        const float4 z = s_zf0[iz];
         float acc = f0_c;
         acc += fxy[0] * z.x;
         acc += fxy[1] * z.y;
@@ -482,172 +503,8 @@ k_finalize(const double *sum, const float2 *sumk, int kahan,
   }
 }
 
-// Batched-mode finalize: the window is the crop (W = Qc, offset 0), so sum
-// and output share the flat index; each thread takes two consecutive voxels
-// with 16-byte loads and stores.  Same per-voxel arithmetic as k_finalize.
-template <bool F64>
-__global__ void k_finalize_flat(const double *sum, const float2 *sumk, int kahan,
-                                const unsigned int *C2, const int *C1, int Qc,
-                                float inv_nstruct, const float *f0tab,
-                                const float4 *zf0, int use_f0, float f0_c,
-                                float f0_invz, double *out64, float *out32) {
-  const int n = Qc * Qc * Qc;  // < 2^31 (checked by the caller)
-  const int npair = (n + 1) / 2;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npair;
-       p += gridDim.x * blockDim.x) {
-    const int i0 = 2 * p;
-    const bool two = i0 + 1 < n;
-    // (line, iz) of the pair's first voxel; the second is the next voxel
-    const int line0 = i0 / Qc, iz0 = i0 - line0 * Qc;
-    unsigned cnt[2] = {0u, 0u};
-#pragma unroll
-    for (int e = 0; e < 2; ++e) {
-      if (e == 1 && !two) break;
-      int line = line0, iz = iz0 + e;
-      if (iz == Qc) { iz = 0; ++line; }
-      cnt[e] = C2[line] * (unsigned)__ldg(C1 + iz);
-    }
-    // voxels no pixel was binned into hold a zero sum and I = 0: a pair
-    // of them (whole warps where a (qy, qx) line is never hit) skips the
-    // sum load and the float64 multiply
-    if ((cnt[0] | cnt[1]) == 0u) {
-      if (two) {
-        if (F64) reinterpret_cast<double2 *>(out64)[p] = make_double2(0.0, 0.0);
-        else reinterpret_cast<float2 *>(out32)[p] = make_float2(0.f, 0.f);
-      } else {
-        if (F64) out64[i0] = 0.0;
-        else out32[i0] = 0.f;
-      }
-      continue;
-    }
-    double s[2] = {0.0, 0.0};
-    float s32[2] = {0.f, 0.f};
-    if (kahan) {
-      for (int e = 0; e < 2; ++e)
-        if (e == 0 || two) {
-          const float2 sc = sumk[i0 + e];
-          if (F64) s[e] = f2d_exact(sc.x) - f2d_exact(sc.y);
-          else s32[e] = sc.x - sc.y;
-        }
-    } else if (two) {
-      const double2 v = reinterpret_cast<const double2 *>(sum)[p];
-      s[0] = v.x; s[1] = v.y;
-    } else {
-      s[0] = sum[i0];
-    }
-    if (!F64 && !kahan) {
-      s32[0] = d2f_rn(s[0]);
-      s32[1] = d2f_rn(s[1]);
-    }
-    double I[2] = {0.0, 0.0};
-    float I32[2] = {0.f, 0.f};
-#pragma unroll
-    for (int e = 0; e < 2; ++e) {
-      if (e == 1 && !two) break;
-      int line = line0, iz = iz0 + e;
-      if (iz == Qc) { iz = 0; ++line; }
-      float scale = cnt[e] ? inv_nstruct / small_u2f(cnt[e]) : 0.f;
-      if (use_f0) {
-        const int iy = line / Qc, ix = line - iy * Qc;
-        const float4 z = __ldg(zf0 + iz);
-        float acc = f0_c;
-        acc += (__ldg(f0tab + ix) * __ldg(f0tab + Qc + iy)) * z.x;
-        acc += (__ldg(f0tab + 3 * Qc + ix) * __ldg(f0tab + 4 * Qc + iy)) * z.y;
-        acc += (__ldg(f0tab + 6 * Qc + ix) * __ldg(f0tab + 7 * Qc + iy)) * z.z;
-        acc += (__ldg(f0tab + 9 * Qc + ix) * __ldg(f0tab + 10 * Qc + iy)) * z.w;
-        const float fq = acc * f0_invz;
-        scale *= fq * fq;
-      }
-      if (F64) I[e] = s[e] * f2d_exact(scale);
-      else I32[e] = s32[e] * scale;
-    }
-    if (two) {
-      if (F64) reinterpret_cast<double2 *>(out64)[p] = make_double2(I[0], I[1]);
-      else reinterpret_cast<float2 *>(out32)[p] = make_float2(I32[0], I32[1]);
-    } else {
-      if (F64) out64[i0] = I[0];
-      else out32[i0] = I32[0];
-    }
-  }
-}
-
-// The step's float32 finalize over the flat crop (window = crop) for the
-// float64 sums: four consecutive voxels per thread and iteration, their
-// count factors, sums (two 16-byte loads) and f0 factors loaded together,
-// one 16-byte store; the same per-voxel arithmetic as
-// k_finalize_flat<false>.  n4 = Qc^3 / 4 quads; the caller handles no tail
-// (k_finalize_flat<false> covers the last Qc^3 mod 4 voxels).
-__global__ void __launch_bounds__(256)
-k_finalize32_quad(const double *__restrict__ sum, const unsigned int *__restrict__ C2,
-                  const int *__restrict__ C1, int Qc, float inv_nstruct,
-                  const float *__restrict__ f0tab, const float4 *__restrict__ zf0,
-                  int use_f0, float f0_c, float f0_invz, float *__restrict__ out32,
-                  int64_t n4) {
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i0 = 4 * q;
-    int line = (int)(i0 / Qc), iz = (int)(i0 - (int64_t)line * Qc);
-    int lines[4], izs[4];
-    unsigned cnt[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      lines[e] = line;
-      izs[e] = iz;
-      cnt[e] = __ldg(C2 + line) * (unsigned)__ldg(C1 + iz);
-      if (++iz == Qc) { iz = 0; ++line; }
-    }
-    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-    if ((cnt[0] | cnt[1] | cnt[2] | cnt[3]) != 0u) {
-      const double2 a = reinterpret_cast<const double2 *>(sum)[2 * q];
-      const double2 b = reinterpret_cast<const double2 *>(sum)[2 * q + 1];
-      const float s[4] = {d2f_rn(a.x), d2f_rn(a.y), d2f_rn(b.x), d2f_rn(b.y)};
-      float I[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        float scale = cnt[e] ? inv_nstruct / small_u2f(cnt[e]) : 0.f;
-        if (use_f0) {
-          const int iy = lines[e] / Qc, ix = lines[e] - iy * Qc;
-          const float4 z = __ldg(zf0 + izs[e]);
-          float acc = f0_c;
-          acc += (__ldg(f0tab + ix) * __ldg(f0tab + Qc + iy)) * z.x;
-          acc += (__ldg(f0tab + 3 * Qc + ix) * __ldg(f0tab + 4 * Qc + iy)) * z.y;
-          acc += (__ldg(f0tab + 6 * Qc + ix) * __ldg(f0tab + 7 * Qc + iy)) * z.z;
-          acc += (__ldg(f0tab + 9 * Qc + ix) * __ldg(f0tab + 10 * Qc + iy)) * z.w;
-          const float fq = acc * f0_invz;
-          scale *= fq * fq;
-        }
-        I[e] = s[e] * scale;
-      }
-      o = make_float4(I[0], I[1], I[2], I[3]);
-    }
-    reinterpret_cast<float4 *>(out32)[q] = o;
-  }
-}
-
-// The last (at most three) voxels of the flat float32 finalize after the
-// quads, one thread each.
-__global__ void k_finalize_tail32(const double *sum, const unsigned int *C2,
-                                  const int *C1, int Qc, float inv_nstruct,
-                                  const float *f0tab, const float4 *zf0, int use_f0,
-                                  float f0_c, float f0_invz, float *out32,
-                                  int64_t begin, int64_t end) {
-  const int64_t i = begin + threadIdx.x;
-  if (i >= end) return;
-  const int line = (int)(i / Qc), iz = (int)(i - (int64_t)line * Qc);
-  const unsigned cnt = C2[line] * (unsigned)C1[iz];
-  float scale = cnt ? inv_nstruct / small_u2f(cnt) : 0.f;
-  if (use_f0) {
-    const int iy = line / Qc, ix = line - iy * Qc;
-    const float4 z = zf0[iz];
-    float acc = f0_c;
-    acc += (f0tab[ix] * f0tab[Qc + iy]) * z.x;
-    acc += (f0tab[3 * Qc + ix] * f0tab[4 * Qc + iy]) * z.y;
-    acc += (f0tab[6 * Qc + ix] * f0tab[7 * Qc + iy]) * z.z;
-    acc += (f0tab[9 * Qc + ix] * f0tab[10 * Qc + iy]) * z.w;
-    const float fq = acc * f0_invz;
-    scale *= fq * fq;
-  }
-  out32[i] = cnt ? d2f_rn(sum[i]) * scale : 0.f;
+size_t finalize_smem(int Qc, bool use_f0) {
+  return (size_t)Qc * ((use_f0 ? sizeof(float4) : 0) + sizeof(float));
 }
 
 // Shell code of every window voxel (voxelgrids.py:651-652, :659-664, :706):
@@ -1006,48 +863,30 @@ int enqueue_finalize(gw_voxel_plan *P, bool f64) {
     float2 *sumk = P->d_sumk ? P->d_sumk + t * P->sum_stride : nullptr;
     double *o64 = f64 ? P->d_iq64 + t * P->iq_stride : nullptr;
     float *o32 = f64 ? nullptr : P->d_iq32 + t * P->iq_stride;
-    if (P->W == P->Qc && P->lo == P->wlo && (int64_t)Qc3 < ((int64_t)1 << 31) - 2) {
+    {
       gw::KTimer tm(ctx, GW_K_FINALIZE);
-      const int64_t pairs = ((int64_t)Qc3 + 1) / 2;
-      const int blocks = (int)std::min<int64_t>((pairs + 255) / 256, 16 * ctx->sm_count);
-      if (f64) {
-        k_finalize_flat<true><<<blocks, 256, 0, st>>>(
-            sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
-            P->p.f0_z > 0, f0c, f0iz, o64, o32);
-        GW_LAUNCHED(ctx);
-      } else if (!kahan) {
-        // quads of voxels, then the Qc^3 mod 4 last ones by the pair kernel
-        // (it starts at an even voxel: its pairs from that one on)
-        const int64_t n4 = (int64_t)Qc3 / 4;
-        const int qb = (int)std::min<int64_t>((n4 + 255) / 256, 8 * ctx->sm_count);
-        k_finalize32_quad<<<std::max(qb, 1), 256, 0, st>>>(
-            sum, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
-            P->p.f0_z > 0, f0c, f0iz, o32, n4);
-        GW_LAUNCHED(ctx);
-        const int64_t done = 4 * n4;
-        if (done < (int64_t)Qc3) {
-          k_finalize_tail32<<<1, 32, 0, st>>>(sum, P->d_C2, P->d_C1, P->Qc, inv_ns,
-                                               P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c,
-                                               f0iz, o32, done, (int64_t)Qc3);
-          GW_LAUNCHED(ctx);
-        }
-      } else {
-        k_finalize_flat<false><<<blocks, 256, 0, st>>>(
-            sum, sumk, kahan, P->d_C2, P->d_C1, P->Qc, inv_ns, P->d_f0, P->d_zf0,
-            P->p.f0_z > 0, f0c, f0iz, o64, o32);
-        GW_LAUNCHED(ctx);
+      const bool use_f0 = P->p.f0_z > 0;
+      const size_t smem = finalize_smem(P->Qc, use_f0);
+      // above the default 48 KB (crops beyond about 2400 voxels a side)
+      static size_t smem_set[2] = {0, 0};
+      if (smem > (48u << 10) && smem > smem_set[f64]) {
+        if (f64)
+          GW_CUDA(cudaFuncSetAttribute(k_finalize<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        else
+          GW_CUDA(cudaFuncSetAttribute(k_finalize<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set[f64] = smem;
       }
-    } else {
-      gw::KTimer tm(ctx, GW_K_FINALIZE);
       const int blocks = std::min((P->Qc * P->Qc + 7) / 8, 16 * ctx->sm_count);
       if (f64)
-        k_finalize<true><<<blocks, 256, 0, st>>>(
+        k_finalize<true><<<blocks, 256, smem, st>>>(
             sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
-            inv_ns, P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
+            inv_ns, P->d_f0, P->d_zf0, use_f0, f0c, f0iz, o64, o32);
       else
-        k_finalize<false><<<blocks, 256, 0, st>>>(
+        k_finalize<false><<<blocks, 256, smem, st>>>(
             sum, sumk, kahan, P->d_C2, P->d_C1, P->W, P->lo - P->wlo, P->Qc,
-            inv_ns, P->d_f0, P->d_zf0, P->p.f0_z > 0, f0c, f0iz, o64, o32);
+            inv_ns, P->d_f0, P->d_zf0, use_f0, f0c, f0iz, o64, o32);
       GW_LAUNCHED(ctx);
     }
     if (K > 0 && P->shell_mode == GW_SHELLS_REFERENCE) {

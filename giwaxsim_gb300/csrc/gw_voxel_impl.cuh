@@ -372,8 +372,10 @@ struct RowShared {
 // floor division, valid mask, np.add.at): NB window rows starting at row0
 // of the batch, row f into buf[f * ldm + 0 .. L) (zeroed first), by shared
 // atomics.  Sets up rs (slot, window row, atom range and constants of every
-// row) and leaves the block synchronised.
-template <int NB, int NT, bool BIL>
+// row) and leaves the block synchronised.  REAL (real grids, nearest bin):
+// each atom adds Re(f conj(u)) to the .x of its element only, u the row's
+// unit phase (the row is u times that real row): one shared atomic per atom.
+template <int NB, int NT, bool BIL, bool REAL = false>
 __device__ __forceinline__ void deposit_rows(const SliceArgs &a, int L,
                                              int slice0, int n_sl, int n_rows,
                                              int row0, float2 *buf, int ldm,
@@ -419,8 +421,13 @@ __device__ __forceinline__ void deposit_rows(const SliceArgs &a, int L,
       const float4 q = a.xyf_s[at];
       if (deposit_column(a, rs.d[f], make_float2(q.x, q.y), at, yy)) {
         if (yy < a.Ly) {
-          atomicAdd(&buf[f * ldm + yy].x, q.z);
-          atomicAdd(&buf[f * ldm + yy].y, q.w);
+          if constexpr (REAL) {
+            const float2 u = rs.k[f].u;
+            atomicAdd(&buf[f * ldm + yy].x, fmaf(q.z, u.x, q.w * u.y));
+          } else {
+            atomicAdd(&buf[f * ldm + yy].x, q.z);
+            atomicAdd(&buf[f * ldm + yy].y, q.w);
+          }
         } else {
           dev_error(a.err, GW_DEVERR_BOX);
         }

@@ -191,15 +191,31 @@ class HostPool:
     still references it) is handed out again instead.  Arrays given out are
     ordinary float64 arrays owned by the caller for as long as it keeps
     them; the pool keeps at most `per_shape` buffers per shape and
-    `max_bytes` in all."""
+    `max_bytes` in all.  Kept buffers are page-locked (gw_host_pin) when
+    `pin` is on, so that the result copies into them run at the link's
+    speed rather than through the driver's staging buffers; clear()
+    releases them (at exit too)."""
 
-    def __init__(self, min_bytes=64 << 20, per_shape=2, max_bytes=4 << 30):
+    def __init__(self, min_bytes=64 << 20, per_shape=2, max_bytes=4 << 30,
+                 pin=True):
         import sys
         import threading
         self._refs = sys.getrefcount
         self._lock = threading.Lock()
         self.min_bytes, self.per_shape, self.max_bytes = min_bytes, per_shape, max_bytes
+        self.pin = pin
         self._bufs = {}
+        self._pinned = []
+
+    def _pin(self, b):
+        """Page-lock b (kept by the pool until clear()); a refusal leaves it
+        pageable."""
+        try:
+            ok = N.lib().gw_host_pin(ctypes.c_void_p(b.ctypes.data), b.nbytes) == N.GW_OK
+        except N.NativeLibraryMissing:
+            ok = False
+        if ok:
+            self._pinned.append(b)
 
     def empty(self, shape, dtype=np.float64):
         shape, dtype = tuple(int(v) for v in shape), np.dtype(dtype)
@@ -218,14 +234,22 @@ class HostPool:
             b = np.empty(shape, dtype)
             if len(bufs) < self.per_shape and held + nbytes <= self.max_bytes:
                 bufs.append(b)
+                if self.pin:
+                    self._pin(b)
             return b.view()
 
     def clear(self):
+        """Drop the kept buffers (arrays handed out stay valid), releasing
+        their page locks first."""
         with self._lock:
+            for b in self._pinned:
+                N.lib().gw_host_unpin(ctypes.c_void_p(b.ctypes.data))
+            self._pinned.clear()
             self._bufs.clear()
 
 
 HOST_POOL = HostPool()
+atexit.register(HOST_POOL.clear)  # page locks released before the driver goes
 
 
 class VoxelPlan:

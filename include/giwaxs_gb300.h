@@ -53,6 +53,13 @@ size_t gw_last_error(char *buf, size_t len);
  * were out of memory (after < 0 turns it off).  The environment variable
  * GW_FAIL_ALLOC_AFTER=n does the same counting from process start. */
 int gw_set_alloc_fault(int64_t after);
+/* Page-lock an existing host buffer (cudaHostRegister) so that the copies of
+ * results into it and of inputs from it run at the link's speed, and release
+ * it again (before the buffer is freed).  No counterpart in the reference
+ * (its results are numpy arrays on the host).  GW_ERR_CUDA when the driver
+ * refuses (the buffer stays usable, unpinned). */
+int gw_host_pin(void *ptr, uint64_t bytes);
+int gw_host_unpin(void *ptr);
 
 /* ---- context ----------------------------------------------------------- */
 typedef struct gw_ctx gw_ctx;

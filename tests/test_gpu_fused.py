@@ -97,8 +97,10 @@ def test_fused_options_vs_stockham(opt):
             kw["average"] = "separate"
     outs = {}
     for tr in ("fused", "stockham"):
+        # shells need the general path (no real grids)
         plan = F.VoxelPlan(geom, structures, phis=phis, fill_bkg=True, smooth=1,
-                           fft_y=1024, fft_z=1280, transform=tr, **kw)
+                           fft_y=1024, fft_z=1280, transform=tr,
+                           real=False if opt == "shells" else None, **kw)
         plan.set_atoms()
         if opt == "shells":
             lower = np.array([0.0, 0.7, 1.4])

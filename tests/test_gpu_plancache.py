@@ -114,3 +114,21 @@ def test_result_copy_into_resident_buffer_fills_every_line():
         assert np.any(out.reshape(-1, plan.Qc)[~empty_lines] != 0)
     finally:
         plan.close()
+
+
+def test_host_pool_pins_kept_buffers():
+    """Kept result buffers are page-locked once and released by clear();
+    a buffer handed out again is the same memory."""
+    pool = F.HostPool(min_bytes=1 << 20, per_shape=1)
+    a = pool.empty((256, 1024))
+    assert len(pool._pinned) == 1
+    ptr = a.ctypes.data
+    del a
+    b = pool.empty((256, 1024))          # recycled: no second page lock
+    assert b.ctypes.data == ptr and len(pool._pinned) == 1
+    c = pool.empty((256, 1024))          # b still held: a fresh, unkept one
+    assert c.ctypes.data != ptr and len(pool._pinned) == 1
+    pool.clear()
+    assert pool._pinned == []
+    b[:] = 1.0                           # still ordinary memory
+    assert b.sum() == 256 * 1024
