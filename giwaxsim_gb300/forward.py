@@ -215,7 +215,9 @@ class HostPool:
         except N.NativeLibraryMissing:
             ok = False
         if ok:
-            self._pinned.append(b)
+            # the address only: a reference here would keep the buffer
+            # from ever being handed out again (see empty())
+            self._pinned.append(b.ctypes.data)
 
     def empty(self, shape, dtype=np.float64):
         shape, dtype = tuple(int(v) for v in shape), np.dtype(dtype)
@@ -242,8 +244,8 @@ class HostPool:
         """Drop the kept buffers (arrays handed out stay valid), releasing
         their page locks first."""
         with self._lock:
-            for b in self._pinned:
-                N.lib().gw_host_unpin(ctypes.c_void_p(b.ctypes.data))
+            for ptr in self._pinned:
+                N.lib().gw_host_unpin(ctypes.c_void_p(ptr))
             self._pinned.clear()
             self._bufs.clear()
 

@@ -141,3 +141,41 @@ def test_detector_model_keeps_one_context(monkeypatch):
     t.start()
     t.join()
     assert seen[0] is not m.ctx
+
+
+def test_host_pool_recycles_pinned_buffers(monkeypatch):
+    """A kept buffer is page-locked once, handed out again once its result
+    is dropped, and unlocked by clear() (the pool keeps addresses, not
+    references, of what it locked)."""
+    import numpy as np
+    from giwaxsim_gb300 import _native as N
+    from giwaxsim_gb300.forward import HostPool
+
+    class FakePin:
+        def __init__(self):
+            self.pinned, self.unpinned = [], []
+
+        def gw_host_pin(self, ptr, n):
+            self.pinned.append(ptr.value)
+            return 0
+
+        def gw_host_unpin(self, ptr):
+            self.unpinned.append(ptr.value)
+            return 0
+
+    fake = FakePin()
+    monkeypatch.setattr(N, "lib", lambda: fake)
+    pool = HostPool(min_bytes=1 << 20, per_shape=1)
+    a = pool.empty((256, 1024))
+    ptr = a.ctypes.data
+    del a
+    b = pool.empty((256, 1024))
+    assert b.ctypes.data == ptr and fake.pinned == [ptr]
+    c = pool.empty((256, 1024))          # b still held: a fresh, unkept one
+    assert c.ctypes.data != ptr and fake.pinned == [ptr]
+    small = pool.empty((4, 4))           # below min_bytes: never locked
+    assert small.shape == (4, 4) and fake.pinned == [ptr]
+    pool.clear()
+    assert fake.unpinned == [ptr] and pool._pinned == []
+    b[:] = 1.0
+    assert b.sum() == 256 * 1024
