@@ -968,6 +968,14 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: invalid geometry");
   if (p->smooth < 0)
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: smooth must be >= 0");
+  // real grids take each structure's phase from its average voxel f
+  if (p->real_grids)
+    for (int t = 0; t < n_struct; ++t) {
+      const double re = structs[t].avg_f_re, im = structs[t].avg_f_im;
+      if (!std::isfinite(re) || !std::isfinite(im) || (re == 0.0 && im == 0.0))
+        return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: real_grids needs a finite, "
+                                    "nonzero average voxel f for every structure");
+    }
   if (p->block_variant < 0 || p->block_variant >= gwv::fused_variant_count())
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: block_variant must be 0.." +
                                     std::to_string(gwv::fused_variant_count() - 1));

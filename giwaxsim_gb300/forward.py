@@ -318,6 +318,8 @@ class VoxelPlan:
                 rg = coord_ranges(coords) if ranges is None else ranges[i]
                 geom.check_bounds(coords, rg)
                 xb, yb, zb, avg, mv = structure_constants(coords, fv, r, rg)
+            # real grids take the phase of avg (a finite, nonzero value)
+            all_real = all_real and bool(np.isfinite(avg) and avg != 0)
             st[i] = (begin, len(coords), xb, yb, zb, avg.real, avg.imag, mv)
             begin += len(coords)
             xyz.append(coords)
@@ -363,7 +365,8 @@ class VoxelPlan:
                     and "fused" not in (ty, tz))
         elif real and not all_real:
             raise ValueError("real=True needs every structure's f values to be "
-                             "real multiples of one complex value")
+                             "real multiples of one complex value, with a finite, "
+                             "nonzero average voxel f")
         p.real_grids = int(bool(real))
         self.params = p
         self.Qc = geom.crop_hi - geom.crop_lo + 1

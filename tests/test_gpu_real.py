@@ -150,6 +150,14 @@ def test_plans_that_keep_the_general_path():
                deposit="bilinear")["info"]["real"] == 0
     assert run(geom, [(xyz, fv, None)], PHIS, False, 0,
                transform="fused", fft_y=1024, fft_z=1024)["info"]["real"] == 0
+    # one atom: zero extents, no finite average voxel f to take the phase of
+    one = np.array([[1.3, -0.4, 2.2]])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        assert run(geom, [(one, np.array([6.0 + 2.0j]), None)], PHIS, False, 0,
+                   f0_element=None)["info"]["real"] == 0
+        with pytest.raises(ValueError):
+            F.VoxelPlan(geom, [(one, np.array([6.0 + 2.0j]), None)], phis=PHIS,
+                        f0_element=None, real=True)
     plan = F.VoxelPlan(geom, [(xyz, fv, None)], phis=PHIS)
     try:
         assert plan.info()["real"] == 1
