@@ -255,16 +255,16 @@ struct GradRow {
 
 template <int M>
 struct RowLoadAdj {
-  const SliceArgs *a;
-  const GradRow *gr;
+  const float2 *G1, *Aa;  // by value: no reads through the parameters
+  int nc, Lz;
   const int *r_slot, *r_zz;
   int row0, n_rows;
   __device__ float2 operator()(int f, int n) const {
     const int row = row0 + f;
-    if (row >= n_rows || n >= gr->nc) return make_float2(0.f, 0.f);
+    if (row >= n_rows || n >= nc) return make_float2(0.f, 0.f);
     const int slot = r_slot[f], zz = r_zz[f];
-    const float2 g = gr->G1[((size_t)slot * gr->nc + n) * a->Lz + zz];
-    return cmul(conjf2(g), __ldg(gr->Aa + n));
+    const float2 g = G1[((size_t)slot * nc + n) * Lz + zz];
+    return cmul(conjf2(g), __ldg(Aa + n));
   }
 };
 
@@ -304,7 +304,7 @@ k_row_bwd(SliceArgs a, GradRow gr, int slice0, int n_sl, int n_rows) {
     r_cnt[NB] = acc;
   }
   __syncthreads();
-  RowLoadAdj<M> ld{&a, &gr, r_slot, r_zz, row0, n_rows};
+  RowLoadAdj<M> ld{gr.G1, gr.Aa, gr.nc, a.Lz, r_slot, r_zz, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, true>(buf, tw, nullptr, ld, NoStore());
   fft_run<M, NB, NT, true, 0, true, 0, false>(buf, tw, gr.Ha, NoLoad(), NoStore());
   // G_D on the window, and the per-row sums of G_D m and G_D dm/dsigma

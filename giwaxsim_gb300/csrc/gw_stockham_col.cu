@@ -46,7 +46,7 @@ __host__ __device__ constexpr bool col_tma_ok() {
 // sums; with mirrored binning (real grids) also at (2 m_zero - m,
 // 2 r_zero - mr) for m > m_zero.
 struct ColBin {
-  const BinArgs *bn;
+  BinArgs bn;       // by value: no reads through a pointer to the parameters
   const int *cofs;
   const float2 *B;
   float2 cbg;
@@ -54,23 +54,23 @@ struct ColBin {
   int64_t soff;  // sum-grid offset of the slice's structure (separate mode)
   __device__ void add(int co, int ro, float I) const {
     if (co < 0 || ro < 0) return;
-    if (bn->shell && !shell_member(bn->shell[co + ro], bn->shell_k)) return;
-    if (bn->kahan) kahan_add(bn->sumk + soff + co + ro, I);
-    else atomicAdd(bn->sum + soff + co + ro, f2d_exact(I));
+    if (bn.shell && !shell_member(bn.shell[co + ro], bn.shell_k)) return;
+    if (bn.kahan) kahan_add(bn.sumk + soff + co + ro, I);
+    else atomicAdd(bn.sum + soff + co + ro, f2d_exact(I));
   }
   __device__ void operator()(int f, int mr, float2 v) const {
     const int m = moff + j0 + f;
     if (mr >= nr || m >= nc) return;
-    const int co = cofs[m], ro = bn->rowofs[mr];
+    const int co = cofs[m], ro = bn.rowofs[mr];
     // the band's extra even-width column (m = 2 m_zero + 1) has no mirror
-    const bool mir = bn->mirror && m > bn->m_zero && m <= 2 * bn->m_zero;
-    const int cm = mir ? cofs[2 * bn->m_zero - m] : -1;
-    const int rm = mir ? bn->rowofs[2 * bn->r_zero - mr] : -1;
+    const bool mir = bn.mirror && m > bn.m_zero && m <= 2 * bn.m_zero;
+    const int cm = mir ? cofs[2 * bn.m_zero - m] : -1;
+    const int rm = mir ? bn.rowofs[2 * bn.r_zero - mr] : -1;
     if ((co < 0 || ro < 0) && (cm < 0 || rm < 0)) return;
     float2 X = cmul(v, __ldg(B + mr));
-    if (bn->k0 + m == 0 && bn->kz0 + mr == 0) {
-      X.x += cbg.x * bn->dc_scale;
-      X.y += cbg.y * bn->dc_scale;
+    if (bn.k0 + m == 0 && bn.kz0 + mr == 0) {
+      X.x += cbg.x * bn.dc_scale;
+      X.y += cbg.y * bn.dc_scale;
     }
     const float I = X.x * X.x + X.y * X.y;
     add(co, ro, I);
@@ -144,7 +144,7 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc, int nf,
     fft_run<M, NB, NT, false, 1, false, 0, true, HALF, false>(buf, tw, nullptr, ld,
                                                              NoStore());
   }
-  ColBin st{&bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, j0, moff,
+  ColBin st{bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, j0, moff,
             bn.sstride * (int64_t)(sl / a.n_phi)};
   fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), st);
 }

@@ -24,17 +24,20 @@ namespace {
 // memory.  The row buffers share storage with the FFT buffer: the first pass
 // reads all its inputs before it writes.
 template <int M>
+// Functors hold what they read by value (registers), never a pointer to
+// the kernel's parameters.
 struct RowLoad {
-  const SliceArgs *a;
-  const CztArgs *cz;
+  RowValueArgs va;
+  const float2 *A;        // forward chirp
+  int L;                  // window length
   const float2 *rows;     // row f at rows + f * LDM
   const RowConst *rc;     // per block row (shared memory)
   int row0, n_rows;
   __device__ float2 operator()(int f, int n) const {
     const int row = row0 + f;
-    if (row >= n_rows || n >= cz->L) return make_float2(0.f, 0.f);
+    if (row >= n_rows || n >= L) return make_float2(0.f, 0.f);
     const float2 dep = rows[f * FftPlan<M>::LDM + n];
-    return cmul(d_value_row(*a, rc[f], n, dep), __ldg(cz->A + n));
+    return cmul(d_value_row(va, rc[f], n, dep), __ldg(A + n));
   }
 };
 
@@ -64,7 +67,7 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   const int row0 = blockIdx.x * NB;
   deposit_rows<NB, NT, BIL>(a, cz.L, slice0, n_sl, n_rows, row0, buf, LDM, rs);
-  RowLoad<M> ld{&a, &cz, buf, rs.k, row0, n_rows};
+  RowLoad<M> ld{row_value_args(a), cz.A, cz.L, buf, rs.k, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false, HALF, false>(buf, tw, nullptr, ld,
                                                             NoStore());
   RowStore stv{cz.B, F1, row0, n_rows, nc_out};
@@ -85,13 +88,14 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
 // F1[row][j] = u_row Y_row[m_zero + j], j < nf.
 template <int M>
 struct RowLoadPair {
-  const SliceArgs *a;
-  const CztArgs *cz;
+  RowValueArgs va;
+  const float2 *A;        // forward chirp
+  int L;                  // window length
   const float2 *rows;     // block row r at rows + r * (LDM / 2)
   const RowConst *rc;     // per block row (shared memory)
   int row0, n_rows;       // row0: the block's first window row
   __device__ float2 operator()(int f, int n) const {
-    if (n >= cz->L) return make_float2(0.f, 0.f);
+    if (n >= L) return make_float2(0.f, 0.f);
     constexpr int HL = FftPlan<M>::LDM / 2;
     float re = 0.f, im = 0.f;
     const int ra = 2 * f, rb = 2 * f + 1;
@@ -100,16 +104,16 @@ struct RowLoadPair {
     if (row0 + ra < n_rows) {
       const float2 u = rc[ra].u;
       const float r = rows[ra * HL + n].x;
-      const float2 d = d_value_row(*a, rc[ra], n, make_float2(r * u.x, r * u.y));
+      const float2 d = d_value_row(va, rc[ra], n, make_float2(r * u.x, r * u.y));
       re = d.x * u.x + d.y * u.y;  // Re(d conj(u))
     }
     if (row0 + rb < n_rows) {
       const float2 u = rc[rb].u;
       const float r = rows[rb * HL + n].x;
-      const float2 d = d_value_row(*a, rc[rb], n, make_float2(r * u.x, r * u.y));
+      const float2 d = d_value_row(va, rc[rb], n, make_float2(r * u.x, r * u.y));
       im = d.x * u.x + d.y * u.y;
     }
-    return cmul(make_float2(re, im), __ldg(cz->A + n));
+    return cmul(make_float2(re, im), __ldg(A + n));
   }
 };
 
@@ -129,7 +133,7 @@ k_row_czt_real(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   const int row0 = blockIdx.x * 2 * NB;
   deposit_rows<2 * NB, NT, false, true>(a, cz.L, slice0, n_sl, n_rows, row0, buf,
                                         LDM / 2, rs);
-  RowLoadPair<M> ld{&a, &cz, buf, rs.k, row0, n_rows};
+  RowLoadPair<M> ld{row_value_args(a), cz.A, cz.L, buf, rs.k, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false, HALF, false>(buf, tw, nullptr, ld,
                                                             NoStore());
   // the inverse transform stays in shared memory (natural order; with HALF

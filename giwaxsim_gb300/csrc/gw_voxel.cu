@@ -423,13 +423,15 @@ __global__ void k_col_tables(const gw_phi *ph, int g, int k0, int nc,
 // with the z reciprocals and the four f0 z factors staged in shared memory
 // per block and, per line, C2's factor and the (qx, qy) part of the
 // separable f0 sum in registers.  A line with C2 = 0 holds no binned pixel:
-// zeros, no sum read; so does a voxel with C1 = 0.  F64: the float64 I(q)
+// zeros, no sum read; a voxel with C1 = 0 gets a zero factor.  F64: the float64 I(q)
 // (the sum times the float32 factor, one float64 multiply); otherwise the
 // float32 I(q) the detector gathers from, computed in float32 from the sum
 // rounded to float (no float64 arithmetic: on this GPU the float64 pipe is
 // the slow one), within 1.5 float32 ulps of the float64 I(q) rounded (both
 // use the same factor).  Dynamic shared memory: Qc float4 (use_f0) + Qc
 // floats.
+constexpr int kFinU = 8;  // voxels per lane per round of k_finalize
+
 template <bool F64>
 __global__ void __launch_bounds__(256)
 k_finalize(const double *__restrict__ sum, const float2 *__restrict__ sumk, int kahan,
@@ -470,35 +472,51 @@ k_finalize(const double *__restrict__ sum, const float2 *__restrict__ sumk, int 
         fxy[i] = __ldg(t + ix) * __ldg(t + Qc + iy);
       }
     }
-#pragma unroll 4
-    for (int iz = lane; iz < Qc; iz += 32) {
-      const float rz = s_rc1[iz];
-      double s = 0.0;
-      float s32 = 0.f;
-      if (rz != 0.f) {
+    // kFinU voxels per lane per round: every sum load of the round is
+    // issued before the first is used (a voxel with C1 = 0 loads its zero
+    // sum too), so each warp keeps kFinU loads in flight.  Both sum kinds
+    // are 8 bytes a voxel: loaded as raw words, read as a float64 or as a
+    // (sum, compensation) float pair.
+    const unsigned long long *raw =
+        kahan ? reinterpret_cast<const unsigned long long *>(sumk) + wbase
+              : reinterpret_cast<const unsigned long long *>(sum) + wbase;
+    for (int iz0 = 0; iz0 < Qc; iz0 += 32 * kFinU) {
+      unsigned long long w[kFinU];
+#pragma unroll
+      for (int u = 0; u < kFinU; ++u) {
+        const int iz = iz0 + u * 32 + lane;
+        w[u] = iz < Qc ? raw[iz] : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < kFinU; ++u) {
+        const int iz = iz0 + u * 32 + lane;
+        if (iz >= Qc) break;
+        double s = 0.0;
+        float s32 = 0.f;
         if (kahan) {
-          const float2 sc = sumk[wbase + iz];
-          if (F64) s = f2d_exact(sc.x) - f2d_exact(sc.y);
-          else s32 = sc.x - sc.y;
+          const float sx = __uint_as_float((unsigned)w[u]);
+          const float sc = __uint_as_float((unsigned)(w[u] >> 32));
+          if (F64) s = f2d_exact(sx) - f2d_exact(sc);
+          else s32 = sx - sc;
         } else if (F64) {
-          s = sum[wbase + iz];
+          s = __longlong_as_double((long long)w[u]);
         } else {
-          s32 = d2f_rn(sum[wbase + iz]);
+          s32 = d2f_rn(__longlong_as_double((long long)w[u]));
         }
+        float scale = r2 * s_rc1[iz];
+        if (use_f0) {
+          const float4 z = s_zf0[iz];
+          float acc = f0_c;
+          acc += fxy[0] * z.x;
+          acc += fxy[1] * z.y;
+          acc += fxy[2] * z.z;
+          acc += fxy[3] * z.w;
+          const float fq = acc * f0_invz;
+          scale *= fq * fq;
+        }
+        if (F64) out64[obase + iz] = s * f2d_exact(scale);
+        else out32[obase + iz] = s32 * scale;
       }
-      float scale = r2 * rz;
-      if (use_f0) {
-        const float4 z = s_zf0[iz];
-        float acc = f0_c;
-        acc += fxy[0] * z.x;
-        acc += fxy[1] * z.y;
-        acc += fxy[2] * z.z;
-        acc += fxy[3] * z.w;
-        const float fq = acc * f0_invz;
-        scale *= fq * fq;
-      }
-      if (F64) out64[obase + iz] = s * f2d_exact(scale);
-      else out32[obase + iz] = s32 * scale;
     }
   }
 }

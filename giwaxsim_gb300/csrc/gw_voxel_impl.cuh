@@ -246,7 +246,20 @@ __device__ __forceinline__ RowConst row_const(const SliceArgs &a, int slot,
 
 // d_value of element yy of a row with constants k: the same operations in
 // the same order.
-__device__ __forceinline__ float2 d_value_row(const SliceArgs &a,
+// The slice arguments the per-element grid value reads, by value: a
+// transform functor holding them in registers reads no field through a
+// pointer to the kernel's parameter block (a generic load per element).
+struct RowValueArgs {
+  const float2 *amo;
+  const float *my;
+  int fill, smooth_on, y_lo, g, Ly;
+};
+
+__device__ __forceinline__ RowValueArgs row_value_args(const SliceArgs &a) {
+  return RowValueArgs{a.amo, a.my, a.fill, a.smooth_on, a.y_lo, a.g, a.Ly};
+}
+
+__device__ __forceinline__ float2 d_value_row(const RowValueArgs &a,
                                               const RowConst &k, int yy,
                                               float2 dep) {
   float2 v;
@@ -262,6 +275,12 @@ __device__ __forceinline__ float2 d_value_row(const SliceArgs &a,
     v = make_float2(v.x * m + k.cd.x * (1.f - m), v.y * m + k.cd.y * (1.f - m));
   }
   return v;
+}
+
+__device__ __forceinline__ float2 d_value_row(const SliceArgs &a,
+                                              const RowConst &k, int yy,
+                                              float2 dep) {
+  return d_value_row(row_value_args(a), k, yy, dep);
 }
 
 // Window column of sorted atom `at` in slice `sl` (nearest-bin deposit):
