@@ -20,6 +20,7 @@ GW_ACCUM_FP64, GW_ACCUM_KAHAN32 = 0, 1
 GW_DEPOSIT_NEAREST, GW_DEPOSIT_BILINEAR = 0, 1
 GW_SHELLS_PER_SHELL, GW_SHELLS_REFERENCE = 1, 2
 GW_TRANSFORM_AUTO, GW_TRANSFORM_STOCKHAM, GW_TRANSFORM_FUSED = 0, 1, 2
+GW_BINNING_AUTO, GW_BINNING_ATOMIC, GW_BINNING_GATHER = 0, 1, 2
 
 # every symbol include/giwaxs_gb300.h declares
 EXPORTS = [
@@ -76,7 +77,8 @@ class VoxelParams(ctypes.Structure):
                 ("batch_slices", ctypes.c_int32), ("deposit", ctypes.c_int32),
                 ("fft_y", ctypes.c_int32), ("fft_z", ctypes.c_int32),
                 ("transform_y", ctypes.c_int32), ("transform_z", ctypes.c_int32),
-                ("block_variant", ctypes.c_int32), ("real_grids", ctypes.c_int32)]
+                ("block_variant", ctypes.c_int32), ("real_grids", ctypes.c_int32),
+                ("binning", ctypes.c_int32)]
 
 
 class Structure(ctypes.Structure):

@@ -52,6 +52,8 @@ struct ColBin {
   float2 cbg;
   int nr, nc, j0, moff;
   int64_t soff;  // sum-grid offset of the slice's structure (separate mode)
+  float *gcol;   // gather binning: the slice's pixels of F1 column j0, then
+                 // j0 + 1, .. (Nr each); null: atomic adds
   __device__ void add(int co, int ro, float I) const {
     if (co < 0 || ro < 0) return;
     if (bn.shell && !shell_member(bn.shell[co + ro], bn.shell_k)) return;
@@ -73,6 +75,10 @@ struct ColBin {
       X.y += cbg.y * bn.dc_scale;
     }
     const float I = X.x * X.x + X.y * X.y;
+    if (gcol) {  // every pixel a voxel line will gather (its own or mirrored)
+      gcol[(size_t)f * nr + mr] = I;
+      return;
+    }
     add(co, ro, I);
     if (mir) add(cm, rm, I);
   }
@@ -145,7 +151,8 @@ k_col_czt_bin(SliceArgs a, CztArgs cz, BinArgs bn, int slice0, int nc, int nf,
                                                              NoStore());
   }
   ColBin st{bn, cofs, cz.B, slice_const(a, sl).cbg, cz.N, nc, j0, moff,
-            bn.sstride * (int64_t)(sl / a.n_phi)};
+            bn.sstride * (int64_t)(sl / a.n_phi),
+            bn.G ? bn.G + ((size_t)sl * nf + j0) * cz.N : nullptr};
   fft_run<M, NB, NT, true, 0, true, 1, false, false, HALF>(buf, tw, cz.H, NoLoad(), st);
 }
 

@@ -525,6 +525,149 @@ size_t finalize_smem(int Qc, bool use_f0) {
   return (size_t)Qc * ((use_f0 ? sizeof(float4) : 0) + sizeof(float));
 }
 
+// Gather binning: the sums of one voxel line in a fixed order, then the
+// finalize of k_finalize.  One warp per (qy, qx) line, lanes along qz,
+// kFinU voxels per lane per round (their pixel loads of an entry issued
+// together).  The line's entries (phi, F1 column, mirrored) are taken in
+// the order of the table (phi, then band column), each over the structures
+// t0 .. t1-1 (the slice t n_phi + phi), each entry's pixel of voxel qz
+// being output row mr of the z table (mirrored: row 2 r_zero - mr).  The
+// pixels are float32 and the running sum is compensated (Kahan) float32,
+// so the result is that of the exact sum to about one float32 ulp, and
+// bit-identical run to run.  Voxels with more than one output row (C1 > 1)
+// take their further rows after the first, in row order.
+// MODE 0: the float32 I(q) (crop, factor, f0 as k_finalize); 1: the float64
+// I(q) from the same sum; 2: the float64 sums into the window grid (crop
+// = window, off = 0; no factor).
+template <int MODE>
+__global__ void __launch_bounds__(256)
+k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
+         const int2 *__restrict__ lent, const int *__restrict__ zptr,
+         const int *__restrict__ zrows, int nf, int nr, int r_zero, int n_phi,
+         int t0, int t1, const unsigned int *__restrict__ C2,
+         const int *__restrict__ C1, int W, int off, int Qc, float inv_nstruct,
+         const float *__restrict__ f0tab, const float4 *__restrict__ zf0,
+         int use_f0, float f0_c, float f0_invz, double *__restrict__ out64,
+         float *__restrict__ out32) {
+  extern __shared__ float4 s_zf0[];
+  float *s_rc1 = reinterpret_cast<float *>(s_zf0 + (use_f0 ? Qc : 0));
+  int *s_row = reinterpret_cast<int *>(s_rc1 + Qc);  // first output row per qz
+  for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
+    s_rc1[iz] = z_count_factor((unsigned)C1[iz + off]);
+    if (use_f0) s_zf0[iz] = zf0[iz];
+    const int r0 = zptr[iz + off];
+    s_row[iz] = zptr[iz + off + 1] > r0 ? zrows[r0] : -1;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int n_lines = Qc * Qc;
+  const int stride = gridDim.x * (blockDim.x >> 5);
+  for (int line = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       line < n_lines; line += stride) {
+    const int iy = line / Qc, ix = line - iy * Qc;
+    const int wl = (iy + off) * W + ix + off;
+    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
+    const int e0 = lptr[wl], e1 = lptr[wl + 1];
+    if (e0 == e1) {
+      for (int iz = lane; iz < Qc; iz += 32) {
+        if (MODE == 0) out32[obase + iz] = 0.f;
+        else out64[obase + iz] = 0.0;
+      }
+      continue;
+    }
+    float r2 = 0.f;
+    float fxy[4] = {0.f, 0.f, 0.f, 0.f};
+    if (MODE != 2) {
+      r2 = line_count_factor(C2[wl], inv_nstruct);
+      if (use_f0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float *t = f0tab + i * 3 * Qc;
+          fxy[i] = __ldg(t + ix) * __ldg(t + Qc + iy);
+        }
+      }
+    }
+    for (int iz0 = 0; iz0 < Qc; iz0 += 32 * kFinU) {
+      float hi[kFinU], lo[kFinU];
+      int mr[kFinU];
+#pragma unroll
+      for (int u = 0; u < kFinU; ++u) {
+        const int iz = iz0 + u * 32 + lane;
+        hi[u] = 0.f;
+        lo[u] = 0.f;
+        mr[u] = iz < Qc ? s_row[iz] : -1;
+      }
+      for (int e = e0; e < e1; ++e) {
+        const int2 en = __ldg(lent + e);
+        const int j = en.y >> 1;
+        const bool flip = en.y & 1;
+        for (int t = t0; t < t1; ++t) {
+          const float *col = G + ((size_t)(t * n_phi + en.x) * nf + j) * nr;
+          float v[kFinU];
+#pragma unroll
+          for (int u = 0; u < kFinU; ++u)
+            v[u] = mr[u] >= 0 ? __ldg(col + (flip ? 2 * r_zero - mr[u] : mr[u])) : 0.f;
+#pragma unroll
+          for (int u = 0; u < kFinU; ++u) {  // Kahan: hi + lo carries the sum
+            const float y = v[u] - lo[u];
+            const float s = hi[u] + y;
+            lo[u] = (s - hi[u]) - y;
+            hi[u] = s;
+          }
+        }
+      }
+      // further output rows of a voxel (C1 > 1), rare
+#pragma unroll
+      for (int u = 0; u < kFinU; ++u) {
+        const int iz = iz0 + u * 32 + lane;
+        if (iz >= Qc) continue;
+        const int r1 = zptr[iz + off + 1];
+        for (int rr = zptr[iz + off] + 1; rr < r1; ++rr) {
+          const int m2 = zrows[rr];
+          for (int e = e0; e < e1; ++e) {
+            const int2 en = __ldg(lent + e);
+            const int j = en.y >> 1;
+            const int row = (en.y & 1) ? 2 * r_zero - m2 : m2;
+            for (int t = t0; t < t1; ++t) {
+              const float x = __ldg(G + ((size_t)(t * n_phi + en.x) * nf + j) * nr + row);
+              const float y = x - lo[u];
+              const float s = hi[u] + y;
+              lo[u] = (s - hi[u]) - y;
+              hi[u] = s;
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kFinU; ++u) {
+        const int iz = iz0 + u * 32 + lane;
+        if (iz >= Qc) break;
+        if (MODE == 2) {
+          out64[obase + iz] = f2d_exact(hi[u]) - f2d_exact(lo[u]);
+          continue;
+        }
+        float scale = r2 * s_rc1[iz];
+        if (use_f0) {
+          const float4 z = s_zf0[iz];
+          float acc = f0_c;
+          acc += fxy[0] * z.x;
+          acc += fxy[1] * z.y;
+          acc += fxy[2] * z.z;
+          acc += fxy[3] * z.w;
+          const float fq = acc * f0_invz;
+          scale *= fq * fq;
+        }
+        if (MODE == 1) out64[obase + iz] = (f2d_exact(hi[u]) - f2d_exact(lo[u])) * f2d_exact(scale);
+        else out32[obase + iz] = (hi[u] - lo[u]) * scale;
+      }
+    }
+  }
+}
+
+size_t gather_smem(int Qc, bool use_f0) {
+  return finalize_smem(Qc, use_f0) + (size_t)Qc * sizeof(int);
+}
+
 // Shell code of every window voxel (voxelgrids.py:651-652, :659-664, :706):
 // |q| = sqrt((qx^2 + qy^2) + qz^2) as numpy evaluates the meshgrid sum, and
 // shell k holds lower[k] < |q| <= upper[k].  Shells are increasing, so a
@@ -867,9 +1010,55 @@ constexpr int kSetupChunk = 32768;
 // Average, crop and f0 factor of every I(q) grid the plan produces: the
 // float32 grid the detector reads (f64 false; part of every execute) or the
 // float64 grid (f64 true; made when a caller asks for float64 I(q)).
+// Whether this execute bins by gather (multi-q shells bin atomically).
+bool gathering(const gw_voxel_plan *P) { return P->gather && P->n_shells == 0; }
+
+// k_gather over the structures of output t (all of them when averaged):
+// mode 0 / 1 into the float32 / float64 I(q) of output t, mode 2 into sum
+// grid t (window).
+int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
+  gw_ctx *ctx = P->ctx;
+  const bool sep = P->p.average == GW_STRUCTS_SEPARATE;
+  const int t0 = sep ? t : 0, t1 = sep ? t + 1 : P->n_struct;
+  const bool sums = mode == 2;
+  const bool use_f0 = !sums && P->p.f0_z > 0;
+  const int Q = sums ? P->W : P->Qc, off = sums ? 0 : P->lo - P->wlo;
+  const float f0c = (float)P->p.f0_coef[8];
+  const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
+  const float inv_ns = P->p.average == GW_STRUCTS_AVERAGE ? 1.0f / (float)P->n_struct : 1.0f;
+  const size_t smem = gather_smem(Q, use_f0);
+  static size_t smem_set[3] = {0, 0, 0};
+  if (smem > (48u << 10) && smem > smem_set[mode]) {
+    cudaError_t e = mode == 0 ? cudaFuncSetAttribute(k_gather<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                  : mode == 1 ? cudaFuncSetAttribute(k_gather<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                              : cudaFuncSetAttribute(k_gather<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    GW_CUDA(e);
+    smem_set[mode] = smem;
+  }
+  const int blocks = std::min((Q * Q + 7) / 8, 16 * ctx->sm_count);
+  float *o32 = mode == 0 ? P->d_iq32 + t * P->iq_stride : nullptr;
+  double *o64 = mode == 1 ? P->d_iq64 + t * P->iq_stride
+              : mode == 2 ? P->d_sum + t * P->sum_stride : nullptr;
+  gw::KTimer tm(ctx, GW_K_FINALIZE);
+#define GW_GATHER_ARGS                                                             \
+  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->Nf, P->Nr, P->r_zero,    \
+      P->n_phi, t0, t1, P->d_C2, P->d_C1, P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, \
+      use_f0, f0c, f0iz, o64, o32
+  if (mode == 0) k_gather<0><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+  else if (mode == 1) k_gather<1><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+  else k_gather<2><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+#undef GW_GATHER_ARGS
+  GW_LAUNCHED(ctx);
+  return GW_OK;
+}
+
 int enqueue_finalize(gw_voxel_plan *P, bool f64) {
   gw_ctx *ctx = P->ctx;
   cudaStream_t st = ctx->stream;
+  if (gathering(P)) {
+    for (int t = 0; t < P->n_out; ++t) GW_TRY(enqueue_gather(P, f64 ? 1 : 0, t));
+    return GW_OK;
+  }
   const int K = P->n_shells;
   const float f0c = (float)P->p.f0_coef[8];
   const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
@@ -922,9 +1111,11 @@ int enqueue_finalize(gw_voxel_plan *P, bool f64) {
 int enqueue(gw_voxel_plan *P) {
   gw_ctx *ctx = P->ctx;
   cudaStream_t st = ctx->stream;
+  // gather binning stores every pixel and sums afterwards: no sum grid to
+  // clear
   if (P->p.accum == GW_ACCUM_KAHAN32)
     GW_CUDA(cudaMemsetAsync(P->d_sumk, 0, P->sum_stride * P->n_out * sizeof(float2), st));
-  else
+  else if (!gathering(P))
     GW_CUDA(cudaMemsetAsync(P->d_sum, 0, P->sum_stride * P->n_out * sizeof(double), st));
   SliceArgs a = slice_args(P);
   CztArgs cy{P->My, P->Ly, P->Nc, P->d_Ay, P->d_Hy, P->d_By, P->d_twy};
@@ -933,7 +1124,8 @@ int enqueue(gw_voxel_plan *P) {
              P->p.accum == GW_ACCUM_KAHAN32, P->k0, P->kz0,
              (float)((double)P->g * (double)P->g),
              P->n_out > 1 ? (int64_t)P->sum_stride : 0, nullptr, 0,
-             P->wait_polls, P->real ? 1 : 0, P->m_zero, P->r_zero};
+             P->wait_polls, P->real ? 1 : 0, P->m_zero, P->r_zero,
+             gathering(P) ? P->d_G : nullptr};
   // Multi-q form factors: one pass per shell with that shell's atom f
   // values and average voxel f, binning only the shell's voxels into the
   // common sums (GW_SHELLS_PER_SHELL); or the reference's single pass with
@@ -994,6 +1186,9 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
         return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: real_grids needs a finite, "
                                     "nonzero average voxel f for every structure");
     }
+  if (p->binning < GW_BINNING_AUTO || p->binning > GW_BINNING_GATHER)
+    return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: binning must be GW_BINNING_AUTO, "
+                                "_ATOMIC or _GATHER");
   if (p->block_variant < 0 || p->block_variant >= gwv::fused_variant_count())
     return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: block_variant must be 0.." +
                                     std::to_string(gwv::fused_variant_count() - 1));
@@ -1298,6 +1493,67 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       return gw::cuda_fail(e, "column tables", __FILE__, __LINE__);
     }
   }
+  // gather binning: where it applies and the pixel store fits the budget
+  // (GW_GATHER_MAX_MB, default 8192)
+  {
+    const size_t g_bytes = (size_t)P->n_slices * P->Nf * P->Nr * sizeof(float);
+    const char *env = getenv("GW_GATHER_MAX_MB");
+    const size_t cap = (env ? (size_t)std::max(0L, atol(env)) : (size_t)8192) << 20;
+    const bool can = !P->plain && p->accum == GW_ACCUM_FP64 && !P->fused_z && g_bytes <= cap;
+    if (p->binning == GW_BINNING_GATHER && !can) {
+      gw_voxel_plan_destroy(P);
+      return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: gather binning needs a batched, "
+                                  "float64-accumulating plan without the fused column "
+                                  "kernel, and a pixel store within GW_GATHER_MAX_MB");
+    }
+    if (p->binning != GW_BINNING_ATOMIC && can) {
+      // the line entries, in table order (phi, band column): counting sort
+      // by window line
+      std::vector<int> cof((size_t)n_phi * P->Nc);
+      cudaError_t e = cudaMemcpy(cof.data(), P->d_colofs, cof.size() * sizeof(int),
+                                 cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) {
+        gw_voxel_plan_destroy(P);
+        return gw::cuda_fail(e, "column tables", __FILE__, __LINE__);
+      }
+      const int W = P->W;
+      std::vector<int> lptr((size_t)W * W + 1, 0);
+      for (int co : cof)
+        if (co >= 0) ++lptr[co / W + 1];
+      for (size_t i = 1; i < lptr.size(); ++i) lptr[i] += lptr[i - 1];
+      std::vector<int2> lent(std::max(lptr.back(), 1));
+      std::vector<int> fill(lptr.begin(), lptr.end() - 1);
+      for (int q = 0; q < n_phi; ++q)
+        for (int m = 0; m < P->Nc; ++m) {
+          const int co = cof[(size_t)q * P->Nc + m];
+          if (co < 0) continue;
+          // F1 column of table column m: itself, or with real grids its
+          // mirror's (rows mirrored) below m_zero
+          int j = m, flip = 0;
+          if (P->real) {
+            if (m >= P->m_zero) j = m - P->m_zero;
+            else { j = P->m_zero - m; flip = 1; }
+          }
+          lent[fill[co / W]++] = make_int2(q, 2 * j + flip);
+        }
+      // output rows of every window z, ascending
+      std::vector<int> zptr((size_t)W + 1, 0);
+      for (int ro : rowofs)
+        if (ro >= 0) ++zptr[ro + 1];
+      for (int i = 1; i <= W; ++i) zptr[i] += zptr[i - 1];
+      std::vector<int> zrows(std::max(zptr.back(), 1));
+      std::vector<int> zfill(zptr.begin(), zptr.end() - 1);
+      for (int mr = 0; mr < P->Nr; ++mr)
+        if (rowofs[mr] >= 0) zrows[zfill[rowofs[mr]]++] = mr;
+      if ((st = upload(&P->d_lptr, lptr, &B)) || (st = upload(&P->d_lent, lent, &B)) ||
+          (st = upload(&P->d_zptr, zptr, &B)) || (st = upload(&P->d_zrows, zrows, &B)) ||
+          (st = alloc(&P->d_G, g_bytes / sizeof(float), &B))) {
+        gw_voxel_plan_destroy(P);
+        return st;
+      }
+      P->gather = true;
+    }
+  }
   *out = P;
   return GW_OK;
 }
@@ -1317,7 +1573,8 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_perm, P->d_ybnd, P->d_roff, P->d_zhist, P->d_rowstart,
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
                   P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0,
-                  P->d_fty, P->d_ftz};
+                  P->d_fty, P->d_ftz, P->d_G, P->d_lptr, P->d_lent, P->d_zptr,
+                  P->d_zrows};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;
@@ -1588,6 +1845,8 @@ extern "C" int gw_voxel_get_sums(gw_voxel_plan *P, double *sums) {
     GW_TRY(gw::check_device_error(P->ctx, "voxel stage"));
     for (size_t i = 0; i < W3; ++i) s[i] = (double)k[i].x - (double)k[i].y;
   } else {
+    // gather binning keeps no sum grid: made from the stored pixels here
+    if (gwv::gathering(P)) GW_TRY(gwv::enqueue_gather(P, 2, 0));
     GW_CUDA(cudaMemcpyAsync(s.data(), P->d_sum, W3 * sizeof(double),
                             cudaMemcpyDeviceToHost, P->ctx->stream));
     GW_TRY(gw::check_device_error(P->ctx, "voxel stage"));
@@ -1607,7 +1866,7 @@ extern "C" int gw_voxel_info(gw_voxel_plan *P, int64_t *info, int32_t n) {
                        P->y_lo, P->z_lo, P->k0, P->kz0, P->n_slices,
                        (int64_t)P->bytes, P->graph_kernels,
                        (int64_t)P->f1_tma, (int64_t)P->fused_y,
-                       (int64_t)P->fused_z, (int64_t)P->real};
+                       (int64_t)P->fused_z, (int64_t)P->real, (int64_t)P->gather};
   const int k = std::min<int>(n, (int)(sizeof v / sizeof v[0]));
   for (int i = 0; i < k; ++i) info[i] = v[i];
   return k;

@@ -82,6 +82,9 @@ struct BinArgs {
   // binned again at its mirror (2 m_zero - m, 2 r_zero - mr), where
   // |F(-ky, -kz)|^2 = |F(ky, kz)|^2
   int mirror, m_zero, r_zero;
+  // gather binning: store |F|^2 of (slice, F1 column, output row) at
+  // G[(slice * nf + column) * Nr + row] instead of adding it (null: add)
+  float *G;
 };
 
 // Default poll limit of a bounded wait for an asynchronous tile load: far
@@ -589,6 +592,17 @@ struct gw_voxel_plan {
   bool real = false;
   int m_zero = 0, r_zero = 0;
   int Nf = 0;  // F1 row pitch (columns stored): Nc, or Nc - m_zero
+  // gather binning (gw_voxel_params.binning): the column kernels store each
+  // slice's |F|^2 pixels in d_G ([slice][F1 column][output row], float32)
+  // and k_gather adds every voxel line's pixels in a fixed order.  Window
+  // line l takes the entries d_lent[d_lptr[l] .. d_lptr[l+1]) = (phi, F1
+  // column * 2 + mirrored), each over every structure's slice of that phi;
+  // window z takes the output rows d_zrows[d_zptr[z] .. d_zptr[z+1]) (a
+  // mirrored entry reads row 2 r_zero - mr)
+  bool gather = false;
+  float *d_G = nullptr;
+  int *d_lptr = nullptr, *d_zptr = nullptr, *d_zrows = nullptr;
+  int2 *d_lent = nullptr;
   // fused chirp-z kernels (gw_czt2.cuh) along y / z, with their twiddles
   bool fused_y = false, fused_z = false;
   float2 *d_fty = nullptr, *d_ftz = nullptr;

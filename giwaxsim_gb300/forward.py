@@ -262,13 +262,14 @@ class VoxelPlan:
     are real multiples of one complex value in a batched, nearest-bin plan
     without a fused kernel asked for; False keeps the general path (needed
     for set_shells and backward); True asks for it and refuses f values
-    that do not allow it."""
+    that do not allow it.  binning: "auto" (gather where it applies),
+    "atomic" or "gather" (gw_voxel_params.binning)."""
 
     def __init__(self, geom, structures, phis=None, fill_bkg=False, smooth=0,
                  mode="batched", accum="fp64", average=True, f0_element="C",
                  batch_slices=0, constants=None, deposit="nearest", fft_y=0,
                  fft_z=0, tune=False, ctx=None, create=True, ranges=None,
-                 transform="auto", block_variant=0, real=None):
+                 transform="auto", block_variant=0, real=None, binning="auto"):
         self.geom = geom
         self.handle = None
         self.reused = False          # handed out again by PlanCache
@@ -284,7 +285,8 @@ class VoxelPlan:
                                  smooth=smooth, mode=mode, accum=accum,
                                  average=average, f0_element=f0_element,
                                  constants=constants, deposit=deposit,
-                                 real=real, ctx=self.ctx, **choice)
+                                 real=real, binning=binning, ctx=self.ctx,
+                                 **choice)
 
             self.tuned = autotune.tune(make, len(structures), fill_bkg, smooth,
                                        deposit, ctx=self.ctx)
@@ -368,6 +370,8 @@ class VoxelPlan:
                              "real multiples of one complex value, with a finite, "
                              "nonzero average voxel f")
         p.real_grids = int(bool(real))
+        p.binning = {"auto": N.GW_BINNING_AUTO, "atomic": N.GW_BINNING_ATOMIC,
+                     "gather": N.GW_BINNING_GATHER}[binning]
         self.params = p
         self.Qc = geom.crop_hi - geom.crop_lo + 1
         if create:
@@ -513,7 +517,8 @@ class VoxelPlan:
         n = N.lib().gw_voxel_info(self.handle, N.ptr(v), 24)
         keys = ["crop", "batch", "Ly", "Lz", "Nc", "Nr", "My", "Mz", "y_lo",
                 "z_lo", "k0", "kz0", "n_slices", "device_bytes",
-                "graph_kernels", "col_tma", "fused_y", "fused_z", "real"]
+                "graph_kernels", "col_tma", "fused_y", "fused_z", "real",
+                "gather"]
         return dict(zip(keys, (int(x) for x in v[:n])))
 
     def debug_deposit(self, slice_index):

@@ -111,6 +111,8 @@ enum { GW_SHELLS_PER_SHELL = 1, GW_SHELLS_REFERENCE = 2 };
 
 enum { GW_TRANSFORM_AUTO = 0, GW_TRANSFORM_STOCKHAM = 1, GW_TRANSFORM_FUSED = 2 };
 
+enum { GW_BINNING_AUTO = 0, GW_BINNING_ATOMIC = 1, GW_BINNING_GATHER = 2 };
+
 typedef struct gw_voxel_params {
   int32_t grid_size;    /* g = ceil(2pi/(dq*r))          comparison.py:710 */
   double r_voxel_size;  /* r                                               */
@@ -164,6 +166,20 @@ typedef struct gw_voxel_params {
                            half a transform buffer; no shells, no backward.
                            gw_voxel_info reports whether it runs.  0: the
                            general path.                                   */
+  int32_t binning;      /* how |F|^2 pixels reach the voxel sums.
+                           GW_BINNING_ATOMIC: float64 atomic adds as the
+                           column transforms produce them (the sum's
+                           rounding depends on arrival order);
+                           GW_BINNING_GATHER: the column transforms store
+                           every slice's pixels, then one pass per voxel
+                           line adds its pixels in a fixed order
+                           (compensated float32) and finalizes: no atomics,
+                           bit-identical results run to run (batched plans
+                           with float64 accumulation; GW_ERR_ARG
+                           otherwise, or when the pixel store would exceed
+                           the device budget); GW_BINNING_AUTO: gather where
+                           it applies, else atomic.  Multi-q shells always
+                           bin atomically.                                 */
 } gw_voxel_params;
 
 typedef struct gw_structure {
@@ -249,7 +265,8 @@ int gw_voxel_get_sums(gw_voxel_plan *plan, double *sums);
  * z_lo, k0, kz0, n_slices, device_bytes, graph_kernels, col_tma (1 when
  * the column kernel loads its tiles by TMA), fused_y, fused_z (1 when the
  * fused chirp-z kernel runs along that axis), real (1 when the real-grid
- * path runs)].  Returns the number written (at most n). */
+ * path runs), gather (1 when the gather binning runs)].  Returns the number
+ * written (at most n). */
 int gw_voxel_info(gw_voxel_plan *plan, int64_t *info, int32_t n);
 /* Deposit indices of one slice (after execute): y,z voxel index per atom of
  * that slice's structure, -1 where the reference's valid_mask drops it
