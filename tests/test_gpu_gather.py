@@ -5,7 +5,8 @@ general grids, fill/smoothing, several structures averaged and separate,
 float64 sums and I(q) on request, graph replay, multi-q shells (which bin
 atomically on a gather plan), and the plans it refuses.  Counts bit-exact;
 intensities by normwise relative L2 <= 1e-5 against the oracle and 1e-6
-between the two binnings; gather results bit-identical run to run."""
+between the two binnings; results bit-identical run to run where the
+deposit is (one f value per structure)."""
 import os
 
 import numpy as np
@@ -74,9 +75,15 @@ def test_gather_vs_atomic_and_oracle(kind, fill, smooth):
     assert rel_l2(ga["iq"], ref["iq"]) <= RTOL
     assert rel_l2(ga["iq"], at["iq"]) <= 1e-6
     assert rel_l2(ga["sums"], at["sums"]) <= 1e-6
-    # the same bits on every execute
+    # the same bits on every execute where the deposit's shared-memory sums
+    # are order-independent (one f value: every partial sum is k f); with
+    # several f values a cell of three or more atoms rounds by arrival
+    # order in float32, the binning adds nothing to that
     for x in ga["iq32"][1:]:
-        assert np.array_equal(x.view(np.uint32), ga["iq32"][0].view(np.uint32))
+        if kind == "real":
+            assert np.array_equal(x.view(np.uint32), ga["iq32"][0].view(np.uint32))
+        else:
+            assert rel_l2(x, ga["iq32"][0]) <= 1e-6
     # float32 I(q) within 2 ulps of the float64 I(q) rounded, zero together
     r32 = ga["iq"].astype(np.float32)
     i32 = ga["iq32"][0]
