@@ -367,7 +367,8 @@ def run_gb300(args, world, rank, local, pg):
     peak, peak_kind = measured_peaks()
 
     # voxels with a count (the finalize reads their sums only)
-    counted = int(np.count_nonzero(plan.counts()))
+    cnt = plan.counts()
+    counted = (int(np.count_nonzero(cnt)), int(cnt.sum()))
 
     def kernel_roof(name):
         ms_tot, nl = kt[name]
@@ -690,7 +691,7 @@ def f1_columns(info):
     return info["Nc"] + info["k0"] if info.get("real") else info["Nc"]
 
 
-def algorithmic_bytes(name, info, w, S, dargs, Qc, counted=None):
+def algorithmic_bytes(name, info, w, S, dargs, Qc, counted=(None, None)):
     """Bytes a launch of `name` must move at minimum (its inputs read once,
     outputs written once), per the plan's sizes; S = slices per launch.
     The row stage's input is the window grid (complex; real with real
@@ -700,14 +701,23 @@ def algorithmic_bytes(name, info, w, S, dargs, Qc, counted=None):
     if name == "row_czt":
         return S * info["Lz"] * (info["Ly"] * (4 if info.get("real") else 8) + nf * 8)
     if name == "col_czt_bin":
+        if info.get("gather"):
+            # F1 read + every pixel stored once (float32) for the gather
+            return S * (info["Lz"] * nf * 8 + info["Nr"] * nf * 4)
+        # F1 read + float64 read-modify-write of every band pixel
         return S * (info["Lz"] * nf * 8 + info["Nr"] * info["Nc"] * 16)
     if name == "detector":
         npx = dargs["num_pixels"] ** 2
         return len(dargs["psis"]) * npx * 4 + npx * 8
+    nonzero, binned = counted
+    if name == "finalize" and info.get("gather"):
+        # every binned pixel read once (float32), the float32 I(q) of every
+        # voxel written (the line and z tables are a few MB)
+        return (Qc ** 3 if binned is None else binned) * 4 + Qc ** 3 * 4
     if name == "finalize":
         # the float64 sum of every voxel with a count, the float32 I(q) of
         # every voxel (the count factor tables are a few KB)
-        return (Qc ** 3 if counted is None else counted) * 8 + Qc ** 3 * 4
+        return (Qc ** 3 if nonzero is None else nonzero) * 8 + Qc ** 3 * 4
     return None
 
 
