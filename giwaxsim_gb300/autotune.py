@@ -14,9 +14,11 @@ the plan's own inputs (graph replays, device events):
   block_variant    block shape of the fused kernels: sequences per block and
                    register cap (occupancy against register spills).
 
-The search is staged (rows, then columns, then batch, then block shape),
-each stage keeping the best of the previous ones: the two transform kernels
-are separate launches whose times add.  Results are cached per device and
+The search is staged (row length, column length, the kernel families of
+both axes together, batch, block shape), each stage keeping the best of
+the previous ones: the two transform kernels are separate launches whose
+times add, but a fused kernel on either axis changes the whole plan (no
+real-grid path, atomic binning), so the families are timed as pairs.  Results are cached per device and
 plan shape in a JSON file ($GIWAXSIM_GB300_TUNE_CACHE, default
 ~/.cache/giwaxsim_gb300/tune.json), so a shape is tuned once.  tune()
 returns the keyword arguments for VoxelPlan.
@@ -67,7 +69,7 @@ def length_candidates(need, count=2):
 
 def shape_key(ctx, info, n_structures, fill_bkg, smooth, deposit):
     return "|".join(str(x) for x in (
-        "v3", ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
+        "v4", ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
         info.get("real", 0),
         info["n_slices"], n_structures, int(bool(fill_bkg)),
         int(bool(smooth)), deposit))
@@ -134,18 +136,19 @@ def tune(make_plan, n_structures, fill_bkg=False, smooth=0,
         res = [r for r in res if r[0] is not None]
         return min(res, key=lambda r: r[0])
 
-    families = ("fused", "stockham")
     best = dict(default, fft_y=info["My"], fft_z=info["Mz"],
                 batch_slices=info["batch"])
     default_ms = time_choice(best)
-    # rows: length x kernel family
+    # transform lengths, rows then columns, with the default kernels
     ys = length_candidates(info["Ly"] + info["Nc"] - 1)
-    _, best = best_of([dict(best, fft_y=m, transform=[fam, best["transform"][1]])
-                       for m in ys for fam in families])
-    # columns
+    _, best = best_of([dict(best, fft_y=m) for m in ys])
     zs = length_candidates(info["Lz"] + info["Nr"] - 1)
-    _, best = best_of([dict(best, fft_z=m, transform=[best["transform"][0], fam])
-                       for m in zs for fam in families])
+    _, best = best_of([dict(best, fft_z=m) for m in zs])
+    # kernel families of both axes together: a fused kernel on either axis
+    # takes the plan off the real-grid path and off gather binning, so the
+    # axes are not independent
+    _, best = best_of([dict(best, transform=[fy, fz])
+                       for fy in ("auto", "fused") for fz in ("auto", "fused")])
     # slices per batch
     S = info["batch"]
     batches = sorted({S, max(1, S // 2), min(info["n_slices"], 2 * S, 4096)})

@@ -89,6 +89,15 @@ template <> struct FftShape<5120> { static constexpr int NB = 1,  NT = 320, MINB
 template <> struct FftShape<6144> { static constexpr int NB = 1,  NT = 384, MINB = 2; };
 template <> struct FftShape<8192> { static constexpr int NB = 1,  NT = 512, MINB = 1; };
 
+// Blocks per SM the pruned row kernels (window and band within M/2) are
+// sized for: their 1280-point form fits four 320-thread blocks in 48
+// registers without spills (measured 10 % faster than three); the other
+// lengths keep MINB.
+template <int M>
+__host__ __device__ constexpr int minb_pruned_rows() {
+  return M == 1280 ? 4 : FftShape<M>::MINB;
+}
+
 // The supported lengths, ascending.
 constexpr int kFftSizes[] = {64, 128, 256, 384, 512, 640, 768, 1024, 1280,
                              1536, 2048, 2560, 3072, 4096, 5120, 6144, 8192};

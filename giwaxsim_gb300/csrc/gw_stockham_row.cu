@@ -54,7 +54,8 @@ struct RowStore {
 // HALF: the window (L) and the band (N) both fit in M / 2, so the forward
 // transform's first pass and the inverse transform's last pass are pruned.
 template <int M, bool BIL, bool HALF>
-__global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
+__global__ void __launch_bounds__(FftShape<M>::NT,
+                                  HALF ? minb_pruned_rows<M>() : FftShape<M>::MINB)
 k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
           int nc_out, float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
@@ -118,7 +119,8 @@ struct RowLoadPair {
 };
 
 template <int M, bool HALF>
-__global__ void __launch_bounds__(FftShape<M>::NT, FftShape<M>::MINB)
+__global__ void __launch_bounds__(FftShape<M>::NT,
+                                  HALF ? minb_pruned_rows<M>() : FftShape<M>::MINB)
 k_row_czt_real(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
                int m_zero, int nf, float2 *F1) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;

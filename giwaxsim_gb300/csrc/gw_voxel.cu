@@ -526,32 +526,119 @@ size_t finalize_smem(int Qc, bool use_f0) {
 }
 
 // Gather binning: the sums of one voxel line in a fixed order, then the
-// finalize of k_finalize.  One warp per (qy, qx) line, lanes along qz,
-// kFinU voxels per lane per round (their pixel loads of an entry issued
-// together).  The line's entries (phi, F1 column, mirrored) are taken in
-// the order of the table (phi, then band column), each over the structures
-// t0 .. t1-1 (the slice t n_phi + phi), each entry's pixel of voxel qz
-// being output row mr of the z table (mirrored: row 2 r_zero - mr).  The
-// pixels are float32 and the running sum is compensated (Kahan) float32,
-// so the result is that of the exact sum to about one float32 ulp, and
-// bit-identical run to run.  Voxels with more than one output row (C1 > 1)
-// take their further rows after the first, in row order.
+// finalize of k_finalize.  Lanes run along qz, kGU voxels per lane per
+// round.  A line's entries (phi, F1 column, mirrored) are taken in table
+// order (phi, then band column), kGatherE at a time (their pixel loads
+// issued together), each over the structures t0 .. t1-1 (the slice
+// t n_phi + phi); the pixel of voxel qz is output row mr of the z table
+// (mirrored: row 2 r_zero - mr).  Pixels are float32 and the running sum is
+// compensated (Kahan) float32: the exact sum to about one float32 ulp, the
+// same bits on every run.  Voxels with further output rows (C1 > 1) take
+// them after the first, in row order.  Lines with up to kGatherHeavy
+// entries take one warp each (grid-stride); the heavier lines (near the
+// rotation axis every phi meets) are listed in `heavy` and take one block
+// each, its warps splitting the entries in eight fixed parts whose partial
+// sums are added in warp order.
 // MODE 0: the float32 I(q) (crop, factor, f0 as k_finalize); 1: the float64
-// I(q) from the same sum; 2: the float64 sums into the window grid (crop
+// I(q) from the same sums; 2: the float64 sums into the window grid (crop
 // = window, off = 0; no factor).
+constexpr int kGatherE = 4;       // entries whose loads are issued together
+constexpr int kGU = 4;            // voxels per lane per round
+constexpr int kGatherHeavy = 64;
+
+__device__ __forceinline__ void kahan_step(float &hi, float &lo, float x) {
+  const float y = x - lo;
+  const float s = hi + y;
+  lo = (s - hi) - y;
+  hi = s;
+}
+
+// Entries [e0, e1) of a line into the lane's kGU accumulators.  Pixel
+// offsets are 32-bit (the pixel store holds fewer than 2^31 floats).
+__device__ __forceinline__ void gather_entries(const float *__restrict__ G,
+                                               const int2 *__restrict__ lent,
+                                               int e0, int e1, int t0, int t1,
+                                               int n_phi, int nf, int nr, int r_zero,
+                                               const int (&mr)[kGU],
+                                               float (&hi)[kGU], float (&lo)[kGU]) {
+  int mf[kGU];  // mirrored rows
+#pragma unroll
+  for (int u = 0; u < kGU; ++u) mf[u] = 2 * r_zero - mr[u];
+#pragma unroll 1
+  for (int e = e0; e < e1; e += kGatherE) {
+    const int ne = min(kGatherE, e1 - e);
+    unsigned colo[kGatherE];
+    bool flip[kGatherE];
+#pragma unroll
+    for (int k = 0; k < kGatherE; ++k) {
+      const int2 en = k < ne ? __ldg(lent + e + k) : make_int2(0, 0);
+      colo[k] = ((unsigned)(t0 * n_phi + en.x) * (unsigned)nf + (unsigned)(en.y >> 1)) *
+                (unsigned)nr;
+      flip[k] = en.y & 1;
+    }
+    const unsigned tstep = (unsigned)n_phi * (unsigned)nf * (unsigned)nr;
+#pragma unroll 1
+    for (int t = t0; t < t1; ++t) {
+      float v[kGatherE][kGU];
+#pragma unroll
+      for (int k = 0; k < kGatherE; ++k)
+#pragma unroll
+        for (int u = 0; u < kGU; ++u)
+          v[k][u] = (k < ne && mr[u] >= 0)
+                        ? __ldg(G + colo[k] + (unsigned)(flip[k] ? mf[u] : mr[u]))
+                        : 0.f;
+#pragma unroll
+      for (int k = 0; k < kGatherE; ++k) {
+        if (k >= ne) break;
+#pragma unroll
+        for (int u = 0; u < kGU; ++u) kahan_step(hi[u], lo[u], v[k][u]);
+      }
+#pragma unroll
+      for (int k = 0; k < kGatherE; ++k) colo[k] += tstep;
+    }
+  }
+}
+
+template <int MODE>
+__device__ __forceinline__ void gather_store(float hi, float lo, int iz, size_t obase,
+                                             float r2, const float *s_rc1,
+                                             const float4 *s_zf0, const float (&fxy)[4],
+                                             int use_f0, float f0_c, float f0_invz,
+                                             double *out64, float *out32) {
+  if (MODE == 2) {
+    out64[obase + iz] = f2d_exact(hi) - f2d_exact(lo);
+    return;
+  }
+  float scale = r2 * s_rc1[iz];
+  if (use_f0) {
+    const float4 z = s_zf0[iz];
+    float acc = f0_c;
+    acc += fxy[0] * z.x;
+    acc += fxy[1] * z.y;
+    acc += fxy[2] * z.z;
+    acc += fxy[3] * z.w;
+    const float fq = acc * f0_invz;
+    scale *= fq * fq;
+  }
+  if (MODE == 1) out64[obase + iz] = (f2d_exact(hi) - f2d_exact(lo)) * f2d_exact(scale);
+  else out32[obase + iz] = (hi - lo) * scale;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256)
 k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
          const int2 *__restrict__ lent, const int *__restrict__ zptr,
-         const int *__restrict__ zrows, int nf, int nr, int r_zero, int n_phi,
-         int t0, int t1, const unsigned int *__restrict__ C2,
-         const int *__restrict__ C1, int W, int off, int Qc, float inv_nstruct,
-         const float *__restrict__ f0tab, const float4 *__restrict__ zf0,
-         int use_f0, float f0_c, float f0_invz, double *__restrict__ out64,
-         float *__restrict__ out32) {
+         const int *__restrict__ zrows, const int *__restrict__ heavy, int n_heavy,
+         int nf, int nr, int r_zero, int n_phi, int t0, int t1,
+         const unsigned int *__restrict__ C2, const int *__restrict__ C1, int W,
+         int off, int Qc, float inv_nstruct, const float *__restrict__ f0tab,
+         const float4 *__restrict__ zf0, int use_f0, float f0_c, float f0_invz,
+         double *__restrict__ out64, float *__restrict__ out32) {
   extern __shared__ float4 s_zf0[];
   float *s_rc1 = reinterpret_cast<float *>(s_zf0 + (use_f0 ? Qc : 0));
   int *s_row = reinterpret_cast<int *>(s_rc1 + Qc);  // first output row per qz
+  // [8][Qc] partial sums: 8-byte aligned (20 Qc or 4 Qc bytes before s_row)
+  float2 *s_part = reinterpret_cast<float2 *>(s_row + Qc);
   for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
     s_rc1[iz] = z_count_factor((unsigned)C1[iz + off]);
     if (use_f0) s_zf0[iz] = zf0[iz];
@@ -559,24 +646,10 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     s_row[iz] = zptr[iz + off + 1] > r0 ? zrows[r0] : -1;
   }
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int n_lines = Qc * Qc;
-  const int stride = gridDim.x * (blockDim.x >> 5);
-  for (int line = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-       line < n_lines; line += stride) {
-    const int iy = line / Qc, ix = line - iy * Qc;
-    const int wl = (iy + off) * W + ix + off;
-    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
-    const int e0 = lptr[wl], e1 = lptr[wl + 1];
-    if (e0 == e1) {
-      for (int iz = lane; iz < Qc; iz += 32) {
-        if (MODE == 0) out32[obase + iz] = 0.f;
-        else out64[obase + iz] = 0.0;
-      }
-      continue;
-    }
-    float r2 = 0.f;
-    float fxy[4] = {0.f, 0.f, 0.f, 0.f};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto line_consts = [&](int iy, int ix, int wl, float &r2, float (&fxy)[4]) {
+    r2 = 0.f;
+    fxy[0] = fxy[1] = fxy[2] = fxy[3] = 0.f;
     if (MODE != 2) {
       r2 = line_count_factor(C2[wl], inv_nstruct);
       if (use_f0) {
@@ -587,85 +660,158 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
         }
       }
     }
-    for (int iz0 = 0; iz0 < Qc; iz0 += 32 * kFinU) {
-      float hi[kFinU], lo[kFinU];
-      int mr[kFinU];
+  };
+  if ((int)blockIdx.x < n_heavy) {
+    // a heavy line: the block's eight warps split its entries
+    const int wl = heavy[blockIdx.x];
+    const int iy = wl / W - off, ix = wl % W - off;
+    if (iy < 0 || iy >= Qc || ix < 0 || ix >= Qc) return;
+    const int e0 = lptr[wl], ne = lptr[wl + 1] - e0;
+    const int nw = blockDim.x >> 5;
+    const int eb = e0 + (int)((int64_t)ne * warp / nw);
+    const int ee = e0 + (int)((int64_t)ne * (warp + 1) / nw);
+    for (int iz0 = 0; iz0 < Qc; iz0 += 32 * kGU) {
+      float hi[kGU], lo[kGU];
+      int mr[kGU];
 #pragma unroll
-      for (int u = 0; u < kFinU; ++u) {
+      for (int u = 0; u < kGU; ++u) {
         const int iz = iz0 + u * 32 + lane;
-        hi[u] = 0.f;
-        lo[u] = 0.f;
+        hi[u] = lo[u] = 0.f;
         mr[u] = iz < Qc ? s_row[iz] : -1;
       }
-      for (int e = e0; e < e1; ++e) {
-        const int2 en = __ldg(lent + e);
-        const int j = en.y >> 1;
-        const bool flip = en.y & 1;
-        for (int t = t0; t < t1; ++t) {
-          const float *col = G + ((size_t)(t * n_phi + en.x) * nf + j) * nr;
-          float v[kFinU];
+      gather_entries(G, lent, eb, ee, t0, t1, n_phi, nf, nr, r_zero, mr, hi, lo);
 #pragma unroll
-          for (int u = 0; u < kFinU; ++u)
-            v[u] = mr[u] >= 0 ? __ldg(col + (flip ? 2 * r_zero - mr[u] : mr[u])) : 0.f;
-#pragma unroll
-          for (int u = 0; u < kFinU; ++u) {  // Kahan: hi + lo carries the sum
-            const float y = v[u] - lo[u];
-            const float s = hi[u] + y;
-            lo[u] = (s - hi[u]) - y;
-            hi[u] = s;
-          }
-        }
-      }
-      // further output rows of a voxel (C1 > 1), rare
-#pragma unroll
-      for (int u = 0; u < kFinU; ++u) {
+      for (int u = 0; u < kGU; ++u) {
         const int iz = iz0 + u * 32 + lane;
-        if (iz >= Qc) continue;
-        const int r1 = zptr[iz + off + 1];
-        for (int rr = zptr[iz + off] + 1; rr < r1; ++rr) {
-          const int m2 = zrows[rr];
-          for (int e = e0; e < e1; ++e) {
-            const int2 en = __ldg(lent + e);
-            const int j = en.y >> 1;
-            const int row = (en.y & 1) ? 2 * r_zero - m2 : m2;
-            for (int t = t0; t < t1; ++t) {
-              const float x = __ldg(G + ((size_t)(t * n_phi + en.x) * nf + j) * nr + row);
-              const float y = x - lo[u];
-              const float s = hi[u] + y;
-              lo[u] = (s - hi[u]) - y;
-              hi[u] = s;
-            }
-          }
-        }
+        if (iz < Qc) s_part[warp * Qc + iz] = make_float2(hi[u], lo[u]);
       }
+    }
+    __syncthreads();
+    float r2, fxy[4];
+    line_consts(iy, ix, wl, r2, fxy);
+    const size_t obase = MODE == 2 ? (size_t)wl * W : ((size_t)iy * Qc + ix) * Qc;
+    for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
+      float hi = 0.f, lo = 0.f;
+      for (int w = 0; w < nw; ++w) {
+        const float2 p = s_part[w * Qc + iz];
+        kahan_step(hi, lo, p.x);
+        kahan_step(hi, lo, -p.y);
+      }
+      gather_store<MODE>(hi, lo, iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c, f0_invz,
+                         out64, out32);
+    }
+    return;
+  }
+  // the other lines, one warp each
+  const int n_lines = Qc * Qc;
+  const int wpb = blockDim.x >> 5;
+  const int stride = (gridDim.x - n_heavy) * wpb;
+  for (int line = (blockIdx.x - n_heavy) * wpb + warp; line < n_lines; line += stride) {
+    const int iy = line / Qc, ix = line - iy * Qc;
+    const int wl = (iy + off) * W + ix + off;
+    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
+    const int e0 = lptr[wl], e1 = lptr[wl + 1];
+    if (n_heavy > 0 && e1 - e0 > kGatherHeavy) continue;  // a heavy block's
+    if (e0 == e1) {
+      for (int iz = lane; iz < Qc; iz += 32) {
+        if (MODE == 0) out32[obase + iz] = 0.f;
+        else out64[obase + iz] = 0.0;
+      }
+      continue;
+    }
+    float r2, fxy[4];
+    line_consts(iy, ix, wl, r2, fxy);
+    for (int iz0 = 0; iz0 < Qc; iz0 += 32 * kGU) {
+      float hi[kGU], lo[kGU];
+      int mr[kGU];
 #pragma unroll
-      for (int u = 0; u < kFinU; ++u) {
+      for (int u = 0; u < kGU; ++u) {
+        const int iz = iz0 + u * 32 + lane;
+        hi[u] = lo[u] = 0.f;
+        mr[u] = iz < Qc ? s_row[iz] : -1;
+      }
+      gather_entries(G, lent, e0, e1, t0, t1, n_phi, nf, nr, r_zero, mr, hi, lo);
+#pragma unroll
+      for (int u = 0; u < kGU; ++u) {
         const int iz = iz0 + u * 32 + lane;
         if (iz >= Qc) break;
-        if (MODE == 2) {
-          out64[obase + iz] = f2d_exact(hi[u]) - f2d_exact(lo[u]);
-          continue;
-        }
-        float scale = r2 * s_rc1[iz];
-        if (use_f0) {
-          const float4 z = s_zf0[iz];
-          float acc = f0_c;
-          acc += fxy[0] * z.x;
-          acc += fxy[1] * z.y;
-          acc += fxy[2] * z.z;
-          acc += fxy[3] * z.w;
-          const float fq = acc * f0_invz;
-          scale *= fq * fq;
-        }
-        if (MODE == 1) out64[obase + iz] = (f2d_exact(hi[u]) - f2d_exact(lo[u])) * f2d_exact(scale);
-        else out32[obase + iz] = (hi[u] - lo[u]) * scale;
+        gather_store<MODE>(hi[u], lo[u], iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c,
+                           f0_invz, out64, out32);
       }
     }
   }
 }
 
-size_t gather_smem(int Qc, bool use_f0) {
-  return finalize_smem(Qc, use_f0) + (size_t)Qc * sizeof(int);
+// Voxels with more than one output row (C1 > 1, the window z listed in
+// zmulti): their whole sum again over every row, in the order entry, then
+// structure, then row, replacing the first-row value k_gather wrote.  One
+// warp per line with entries, lanes over the listed z.
+template <int MODE>
+__global__ void __launch_bounds__(256)
+k_gather_multi(const float *__restrict__ G, const int *__restrict__ lptr,
+               const int2 *__restrict__ lent, const int *__restrict__ zptr,
+               const int *__restrict__ zrows, const int *__restrict__ zmulti,
+               int n_zmulti, int nf, int nr, int r_zero, int n_phi, int t0, int t1,
+               const unsigned int *__restrict__ C2, const int *__restrict__ C1, int W,
+               int off, int Qc, float inv_nstruct, const float *__restrict__ f0tab,
+               const float4 *__restrict__ zf0, int use_f0, float f0_c, float f0_invz,
+               double *__restrict__ out64, float *__restrict__ out32) {
+  const int lane = threadIdx.x & 31;
+  const int n_lines = Qc * Qc;
+  const int stride = gridDim.x * (blockDim.x >> 5);
+  for (int line = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); line < n_lines;
+       line += stride) {
+    const int iy = line / Qc, ix = line - iy * Qc;
+    const int wl = (iy + off) * W + ix + off;
+    const int e0 = lptr[wl], e1 = lptr[wl + 1];
+    if (e0 == e1) continue;
+    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
+    for (int i = lane; i < n_zmulti; i += 32) {
+      const int wz = zmulti[i], iz = wz - off;
+      if (iz < 0 || iz >= Qc) continue;
+      float hi = 0.f, lo = 0.f;
+      for (int e = e0; e < e1; ++e) {
+        const int2 en = __ldg(lent + e);
+        for (int t = t0; t < t1; ++t) {
+          const float *col = G + ((size_t)(t * n_phi + en.x) * nf + (en.y >> 1)) * nr;
+          for (int rr = zptr[wz]; rr < zptr[wz + 1]; ++rr) {
+            const int m = zrows[rr];
+            kahan_step(hi, lo, __ldg(col + ((en.y & 1) ? 2 * r_zero - m : m)));
+          }
+        }
+      }
+      if (MODE == 2) {
+        out64[obase + iz] = f2d_exact(hi) - f2d_exact(lo);
+        continue;
+      }
+      float scale = line_count_factor(C2[wl], inv_nstruct) * z_count_factor((unsigned)C1[wz]);
+      if (use_f0) {
+        const float4 z = zf0[iz];
+        float fxy[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float *t = f0tab + k * 3 * Qc;
+          fxy[k] = __ldg(t + ix) * __ldg(t + Qc + iy);
+        }
+        float acc = f0_c;
+        acc += fxy[0] * z.x;
+        acc += fxy[1] * z.y;
+        acc += fxy[2] * z.z;
+        acc += fxy[3] * z.w;
+        const float fq = acc * f0_invz;
+        scale *= fq * fq;
+      }
+      if (MODE == 1) out64[obase + iz] = (f2d_exact(hi) - f2d_exact(lo)) * f2d_exact(scale);
+      else out32[obase + iz] = (hi - lo) * scale;
+    }
+  }
+}
+
+// Dynamic shared memory of k_gather: the finalize tables, the first output
+// row per qz, and (heavy lines) eight partial sums per qz.
+size_t gather_smem(int Qc, bool use_f0, bool heavy) {
+  return finalize_smem(Qc, use_f0) + (size_t)Qc * sizeof(int) +
+         (heavy ? (size_t)8 * Qc * sizeof(float2) : 0);
 }
 
 // Shell code of every window voxel (voxelgrids.py:651-652, :659-664, :706):
@@ -1026,7 +1172,10 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
   const float f0c = (float)P->p.f0_coef[8];
   const float f0iz = P->p.f0_z > 0 ? (float)(1.0 / P->p.f0_z) : 1.f;
   const float inv_ns = P->p.average == GW_STRUCTS_AVERAGE ? 1.0f / (float)P->n_struct : 1.0f;
-  const size_t smem = gather_smem(Q, use_f0);
+  // heavy lines take a block each when the block's partial sums fit
+  const bool heavy = P->n_heavy > 0 && gather_smem(Q, use_f0, true) <= (200u << 10);
+  const int n_heavy = heavy ? P->n_heavy : 0;
+  const size_t smem = gather_smem(Q, use_f0, heavy);
   static size_t smem_set[3] = {0, 0, 0};
   if (smem > (48u << 10) && smem > smem_set[mode]) {
     cudaError_t e = mode == 0 ? cudaFuncSetAttribute(k_gather<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
@@ -1035,13 +1184,14 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
     GW_CUDA(e);
     smem_set[mode] = smem;
   }
-  const int blocks = std::min((Q * Q + 7) / 8, 16 * ctx->sm_count);
+  const int blocks = n_heavy + std::min((Q * Q + 7) / 8, 16 * ctx->sm_count);
   float *o32 = mode == 0 ? P->d_iq32 + t * P->iq_stride : nullptr;
   double *o64 = mode == 1 ? P->d_iq64 + t * P->iq_stride
               : mode == 2 ? P->d_sum + t * P->sum_stride : nullptr;
   gw::KTimer tm(ctx, GW_K_FINALIZE);
 #define GW_GATHER_ARGS                                                             \
-  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->Nf, P->Nr, P->r_zero,    \
+  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->d_heavy, n_heavy, P->Nf, \
+      P->Nr, P->r_zero,                                                              \
       P->n_phi, t0, t1, P->d_C2, P->d_C1, P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, \
       use_f0, f0c, f0iz, o64, o32
   if (mode == 0) k_gather<0><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
@@ -1049,6 +1199,18 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
   else k_gather<2><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
 #undef GW_GATHER_ARGS
   GW_LAUNCHED(ctx);
+  if (P->n_zmulti > 0) {
+    const int mb = std::min((Q * Q + 7) / 8, 4 * ctx->sm_count);
+#define GW_GATHER_MULTI_ARGS                                                         \
+  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->d_zmulti, P->n_zmulti,     \
+      P->Nf, P->Nr, P->r_zero, P->n_phi, t0, t1, P->d_C2, P->d_C1, P->W, off, Q,     \
+      inv_ns, P->d_f0, P->d_zf0, use_f0, f0c, f0iz, o64, o32
+    if (mode == 0) k_gather_multi<0><<<mb, 256, 0, ctx->stream>>>(GW_GATHER_MULTI_ARGS);
+    else if (mode == 1) k_gather_multi<1><<<mb, 256, 0, ctx->stream>>>(GW_GATHER_MULTI_ARGS);
+    else k_gather_multi<2><<<mb, 256, 0, ctx->stream>>>(GW_GATHER_MULTI_ARGS);
+#undef GW_GATHER_MULTI_ARGS
+    GW_LAUNCHED(ctx);
+  }
   return GW_OK;
 }
 
@@ -1499,7 +1661,9 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
     const size_t g_bytes = (size_t)P->n_slices * P->Nf * P->Nr * sizeof(float);
     const char *env = getenv("GW_GATHER_MAX_MB");
     const size_t cap = (env ? (size_t)std::max(0L, atol(env)) : (size_t)8192) << 20;
-    const bool can = !P->plain && p->accum == GW_ACCUM_FP64 && !P->fused_z && g_bytes <= cap;
+    // (and fewer than 2^31 pixels: the gather addresses them with 32 bits)
+    const bool can = !P->plain && p->accum == GW_ACCUM_FP64 && !P->fused_z &&
+                     g_bytes <= cap && g_bytes / sizeof(float) < ((size_t)1 << 31);
     if (p->binning == GW_BINNING_GATHER && !can) {
       gw_voxel_plan_destroy(P);
       return gw::fail(GW_ERR_ARG, "gw_voxel_plan_create: gather binning needs a batched, "
@@ -1545,7 +1709,20 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       std::vector<int> zfill(zptr.begin(), zptr.end() - 1);
       for (int mr = 0; mr < P->Nr; ++mr)
         if (rowofs[mr] >= 0) zrows[zfill[rowofs[mr]]++] = mr;
-      if ((st = upload(&P->d_lptr, lptr, &B)) || (st = upload(&P->d_lent, lent, &B)) ||
+      // window z with more than one output row
+      std::vector<int> zmulti;
+      for (int z = 0; z < W; ++z)
+        if (zptr[z + 1] - zptr[z] > 1) zmulti.push_back(z);
+      P->n_zmulti = (int)zmulti.size();
+      if (zmulti.empty()) zmulti.push_back(0);
+      // lines with more than kGatherHeavy entries (near the rotation axis)
+      std::vector<int> heavy;
+      for (int l = 0; l < W * W; ++l)
+        if (lptr[l + 1] - lptr[l] > kGatherHeavy) heavy.push_back(l);
+      P->n_heavy = (int)heavy.size();
+      if (heavy.empty()) heavy.push_back(0);
+      if ((st = upload(&P->d_heavy, heavy, &B)) || (st = upload(&P->d_zmulti, zmulti, &B)) ||
+          (st = upload(&P->d_lptr, lptr, &B)) || (st = upload(&P->d_lent, lent, &B)) ||
           (st = upload(&P->d_zptr, zptr, &B)) || (st = upload(&P->d_zrows, zrows, &B)) ||
           (st = alloc(&P->d_G, g_bytes / sizeof(float), &B))) {
         gw_voxel_plan_destroy(P);
@@ -1574,7 +1751,7 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
                   P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0,
                   P->d_fty, P->d_ftz, P->d_G, P->d_lptr, P->d_lent, P->d_zptr,
-                  P->d_zrows};
+                  P->d_zrows, P->d_heavy, P->d_zmulti};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;

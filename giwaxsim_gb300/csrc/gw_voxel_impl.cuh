@@ -603,6 +603,13 @@ struct gw_voxel_plan {
   float *d_G = nullptr;
   int *d_lptr = nullptr, *d_zptr = nullptr, *d_zrows = nullptr;
   int2 *d_lent = nullptr;
+  // window lines with many entries (each takes a whole block)
+  int *d_heavy = nullptr;
+  int n_heavy = 0;
+  // window z with more than one output row (their voxels are summed again
+  // over every row)
+  int *d_zmulti = nullptr;
+  int n_zmulti = 0;
   // fused chirp-z kernels (gw_czt2.cuh) along y / z, with their twiddles
   bool fused_y = false, fused_z = false;
   float2 *d_fty = nullptr, *d_ftz = nullptr;

@@ -88,14 +88,14 @@ def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
     make = lambda **kw: FakePlan(ctx, **kw)  # noqa: E731
     best = T.tune(make, 1, smooth=1.5, ctx=ctx)
     assert best == dict(fft_y=1280, fft_z=1024, batch_slices=51,
-                        transform=("fused", "stockham"), block_variant=2)
-    # the shape probe, the default plan, 3 row candidates (1536 has no fused
-    # shape), 4 column candidates, 2 new batch sizes, 3 new block shapes
-    assert len(FakePlan.made) == 1 + 1 + 3 + 4 + 2 + 3
+                        transform=("fused", "auto"), block_variant=2)
+    # the shape probe, the default plan, 1 new row length, 1 new column
+    # length, 3 new family pairs, 2 new batch sizes, 3 new block shapes
+    assert len(FakePlan.made) == 1 + 1 + 1 + 1 + 3 + 2 + 3
     cache = json.load(open(tmp_path / "tune.json"))
     (entry,) = cache.values()
-    assert entry["choice"]["transform"] == ["fused", "stockham"]
-    assert entry["candidates"] == 14 and entry["ms"] < entry["default_ms"]
+    assert entry["choice"]["transform"] == ["fused", "auto"]
+    assert entry["candidates"] == 11 and entry["ms"] < entry["default_ms"]
     FakePlan.made = []
     assert T.tune(make, 1, smooth=1.5, ctx=ctx) == best
     assert len(FakePlan.made) == 1  # only the shape probe
