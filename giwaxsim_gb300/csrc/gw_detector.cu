@@ -152,6 +152,7 @@ struct OrientFast {
 constexpr int kOrientFloats = sizeof(OrientFast) / 4;
 
 constexpr int kDetThreads = 256, kDetPix = 2, kDetChunk = 128, kDetFlush = 16;
+static_assert(kDetChunk % kDetFlush == 0, "orientation chunks hold whole flush groups");
 
 __device__ __forceinline__ bool fast_axis(float t, float d, int n, int &k) {
   // k = clamp(floor(t + d), 0, n-1) (clamping first is the same: NaN and
@@ -370,37 +371,43 @@ k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
     for (int t = threadIdx.x; t < nc * 3; t += kPlThreads)
       reinterpret_cast<float4 *>(s_ot)[t] = reinterpret_cast<const float4 *>(ot + c0)[t];
     __syncthreads();
-    for (int oo = 0; oo < nc; ++oo) {
-      const PlaneOrient T = s_ot[oo];
-      const int o = c0 + oo;
+    // groups of kDetFlush orientations (chunks start at multiples of it),
+    // two per loop trip, flushed to float64 after each full group
+    for (int g0 = 0; g0 < nc; g0 += kDetFlush) {
+      const int ge = min(g0 + kDetFlush, nc);
+#pragma unroll 2
+      for (int oo = g0; oo < ge; ++oo) {
+        const PlaneOrient T = s_ot[oo];
+        const int o = c0 + oo;
 #pragma unroll
-      for (int k = 0; k < KP; ++k) {
-        int iu, iv;
-        const bool ok = plane_index<ZX>(T, nu1, nv1, xf[k], yf[k], zf[k], iu, iv);
-        const bool need = valid[k] && !ok;
-        const unsigned m = __ballot_sync(0xffffffffu, need);
-        bool inline_exact = false;
-        if (m) {
-          int base = 0;
-          const int leader = __ffs(m) - 1;
-          if (lane == leader) base = atomicAdd(wl_count, __popc(m));
-          base = __shfl_sync(0xffffffffu, base, leader);
-          if (need) {
-            const int slot = base + __popc(m & ((1u << lane) - 1u));
-            if (slot < wl_cap) wl[slot] = make_int2(pix[k], o);
-            else inline_exact = true;
+        for (int k = 0; k < KP; ++k) {
+          int iu, iv;
+          const bool ok = plane_index<ZX>(T, nu1, nv1, xf[k], yf[k], zf[k], iu, iv);
+          const bool need = valid[k] && !ok;
+          const unsigned m = __ballot_sync(0xffffffffu, need);
+          bool inline_exact = false;
+          if (m) {
+            int base = 0;
+            const int leader = __ffs(m) - 1;
+            if (lane == leader) base = atomicAdd(wl_count, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+              const int slot = base + __popc(m & ((1u << lane) - 1u));
+              if (slot < wl_cap) wl[slot] = make_int2(pix[k], o);
+              else inline_exact = true;
+            }
           }
+          float v = 0.f;
+          if (valid[k] && ok) v = SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv);
+          if (inline_exact) {
+            double x, y, z;
+            base_point(a, pix[k] / a.nh, pix[k] % a.nh, x, y, z);
+            v = __ldg(a.iq + gather_index(a, o, x, y, z));
+          }
+          if (valid[k] && (ok || inline_exact)) part[k] = fmaf(v, T.e.z, part[k]);
         }
-        float v = 0.f;
-        if (valid[k] && ok) v = SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv);
-        if (inline_exact) {
-          double x, y, z;
-          base_point(a, pix[k] / a.nh, pix[k] % a.nh, x, y, z);
-          v = __ldg(a.iq + gather_index(a, o, x, y, z));
-        }
-        if (valid[k] && (ok || inline_exact)) part[k] = fmaf(v, T.e.z, part[k]);
       }
-      if ((o + 1) % kDetFlush == 0) {
+      if (ge - g0 == kDetFlush) {
 #pragma unroll
         for (int k = 0; k < KP; ++k) { acc[k] += f2d_exact(part[k]); part[k] = 0.f; }
       }

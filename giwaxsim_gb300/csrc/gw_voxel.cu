@@ -599,6 +599,42 @@ __device__ __forceinline__ void gather_entries(const float *__restrict__ G,
   }
 }
 
+// Entries [e0, e1) of a line into one voxel's accumulator (its first
+// output row mr), kGatherV entries' loads in flight.
+constexpr int kGatherV = 8;
+
+__device__ __forceinline__ void gather_voxel(const float *__restrict__ G,
+                                             const int2 *__restrict__ lent, int e0,
+                                             int e1, int t0, int t1, int n_phi, int nf,
+                                             int nr, int r_zero, int mr, float &hi,
+                                             float &lo) {
+  const int mf = 2 * r_zero - mr;
+  const unsigned tstep = (unsigned)n_phi * (unsigned)nf * (unsigned)nr;
+#pragma unroll 1
+  for (int e = e0; e < e1; e += kGatherV) {
+    const int ne = min(kGatherV, e1 - e);
+    unsigned o[kGatherV];
+#pragma unroll
+    for (int k = 0; k < kGatherV; ++k) {
+      const int2 en = k < ne ? __ldg(lent + e + k) : make_int2(0, 0);
+      o[k] = ((unsigned)(t0 * n_phi + en.x) * (unsigned)nf + (unsigned)(en.y >> 1)) *
+                 (unsigned)nr + (unsigned)((en.y & 1) ? mf : mr);
+    }
+#pragma unroll 1
+    for (int t = t0; t < t1; ++t) {
+      float v[kGatherV];
+#pragma unroll
+      for (int k = 0; k < kGatherV; ++k) v[k] = k < ne ? __ldg(G + o[k]) : 0.f;
+#pragma unroll
+      for (int k = 0; k < kGatherV; ++k) {
+        if (k >= ne) break;
+        kahan_step(hi, lo, v[k]);
+        o[k] += tstep;
+      }
+    }
+  }
+}
+
 template <int MODE>
 __device__ __forceinline__ void gather_store(float hi, float lo, int iz, size_t obase,
                                              float r2, const float *s_rc1,
@@ -702,43 +738,35 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     }
     return;
   }
-  // the other lines, one warp each
-  const int n_lines = Qc * Qc;
+  // the other lines: one thread per voxel, a warp per 32 consecutive qz of
+  // a line (many independent loads in flight, the line's entries a
+  // broadcast)
+  const int zchunks = (Qc + 31) / 32;
+  const int64_t nwarps = (int64_t)Qc * Qc * zchunks;
   const int wpb = blockDim.x >> 5;
-  const int stride = (gridDim.x - n_heavy) * wpb;
-  for (int line = (blockIdx.x - n_heavy) * wpb + warp; line < n_lines; line += stride) {
+  const int64_t stride = (int64_t)(gridDim.x - n_heavy) * wpb;
+  for (int64_t gw = (int64_t)(blockIdx.x - n_heavy) * wpb + warp; gw < nwarps; gw += stride) {
+    const int line = (int)(gw / zchunks);
+    const int iz = (int)(gw - (int64_t)line * zchunks) * 32 + lane;
     const int iy = line / Qc, ix = line - iy * Qc;
     const int wl = (iy + off) * W + ix + off;
-    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
     const int e0 = lptr[wl], e1 = lptr[wl + 1];
     if (n_heavy > 0 && e1 - e0 > kGatherHeavy) continue;  // a heavy block's
+    if (iz >= Qc) continue;
+    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
     if (e0 == e1) {
-      for (int iz = lane; iz < Qc; iz += 32) {
-        if (MODE == 0) out32[obase + iz] = 0.f;
-        else out64[obase + iz] = 0.0;
-      }
+      if (MODE == 0) out32[obase + iz] = 0.f;
+      else out64[obase + iz] = 0.0;
       continue;
     }
+    float hi = 0.f, lo = 0.f;
+    const int mr = s_row[iz];
+    if (mr >= 0)
+      gather_voxel(G, lent, e0, e1, t0, t1, n_phi, nf, nr, r_zero, mr, hi, lo);
     float r2, fxy[4];
     line_consts(iy, ix, wl, r2, fxy);
-    for (int iz0 = 0; iz0 < Qc; iz0 += 32 * kGU) {
-      float hi[kGU], lo[kGU];
-      int mr[kGU];
-#pragma unroll
-      for (int u = 0; u < kGU; ++u) {
-        const int iz = iz0 + u * 32 + lane;
-        hi[u] = lo[u] = 0.f;
-        mr[u] = iz < Qc ? s_row[iz] : -1;
-      }
-      gather_entries(G, lent, e0, e1, t0, t1, n_phi, nf, nr, r_zero, mr, hi, lo);
-#pragma unroll
-      for (int u = 0; u < kGU; ++u) {
-        const int iz = iz0 + u * 32 + lane;
-        if (iz >= Qc) break;
-        gather_store<MODE>(hi[u], lo[u], iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c,
-                           f0_invz, out64, out32);
-      }
-    }
+    gather_store<MODE>(hi, lo, iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c, f0_invz,
+                       out64, out32);
   }
 }
 
@@ -1184,7 +1212,8 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
     GW_CUDA(e);
     smem_set[mode] = smem;
   }
-  const int blocks = n_heavy + std::min((Q * Q + 7) / 8, 16 * ctx->sm_count);
+  const int64_t light_warps = (int64_t)Q * Q * ((Q + 31) / 32);
+  const int blocks = n_heavy + (int)std::min<int64_t>((light_warps + 7) / 8, 32 * ctx->sm_count);
   float *o32 = mode == 0 ? P->d_iq32 + t * P->iq_stride : nullptr;
   double *o64 = mode == 1 ? P->d_iq64 + t * P->iq_stride
               : mode == 2 ? P->d_sum + t * P->sum_stride : nullptr;
