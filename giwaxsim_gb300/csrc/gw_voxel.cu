@@ -599,38 +599,35 @@ __device__ __forceinline__ void gather_entries(const float *__restrict__ G,
   }
 }
 
-// Entries [e0, e1) of a line into one voxel's accumulator (its first
-// output row mr), kGatherV entries' loads in flight.
-constexpr int kGatherV = 8;
+// A warp's pass over a span of up to 32 kGatherU voxels of a line (qz =
+// z0 + lane + 32 u): per entry, the pixel loads of all its voxels are
+// issued together, then added (compensated) in entry order.
+constexpr int kGatherU = 16;
 
-__device__ __forceinline__ void gather_voxel(const float *__restrict__ G,
-                                             const int2 *__restrict__ lent, int e0,
-                                             int e1, int t0, int t1, int n_phi, int nf,
-                                             int nr, int r_zero, int mr, float &hi,
-                                             float &lo) {
-  const int mf = 2 * r_zero - mr;
+__device__ __forceinline__ void gather_span(const float *__restrict__ G,
+                                            const int2 *__restrict__ lent, int e0,
+                                            int e1, int t0, int t1, int n_phi, int nf,
+                                            int nr, int r_zero, const int *s_row, int z0,
+                                            int lane, int Qc, float (&hi)[kGatherU],
+                                            float (&lo)[kGatherU]) {
   const unsigned tstep = (unsigned)n_phi * (unsigned)nf * (unsigned)nr;
 #pragma unroll 1
-  for (int e = e0; e < e1; e += kGatherV) {
-    const int ne = min(kGatherV, e1 - e);
-    unsigned o[kGatherV];
-#pragma unroll
-    for (int k = 0; k < kGatherV; ++k) {
-      const int2 en = k < ne ? __ldg(lent + e + k) : make_int2(0, 0);
-      o[k] = ((unsigned)(t0 * n_phi + en.x) * (unsigned)nf + (unsigned)(en.y >> 1)) *
-                 (unsigned)nr + (unsigned)((en.y & 1) ? mf : mr);
-    }
+  for (int e = e0; e < e1; ++e) {
+    const int2 en = __ldg(lent + e);
+    const bool flip = en.y & 1;
+    unsigned col = ((unsigned)(t0 * n_phi + en.x) * (unsigned)nf + (unsigned)(en.y >> 1)) *
+                   (unsigned)nr;
 #pragma unroll 1
-    for (int t = t0; t < t1; ++t) {
-      float v[kGatherV];
+    for (int t = t0; t < t1; ++t, col += tstep) {
+      float v[kGatherU];
 #pragma unroll
-      for (int k = 0; k < kGatherV; ++k) v[k] = k < ne ? __ldg(G + o[k]) : 0.f;
-#pragma unroll
-      for (int k = 0; k < kGatherV; ++k) {
-        if (k >= ne) break;
-        kahan_step(hi, lo, v[k]);
-        o[k] += tstep;
+      for (int u = 0; u < kGatherU; ++u) {
+        const int iz = z0 + lane + 32 * u;
+        const int mr = iz < Qc ? s_row[iz] : -1;
+        v[u] = mr >= 0 ? __ldg(G + col + (unsigned)(flip ? 2 * r_zero - mr : mr)) : 0.f;
       }
+#pragma unroll
+      for (int u = 0; u < kGatherU; ++u) kahan_step(hi[u], lo[u], v[u]);
     }
   }
 }
@@ -738,35 +735,39 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     }
     return;
   }
-  // the other lines: one thread per voxel, a warp per 32 consecutive qz of
-  // a line (many independent loads in flight, the line's entries a
-  // broadcast)
-  const int zchunks = (Qc + 31) / 32;
-  const int64_t nwarps = (int64_t)Qc * Qc * zchunks;
+  // the other lines, one warp each, in spans of 32 kGatherU voxels
+  const int n_lines = Qc * Qc;
   const int wpb = blockDim.x >> 5;
-  const int64_t stride = (int64_t)(gridDim.x - n_heavy) * wpb;
-  for (int64_t gw = (int64_t)(blockIdx.x - n_heavy) * wpb + warp; gw < nwarps; gw += stride) {
-    const int line = (int)(gw / zchunks);
-    const int iz = (int)(gw - (int64_t)line * zchunks) * 32 + lane;
+  const int stride = (gridDim.x - n_heavy) * wpb;
+  for (int line = (blockIdx.x - n_heavy) * wpb + warp; line < n_lines; line += stride) {
     const int iy = line / Qc, ix = line - iy * Qc;
     const int wl = (iy + off) * W + ix + off;
+    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
     const int e0 = lptr[wl], e1 = lptr[wl + 1];
     if (n_heavy > 0 && e1 - e0 > kGatherHeavy) continue;  // a heavy block's
-    if (iz >= Qc) continue;
-    const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
     if (e0 == e1) {
-      if (MODE == 0) out32[obase + iz] = 0.f;
-      else out64[obase + iz] = 0.0;
+      for (int iz = lane; iz < Qc; iz += 32) {
+        if (MODE == 0) out32[obase + iz] = 0.f;
+        else out64[obase + iz] = 0.0;
+      }
       continue;
     }
-    float hi = 0.f, lo = 0.f;
-    const int mr = s_row[iz];
-    if (mr >= 0)
-      gather_voxel(G, lent, e0, e1, t0, t1, n_phi, nf, nr, r_zero, mr, hi, lo);
     float r2, fxy[4];
     line_consts(iy, ix, wl, r2, fxy);
-    gather_store<MODE>(hi, lo, iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c, f0_invz,
-                       out64, out32);
+    for (int z0 = 0; z0 < Qc; z0 += 32 * kGatherU) {
+      float hi[kGatherU], lo[kGatherU];
+#pragma unroll
+      for (int u = 0; u < kGatherU; ++u) hi[u] = lo[u] = 0.f;
+      gather_span(G, lent, e0, e1, t0, t1, n_phi, nf, nr, r_zero, s_row, z0, lane, Qc, hi,
+                  lo);
+#pragma unroll
+      for (int u = 0; u < kGatherU; ++u) {
+        const int iz = z0 + lane + 32 * u;
+        if (iz < Qc)
+          gather_store<MODE>(hi[u], lo[u], iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c,
+                             f0_invz, out64, out32);
+      }
+    }
   }
 }
 
@@ -1212,8 +1213,7 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
     GW_CUDA(e);
     smem_set[mode] = smem;
   }
-  const int64_t light_warps = (int64_t)Q * Q * ((Q + 31) / 32);
-  const int blocks = n_heavy + (int)std::min<int64_t>((light_warps + 7) / 8, 32 * ctx->sm_count);
+  const int blocks = n_heavy + std::min((Q * Q + 7) / 8, 16 * ctx->sm_count);
   float *o32 = mode == 0 ? P->d_iq32 + t * P->iq_stride : nullptr;
   double *o64 = mode == 1 ? P->d_iq64 + t * P->iq_stride
               : mode == 2 ? P->d_sum + t * P->sum_stride : nullptr;
