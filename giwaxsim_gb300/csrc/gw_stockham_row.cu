@@ -102,18 +102,8 @@ struct RowLoadPair {
     const int ra = 2 * f, rb = 2 * f + 1;
     // the deposit holds the real row's atom sum r (deposit_rows<.., REAL>):
     // the grid value there is d_value_row of r u, projected back on u
-    if (row0 + ra < n_rows) {
-      const float2 u = rc[ra].u;
-      const float r = rows[ra * HL + n].x;
-      const float2 d = d_value_row(va, rc[ra], n, make_float2(r * u.x, r * u.y));
-      re = d.x * u.x + d.y * u.y;  // Re(d conj(u))
-    }
-    if (row0 + rb < n_rows) {
-      const float2 u = rc[rb].u;
-      const float r = rows[rb * HL + n].x;
-      const float2 d = d_value_row(va, rc[rb], n, make_float2(r * u.x, r * u.y));
-      im = d.x * u.x + d.y * u.y;
-    }
+    if (row0 + ra < n_rows) re = d_value_row_real(va, rc[ra], n, rows[ra * HL + n].x);
+    if (row0 + rb < n_rows) im = d_value_row_real(va, rc[rb], n, rows[rb * HL + n].x);
     return cmul(make_float2(re, im), __ldg(A + n));
   }
 };

@@ -526,24 +526,24 @@ size_t finalize_smem(int Qc, bool use_f0) {
 }
 
 // Gather binning: the sums of one voxel line in a fixed order, then the
-// finalize of k_finalize.  Lanes run along qz, kGU voxels per lane per
-// round.  A line's entries (phi, F1 column, mirrored) are taken in table
-// order (phi, then band column), kGatherE at a time (their pixel loads
-// issued together), each over the structures t0 .. t1-1 (the slice
-// t n_phi + phi); the pixel of voxel qz is output row mr of the z table
-// (mirrored: row 2 r_zero - mr).  Pixels are float32 and the running sum is
-// compensated (Kahan) float32: the exact sum to about one float32 ulp, the
-// same bits on every run.  Voxels with further output rows (C1 > 1) take
-// them after the first, in row order.  Lines with up to kGatherHeavy
-// entries take one warp each (grid-stride); the heavier lines (near the
-// rotation axis every phi meets) are listed in `heavy` and take one block
-// each, its warps splitting the entries in eight fixed parts whose partial
-// sums are added in warp order.
+// finalize of k_finalize.  A warp runs along qz in spans of 32 kGatherU
+// voxels (qz = z0 + lane + 32 u).  A line's entries (phi, F1 column,
+// mirrored) are taken in table order (phi, then band column), kGatherP at
+// a time with the pixel loads of all their voxels issued together, each
+// over the structures t0 .. t1-1 (the slice t n_phi + phi); the pixel of
+// voxel qz is output row mr of the z table (mirrored: row 2 r_zero - mr).
+// Pixels are float32 and the running sum is compensated (Kahan) float32:
+// the exact sum to about one float32 ulp, the same bits on every run.
+// Voxels with further output rows (C1 > 1) are summed again over all rows
+// by k_gather_multi.  Lines with up to kGatherHeavy entries take one warp
+// each (grid-stride); the heavier lines (near the rotation axis every phi
+// meets) are listed in `heavy` and take one block each, its warps
+// splitting the entries in eight fixed parts whose partial sums are added
+// in warp order.  Three blocks per SM: 79 registers without spills, the
+// loads of 24 warps in flight.
 // MODE 0: the float32 I(q) (crop, factor, f0 as k_finalize); 1: the float64
 // I(q) from the same sums; 2: the float64 sums into the window grid (crop
 // = window, off = 0; no factor).
-constexpr int kGatherE = 4;       // entries whose loads are issued together
-constexpr int kGU = 4;            // voxels per lane per round
 constexpr int kGatherHeavy = 64;
 
 __device__ __forceinline__ void kahan_step(float &hi, float &lo, float x) {
@@ -553,56 +553,11 @@ __device__ __forceinline__ void kahan_step(float &hi, float &lo, float x) {
   hi = s;
 }
 
-// Entries [e0, e1) of a line into the lane's kGU accumulators.  Pixel
-// offsets are 32-bit (the pixel store holds fewer than 2^31 floats).
-__device__ __forceinline__ void gather_entries(const float *__restrict__ G,
-                                               const int2 *__restrict__ lent,
-                                               int e0, int e1, int t0, int t1,
-                                               int n_phi, int nf, int nr, int r_zero,
-                                               const int (&mr)[kGU],
-                                               float (&hi)[kGU], float (&lo)[kGU]) {
-  int mf[kGU];  // mirrored rows
-#pragma unroll
-  for (int u = 0; u < kGU; ++u) mf[u] = 2 * r_zero - mr[u];
-#pragma unroll 1
-  for (int e = e0; e < e1; e += kGatherE) {
-    const int ne = min(kGatherE, e1 - e);
-    unsigned colo[kGatherE];
-    bool flip[kGatherE];
-#pragma unroll
-    for (int k = 0; k < kGatherE; ++k) {
-      const int2 en = k < ne ? __ldg(lent + e + k) : make_int2(0, 0);
-      colo[k] = ((unsigned)(t0 * n_phi + en.x) * (unsigned)nf + (unsigned)(en.y >> 1)) *
-                (unsigned)nr;
-      flip[k] = en.y & 1;
-    }
-    const unsigned tstep = (unsigned)n_phi * (unsigned)nf * (unsigned)nr;
-#pragma unroll 1
-    for (int t = t0; t < t1; ++t) {
-      float v[kGatherE][kGU];
-#pragma unroll
-      for (int k = 0; k < kGatherE; ++k)
-#pragma unroll
-        for (int u = 0; u < kGU; ++u)
-          v[k][u] = (k < ne && mr[u] >= 0)
-                        ? __ldg(G + colo[k] + (unsigned)(flip[k] ? mf[u] : mr[u]))
-                        : 0.f;
-#pragma unroll
-      for (int k = 0; k < kGatherE; ++k) {
-        if (k >= ne) break;
-#pragma unroll
-        for (int u = 0; u < kGU; ++u) kahan_step(hi[u], lo[u], v[k][u]);
-      }
-#pragma unroll
-      for (int k = 0; k < kGatherE; ++k) colo[k] += tstep;
-    }
-  }
-}
-
 // A warp's pass over a span of up to 32 kGatherU voxels of a line (qz =
-// z0 + lane + 32 u): per entry, the pixel loads of all its voxels are
-// issued together, then added (compensated) in entry order.
-constexpr int kGatherU = 16;
+// z0 + lane + 32 u): kGatherP entries at a time, the pixel loads of all
+// their voxels issued together, then added (compensated) in entry order.
+constexpr int kGatherU = 8;
+constexpr int kGatherP = 2;
 
 __device__ __forceinline__ void gather_span(const float *__restrict__ G,
                                             const int2 *__restrict__ lent, int e0,
@@ -611,23 +566,41 @@ __device__ __forceinline__ void gather_span(const float *__restrict__ G,
                                             int lane, int Qc, float (&hi)[kGatherU],
                                             float (&lo)[kGatherU]) {
   const unsigned tstep = (unsigned)n_phi * (unsigned)nf * (unsigned)nr;
-#pragma unroll 1
-  for (int e = e0; e < e1; ++e) {
-    const int2 en = __ldg(lent + e);
-    const bool flip = en.y & 1;
-    unsigned col = ((unsigned)(t0 * n_phi + en.x) * (unsigned)nf + (unsigned)(en.y >> 1)) *
-                   (unsigned)nr;
-#pragma unroll 1
-    for (int t = t0; t < t1; ++t, col += tstep) {
-      float v[kGatherU];
+  int mr[kGatherU];
 #pragma unroll
-      for (int u = 0; u < kGatherU; ++u) {
-        const int iz = z0 + lane + 32 * u;
-        const int mr = iz < Qc ? s_row[iz] : -1;
-        v[u] = mr >= 0 ? __ldg(G + col + (unsigned)(flip ? 2 * r_zero - mr : mr)) : 0.f;
+  for (int u = 0; u < kGatherU; ++u) {
+    const int iz = z0 + lane + 32 * u;
+    mr[u] = iz < Qc ? s_row[iz] : -1;
+  }
+#pragma unroll 1
+  for (int e = e0; e < e1; e += kGatherP) {
+    const int ne = min(kGatherP, e1 - e);
+    unsigned col[kGatherP];
+    bool flip[kGatherP];
+#pragma unroll
+    for (int k = 0; k < kGatherP; ++k) {
+      const int2 en = k < ne ? __ldg(lent + e + k) : make_int2(0, 0);
+      col[k] = ((unsigned)(t0 * n_phi + en.x) * (unsigned)nf + (unsigned)(en.y >> 1)) *
+               (unsigned)nr;
+      flip[k] = en.y & 1;
+    }
+#pragma unroll 1
+    for (int t = t0; t < t1; ++t) {
+      float v[kGatherP][kGatherU];
+#pragma unroll
+      for (int k = 0; k < kGatherP; ++k)
+#pragma unroll
+        for (int u = 0; u < kGatherU; ++u)
+          v[k][u] = (k < ne && mr[u] >= 0)
+                        ? __ldg(G + col[k] + (unsigned)(flip[k] ? 2 * r_zero - mr[u] : mr[u]))
+                        : 0.f;
+#pragma unroll
+      for (int k = 0; k < kGatherP; ++k) {
+        if (k >= ne) break;
+#pragma unroll
+        for (int u = 0; u < kGatherU; ++u) kahan_step(hi[u], lo[u], v[k][u]);
+        col[k] += tstep;
       }
-#pragma unroll
-      for (int u = 0; u < kGatherU; ++u) kahan_step(hi[u], lo[u], v[u]);
     }
   }
 }
@@ -658,7 +631,7 @@ __device__ __forceinline__ void gather_store(float hi, float lo, int iz, size_t 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
          const int2 *__restrict__ lent, const int *__restrict__ zptr,
          const int *__restrict__ zrows, const int *__restrict__ heavy, int n_heavy,
@@ -703,19 +676,15 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     const int nw = blockDim.x >> 5;
     const int eb = e0 + (int)((int64_t)ne * warp / nw);
     const int ee = e0 + (int)((int64_t)ne * (warp + 1) / nw);
-    for (int iz0 = 0; iz0 < Qc; iz0 += 32 * kGU) {
-      float hi[kGU], lo[kGU];
-      int mr[kGU];
+    for (int z0 = 0; z0 < Qc; z0 += 32 * kGatherU) {
+      float hi[kGatherU], lo[kGatherU];
 #pragma unroll
-      for (int u = 0; u < kGU; ++u) {
-        const int iz = iz0 + u * 32 + lane;
-        hi[u] = lo[u] = 0.f;
-        mr[u] = iz < Qc ? s_row[iz] : -1;
-      }
-      gather_entries(G, lent, eb, ee, t0, t1, n_phi, nf, nr, r_zero, mr, hi, lo);
+      for (int u = 0; u < kGatherU; ++u) hi[u] = lo[u] = 0.f;
+      gather_span(G, lent, eb, ee, t0, t1, n_phi, nf, nr, r_zero, s_row, z0, lane, Qc, hi,
+                  lo);
 #pragma unroll
-      for (int u = 0; u < kGU; ++u) {
-        const int iz = iz0 + u * 32 + lane;
+      for (int u = 0; u < kGatherU; ++u) {
+        const int iz = z0 + lane + 32 * u;
         if (iz < Qc) s_part[warp * Qc + iz] = make_float2(hi[u], lo[u]);
       }
     }

@@ -286,6 +286,33 @@ __device__ __forceinline__ float2 d_value_row(const SliceArgs &a,
   return d_value_row(row_value_args(a), k, yy, dep);
 }
 
+// Real grids: Re(d_value_row(a, k, yy, r u) conj(u)) for the real row sum
+// r.  The fill and smoothing values (amo, cd, cbg) are multiples of u, so
+// the projection is taken term by term, in float32 (|u| = 1).
+__device__ __forceinline__ float d_value_row_real(const RowValueArgs &a,
+                                                  const RowConst &k, int yy,
+                                                  float r) {
+  const float cdr = k.cd.x * k.u.x + k.cd.y * k.u.y;
+  float v;
+  if (a.fill) {
+    int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
+    const bool inside = k.zin && yi > k.e.x && yi < k.e.y;
+    if (inside) {
+      const float2 am = a.amo[(size_t)k.slot * a.Ly + yy];
+      v = r + (am.x * k.u.x + am.y * k.u.y);
+    } else {
+      v = cdr;
+    }
+  } else {
+    v = r - (k.cbg.x * k.u.x + k.cbg.y * k.u.y);
+  }
+  if (a.smooth_on) {
+    const float m = k.mz * a.my[(size_t)k.slot * a.Ly + yy];
+    v = v * m + cdr * (1.f - m);
+  }
+  return v;
+}
+
 // Window column of sorted atom `at` in slice `sl` (nearest-bin deposit):
 // false when the valid mask drops it (y index outside [0, g)); yy >= Ly
 // flags a window overflow.
