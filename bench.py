@@ -516,12 +516,13 @@ def _event_ms(ts, fn, reps, flush=None):
 
 def plan_choice(plan):
     """The tuned choices of a plan (lengths, batch, kernel family per axis,
-    block shape) as VoxelPlan keywords, for a replica of it."""
+    block shape, binning) as VoxelPlan keywords, for a replica of it."""
     p = plan.params
     fam = {0: "auto", 1: "stockham", 2: "fused"}
+    binning = {0: "auto", 1: "atomic", 2: "gather"}
     return dict(fft_y=p.fft_y, fft_z=p.fft_z, batch_slices=p.batch_slices,
                 transform=(fam[p.transform_y], fam[p.transform_z]),
-                block_variant=p.block_variant)
+                block_variant=p.block_variant, binning=binning[p.binning])
 
 
 def plain_path_ms(geom, w, items, phis, ctx, ts, reps=2):

@@ -10,6 +10,8 @@ the plan's own inputs (graph replays, device events):
   transform        kernel family per axis: the fused chirp-z kernel (two
                    shared-memory exchanges per convolution, where the length
                    has a fused shape) or the Stockham kernels;
+  binning          float64 atomic adds or the gather binning (the pixels
+                   stored, each voxel summed in a fixed order);
   batch_slices     slices per batch: the L2-sized default, half and double;
   block_variant    block shape of the fused kernels: sequences per block and
                    register cap (occupancy against register spills).
@@ -69,7 +71,7 @@ def length_candidates(need, count=2):
 
 def shape_key(ctx, info, n_structures, fill_bkg, smooth, deposit):
     return "|".join(str(x) for x in (
-        "v4", ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
+        "v5", ctx.device_name(), info["Ly"], info["Nc"], info["Lz"], info["Nr"],
         info.get("real", 0),
         info["n_slices"], n_structures, int(bool(fill_bkg)),
         int(bool(smooth)), deposit))
@@ -83,15 +85,16 @@ def _as_kwargs(choice):
 
 def tune(make_plan, n_structures, fill_bkg=False, smooth=0,
          deposit="nearest", ctx=None, reps=3, use_cache=True, log=None):
-    """Best {fft_y, fft_z, batch_slices, transform, block_variant} for the
-    plan make_plan(**choice) builds (make_plan must accept those keywords;
-    0 / "auto" = the defaults).  Every candidate plan gets its atoms, one
+    """Best {fft_y, fft_z, batch_slices, transform, block_variant,
+    binning} for the plan make_plan(**choice) builds (make_plan must accept
+    those keywords; 0 / "auto" = the defaults).  Every candidate plan gets
+    its atoms, one
     warm-up, a captured graph and `reps` timed replays; a candidate the
     library refuses (a fused family for a length without a fused shape) is
     skipped."""
     ctx = ctx or N.default_context()
     default = dict(fft_y=0, fft_z=0, batch_slices=0,
-                   transform=("auto", "auto"), block_variant=0)
+                   transform=("auto", "auto"), block_variant=0, binning="auto")
     base = make_plan(**_as_kwargs(default))
     try:
         info = base.info()
@@ -149,6 +152,9 @@ def tune(make_plan, n_structures, fill_bkg=False, smooth=0,
     # axes are not independent
     _, best = best_of([dict(best, transform=[fy, fz])
                        for fy in ("auto", "fused") for fz in ("auto", "fused")])
+    # binning: atomic float64 adds or gather (refused where it does not
+    # apply); auto is one of the two
+    _, best = best_of([dict(best, binning=b) for b in ("atomic", "gather")])
     # slices per batch
     S = info["batch"]
     batches = sorted({S, max(1, S // 2), min(info["n_slices"], 2 * S, 4096)})

@@ -401,6 +401,7 @@ int gw_ctx_create(int device, gw_ctx **out) {
   auto *c = new gw_ctx();
   c->device = device;
   c->sm_count = prop.multiProcessorCount;
+  c->l2_bytes = (size_t)prop.l2CacheSize;
   {
     std::lock_guard<std::mutex> lk(g_ctx_mu);
     ++g_ctx_live[device];

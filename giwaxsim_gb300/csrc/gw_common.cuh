@@ -197,6 +197,7 @@ struct gw_ctx {
   cudaStream_t stream = nullptr;
   int64_t launches = 0;
   int sm_count = 0;
+  size_t l2_bytes = 0;
   // device-side error word: first failing check writes its code.
   int *d_err = nullptr;
   // per-kernel timing

@@ -1668,7 +1668,17 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
                                   "float64-accumulating plan without the fused column "
                                   "kernel, and a pixel store within GW_GATHER_MAX_MB");
     }
-    if (p->binning != GW_BINNING_ATOMIC && can) {
+    // auto: gather for one structure on real grids whose float64 sum grid
+    // is larger than L2 -- each atomic is then a DRAM read-modify-write and
+    // the grid's clearing a DRAM pass, while each stored pixel serves two
+    // voxels (its mirror) -- measured faster there (si-100A) and slower
+    // with the grid in L2, several structures (the gather loops over the
+    // structures of every entry) or complex grids (lamellar-200A)
+    const size_t sum_bytes = P->sum_stride * P->n_out * sizeof(double);
+    const bool want = p->binning == GW_BINNING_GATHER ||
+                      (p->binning == GW_BINNING_AUTO && P->real && n_struct == 1 &&
+                       sum_bytes > ctx->l2_bytes);
+    if (want && can) {
       // the line entries, in table order (phi, band column): counting sort
       // by window line
       std::vector<int> cof((size_t)n_phi * P->Nc);

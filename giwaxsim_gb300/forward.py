@@ -294,6 +294,7 @@ class VoxelPlan:
             batch_slices = self.tuned["batch_slices"]
             transform = self.tuned["transform"]
             block_variant = self.tuned["block_variant"]
+            binning = self.tuned.get("binning", binning)
         self.phis = geom.auto_phis if phis is None else np.asarray(phis, np.float64)
         if len(self.phis) < 1:
             raise ValueError("at least one phi is required")

@@ -177,9 +177,11 @@ typedef struct gw_voxel_params {
                            bit-identical results run to run (batched plans
                            with float64 accumulation; GW_ERR_ARG
                            otherwise, or when the pixel store would exceed
-                           the device budget); GW_BINNING_AUTO: gather where
-                           it applies, else atomic.  Multi-q shells always
-                           bin atomically.                                 */
+                           the device budget); GW_BINNING_AUTO: gather for
+                           one structure on real grids whose float64 sum
+                           grid is larger than the L2 cache (the atomics
+                           would go to DRAM), atomic otherwise.  Multi-q
+                           shells always bin atomically.                   */
 } gw_voxel_params;
 
 typedef struct gw_structure {

@@ -66,9 +66,11 @@ def test_gather_vs_atomic_and_oracle(kind, fill, smooth):
     else:  # two elements of different phases: the general path
         fv = np.where(np.arange(n) % 3 == 0, 14.0 + 0.3j, 6.0 + 0.01j)
     s = [(xyz, fv, None)]
-    ga = run(s, fill, smooth, repeat=3, sums=True)
+    ga = run(s, fill, smooth, repeat=3, sums=True, binning="gather")
     at = run(s, fill, smooth, binning="atomic", sums=True)
+    auto = run(s, fill, smooth)  # a sum grid in L2: atomic
     assert ga["info"]["gather"] == 1 and at["info"]["gather"] == 0
+    assert auto["info"]["gather"] == 0
     assert ga["info"]["real"] == (kind == "real")
     ref = O.voxelgrid([(xyz, fv)], *GEOM, PHIS, fill, smooth)
     assert np.array_equal(ga["counts"], ref["count"])
@@ -101,7 +103,7 @@ def test_gather_structures(average):
     s = [(a, np.full(len(a), 6.0 + 0j), None),
          (b, np.full(len(b), 14.1 + 0.4j), None),
          (c, np.full(len(c), 5.9 - 0.1j), None)]
-    ga = run(s, True, 1.0, average=average, graph=True, repeat=2)
+    ga = run(s, True, 1.0, average=average, graph=True, repeat=2, binning="gather")
     at = run(s, True, 1.0, average=average, binning="atomic")
     assert ga["info"]["gather"] == 1
     assert np.array_equal(ga["counts"], at["counts"])
@@ -121,7 +123,7 @@ def test_shells_bin_atomically_on_a_gather_plan():
     f_sh = np.stack([fv * (1.0 - 0.1 * k) for k in range(3)])
     avg = np.array([[0.02 + 0j], [0.019 + 0j], [0.018 + 0j]])
     outs = {}
-    for binning in ("auto", "atomic"):
+    for binning in ("gather", "atomic"):
         plan = F.VoxelPlan(geom, [(xyz, fv, None)], phis=PHIS, fill_bkg=True,
                            smooth=1, real=False, binning=binning)
         plan.set_atoms()
@@ -133,9 +135,9 @@ def test_shells_bin_atomically_on_a_gather_plan():
         plan.execute()                 # shells cleared: gathers again
         outs[binning + "-plain"] = plan.iq().copy()
         plan.close()
-    assert outs["auto"][1] == 1 and outs["atomic"][1] == 0
-    assert rel_l2(outs["auto"][0], outs["atomic"][0]) <= 1e-12
-    assert rel_l2(outs["auto-plain"], outs["atomic-plain"]) <= 1e-6
+    assert outs["gather"][1] == 1 and outs["atomic"][1] == 0
+    assert rel_l2(outs["gather"][0], outs["atomic"][0]) <= 1e-12
+    assert rel_l2(outs["gather-plain"], outs["atomic-plain"]) <= 1e-6
 
 
 def test_plans_gather_refuses(monkeypatch):
@@ -146,15 +148,12 @@ def test_plans_gather_refuses(monkeypatch):
         with pytest.raises(N.GwError) as e:
             F.VoxelPlan(geom, [(xyz, fv, None)], phis=PHIS, binning="gather", **kw)
         assert e.value.status == N.GW_ERR_ARG
-        # auto: the atomic binning
+        # auto: the atomic binning (and for so small a grid anyway)
         p = F.VoxelPlan(geom, [(xyz, fv, None)], phis=PHIS, **kw)
         assert p.info()["gather"] == 0
         p.close()
     # a pixel store over the budget
     monkeypatch.setenv("GW_GATHER_MAX_MB", "0")
-    p = F.VoxelPlan(geom, [(xyz, fv, None)], phis=PHIS)
-    assert p.info()["gather"] == 0
-    p.close()
     with pytest.raises(N.GwError):
         F.VoxelPlan(geom, [(xyz, fv, None)], phis=PHIS, binning="gather")
     monkeypatch.delenv("GW_GATHER_MAX_MB")

@@ -257,7 +257,8 @@ def test_autotuned_plan_vs_oracle(tmp_path, monkeypatch):
     got = gpu_run(geom, [(xyz, fv, None)], phis, False, 1.5, tune=True)
     plan = got["plan"]
     assert set(plan.tuned) == {"fft_y", "fft_z", "batch_slices", "transform",
-                               "block_variant"}
+                               "block_variant", "binning"}
+    assert got["info"]["gather"] == (plan.tuned["binning"] == "gather")
     assert (got["info"]["My"], got["info"]["Mz"]) == (plan.tuned["fft_y"],
                                                       plan.tuned["fft_z"])
     # the families the plan runs: fused where asked for, else Stockham
