@@ -153,6 +153,7 @@ constexpr int kOrientFloats = sizeof(OrientFast) / 4;
 
 constexpr int kDetThreads = 256, kDetPix = 2, kDetChunk = 128, kDetFlush = 16;
 static_assert(kDetChunk % kDetFlush == 0, "orientation chunks hold whole flush groups");
+static_assert(kDetFlush * 2 <= 32, "a flush group's uncertain samples fit one 32-bit mask");
 
 __device__ __forceinline__ bool fast_axis(float t, float d, int n, int &k) {
   // k = clamp(floor(t + d), 0, n-1) (clamping first is the same: NaN and
@@ -339,7 +340,6 @@ k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
   __shared__ PlaneOrient s_ot[kDetChunk];
   constexpr int KP = kPlTH * kPlTW / kPlThreads;  // pixels per thread
   const float nu1 = (float)(pa.nu - 1), nv1 = (float)(pa.nv - 1);
-  const int lane = threadIdx.x & 31;
   const int tiles_x = (a.nh + kPlTW - 1) / kPlTW;
   const int j = (blockIdx.x % tiles_x) * kPlTW + (threadIdx.x % kPlTW);
   const int ib = (blockIdx.x / tiles_x) * kPlTH + threadIdx.x / kPlTW;
@@ -375,36 +375,45 @@ k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
     // two per loop trip, flushed to float64 after each full group
     for (int g0 = 0; g0 < nc; g0 += kDetFlush) {
       const int ge = min(g0 + kDetFlush, nc);
+      // bit (oo - g0) KP + k: a sample whose index is not certain in
+      // float32, replayed in float64 after the group
+      unsigned need_bits = 0;
 #pragma unroll 2
       for (int oo = g0; oo < ge; ++oo) {
         const PlaneOrient T = s_ot[oo];
-        const int o = c0 + oo;
 #pragma unroll
         for (int k = 0; k < KP; ++k) {
           int iu, iv;
           const bool ok = plane_index<ZX>(T, nu1, nv1, xf[k], yf[k], zf[k], iu, iv);
-          const bool need = valid[k] && !ok;
-          const unsigned m = __ballot_sync(0xffffffffu, need);
-          bool inline_exact = false;
-          if (m) {
-            int base = 0;
-            const int leader = __ffs(m) - 1;
-            if (lane == leader) base = atomicAdd(wl_count, __popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (need) {
-              const int slot = base + __popc(m & ((1u << lane) - 1u));
-              if (slot < wl_cap) wl[slot] = make_int2(pix[k], o);
-              else inline_exact = true;
-            }
-          }
-          float v = 0.f;
-          if (valid[k] && ok) v = SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv);
-          if (inline_exact) {
+          if (valid[k] && ok)
+            part[k] = fmaf(SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv), T.e.z,
+                           part[k]);
+          need_bits |= (unsigned)(valid[k] && !ok) << ((oo - g0) * KP + k);
+        }
+      }
+      // the group's uncertain samples go to the worklist (replayed exactly
+      // by k_detector_fix), or, once it is full, are replayed here into the
+      // float64 accumulator
+      if (__any_sync(0xffffffffu, need_bits != 0)) {
+        while (need_bits) {
+          const int b = __ffs(need_bits) - 1;
+          need_bits &= need_bits - 1;
+          const int k = b % KP, o = c0 + g0 + b / KP;
+          int px = pix[0];
+#pragma unroll
+          for (int q = 1; q < KP; ++q)
+            if (k == q) px = pix[q];
+          const int slot = atomicAdd(wl_count, 1);
+          if (slot < wl_cap) {
+            wl[slot] = make_int2(px, o);
+          } else {
             double x, y, z;
-            base_point(a, pix[k] / a.nh, pix[k] % a.nh, x, y, z);
-            v = __ldg(a.iq + gather_index(a, o, x, y, z));
+            base_point(a, px / a.nh, px % a.nh, x, y, z);
+            const double sv = (double)__ldg(a.iq + gather_index(a, o, x, y, z)) * a.w[o];
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+              if (k == q) acc[q] += sv;
           }
-          if (valid[k] && (ok || inline_exact)) part[k] = fmaf(v, T.e.z, part[k]);
         }
       }
       if (ge - g0 == kDetFlush) {
