@@ -535,9 +535,10 @@ size_t finalize_smem(int Qc, bool use_f0) {
 // Pixels are float32 and the running sum is compensated (Kahan) float32:
 // the exact sum to about one float32 ulp, the same bits on every run.
 // Voxels with further output rows (C1 > 1) are summed again over all rows
-// by k_gather_multi.  Lines with up to kGatherHeavy entries take one warp
-// each (grid-stride); the heavier lines (near the rotation axis every phi
-// meets) are listed in `heavy` and take one block each, its warps
+// by k_gather_multi.  Lines with up to kGatherHeavy pixels per voxel
+// (entries times structures) take one warp each (grid-stride); the heavier
+// lines (near the rotation axis every phi meets) are listed in `heavy` and
+// take one block each, its warps
 // splitting the entries in eight fixed parts whose partial sums are added
 // in warp order.  Three blocks per SM: 79 registers without spills, the
 // loads of 24 warps in flight.
@@ -713,7 +714,7 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     const int wl = (iy + off) * W + ix + off;
     const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
     const int e0 = lptr[wl], e1 = lptr[wl + 1];
-    if (n_heavy > 0 && e1 - e0 > kGatherHeavy) continue;  // a heavy block's
+    if (n_heavy > 0 && (e1 - e0) * (t1 - t0) > kGatherHeavy) continue;  // a heavy block's
     if (e0 == e1) {
       for (int iz = lane; iz < Qc; iz += 32) {
         if (MODE == 0) out32[obase + iz] = 0.f;
@@ -1723,10 +1724,12 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
         if (zptr[z + 1] - zptr[z] > 1) zmulti.push_back(z);
       P->n_zmulti = (int)zmulti.size();
       if (zmulti.empty()) zmulti.push_back(0);
-      // lines with more than kGatherHeavy entries (near the rotation axis)
+      // lines with more than kGatherHeavy pixels per voxel (entries times
+      // the structures each output sums; near the rotation axis)
+      const int per_entry = p->average == GW_STRUCTS_SEPARATE ? 1 : n_struct;
       std::vector<int> heavy;
       for (int l = 0; l < W * W; ++l)
-        if (lptr[l + 1] - lptr[l] > kGatherHeavy) heavy.push_back(l);
+        if ((int64_t)(lptr[l + 1] - lptr[l]) * per_entry > kGatherHeavy) heavy.push_back(l);
       P->n_heavy = (int)heavy.size();
       if (heavy.empty()) heavy.push_back(0);
       if ((st = upload(&P->d_heavy, heavy, &B)) || (st = upload(&P->d_zmulti, zmulti, &B)) ||
