@@ -285,8 +285,7 @@ class VoxelPlan:
                                  smooth=smooth, mode=mode, accum=accum,
                                  average=average, f0_element=f0_element,
                                  constants=constants, deposit=deposit,
-                                 real=real, binning=binning, ctx=self.ctx,
-                                 **choice)
+                                 real=real, ctx=self.ctx, **choice)
 
             self.tuned = autotune.tune(make, len(structures), fill_bkg, smooth,
                                        deposit, ctx=self.ctx)
