@@ -385,6 +385,22 @@ __global__ void k_profile(SliceArgs a, int slice0) {
         dev_error(a.err, GW_DEVERR_MASK_WRAP);
     }
   }
+  if (a.pr) {
+    // real grids: the row kernel's per-column table (d_value_row_real);
+    // this thread's own amo and my entries, written above
+    const float2 u = unit_phase(s);
+    const float nan = __int_as_float(0x7fc00000);
+    for (int yy = i0; yy < a.Ly; yy += di) {
+      const size_t o = (size_t)blockIdx.x * a.Ly + yy;
+      float x = 0.f;
+      if (a.fill) {
+        int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
+        const float2 am = a.amo[o];
+        x = (yi > e.x && yi < e.y) ? am.x * u.x + am.y * u.y : nan;
+      }
+      a.pr[o] = make_float2(x, a.smooth_on ? a.my[o] : 1.f);
+    }
+  }
 }
 
 // ---------------------------------------------------------- geometry tables
@@ -1050,7 +1066,7 @@ SliceArgs slice_args(gw_voxel_plan *P) {
   a.roff = P->d_roff;
   a.zstat = P->d_zstat; a.ymax_ord = P->d_ymax; a.extflag = P->d_extflag;
   a.ph = P->d_phis; a.clbase = P->d_clbase; a.ymin_ord = P->d_ymin;
-  a.ext = P->d_ext; a.amo = P->d_amo; a.my = P->d_my;
+  a.ext = P->d_ext; a.amo = P->d_amo; a.my = P->d_my; a.pr = P->d_pr;
   a.mz = P->d_mz; a.gw = P->d_gw; a.sconst = P->d_sconst; a.err = P->ctx->d_err;
   return a;
 }
@@ -1105,6 +1121,7 @@ int enqueue_prep(gw_voxel_plan *P) {
 SliceArgs profile_view(const SliceArgs &a, int s0) {
   SliceArgs v = a;
   v.amo = a.amo + (size_t)s0 * a.Ly;
+  if (a.pr) v.pr = a.pr + (size_t)s0 * a.Ly;
   v.my = a.my + (size_t)s0 * a.Ly;
   v.mz = a.mz + (size_t)s0 * a.Lz;
   return v;
@@ -1629,6 +1646,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       (st = alloc(&P->d_zstat, n_struct, &B)) ||
       (st = alloc(&P->d_F1, (size_t)P->S * P->Lz * P->Nf, &B)) ||
       (st = alloc(&P->d_amo, (size_t)P->n_slices * P->Ly, &B)) ||
+      (P->real && (st = alloc(&P->d_pr, (size_t)P->n_slices * P->Ly, &B))) ||
       (st = alloc(&P->d_my, (size_t)P->n_slices * P->Ly, &B)) ||
       (st = alloc(&P->d_mz, (size_t)P->n_slices * P->Lz, &B)) ||
       (st = upload(&P->d_roff, P->roff_host, &B)) ||
@@ -1762,7 +1780,7 @@ extern "C" int gw_voxel_plan_destroy(gw_voxel_plan *P) {
                   P->d_cursor, P->d_zstat, P->d_ymax, P->d_extflag,
                   P->d_shell, P->d_f_shells, P->d_structs_shells, P->d_zf0,
                   P->d_fty, P->d_ftz, P->d_G, P->d_lptr, P->d_lent, P->d_zptr,
-                  P->d_zrows, P->d_heavy, P->d_zmulti};
+                  P->d_zrows, P->d_heavy, P->d_zmulti, P->d_pr};
   for (void *q : ptrs) gw::dev_free(q);
   delete P;
   return GW_OK;

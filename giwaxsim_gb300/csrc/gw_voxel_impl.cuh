@@ -51,6 +51,10 @@ struct SliceArgs {
   int4 *ext;  // y_min, y_max, z_min, z_max (valid atoms)
   float2 *amo;
   float *my, *mz;
+  // real grids: per slot and window column, (the fill value projected on
+  // the structure's phase, NaN outside the slice's y extent; the y
+  // smoothing factor, 1 without smoothing), made by k_profile
+  float2 *pr;
   const float *gw;  // gaussian weights, 2*radius+1
   float4 *sconst;   // per slice: (Cbg.re, Cbg.im, Cd.re, Cd.im)
   int *err;
@@ -229,6 +233,14 @@ struct RowConst {
                    // grids: the row is u times a real row)
 };
 
+// Unit phase of a structure's average voxel f (real grids: its slice grids
+// are this phase times real grids).
+__device__ __forceinline__ float2 unit_phase(const gw_structure &st) {
+  const double mag = sqrt(st.avg_f_re * st.avg_f_re + st.avg_f_im * st.avg_f_im);
+  return mag > 0.0 ? make_float2((float)(st.avg_f_re / mag), (float)(st.avg_f_im / mag))
+                   : make_float2(1.f, 0.f);
+}
+
 __device__ __forceinline__ RowConst row_const(const SliceArgs &a, int slot,
                                               int sl, int zz) {
   RowConst k;
@@ -240,10 +252,7 @@ __device__ __forceinline__ RowConst row_const(const SliceArgs &a, int slot,
   const int zi = window_row_to_z(a, zz);
   k.zin = zi >= k.e.z && zi < k.e.w;
   k.slot = slot;
-  const gw_structure &st = a.st[sl / a.n_phi];
-  const double mag = sqrt(st.avg_f_re * st.avg_f_re + st.avg_f_im * st.avg_f_im);
-  k.u = mag > 0.0 ? make_float2((float)(st.avg_f_re / mag), (float)(st.avg_f_im / mag))
-                  : make_float2(1.f, 0.f);
+  k.u = unit_phase(a.st[sl / a.n_phi]);
   return k;
 }
 
@@ -255,11 +264,12 @@ __device__ __forceinline__ RowConst row_const(const SliceArgs &a, int slot,
 struct RowValueArgs {
   const float2 *amo;
   const float *my;
+  const float2 *pr;
   int fill, smooth_on, y_lo, g, Ly;
 };
 
 __device__ __forceinline__ RowValueArgs row_value_args(const SliceArgs &a) {
-  return RowValueArgs{a.amo, a.my, a.fill, a.smooth_on, a.y_lo, a.g, a.Ly};
+  return RowValueArgs{a.amo, a.my, a.pr, a.fill, a.smooth_on, a.y_lo, a.g, a.Ly};
 }
 
 __device__ __forceinline__ float2 d_value_row(const RowValueArgs &a,
@@ -288,26 +298,21 @@ __device__ __forceinline__ float2 d_value_row(const SliceArgs &a,
 
 // Real grids: Re(d_value_row(a, k, yy, r u) conj(u)) for the real row sum
 // r.  The fill and smoothing values (amo, cd, cbg) are multiples of u, so
-// the projection is taken term by term, in float32 (|u| = 1).
+// the projection is taken term by term, in float32 (|u| = 1); the slot's
+// projected fill value, its y-extent test and the y smoothing factor come
+// as one 8-byte load of the k_profile table pr.
 __device__ __forceinline__ float d_value_row_real(const RowValueArgs &a,
                                                   const RowConst &k, int yy,
                                                   float r) {
   const float cdr = k.cd.x * k.u.x + k.cd.y * k.u.y;
+  // (k_profile runs, and makes the table, with fill or smoothing only)
+  const float2 t = (a.fill || a.smooth_on) ? a.pr[(size_t)k.slot * a.Ly + yy]
+                                           : make_float2(0.f, 1.f);
   float v;
-  if (a.fill) {
-    int yi = a.y_lo + yy; if (yi < 0) yi += a.g; if (yi >= a.g) yi -= a.g;
-    const bool inside = k.zin && yi > k.e.x && yi < k.e.y;
-    if (inside) {
-      const float2 am = a.amo[(size_t)k.slot * a.Ly + yy];
-      v = r + (am.x * k.u.x + am.y * k.u.y);
-    } else {
-      v = cdr;
-    }
-  } else {
-    v = r - (k.cbg.x * k.u.x + k.cbg.y * k.u.y);
-  }
+  if (a.fill) v = (k.zin && t.x == t.x) ? r + t.x : cdr;
+  else v = r - (k.cbg.x * k.u.x + k.cbg.y * k.u.y);
   if (a.smooth_on) {
-    const float m = k.mz * a.my[(size_t)k.slot * a.Ly + yy];
+    const float m = k.mz * t.y;
     v = v * m + cdr * (1.f - m);
   }
   return v;
@@ -626,6 +631,7 @@ struct gw_voxel_plan {
   // column * 2 + mirrored), each over every structure's slice of that phi;
   // window z takes the output rows d_zrows[d_zptr[z] .. d_zptr[z+1]) (a
   // mirrored entry reads row 2 r_zero - mr)
+  float2 *d_pr = nullptr;  // real grids: the row kernel's column table
   bool gather = false;
   float *d_G = nullptr;
   int *d_lptr = nullptr, *d_zptr = nullptr, *d_zrows = nullptr;
