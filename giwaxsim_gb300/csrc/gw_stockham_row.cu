@@ -133,18 +133,19 @@ k_row_czt_real(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   // synchronised afterwards
   fft_run<M, NB, NT, true, 0, true, 0, false, false, HALF>(buf, tw, cz.H, NoLoad(),
                                                           NoStore());
-  for (int i = threadIdx.x; i < NB * nf; i += NT) {
-    const int f = i / nf, j = i - f * nf;
-    const int m = m_zero + j, mm = m_zero - j;  // k and -k
-    float2 X = make_float2(0.f, 0.f), Xm = make_float2(0.f, 0.f);
-    if (m < cz.N) X = cmul(buf[f * LDM + fft_pad(m)], __ldg(cz.B + m));
-    if (mm >= 0) Xm = cmul(buf[f * LDM + fft_pad(mm)], __ldg(cz.B + mm));
-    // Y_A = (X + conj(Xm)) / 2, Y_B = -i (X - conj(Xm)) / 2
-    const float2 ya = make_float2(0.5f * (X.x + Xm.x), 0.5f * (X.y - Xm.y));
-    const float2 yb = make_float2(0.5f * (X.y + Xm.y), -0.5f * (X.x - Xm.x));
-    const int ra = row0 + 2 * f, rb = ra + 1;
-    if (ra < n_rows) F1[(size_t)ra * nf + j] = cmul(rs.k[2 * f].u, ya);
-    if (rb < n_rows) F1[(size_t)rb * nf + j] = cmul(rs.k[2 * f + 1].u, yb);
+  for (int f = 0; f < NB; ++f) {
+    for (int j = threadIdx.x; j < nf; j += NT) {
+      const int m = m_zero + j, mm = m_zero - j;  // k and -k
+      float2 X = make_float2(0.f, 0.f), Xm = make_float2(0.f, 0.f);
+      if (m < cz.N) X = cmul(buf[f * LDM + fft_pad(m)], __ldg(cz.B + m));
+      if (mm >= 0) Xm = cmul(buf[f * LDM + fft_pad(mm)], __ldg(cz.B + mm));
+      // Y_A = (X + conj(Xm)) / 2, Y_B = -i (X - conj(Xm)) / 2
+      const float2 ya = make_float2(0.5f * (X.x + Xm.x), 0.5f * (X.y - Xm.y));
+      const float2 yb = make_float2(0.5f * (X.y + Xm.y), -0.5f * (X.x - Xm.x));
+      const int ra = row0 + 2 * f, rb = ra + 1;
+      if (ra < n_rows) F1[(size_t)ra * nf + j] = cmul(rs.k[2 * f].u, ya);
+      if (rb < n_rows) F1[(size_t)rb * nf + j] = cmul(rs.k[2 * f + 1].u, yb);
+    }
   }
 }
 
