@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
@@ -215,6 +216,16 @@ namespace gw {
 // thread-local last error message
 void set_error(const std::string &msg);
 int fail(int status, const std::string &msg);
+
+// A named NVTX range over the host-side work of a stage (its launches, or
+// a graph replay), for timeline profilers; without one attached the push
+// and pop cost a few nanoseconds.
+struct Range {
+  explicit Range(const char *name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range &) = delete;
+  Range &operator=(const Range &) = delete;
+};
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 
 // fault injection for allocation failures: GW_FAIL_ALLOC_AFTER=<n> makes the

@@ -801,6 +801,7 @@ extern "C" int gw_detector_execute(gw_detector_plan *P) {
   if (!P) return gw::fail(GW_ERR_ARG, "gw_detector_execute: null plan");
   if (!P->iq) return gw::fail(GW_ERR_STATE, "gw_detector_execute: I(q) not set");
   GW_CUDA(cudaSetDevice(P->ctx->device));
+  gw::Range r("giwaxsim: detector image");
   const int npx = P->p.n_h * P->p.n_v;
   DetArgs a = det_args(P);
   if (P->p.exact) {

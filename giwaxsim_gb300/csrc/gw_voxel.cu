@@ -1321,7 +1321,10 @@ int enqueue(gw_voxel_plan *P) {
       bn.shell = P->shell_mode == GW_SHELLS_PER_SHELL ? P->d_shell : nullptr;
       bn.shell_k = k;
     }
-    GW_TRY(enqueue_prep(P));
+    {
+      gw::Range r("giwaxsim: voxel prep (z sort)");
+      GW_TRY(enqueue_prep(P));
+    }
     // Batched: the per-slice setup of every slice at once (fuller grids,
     // fewer launches); the profile arrays hold every slice and each batch
     // sees its part.  Plain mode keeps the reference's per-rotation order.
@@ -1333,10 +1336,17 @@ int enqueue(gw_voxel_plan *P) {
       const int n = std::min(P->S, P->n_slices - s0);
       const SliceArgs ab = profile_view(a, s0);
       if (P->plain) GW_TRY(enqueue_slice_setup(P, ab, s0, n));
-      GW_TRY(row_dispatch(P, ab, cy, s0, n));
-      GW_TRY(col_dispatch(P, ab, cz, bn, s0, n));
+      {
+        gw::Range r("giwaxsim: voxel rows (deposit + y chirp-z)");
+        GW_TRY(row_dispatch(P, ab, cy, s0, n));
+      }
+      {
+        gw::Range r("giwaxsim: voxel columns (z chirp-z + binning)");
+        GW_TRY(col_dispatch(P, ab, cz, bn, s0, n));
+      }
     }
   }
+  gw::Range r("giwaxsim: voxel finalize");
   return enqueue_finalize(P, false);
 }
 
@@ -1928,6 +1938,7 @@ extern "C" int gw_voxel_execute(gw_voxel_plan *P) {
   if (P->n_atoms < 0) return gw::fail(GW_ERR_STATE, "gw_voxel_execute: atoms not set");
   GW_TRY(shell_state(P, "gw_voxel_execute"));
   GW_CUDA(cudaSetDevice(P->ctx->device));
+  gw::Range r("giwaxsim: voxel execute");
   if (P->gexec) {
     GW_CUDA(cudaGraphLaunch(P->gexec, P->ctx->stream));
     P->ctx->launches += P->graph_kernels;

@@ -19,6 +19,7 @@ comparison branch (img_path) needs fabio and is not provided.
 """
 import argparse
 import glob
+import json
 import os
 import time
 
@@ -95,7 +96,16 @@ def main(config):
     accum = config.get("accum", "fp64")
     mode = config.get("mode", "batched")
     save_folder = config.get("save_folder", os.getcwd())
+    write_metrics = str_to_bool(config.get("metrics", "True"))
     os.makedirs(save_folder, exist_ok=True)
+    # wall time of every stage, written to save_folder/metrics.json (the
+    # device-side ranges of the same stages are NVTX ranges named
+    # "giwaxsim: ...", for timeline profilers)
+    metrics = {"stages": [], "device": None}
+    t_run = time.perf_counter()
+
+    def stage(name, t0, **info):
+        metrics["stages"].append(dict(name=name, seconds=time.perf_counter() - t0, **info))
     if img_path:
         raise NotImplementedError(
             "the experimental-image comparison (img_path) is not provided")
@@ -112,6 +122,7 @@ def main(config):
     slice_phis = phis_linspace(phi_slices) if phi_slices else None
 
     slabs = []
+    t0 = time.perf_counter()
     for path in input_paths:
         if path.lower().endswith(".xyz"):
             cell = (a, b, c, alpha, beta, gamma)
@@ -127,11 +138,16 @@ def main(config):
             raise Exception("at least one unit cell parameter a, b, c, alpha, "
                             "beta, gamma not defined")
         slabs.append(slabmaker_fitting(path, x_size, y_size, z_size, *cell))
+    stage("slabs", t0, atoms=[len(s[0]) for s in slabs])
 
     def detector_and_save(iq, qx, qy, qz, name):
+        t0 = time.perf_counter()
         det_sum, det_h, det_v = detectormaker_fitting(
             iq, qx, qy, qz, num_pixels, max_q, init_vals, init_axs, psis, psi_w,
             phis, phi_w, thetas, theta_w, mirror=mirror, accum=accum)
+        stage("detector", t0, input=name, pixels=int(num_pixels),
+              orientations=int(len(psis) * len(phis) * len(thetas)))
+        t0 = time.perf_counter()
         folder = f"{save_folder}/{name}"
         os.makedirs(folder, exist_ok=True)
         if mirror:
@@ -144,22 +160,39 @@ def main(config):
         np.save(f"{folder}/det_sum.npy", det_sum)
         _save_pngs(folder, det_sum, det_h, det_v)
         save_config_to_txt(config, f"{folder}/config.txt")
+        stage("save", t0, input=name)
         return det_sum, det_h, det_v
+
+    def finish(results):
+        if write_metrics:
+            from . import _native
+            try:
+                metrics["device"] = _native.default_context().device_name()
+            except Exception:  # no device: the metrics still record the host
+                pass
+            metrics["total_seconds"] = time.perf_counter() - t_run
+            with open(f"{save_folder}/metrics.json", "w") as fh:
+                json.dump(metrics, fh, indent=1)
+        return results
 
     results = {}
     if average_inputs and len(slabs) > 1:
+        t0 = time.perf_counter()
         iq, qx, qy, qz = voxelgridmaker_average(
             slabs, r_voxel_size, q_voxel_size, max_q, energy, fill_bkg=fill_bkg,
             smooth=smooth, phis=slice_phis, accum=accum)
+        stage("voxel", t0, input="average", structures=len(slabs))
         results["average"] = detector_and_save(iq, qx, qy, qz, "average")
-        return results
+        return finish(results)
     for (coords, elements), name in zip(slabs, gen_names):
+        t0 = time.perf_counter()
         iq, qx, qy, qz = voxelgridmaker_fitting(
             coords, elements, r_voxel_size, q_voxel_size, max_q, energy,
             fill_bkg=fill_bkg, smooth=smooth, phis=slice_phis, mode=mode,
             accum=accum)
+        stage("voxel", t0, input=name, atoms=len(coords), crop=int(iq.shape[0]))
         results[name] = detector_and_save(iq, qx, qy, qz, name)
-    return results
+    return finish(results)
 
 
 if __name__ == "__main__":

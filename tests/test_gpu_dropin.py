@@ -171,6 +171,14 @@ def test_cli_main(tmp_path):
     saved = np.load(tmp_path / "out" / "cell" / "det_sum.npy")
     assert np.array_equal(saved, det) and det.shape == (12, 12)
     assert (tmp_path / "out" / "cell" / "config.txt").exists()
+    # the run's stage times
+    import json
+    m = json.load(open(tmp_path / "out" / "metrics.json"))
+    names = [st["name"] for st in m["stages"]]
+    assert names == ["slabs", "voxel", "detector", "save"]
+    assert all(st["seconds"] >= 0 for st in m["stages"])
+    assert m["total_seconds"] >= sum(st["seconds"] for st in m["stages"]) * 0.99
+    assert "GB300" in m["device"] or m["device"]
     # same pipeline through the oracle
     slab, el = S.slabmaker_fitting(str(cell), 10, 9, 11, 2.46, 2.46, 6.70, 90,
                                    90, 120)
