@@ -178,7 +178,7 @@ def test_cli_main(tmp_path):
     assert names == ["slabs", "voxel", "detector", "save"]
     assert all(st["seconds"] >= 0 for st in m["stages"])
     assert m["total_seconds"] >= sum(st["seconds"] for st in m["stages"]) * 0.99
-    assert "GB300" in m["device"] or m["device"]
+    assert m["device"]  # the GPU the run used
     # same pipeline through the oracle
     slab, el = S.slabmaker_fitting(str(cell), 10, 9, 11, 2.46, 2.46, 6.70, 90,
                                    90, 120)
