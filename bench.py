@@ -32,11 +32,14 @@ L2_BYTES = 129 * 1024 * 1024
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per slice of the
 # two transform kernels, keyed by (workload, kernel, fft_y, fft_z, real
-# grids), from one ncu --set full capture of a 51-slice launch of that
-# kernel on the same workload and plan shape; a launch's traffic is this
-# times its slices (both kernels move per-slice data only).
+# grids), from one ncu --set full capture of a launch of that kernel on the
+# same workload and plan shape (complex grids and atomic binning: a 51-slice
+# launch; real grids and gather binning: a 102-slice launch); a launch's
+# traffic is this times its slices (both kernels move per-slice data only).
 NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024, 0): (1.48 + 38.03) * 1e6 / 51,
-               ("si-100A", "col_czt_bin", 1280, 1024, 0): (148.42 + 28.70) * 1e6 / 51}
+               ("si-100A", "col_czt_bin", 1280, 1024, 0): (148.42 + 28.70) * 1e6 / 51,
+               ("si-100A", "row_czt", 1280, 1024, 1): (1.76 + 39.42) * 1e6 / 102,
+               ("si-100A", "col_czt_bin", 1280, 1024, 1): (83.23 + 15.74) * 1e6 / 102}
 
 
 def parse():
@@ -384,8 +387,8 @@ def run_gb300(args, world, rank, local, pg):
         r = {"kernel": name, "bound": "hbm", "achieved": achieved,
              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
              "frac": achieved / peak, "traffic": traffic,
-             "traffic_source": "ncu capture of a 51-slice launch, scaled by "
-                               "slices per launch" if traffic else None,
+             "traffic_source": "ncu capture of one launch, scaled by slices "
+                               "per launch" if traffic else None,
              "avg_launch_ms": avg_ms, "launches": nl,
              "slices_per_launch": spl, "algorithmic_bytes_per_launch": algo}
         if name in ("row_czt", "col_czt_bin"):
