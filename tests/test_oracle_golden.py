@@ -186,3 +186,17 @@ def test_shift_peak_maps_vs_reference(name):
     out = apply(m["q_idx"], m["q_w"], z.ravel()).reshape(img.shape)
     ref = d[name + "_out"]
     assert np.abs(out - ref).max() <= 1e-14 * np.abs(ref).max()
+
+
+def test_threaded_crop_oracle_equals_serial():
+    """The threaded, crop-only oracle the bench and the full-size GPU test
+    use gives the serial oracle's counts exactly and its sums to rounding."""
+    from giwaxsim_gb300 import workloads as W
+    rng = np.random.default_rng(3)
+    xyz, _ = W.graphite_slab((12.0, 11.0, 13.0), rng, disp_sigma=0.05)
+    fv = np.full(len(xyz), 6.0 + 0j)
+    phis = np.linspace(0, 180, 20, endpoint=False)
+    a = O.voxelgrid([(xyz, fv)], 0.5, 0.15, 1.5, phis, True, 1.5)
+    b = O.voxelgrid_crop_threaded(xyz, fv, 0.5, 0.15, 1.5, phis, True, 1.5, workers=4)
+    assert np.array_equal(a["count"], b["count"])
+    assert np.abs(a["iq"] - b["iq"]).max() <= 1e-12 * np.abs(a["iq"]).max()
