@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(256, 3)
 k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
          const int2 *__restrict__ lent, const int *__restrict__ zptr,
          const int *__restrict__ zrows, const int *__restrict__ heavy, int n_heavy,
-         int friedel, int nf, int nr, int r_zero, int n_phi, int t0, int t1,
+         int nf, int nr, int r_zero, int n_phi, int t0, int t1,
          const unsigned int *__restrict__ C2, const int *__restrict__ C1, int W,
          int off, int Qc, float inv_nstruct, const float *__restrict__ f0tab,
          const float4 *__restrict__ zf0, int use_f0, float f0_c, float f0_invz,
@@ -709,13 +709,6 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     float r2, fxy[4];
     line_consts(iy, ix, wl, r2, fxy);
     const size_t obase = MODE == 2 ? (size_t)wl * W : ((size_t)iy * Qc + ix) * Qc;
-    // the point mirror of the line (friedel: summed here as well)
-    const int my = Qc - 1 - iy, mx = Qc - 1 - ix;
-    const int wm = (my + off) * W + mx + off;
-    const bool twin = friedel && wm != wl;
-    float r2m = 0.f, fxym[4] = {0.f, 0.f, 0.f, 0.f};
-    if (twin) line_consts(my, mx, wm, r2m, fxym);
-    const size_t obm = MODE == 2 ? (size_t)wm * W : ((size_t)my * Qc + mx) * Qc;
     for (int iz = threadIdx.x; iz < Qc; iz += blockDim.x) {
       float hi = 0.f, lo = 0.f;
       for (int w = 0; w < nw; ++w) {
@@ -725,9 +718,6 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
       }
       gather_store<MODE>(hi, lo, iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c, f0_invz,
                          out64, out32);
-      if (twin)
-        gather_store<MODE>(hi, lo, Qc - 1 - iz, obm, r2m, s_rc1, s_zf0, fxym, use_f0, f0_c,
-                           f0_invz, out64, out32);
     }
     return;
   }
@@ -736,34 +726,20 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
   const int wpb = blockDim.x >> 5;
   const int stride = (gridDim.x - n_heavy) * wpb;
   for (int line = (blockIdx.x - n_heavy) * wpb + warp; line < n_lines; line += stride) {
-    // friedel: the point mirror line (Qc-1-iy, Qc-1-ix) holds the same
-    // pixels mirrored; the lower line of each pair sums both
-    const int mline = n_lines - 1 - line;
-    if (friedel && mline < line) continue;
-    const bool twin = friedel && mline != line;
     const int iy = line / Qc, ix = line - iy * Qc;
     const int wl = (iy + off) * W + ix + off;
     const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
-    const int my = Qc - 1 - iy, mx = Qc - 1 - ix;
-    const int wm = (my + off) * W + mx + off;
-    const size_t obm = MODE == 2 ? (size_t)wm * W : (size_t)mline * Qc;
     const int e0 = lptr[wl], e1 = lptr[wl + 1];
     if (n_heavy > 0 && (e1 - e0) * (t1 - t0) > kGatherHeavy) continue;  // a heavy block's
     if (e0 == e1) {
       for (int iz = lane; iz < Qc; iz += 32) {
         if (MODE == 0) out32[obase + iz] = 0.f;
         else out64[obase + iz] = 0.0;
-        if (twin) {
-          if (MODE == 0) out32[obm + iz] = 0.f;
-          else out64[obm + iz] = 0.0;
-        }
       }
       continue;
     }
     float r2, fxy[4];
     line_consts(iy, ix, wl, r2, fxy);
-    float r2m = 0.f, fxym[4] = {0.f, 0.f, 0.f, 0.f};
-    if (twin) line_consts(my, mx, wm, r2m, fxym);
     for (int z0 = 0; z0 < Qc; z0 += 32 * kGatherU) {
       float hi[kGatherU], lo[kGatherU];
 #pragma unroll
@@ -773,13 +749,9 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
 #pragma unroll
       for (int u = 0; u < kGatherU; ++u) {
         const int iz = z0 + lane + 32 * u;
-        if (iz < Qc) {
+        if (iz < Qc)
           gather_store<MODE>(hi[u], lo[u], iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c,
                              f0_invz, out64, out32);
-          if (twin)
-            gather_store<MODE>(hi[u], lo[u], Qc - 1 - iz, obm, r2m, s_rc1, s_zf0, fxym,
-                               use_f0, f0_c, f0_invz, out64, out32);
-        }
       }
     }
   }
@@ -1234,8 +1206,8 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
               : mode == 2 ? P->d_sum + t * P->sum_stride : nullptr;
   gw::KTimer tm(ctx, GW_K_FINALIZE);
 #define GW_GATHER_ARGS                                                             \
-  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->d_heavy, n_heavy,         \
-      P->friedel ? 1 : 0, P->Nf, P->Nr, P->r_zero,                                   \
+  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->d_heavy, n_heavy, P->Nf, \
+      P->Nr, P->r_zero,                                                              \
       P->n_phi, t0, t1, P->d_C2, P->d_C1, P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, \
       use_f0, f0c, f0iz, o64, o32
   if (mode == 0) k_gather<0><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
@@ -1774,30 +1746,6 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       std::vector<int> zfill(zptr.begin(), zptr.end() - 1);
       for (int mr = 0; mr < P->Nr; ++mr)
         if (rowofs[mr] >= 0) zrows[zfill[rowofs[mr]]++] = mr;
-      // Friedel symmetry of real grids: a voxel line's pixels are those of
-      // its point mirror (-qy, -qx), mirrored in qz, when the column and
-      // row tables map every band column and row's mirror onto the mirror
-      // line and z -- checked exactly here (a pixel on an exact bin edge
-      // would break it); the gather then sums each mirror pair of lines
-      // once.  It needs the crop centred in the window.
-      bool fr = P->real && W - 1 - 2 * (P->lo - P->wlo) == P->Qc - 1;
-      for (int mr = 0; fr && mr < P->Nr; ++mr) {
-        const int ra = rowofs[mr], rb = rowofs[2 * P->r_zero - mr];
-        fr = (ra < 0 && rb < 0) || (ra >= 0 && rb == W - 1 - ra);
-      }
-      for (int q = 0; fr && q < n_phi; ++q)
-        for (int m = 0; fr && m < P->Nc; ++m) {
-          const int c = cof[(size_t)q * P->Nc + m];
-          const int mm = 2 * P->m_zero - m;
-          const int cm = (mm >= 0 && mm < P->Nc) ? cof[(size_t)q * P->Nc + mm] : -1;
-          if (c < 0 || cm < 0) {
-            fr = (c < 0) == (cm < 0);
-          } else {
-            const int l = c / W, wy = l / W, wx = l - wy * W;
-            fr = cm / W == (W - 1 - wy) * W + (W - 1 - wx);
-          }
-        }
-      P->friedel = fr;
       // window z with more than one output row
       std::vector<int> zmulti;
       for (int z = 0; z < W; ++z)
@@ -1809,9 +1757,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       const int per_entry = p->average == GW_STRUCTS_SEPARATE ? 1 : n_struct;
       std::vector<int> heavy;
       for (int l = 0; l < W * W; ++l)
-        if ((int64_t)(lptr[l + 1] - lptr[l]) * per_entry > kGatherHeavy &&
-            !(P->friedel && W * W - 1 - l < l))  // the pair's lower line sums both
-          heavy.push_back(l);
+        if ((int64_t)(lptr[l + 1] - lptr[l]) * per_entry > kGatherHeavy) heavy.push_back(l);
       P->n_heavy = (int)heavy.size();
       if (heavy.empty()) heavy.push_back(0);
       if ((st = upload(&P->d_heavy, heavy, &B)) || (st = upload(&P->d_zmulti, zmulti, &B)) ||
@@ -2137,8 +2083,7 @@ extern "C" int gw_voxel_info(gw_voxel_plan *P, int64_t *info, int32_t n) {
                        P->y_lo, P->z_lo, P->k0, P->kz0, P->n_slices,
                        (int64_t)P->bytes, P->graph_kernels,
                        (int64_t)P->f1_tma, (int64_t)P->fused_y,
-                       (int64_t)P->fused_z, (int64_t)P->real, (int64_t)P->gather,
-                       (int64_t)P->friedel};
+                       (int64_t)P->fused_z, (int64_t)P->real, (int64_t)P->gather};
   const int k = std::min<int>(n, (int)(sizeof v / sizeof v[0]));
   for (int i = 0; i < k; ++i) info[i] = v[i];
   return k;

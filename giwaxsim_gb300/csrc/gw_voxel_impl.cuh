@@ -636,9 +636,6 @@ struct gw_voxel_plan {
   float *d_G = nullptr;
   int *d_lptr = nullptr, *d_zptr = nullptr, *d_zrows = nullptr;
   int2 *d_lent = nullptr;
-  // the line and z tables are point-symmetric (real grids): each mirror
-  // pair of lines is summed once
-  bool friedel = false;
   // window lines with many entries (each takes a whole block)
   int *d_heavy = nullptr;
   int n_heavy = 0;

@@ -71,8 +71,6 @@ def test_gather_vs_atomic_and_oracle(kind, fill, smooth):
     auto = run(s, fill, smooth)  # a sum grid in L2: atomic
     assert ga["info"]["gather"] == 1 and at["info"]["gather"] == 0
     assert auto["info"]["gather"] == 0
-    # real grids: the point-mirror line pairs are summed once
-    assert ga["info"]["friedel"] == (kind == "real")
     assert ga["info"]["real"] == (kind == "real")
     ref = O.voxelgrid([(xyz, fv)], *GEOM, PHIS, fill, smooth)
     assert np.array_equal(ga["counts"], ref["count"])
