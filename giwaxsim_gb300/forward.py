@@ -152,13 +152,15 @@ def real_multiples(fv):
     f = np.asarray(fv, dtype=complex).ravel()
     if f.size == 0:
         return False
+    if (f == f[0]).all():  # one value (one element, no weights): one pass
+        return bool(f[0] != 0)
     ref = f[np.argmax(np.abs(f))]
     if ref == 0:
         return False
     cross = f.imag * ref.real - f.real * ref.imag  # Im(f conj(ref))
     if np.max(np.abs(cross)) > 1e-6 * abs(ref) * np.max(np.abs(f)):
         return False
-    return abs(np.sum(f)) > 1e-3 * np.sum(np.abs(f))
+    return bool(abs(np.sum(f)) > 1e-3 * np.sum(np.abs(f)))
 
 
 def coord_ranges(coords):
