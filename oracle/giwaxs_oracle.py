@@ -405,15 +405,17 @@ def voxelgrid(structures, r_voxel_size, q_voxel_size, max_q, phis=None,
 
 
 def _crop_chunk(payload):
-    (coords, fv, phis, g, r, fill, smooth, q, consts, lo, Qc) = payload
+    (coords, fv, phis, g, r, fill, smooth, q, consts, lo, Qc, vsum, vcnt,
+     lock) = payload
     xb, yb, zb, avg = consts
-    out = []
     for phi in phis:
         grid, _ = project_slice(coords, fv, phi, g, r, avg, xb, yb, zb, fill,
                                 smooth)
         hx, hy, vz = slice_axes(g, r, phi)
-        out.append(crop_pairs(slice_intensity(grid), hx, hy, vz, q, lo, Qc))
-    return out
+        i, v = crop_pairs(slice_intensity(grid), hx, hy, vz, q, lo, Qc)
+        with lock:  # process_file2's np.add.at, one slice at a time
+            np.add.at(vsum, i, v)
+            np.add.at(vcnt, i, 1.0)
 
 
 def voxelgrid_crop_threaded(coords, f_values, r_voxel_size, q_voxel_size,
@@ -421,12 +423,10 @@ def voxelgrid_crop_threaded(coords, f_values, r_voxel_size, q_voxel_size,
     """voxelgrid() for one structure, with the slices spread over `workers`
     threads as the reference's driver does (comparison.py:759-763) and only
     the cropped cube accumulated (downselect_voxelgrid keeps nothing else).
-    Threads return each slice's (crop index, intensity) pairs and one
-    bincount over all of them makes the sums and counts (process_file2's
-    np.add.at, voxelgrids.py:502-503, without the reference's unguarded
-    concurrent updates, which lose some).  Sums are added in another order
-    than the serial voxelgrid() (differences at the float64 rounding
-    level); counts are identical.
+    Threads add their slices into one shared pair of grids under a lock:
+    the reference's unguarded np.add.at from threads loses updates.  Sums
+    are added in another order than the serial voxelgrid() (differences at
+    the float64 rounding level); counts are identical.
     Returns dict(iq, count, q) over the crop."""
     from concurrent.futures import ThreadPoolExecutor
     grid_size, q, _ = voxel_geometry(r_voxel_size, q_voxel_size, max_q, coords)
@@ -434,16 +434,14 @@ def voxelgrid_crop_threaded(coords, f_values, r_voxel_size, q_voxel_size,
     phis = np.asarray(phis)
     chunks = [c for c in (phis[i::workers] for i in range(workers)) if len(c)]
     consts = structure_constants(coords, f_values, r_voxel_size)
+    vsum = np.zeros(Qc ** 3)
+    vcnt = np.zeros(Qc ** 3)
+    lock = threading.Lock()
     _lib()  # build/load the helper before the threads use it
     with ThreadPoolExecutor(max_workers=workers) as ex:
-        parts = [pv for res in ex.map(_crop_chunk, [
+        list(ex.map(_crop_chunk, [
             (coords, f_values, c, grid_size, r_voxel_size, fill_bkg, smooth,
-             q, consts, lo, Qc) for c in chunks]) for pv in res]
-    idx = np.concatenate([p[0] for p in parts])
-    val = np.concatenate([p[1] for p in parts])
-    del parts
-    vsum = np.bincount(idx, weights=val, minlength=Qc ** 3)
-    vcnt = np.bincount(idx, minlength=Qc ** 3).astype(np.float64)
+             q, consts, lo, Qc, vsum, vcnt, lock) for c in chunks]))
     iq = np.divide(vsum, vcnt, out=np.zeros_like(vsum), where=vcnt != 0)
     qc = q[lo:lo + Qc]
     iq = add_f0_q_3d(iq.reshape(Qc, Qc, Qc), qc, qc, qc, "C")
