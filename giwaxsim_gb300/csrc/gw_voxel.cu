@@ -542,8 +542,8 @@ size_t finalize_smem(int Qc, bool use_f0) {
 }
 
 // Gather binning: the sums of one voxel line in a fixed order, then the
-// finalize of k_finalize.  A warp runs along qz in spans of 32 kGatherU
-// voxels (qz = z0 + lane + 32 u).  A line's entries (phi, F1 column,
+// finalize of k_finalize.  A warp runs along qz in spans of 32 U voxels
+// (qz = z0 + lane + 32 u).  A line's entries (phi, F1 column,
 // mirrored) are taken in table order (phi, then band column), kGatherP at
 // a time with the pixel loads of all their voxels issued together, each
 // over the structures t0 .. t1-1 (the slice t n_phi + phi); the pixel of
@@ -556,8 +556,8 @@ size_t finalize_smem(int Qc, bool use_f0) {
 // lines (near the rotation axis every phi meets) are listed in `heavy` and
 // take one block each, its warps
 // splitting the entries in eight fixed parts whose partial sums are added
-// in warp order.  Three blocks per SM: 79 registers without spills, the
-// loads of 24 warps in flight.
+// in warp order.  Three blocks per SM (measured faster than two without
+// the few spilled registers of U = 13).
 // MODE 0: the float32 I(q) (crop, factor, f0 as k_finalize); 1: the float64
 // I(q) from the same sums; 2: the float64 sums into the window grid (crop
 // = window, off = 0; no factor).
@@ -570,22 +570,24 @@ __device__ __forceinline__ void kahan_step(float &hi, float &lo, float x) {
   hi = s;
 }
 
-// A warp's pass over a span of up to 32 kGatherU voxels of a line (qz =
-// z0 + lane + 32 u): kGatherP entries at a time, the pixel loads of all
-// their voxels issued together, then added (compensated) in entry order.
-constexpr int kGatherU = 8;
-constexpr int kGatherP = 2;
+// A warp's pass over a span of up to 32 U voxels of a line (qz = z0 +
+// lane + 32 u): kGatherP entries at a time, the pixel loads of all their
+// voxels issued together, then added (compensated) in entry order.  U is
+// picked per launch so that a span covers a whole line (U = 13: lines of up
+// to 416 voxels; U = 7: up to 224).
+constexpr int kGatherP = 1;
 
+template <int U>
 __device__ __forceinline__ void gather_span(const float *__restrict__ G,
                                             const int2 *__restrict__ lent, int e0,
                                             int e1, int t0, int t1, int n_phi, int nf,
                                             int nr, int r_zero, const int *s_row, int z0,
-                                            int lane, int Qc, float (&hi)[kGatherU],
-                                            float (&lo)[kGatherU]) {
+                                            int lane, int Qc, float (&hi)[U],
+                                            float (&lo)[U]) {
   const unsigned tstep = (unsigned)n_phi * (unsigned)nf * (unsigned)nr;
-  int mr[kGatherU];
+  int mr[U];
 #pragma unroll
-  for (int u = 0; u < kGatherU; ++u) {
+  for (int u = 0; u < U; ++u) {
     const int iz = z0 + lane + 32 * u;
     mr[u] = iz < Qc ? s_row[iz] : -1;
   }
@@ -603,11 +605,11 @@ __device__ __forceinline__ void gather_span(const float *__restrict__ G,
     }
 #pragma unroll 1
     for (int t = t0; t < t1; ++t) {
-      float v[kGatherP][kGatherU];
+      float v[kGatherP][U];
 #pragma unroll
       for (int k = 0; k < kGatherP; ++k)
 #pragma unroll
-        for (int u = 0; u < kGatherU; ++u)
+        for (int u = 0; u < U; ++u)
           v[k][u] = (k < ne && mr[u] >= 0)
                         ? __ldg(G + col[k] + (unsigned)(flip[k] ? 2 * r_zero - mr[u] : mr[u]))
                         : 0.f;
@@ -615,7 +617,7 @@ __device__ __forceinline__ void gather_span(const float *__restrict__ G,
       for (int k = 0; k < kGatherP; ++k) {
         if (k >= ne) break;
 #pragma unroll
-        for (int u = 0; u < kGatherU; ++u) kahan_step(hi[u], lo[u], v[k][u]);
+        for (int u = 0; u < U; ++u) kahan_step(hi[u], lo[u], v[k][u]);
         col[k] += tstep;
       }
     }
@@ -647,7 +649,7 @@ __device__ __forceinline__ void gather_store(float hi, float lo, int iz, size_t 
   else out32[obase + iz] = (hi - lo) * scale;
 }
 
-template <int MODE>
+template <int MODE, int U>
 __global__ void __launch_bounds__(256, 3)
 k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
          const int2 *__restrict__ lent, const int *__restrict__ zptr,
@@ -693,14 +695,14 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     const int nw = blockDim.x >> 5;
     const int eb = e0 + (int)((int64_t)ne * warp / nw);
     const int ee = e0 + (int)((int64_t)ne * (warp + 1) / nw);
-    for (int z0 = 0; z0 < Qc; z0 += 32 * kGatherU) {
-      float hi[kGatherU], lo[kGatherU];
+    for (int z0 = 0; z0 < Qc; z0 += 32 * U) {
+      float hi[U], lo[U];
 #pragma unroll
-      for (int u = 0; u < kGatherU; ++u) hi[u] = lo[u] = 0.f;
+      for (int u = 0; u < U; ++u) hi[u] = lo[u] = 0.f;
       gather_span(G, lent, eb, ee, t0, t1, n_phi, nf, nr, r_zero, s_row, z0, lane, Qc, hi,
                   lo);
 #pragma unroll
-      for (int u = 0; u < kGatherU; ++u) {
+      for (int u = 0; u < U; ++u) {
         const int iz = z0 + lane + 32 * u;
         if (iz < Qc) s_part[warp * Qc + iz] = make_float2(hi[u], lo[u]);
       }
@@ -721,7 +723,7 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     }
     return;
   }
-  // the other lines, one warp each, in spans of 32 kGatherU voxels
+  // the other lines, one warp each, in spans of 32 U voxels
   const int n_lines = Qc * Qc;
   const int wpb = blockDim.x >> 5;
   const int stride = (gridDim.x - n_heavy) * wpb;
@@ -740,14 +742,14 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     }
     float r2, fxy[4];
     line_consts(iy, ix, wl, r2, fxy);
-    for (int z0 = 0; z0 < Qc; z0 += 32 * kGatherU) {
-      float hi[kGatherU], lo[kGatherU];
+    for (int z0 = 0; z0 < Qc; z0 += 32 * U) {
+      float hi[U], lo[U];
 #pragma unroll
-      for (int u = 0; u < kGatherU; ++u) hi[u] = lo[u] = 0.f;
+      for (int u = 0; u < U; ++u) hi[u] = lo[u] = 0.f;
       gather_span(G, lent, e0, e1, t0, t1, n_phi, nf, nr, r_zero, s_row, z0, lane, Qc, hi,
                   lo);
 #pragma unroll
-      for (int u = 0; u < kGatherU; ++u) {
+      for (int u = 0; u < U; ++u) {
         const int iz = z0 + lane + 32 * u;
         if (iz < Qc)
           gather_store<MODE>(hi[u], lo[u], iz, obase, r2, s_rc1, s_zf0, fxy, use_f0, f0_c,
@@ -1194,9 +1196,14 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
   const size_t smem = gather_smem(Q, use_f0, heavy);
   static size_t smem_set[3] = {0, 0, 0};
   if (smem > (48u << 10) && smem > smem_set[mode]) {
-    cudaError_t e = mode == 0 ? cudaFuncSetAttribute(k_gather<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                  : mode == 1 ? cudaFuncSetAttribute(k_gather<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                              : cudaFuncSetAttribute(k_gather<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = mode == 0 ? cudaFuncSetAttribute(k_gather<0, 13>, at, (int)smem)
+                  : mode == 1 ? cudaFuncSetAttribute(k_gather<1, 13>, at, (int)smem)
+                              : cudaFuncSetAttribute(k_gather<2, 13>, at, (int)smem);
+    if (e == cudaSuccess)
+      e = mode == 0 ? cudaFuncSetAttribute(k_gather<0, 7>, at, (int)smem)
+        : mode == 1 ? cudaFuncSetAttribute(k_gather<1, 7>, at, (int)smem)
+                    : cudaFuncSetAttribute(k_gather<2, 7>, at, (int)smem);
     GW_CUDA(e);
     smem_set[mode] = smem;
   }
@@ -1210,9 +1217,18 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
       P->Nr, P->r_zero,                                                              \
       P->n_phi, t0, t1, P->d_C2, P->d_C1, P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, \
       use_f0, f0c, f0iz, o64, o32
-  if (mode == 0) k_gather<0><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
-  else if (mode == 1) k_gather<1><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
-  else k_gather<2><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+  // spans covering a whole line: 7 voxels a lane up to 224 a line, else 13
+  const bool u7 = Q <= 7 * 32;
+  if (mode == 0) {
+    if (u7) k_gather<0, 7><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+    else k_gather<0, 13><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+  } else if (mode == 1) {
+    if (u7) k_gather<1, 7><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+    else k_gather<1, 13><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+  } else {
+    if (u7) k_gather<2, 7><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+    else k_gather<2, 13><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
+  }
 #undef GW_GATHER_ARGS
   GW_LAUNCHED(ctx);
   if (P->n_zmulti > 0) {
