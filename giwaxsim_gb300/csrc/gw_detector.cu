@@ -289,6 +289,11 @@ struct PlaneOrient {
   float4 u, v, e;
 };
 constexpr int kPlTW = 32, kPlTH = 32, kPlThreads = 512;
+// A compile-time bool as a value (selects a lambda's instantiation).
+template <bool B>
+struct BoolC {
+  static constexpr bool value = B;
+};
 constexpr size_t kPlaneSmemMax = 200 * 1024;
 
 __global__ void k_plane_extract(DetArgs a, PlaneArgs pa, float *P) {
@@ -365,63 +370,71 @@ k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
     acc[k] = 0.0;
     part[k] = 0.f;
   }
-  for (int c0 = 0; c0 < a.n_orient; c0 += kDetChunk) {
-    const int nc = min(kDetChunk, a.n_orient - c0);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc * 3; t += kPlThreads)
-      reinterpret_cast<float4 *>(s_ot)[t] = reinterpret_cast<const float4 *>(ot + c0)[t];
-    __syncthreads();
-    // groups of kDetFlush orientations (chunks start at multiples of it),
-    // two per loop trip, flushed to float64 after each full group
-    for (int g0 = 0; g0 < nc; g0 += kDetFlush) {
-      const int ge = min(g0 + kDetFlush, nc);
-      // bit (oo - g0) KP + k: a sample whose index is not certain in
-      // float32, replayed in float64 after the group
-      unsigned need_bits = 0;
-#pragma unroll 2
-      for (int oo = g0; oo < ge; ++oo) {
-        const PlaneOrient T = s_ot[oo];
-#pragma unroll
-        for (int k = 0; k < KP; ++k) {
-          int iu, iv;
-          const bool ok = plane_index<ZX>(T, nu1, nv1, xf[k], yf[k], zf[k], iu, iv);
-          if (valid[k] && ok)
-            part[k] = fmaf(SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv), T.e.z,
-                           part[k]);
-          need_bits |= (unsigned)(valid[k] && !ok) << ((oo - g0) * KP + k);
-        }
-      }
-      // the group's uncertain samples go to the worklist (replayed exactly
-      // by k_detector_fix), or, once it is full, are replayed here into the
-      // float64 accumulator
-      if (__any_sync(0xffffffffu, need_bits != 0)) {
-        while (need_bits) {
-          const int b = __ffs(need_bits) - 1;
-          need_bits &= need_bits - 1;
-          const int k = b % KP, o = c0 + g0 + b / KP;
-          int px = pix[0];
-#pragma unroll
-          for (int q = 1; q < KP; ++q)
-            if (k == q) px = pix[q];
-          const int slot = atomicAdd(wl_count, 1);
-          if (slot < wl_cap) {
-            wl[slot] = make_int2(px, o);
-          } else {
-            double x, y, z;
-            base_point(a, px / a.nh, px % a.nh, x, y, z);
-            const double sv = (double)__ldg(a.iq + gather_index(a, o, x, y, z)) * a.w[o];
-#pragma unroll
-            for (int q = 0; q < KP; ++q)
-              if (k == q) acc[q] += sv;
+  // tiles wholly inside the detector (all but the last tile row and
+  // column) run the loop without the per-pixel validity tests
+  auto orient_loop = [&](auto all_valid) {
+    constexpr bool AV = decltype(all_valid)::value;
+    for (int c0 = 0; c0 < a.n_orient; c0 += kDetChunk) {
+      const int nc = min(kDetChunk, a.n_orient - c0);
+      __syncthreads();
+      for (int t = threadIdx.x; t < nc * 3; t += kPlThreads)
+        reinterpret_cast<float4 *>(s_ot)[t] = reinterpret_cast<const float4 *>(ot + c0)[t];
+      __syncthreads();
+      // groups of kDetFlush orientations (chunks start at multiples of it),
+      // two per loop trip, flushed to float64 after each full group
+      for (int g0 = 0; g0 < nc; g0 += kDetFlush) {
+        const int ge = min(g0 + kDetFlush, nc);
+        // bit (oo - g0) KP + k: a sample whose index is not certain in
+        // float32, replayed in float64 after the group
+        unsigned need_bits = 0;
+  #pragma unroll 2
+        for (int oo = g0; oo < ge; ++oo) {
+          const PlaneOrient T = s_ot[oo];
+  #pragma unroll
+          for (int k = 0; k < KP; ++k) {
+            int iu, iv;
+            const bool ok = plane_index<ZX>(T, nu1, nv1, xf[k], yf[k], zf[k], iu, iv);
+            if ((AV || valid[k]) && ok)
+              part[k] = fmaf(SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv), T.e.z,
+                             part[k]);
+            need_bits |= (unsigned)((AV || valid[k]) && !ok) << ((oo - g0) * KP + k);
           }
         }
-      }
-      if (ge - g0 == kDetFlush) {
-#pragma unroll
-        for (int k = 0; k < KP; ++k) { acc[k] += f2d_exact(part[k]); part[k] = 0.f; }
+        // the group's uncertain samples go to the worklist (replayed exactly
+        // by k_detector_fix), or, once it is full, are replayed here into the
+        // float64 accumulator
+        if (__any_sync(0xffffffffu, need_bits != 0)) {
+          while (need_bits) {
+            const int b = __ffs(need_bits) - 1;
+            need_bits &= need_bits - 1;
+            const int k = b % KP, o = c0 + g0 + b / KP;
+            int px = pix[0];
+  #pragma unroll
+            for (int q = 1; q < KP; ++q)
+              if (k == q) px = pix[q];
+            const int slot = atomicAdd(wl_count, 1);
+            if (slot < wl_cap) {
+              wl[slot] = make_int2(px, o);
+            } else {
+              double x, y, z;
+              base_point(a, px / a.nh, px % a.nh, x, y, z);
+              const double sv = (double)__ldg(a.iq + gather_index(a, o, x, y, z)) * a.w[o];
+  #pragma unroll
+              for (int q = 0; q < KP; ++q)
+                if (k == q) acc[q] += sv;
+            }
+          }
+        }
+        if (ge - g0 == kDetFlush) {
+  #pragma unroll
+          for (int k = 0; k < KP; ++k) { acc[k] += f2d_exact(part[k]); part[k] = 0.f; }
+        }
       }
     }
-  }
+  };
+  const int tile_i = (blockIdx.x / tiles_x) * kPlTH, tile_j = (blockIdx.x % tiles_x) * kPlTW;
+  if (tile_i + kPlTH <= a.nv && tile_j + kPlTW <= a.nh) orient_loop(BoolC<true>{});
+  else orient_loop(BoolC<false>{});
 #pragma unroll
   for (int k = 0; k < KP; ++k)
     if (valid[k]) acc_out[pix[k]] = acc[k] + f2d_exact(part[k]);
