@@ -13,10 +13,15 @@
 //  * Only the output rows/columns whose pixels land in the cropped cube are
 //    produced: each 1-D DFT is a band-limited chirp-z transform
 //    X[k0+m] = B[m] * sum_n (D[n] A[n]) h[m-n], evaluated as a circular
-//    convolution with power-of-two shared-memory FFTs (gw_fft.cuh).
+//    convolution with mixed-radix shared-memory FFTs (gw_fft.cuh).
 //  * Row transforms (along y) write an intermediate F1[slice][z][col];
-//    column transforms (along z) finish the DFT and bin |F|^2 straight into
-//    the float64 sum grid of the cropped cube with atomics.
+//    column transforms (along z) finish the DFT and either bin |F|^2 into
+//    the float64 sum grid of the cropped cube with atomics, or store each
+//    pixel for the gather binning (k_gather: every voxel summed in a fixed
+//    order, then finalized in the same pass).
+//  * Real grids (one phase per structure): two window rows per row
+//    transform, only the columns ky >= 0, mirrored binning
+//    (gw_stockham_row.cu, gw_stockham_col.cu).
 //  * Counts depend only on geometry and factor as C2[qy,qx] * C1[qz]; the
 //    count grid is never materialised.
 // Plain mode keeps the reference's structure: the full g x g grid with its
