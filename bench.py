@@ -458,7 +458,12 @@ def run_gb300(args, world, rank, local, pg):
             "detector_only_s": det_ms / 1e3,
             "plain": (n_slices / plain / len(items) + det_ms / 1e3) if plain else None},
         "plain_slices_per_s": plain,
-        "batched_vs_plain": (value / world / plain) if plain else None,
+        # seconds per detector image, plain over batched (the detector
+        # the same on both); the voxel stage alone in slices_batched_vs_plain
+        "batched_vs_plain": ((n_slices / plain / len(items) + det_ms / 1e3)
+                             / (ms_per_step / 1e3 / len(items) + det_ms / 1e3))
+                            if plain else None,
+        "slices_batched_vs_plain": (value / world / plain) if plain else None,
         "gpu_launches": int(launches),
         "e2e": e2e, "roofline": roof, "rooflines": rooflines,
         "kernel_ms": kernel_share,
