@@ -21,7 +21,7 @@ namespace gw {
 // True when every page of [p, p + bytes) is resident (a recycled result
 // buffer): such a destination needs no faulting in before a copy.  False
 // when the query fails (not a mapping the kernel reports on).
-static bool host_resident(const void *p, size_t bytes) {
+bool host_resident(const void *p, size_t bytes) {
   long pg = sysconf(_SC_PAGESIZE);
   const size_t page = pg > 0 ? (size_t)pg : 4096;
   const uintptr_t lo = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)(page - 1);
@@ -51,6 +51,14 @@ void prefault_host(void *p, size_t bytes) {
     });
   }
   for (auto &x : th) x.join();
+}
+
+int copy_stream_ready(gw_ctx *c) {
+  if (!c->copy_stream)
+    GW_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t &e : c->copy_ev)
+    if (!e) GW_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return GW_OK;
 }
 
 int copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t st) {
@@ -429,7 +437,11 @@ int gw_ctx_destroy(gw_ctx *c) {
   for (cudaEvent_t e : c->ev_free) cudaEventDestroy(e);
   for (cudaEvent_t e : c->mark)
     if (e) cudaEventDestroy(e);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+  for (cudaEvent_t e : c->copy_ev)
+    if (e) cudaEventDestroy(e);
   gw::dev_free(c->d_err);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   {
     std::lock_guard<std::mutex> lk(g_ctx_mu);

@@ -209,6 +209,10 @@ struct gw_ctx {
   double kms[GW_K_COUNT] = {};
   int64_t kn[GW_K_COUNT] = {};
   cudaEvent_t mark[2] = {nullptr, nullptr};  // gw_ctx_mark / gw_ctx_elapsed_ms
+  // a second stream, and its events, for result copies that overlap the
+  // stream's kernels (made on first use)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[17] = {};
 };
 
 namespace gw {
@@ -250,6 +254,10 @@ void prefault_host(void *p, size_t bytes);
 // after the copy is enqueued; pageable destinations complete before), with
 // the destination's page faulting pipelined ahead of the copy.
 int copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t st);
+// every page of [p, p + bytes) resident in host memory
+bool host_resident(const void *p, size_t bytes);
+// the context's copy stream and events, made on first use
+int copy_stream_ready(gw_ctx *c);
 
 }  // namespace gw
 

@@ -181,10 +181,8 @@ __device__ __forceinline__ unsigned flt_ord(float f) {
 __device__ __forceinline__ float ord_flt(unsigned o) {
   return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
 }
-__device__ __forceinline__ void y_interval(const SliceArgs &a, int64_t at,
-                                           float cs, float sn, float &lo,
-                                           float &hi) {
-  const float4 q = a.xyf_s[at];
+__device__ __forceinline__ void y_interval(const float4 q, float cs, float sn,
+                                           float &lo, float &hi) {
   const float xs = q.x * sn, yc = q.y * cs;
   const float t = fmaf(q.y, cs, xs);
   const float d = 10.f * 5.9604645e-8f * (fabsf(xs) + fabsf(yc));
@@ -201,79 +199,145 @@ __global__ void k_yreset(unsigned *ybnd, int s0, int n) {
   }
 }
 
-__global__ void k_ybound(SliceArgs a, int slice0) {
-  const int sl = slice0 + blockIdx.y;
-  const int t = sl / a.n_phi, p = sl % a.n_phi;
-  const gw_structure s = a.st[t];
-  const float cs = (float)a.ph[p].cos_phi, sn = (float)a.ph[p].sin_phi;
-  unsigned lo = ~0u, hi = 0u;  // ordered: min of (y'+d), max of (y'-d)
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
-    float l, h;
-    y_interval(a, s.atom_begin + i, cs, sn, l, h);
-    lo = min(lo, flt_ord(h));
-    hi = max(hi, flt_ord(l));
-  }
-  // block reduction, then one atomic per block and bound
-  __shared__ unsigned s_lo[32], s_hi[32];
-  for (int o = 16; o > 0; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  }
+// Both passes give a block kYS consecutive slices of the batch: a thread
+// loads an atom once and evaluates it for each of them (the atoms stay in
+// L2; one load per atom and slice made the passes L2-bound).  Slices of
+// different structures in one block are taken as runs of the same
+// structure, each over its own atoms.
+constexpr int kYS = 4;
+
+// Run [kb, ke) of the block's slices k0 + k that share one structure.
+__device__ __forceinline__ int y_run_end(const SliceArgs &a, int first, int kb,
+                                         int ns) {
+  const int t = (first + kb) / a.n_phi;
+  int ke = kb + 1;
+  while (ke < ns && (first + ke) / a.n_phi == t) ++ke;
+  return ke;
+}
+
+// Block reduction of kYS (min, max) pairs; thread 0 gets the results.
+template <typename T>
+__device__ __forceinline__ void y_block_reduce(T (&lo)[kYS], T (&hi)[kYS]) {
+  __shared__ T s_lo[kYS][32], s_hi[kYS][32];
   const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if ((threadIdx.x & 31) == 0) { s_lo[w] = lo; s_hi[w] = hi; }
+#pragma unroll
+  for (int k = 0; k < kYS; ++k) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = min(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+      hi[k] = max(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+    }
+    if ((threadIdx.x & 31) == 0) { s_lo[k][w] = lo[k]; s_hi[k][w] = hi[k]; }
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int k = 1; k < nw; ++k) { lo = min(lo, s_lo[k]); hi = max(hi, s_hi[k]); }
-    if (lo != ~0u) {
-      atomicMin(a.ybnd + 2 * (size_t)sl, lo);
-      atomicMax(a.ybnd + 2 * (size_t)sl + 1, hi);
+#pragma unroll
+    for (int k = 0; k < kYS; ++k)
+      for (int j = 1; j < nw; ++j) {
+        lo[k] = min(lo[k], s_lo[k][j]);
+        hi[k] = max(hi[k], s_hi[k][j]);
+      }
+  }
+}
+
+__global__ void k_ybound(SliceArgs a, int slice0, int n) {
+  const int first = slice0 + blockIdx.y * kYS;
+  const int ns = min(kYS, slice0 + n - first);
+  float cs[kYS], sn[kYS];
+  unsigned lo[kYS], hi[kYS];  // ordered: min of (y'+d), max of (y'-d)
+#pragma unroll
+  for (int k = 0; k < kYS; ++k) {
+    const int p = (first + min(k, ns - 1)) % a.n_phi;
+    cs[k] = (float)a.ph[p].cos_phi;
+    sn[k] = (float)a.ph[p].sin_phi;
+    lo[k] = ~0u;
+    hi[k] = 0u;
+  }
+  for (int kb = 0; kb < ns;) {
+    const int ke = y_run_end(a, first, kb, ns);
+    const gw_structure s = a.st[(first + kb) / a.n_phi];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+         i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+      const float4 q = a.xyf_s[s.atom_begin + i];
+#pragma unroll
+      for (int k = 0; k < kYS; ++k) {
+        if (k < kb || k >= ke) continue;
+        float l, h;
+        y_interval(q, cs[k], sn[k], l, h);
+        lo[k] = min(lo[k], flt_ord(h));
+        hi[k] = max(hi[k], flt_ord(l));
+      }
+    }
+    kb = ke;
+  }
+  // block reduction, then one atomic per block, slice and bound
+  y_block_reduce(lo, hi);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < kYS; ++k) {
+      if (k >= ns || lo[k] == ~0u) continue;
+      atomicMin(a.ybnd + 2 * (size_t)(first + k), lo[k]);
+      atomicMax(a.ybnd + 2 * (size_t)(first + k) + 1, hi[k]);
     }
   }
 }
 
-__global__ void k_yminmax(SliceArgs a, int slice0) {
-  const int sl = slice0 + blockIdx.y;
-  const int t = sl / a.n_phi, p = sl % a.n_phi;
-  const gw_structure s = a.st[t];
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+__global__ void k_yminmax(SliceArgs a, int slice0, int n) {
+  const int first = slice0 + blockIdx.y * kYS;
+  const int ns = min(kYS, slice0 + n - first);
+  if (blockIdx.x == 0 && threadIdx.x < ns) {
     // background constant C = avg_voxel_f * max_voxels (voxelgrids.py:358,365):
     // Cbg is what the transformed window excludes (batched mode), Cd what
     // stays inside it
+    const int sl = first + threadIdx.x;
+    const gw_structure s = a.st[sl / a.n_phi];
     const float2 c = make_float2((float)GW_DMUL(s.avg_f_re, s.max_voxels),
                                  (float)GW_DMUL(s.avg_f_im, s.max_voxels));
     const bool bg = !a.plain && (a.fill || a.smooth_on);
     a.sconst[sl] = bg ? make_float4(c.x, c.y, 0.f, 0.f)
                       : make_float4(0.f, 0.f, c.x, c.y);
   }
-  const double c = a.ph[p].cos_phi, sn = a.ph[p].sin_phi;
-  const float csf = (float)c, snf = (float)sn;
-  const float blo = ord_flt(a.ybnd[2 * (size_t)sl]);
-  const float bhi = ord_flt(a.ybnd[2 * (size_t)sl + 1]);
-  unsigned long long lo = ~0ULL, hi = 0ULL;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-       i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
-    float l, h;
-    y_interval(a, s.atom_begin + i, csf, snf, l, h);
-    if (l <= blo || h >= bhi) {
-      const unsigned long long v = dbl_ord(rot_y(a.xyz_s + 3 * (s.atom_begin + i), c, sn));
-      lo = min(lo, v);
-      hi = max(hi, v);
+  double c[kYS], sn[kYS];
+  float blo[kYS], bhi[kYS];
+  unsigned long long lo[kYS], hi[kYS];
+#pragma unroll
+  for (int k = 0; k < kYS; ++k) {
+    const int sl = first + min(k, ns - 1);
+    const int p = sl % a.n_phi;
+    c[k] = a.ph[p].cos_phi;
+    sn[k] = a.ph[p].sin_phi;
+    blo[k] = ord_flt(a.ybnd[2 * (size_t)sl]);
+    bhi[k] = ord_flt(a.ybnd[2 * (size_t)sl + 1]);
+    lo[k] = ~0ULL;
+    hi[k] = 0ULL;
+  }
+  for (int kb = 0; kb < ns;) {
+    const int ke = y_run_end(a, first, kb, ns);
+    const gw_structure s = a.st[(first + kb) / a.n_phi];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+         i < s.atom_count; i += (int64_t)gridDim.x * blockDim.x) {
+      const float4 q = a.xyf_s[s.atom_begin + i];
+#pragma unroll
+      for (int k = 0; k < kYS; ++k) {
+        if (k < kb || k >= ke) continue;
+        float l, h;
+        y_interval(q, (float)c[k], (float)sn[k], l, h);
+        if (l <= blo[k] || h >= bhi[k]) {
+          const unsigned long long v =
+              dbl_ord(rot_y(a.xyz_s + 3 * (s.atom_begin + i), c[k], sn[k]));
+          lo[k] = min(lo[k], v);
+          hi[k] = max(hi[k], v);
+        }
+      }
     }
+    kb = ke;
   }
-  __shared__ unsigned long long s_lo[32], s_hi[32];
-  for (int o = 16; o > 0; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  }
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if ((threadIdx.x & 31) == 0) { s_lo[w] = lo; s_hi[w] = hi; }
-  __syncthreads();
+  y_block_reduce(lo, hi);
   if (threadIdx.x == 0) {
-    for (int k = 1; k < nw; ++k) { lo = min(lo, s_lo[k]); hi = max(hi, s_hi[k]); }
-    if (lo != ~0ULL) {
-      atomicMin(a.ymin_ord + sl, lo);
-      atomicMax(a.ymax_ord + sl, hi);
+#pragma unroll
+    for (int k = 0; k < kYS; ++k) {
+      if (k >= ns || lo[k] == ~0ULL) continue;
+      atomicMin(a.ymin_ord + first + k, lo[k]);
+      atomicMax(a.ymax_ord + first + k, hi[k]);
     }
   }
 }
@@ -659,9 +723,9 @@ __global__ void __launch_bounds__(256, 3)
 k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
          const int2 *__restrict__ lent, const int *__restrict__ zptr,
          const int *__restrict__ zrows, const int *__restrict__ heavy, int n_heavy,
-         int nf, int nr, int r_zero, int n_phi, int t0, int t1,
-         const unsigned int *__restrict__ C2, const int *__restrict__ C1, int W,
-         int off, int Qc, float inv_nstruct, const float *__restrict__ f0tab,
+         int heavy_on, int line_lo, int line_hi, int nf, int nr, int r_zero, int n_phi,
+         int t0, int t1, const unsigned int *__restrict__ C2, const int *__restrict__ C1,
+         int W, int off, int Qc, float inv_nstruct, const float *__restrict__ f0tab,
          const float4 *__restrict__ zf0, int use_f0, float f0_c, float f0_invz,
          double *__restrict__ out64, float *__restrict__ out32) {
   extern __shared__ float4 s_zf0[];
@@ -728,16 +792,17 @@ k_gather(const float *__restrict__ G, const int *__restrict__ lptr,
     }
     return;
   }
-  // the other lines, one warp each, in spans of 32 U voxels
-  const int n_lines = Qc * Qc;
+  // the other lines of [line_lo, line_hi), one warp each, in spans of 32 U
+  // voxels
   const int wpb = blockDim.x >> 5;
   const int stride = (gridDim.x - n_heavy) * wpb;
-  for (int line = (blockIdx.x - n_heavy) * wpb + warp; line < n_lines; line += stride) {
+  for (int line = line_lo + (blockIdx.x - n_heavy) * wpb + warp; line < line_hi;
+       line += stride) {
     const int iy = line / Qc, ix = line - iy * Qc;
     const int wl = (iy + off) * W + ix + off;
     const size_t obase = MODE == 2 ? (size_t)wl * W : (size_t)line * Qc;
     const int e0 = lptr[wl], e1 = lptr[wl + 1];
-    if (n_heavy > 0 && (e1 - e0) * (t1 - t0) > kGatherHeavy) continue;  // a heavy block's
+    if (heavy_on && (e1 - e0) * (t1 - t0) > kGatherHeavy) continue;  // a heavy block's
     if (e0 == e1) {
       for (int iz = lane; iz < Qc; iz += 32) {
         if (MODE == 0) out32[obase + iz] = 0.f;
@@ -773,16 +838,16 @@ __global__ void __launch_bounds__(256)
 k_gather_multi(const float *__restrict__ G, const int *__restrict__ lptr,
                const int2 *__restrict__ lent, const int *__restrict__ zptr,
                const int *__restrict__ zrows, const int *__restrict__ zmulti,
-               int n_zmulti, int nf, int nr, int r_zero, int n_phi, int t0, int t1,
-               const unsigned int *__restrict__ C2, const int *__restrict__ C1, int W,
-               int off, int Qc, float inv_nstruct, const float *__restrict__ f0tab,
-               const float4 *__restrict__ zf0, int use_f0, float f0_c, float f0_invz,
-               double *__restrict__ out64, float *__restrict__ out32) {
+               int n_zmulti, int line_lo, int line_hi, int nf, int nr, int r_zero,
+               int n_phi, int t0, int t1, const unsigned int *__restrict__ C2,
+               const int *__restrict__ C1, int W, int off, int Qc, float inv_nstruct,
+               const float *__restrict__ f0tab, const float4 *__restrict__ zf0,
+               int use_f0, float f0_c, float f0_invz, double *__restrict__ out64,
+               float *__restrict__ out32) {
   const int lane = threadIdx.x & 31;
-  const int n_lines = Qc * Qc;
   const int stride = gridDim.x * (blockDim.x >> 5);
-  for (int line = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); line < n_lines;
-       line += stride) {
+  for (int line = line_lo + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       line < line_hi; line += stride) {
     const int iy = line / Qc, ix = line - iy * Qc;
     const int wl = (iy + off) * W + ix + off;
     const int e0 = lptr[wl], e1 = lptr[wl + 1];
@@ -1145,10 +1210,11 @@ int enqueue_slice_setup(gw_voxel_plan *P, const SliceArgs &a, int s0, int n) {
     GW_LAUNCHED(ctx);
     // a few blocks per slice (grid-stride over the atoms), one atomic per
     // block: the slice's two words are the only targets
-    const int nblk_y = std::min(nblk_at, 8);
-    k_ybound<<<dim3(nblk_y, n), 256, 0, st>>>(a, s0);
+    const int nblk_y = std::min(nblk_at, 16);
+    const int ngrp = (n + kYS - 1) / kYS;
+    k_ybound<<<dim3(nblk_y, ngrp), 256, 0, st>>>(a, s0, n);
     GW_LAUNCHED(ctx);
-    k_yminmax<<<dim3(nblk_y, n), 256, 0, st>>>(a, s0);
+    k_yminmax<<<dim3(nblk_y, ngrp), 256, 0, st>>>(a, s0, n);
     GW_LAUNCHED(ctx);
   }
   {
@@ -1185,7 +1251,10 @@ bool gathering(const gw_voxel_plan *P) { return P->gather && P->n_shells == 0; }
 // k_gather over the structures of output t (all of them when averaged):
 // mode 0 / 1 into the float32 / float64 I(q) of output t, mode 2 into sum
 // grid t (window).
-int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
+// Output lines [line_lo, line_hi) of the crop (line = iy Q + ix; -1: all):
+// the light lines in that range and the heavy lines among them (a run of the
+// ascending heavy list), then the C1 > 1 voxels of the same lines.
+int enqueue_gather(gw_voxel_plan *P, int mode, int t, int line_lo, int line_hi) {
   gw_ctx *ctx = P->ctx;
   const bool sep = P->p.average == GW_STRUCTS_SEPARATE;
   const int t0 = sep ? t : 0, t1 = sep ? t + 1 : P->n_struct;
@@ -1197,7 +1266,19 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
   const float inv_ns = P->p.average == GW_STRUCTS_AVERAGE ? 1.0f / (float)P->n_struct : 1.0f;
   // heavy lines take a block each when the block's partial sums fit
   const bool heavy = P->n_heavy > 0 && gather_smem(Q, use_f0, true) <= (200u << 10);
-  const int n_heavy = heavy ? P->n_heavy : 0;
+  if (line_hi < 0) line_hi = Q * Q;
+  if (line_lo >= line_hi) return GW_OK;
+  int h0 = 0, n_heavy = 0;
+  if (heavy) {
+    // window line of crop line L; heavy lines outside the crop, listed
+    // between two crop lines, are skipped by the kernel
+    auto wline = [&](int L) {
+      return L >= Q * Q ? P->W * P->W : (L / Q + off) * P->W + L % Q + off;
+    };
+    const auto b = P->h_heavy.begin(), e = P->h_heavy.end();
+    h0 = (int)(std::lower_bound(b, e, wline(line_lo)) - b);
+    n_heavy = (int)(std::lower_bound(b, e, wline(line_hi)) - b) - h0;
+  }
   const size_t smem = gather_smem(Q, use_f0, heavy);
   static size_t smem_set[3] = {0, 0, 0};
   if (smem > (48u << 10) && smem > smem_set[mode]) {
@@ -1212,16 +1293,17 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
     GW_CUDA(e);
     smem_set[mode] = smem;
   }
-  const int blocks = n_heavy + std::min((Q * Q + 7) / 8, 16 * ctx->sm_count);
+  const int n_lines = line_hi - line_lo;
+  const int blocks = n_heavy + std::max(1, std::min((n_lines + 7) / 8, 16 * ctx->sm_count));
   float *o32 = mode == 0 ? P->d_iq32 + t * P->iq_stride : nullptr;
   double *o64 = mode == 1 ? P->d_iq64 + t * P->iq_stride
               : mode == 2 ? P->d_sum + t * P->sum_stride : nullptr;
   gw::KTimer tm(ctx, GW_K_FINALIZE);
 #define GW_GATHER_ARGS                                                             \
-  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->d_heavy, n_heavy, P->Nf, \
-      P->Nr, P->r_zero,                                                              \
-      P->n_phi, t0, t1, P->d_C2, P->d_C1, P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, \
-      use_f0, f0c, f0iz, o64, o32
+  P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->d_heavy + h0, n_heavy,    \
+      (int)heavy, line_lo, line_hi, P->Nf, P->Nr, P->r_zero, P->n_phi, t0, t1,       \
+      P->d_C2, P->d_C1, P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, use_f0, f0c, f0iz, \
+      o64, o32
   // spans covering a whole line: 7 voxels a lane up to 224 a line, else 13
   const bool u7 = Q <= 7 * 32;
   if (mode == 0) {
@@ -1237,11 +1319,11 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t) {
 #undef GW_GATHER_ARGS
   GW_LAUNCHED(ctx);
   if (P->n_zmulti > 0) {
-    const int mb = std::min((Q * Q + 7) / 8, 4 * ctx->sm_count);
+    const int mb = std::max(1, std::min((n_lines + 7) / 8, 4 * ctx->sm_count));
 #define GW_GATHER_MULTI_ARGS                                                         \
   P->d_G, P->d_lptr, P->d_lent, P->d_zptr, P->d_zrows, P->d_zmulti, P->n_zmulti,     \
-      P->Nf, P->Nr, P->r_zero, P->n_phi, t0, t1, P->d_C2, P->d_C1, P->W, off, Q,     \
-      inv_ns, P->d_f0, P->d_zf0, use_f0, f0c, f0iz, o64, o32
+      line_lo, line_hi, P->Nf, P->Nr, P->r_zero, P->n_phi, t0, t1, P->d_C2, P->d_C1, \
+      P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, use_f0, f0c, f0iz, o64, o32
     if (mode == 0) k_gather_multi<0><<<mb, 256, 0, ctx->stream>>>(GW_GATHER_MULTI_ARGS);
     else if (mode == 1) k_gather_multi<1><<<mb, 256, 0, ctx->stream>>>(GW_GATHER_MULTI_ARGS);
     else k_gather_multi<2><<<mb, 256, 0, ctx->stream>>>(GW_GATHER_MULTI_ARGS);
@@ -1780,6 +1862,7 @@ extern "C" int gw_voxel_plan_create(gw_ctx *ctx, const gw_voxel_params *p,
       for (int l = 0; l < W * W; ++l)
         if ((int64_t)(lptr[l + 1] - lptr[l]) * per_entry > kGatherHeavy) heavy.push_back(l);
       P->n_heavy = (int)heavy.size();
+      P->h_heavy = heavy;
       if (heavy.empty()) heavy.push_back(0);
       if ((st = upload(&P->d_heavy, heavy, &B)) || (st = upload(&P->d_zmulti, zmulti, &B)) ||
           (st = upload(&P->d_lptr, lptr, &B)) || (st = upload(&P->d_lent, lent, &B)) ||
@@ -2011,6 +2094,41 @@ extern "C" int gw_voxel_get_iq(gw_voxel_plan *P, double *iq, int32_t on_device) 
   if (!P || !iq) return gw::fail(GW_ERR_ARG, "gw_voxel_get_iq: null argument");
   if (!P->executed) return gw::fail(GW_ERR_STATE, "gw_voxel_get_iq: plan not executed");
   const size_t n = (size_t)P->Qc * P->Qc * P->Qc;
+  // Gather binning into a resident host array: the float64 grid is made in
+  // GW_IQ_CHUNKS runs of lines (default 8; 1 or less: in one launch), each
+  // copied out on the copy stream as soon as it is made, so that the
+  // gather and the device-to-host copy overlap.
+  const char *kc = getenv("GW_IQ_CHUNKS");
+  const int K = std::min(16, kc ? atoi(kc) : 8);
+  if (!P->iq64_valid && !on_device && P->n_out == 1 && K > 1 && gwv::gathering(P) &&
+      gw::host_resident(iq, n * sizeof(double))) {
+    GW_CUDA(cudaSetDevice(P->ctx->device));
+    gw_ctx *c = P->ctx;
+    GW_TRY(gw::copy_stream_ready(c));
+    const int lines = P->Qc * P->Qc;
+    int st = GW_OK;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < K && st == GW_OK && e == cudaSuccess; ++k) {
+      const int l0 = (int)((int64_t)lines * k / K);
+      const int l1 = (int)((int64_t)lines * (k + 1) / K);
+      st = gwv::enqueue_gather(P, 1, 0, l0, l1);
+      if (st != GW_OK) break;
+      e = cudaEventRecord(c->copy_ev[k], c->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->copy_ev[k], 0);
+      const size_t o = (size_t)l0 * P->Qc;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(iq + o, P->d_iq64 + o, (size_t)(l1 - l0) * P->Qc * sizeof(double),
+                            cudaMemcpyDeviceToHost, c->copy_stream);
+    }
+    // the stream waits for every copy (also after a failed launch)
+    cudaError_t j = cudaEventRecord(c->copy_ev[16], c->copy_stream);
+    if (j == cudaSuccess) j = cudaStreamWaitEvent(c->stream, c->copy_ev[16], 0);
+    if (st != GW_OK) return st;
+    if (e != cudaSuccess) return gw::cuda_fail(e, "chunked result copy", __FILE__, __LINE__);
+    if (j != cudaSuccess) return gw::cuda_fail(j, "chunked result copy", __FILE__, __LINE__);
+    P->iq64_valid = true;
+    return gw::check_device_error(P->ctx, "voxel stage");
+  }
   // the float64 grid is made when asked for: an execute writes only the
   // float32 grid the detector reads
   if (!P->iq64_valid) {
@@ -2104,7 +2222,8 @@ extern "C" int gw_voxel_info(gw_voxel_plan *P, int64_t *info, int32_t n) {
                        P->y_lo, P->z_lo, P->k0, P->kz0, P->n_slices,
                        (int64_t)P->bytes, P->graph_kernels,
                        (int64_t)P->f1_tma, (int64_t)P->fused_y,
-                       (int64_t)P->fused_z, (int64_t)P->real, (int64_t)P->gather};
+                       (int64_t)P->fused_z, (int64_t)P->real, (int64_t)P->gather,
+                       P->gather ? P->n_heavy : 0, P->gather ? P->n_zmulti : 0};
   const int k = std::min<int>(n, (int)(sizeof v / sizeof v[0]));
   for (int i = 0; i < k; ++i) info[i] = v[i];
   return k;

@@ -639,6 +639,7 @@ struct gw_voxel_plan {
   // window lines with many entries (each takes a whole block)
   int *d_heavy = nullptr;
   int n_heavy = 0;
+  std::vector<int> h_heavy;  // the heavy window lines, ascending (host copy)
   // window z with more than one output row (their voxels are summed again
   // over every row)
   int *d_zmulti = nullptr;
@@ -704,6 +705,7 @@ int fused_col_block(const gw_voxel_plan *P);
 // Average, crop and f0 factor into the float32 (f64 false) or the float64
 // I(q) grids.
 int enqueue_finalize(gw_voxel_plan *P, bool f64);
+int enqueue_gather(gw_voxel_plan *P, int mode, int t, int line_lo = 0, int line_hi = -1);
 // Number of window rows of slices [s0, s0+n).
 int batch_rows(gw_voxel_plan *P, int s0, int n);
 void grad_state_destroy(gw_grad_state *g);

@@ -520,7 +520,7 @@ class VoxelPlan:
         keys = ["crop", "batch", "Ly", "Lz", "Nc", "Nr", "My", "Mz", "y_lo",
                 "z_lo", "k0", "kz0", "n_slices", "device_bytes",
                 "graph_kernels", "col_tma", "fused_y", "fused_z", "real",
-                "gather"]
+                "gather", "heavy_lines", "multi_rows"]
         return dict(zip(keys, (int(x) for x in v[:n])))
 
     def debug_deposit(self, slice_index):

@@ -267,8 +267,10 @@ int gw_voxel_get_sums(gw_voxel_plan *plan, double *sums);
  * z_lo, k0, kz0, n_slices, device_bytes, graph_kernels, col_tma (1 when
  * the column kernel loads its tiles by TMA), fused_y, fused_z (1 when the
  * fused chirp-z kernel runs along that axis), real (1 when the real-grid
- * path runs), gather (1 when the gather binning runs)].  Returns the number
- * written (at most n). */
+ * path runs), gather (1 when the gather binning runs), heavy_lines (gather:
+ * window lines summed by a whole block each), multi_rows (gather: window z
+ * with more than one output row)].  Returns the number written (at most
+ * n). */
 int gw_voxel_info(gw_voxel_plan *plan, int64_t *info, int32_t n);
 /* Deposit indices of one slice (after execute): y,z voxel index per atom of
  * that slice's structure, -1 where the reference's valid_mask drops it

@@ -158,3 +158,33 @@ def test_plans_gather_refuses(monkeypatch):
         F.VoxelPlan(geom, [(xyz, fv, None)], phis=PHIS, binning="gather")
     monkeypatch.delenv("GW_GATHER_MAX_MB")
     assert os.environ.get("GW_GATHER_MAX_MB") is None
+
+
+def test_chunked_result_copy(monkeypatch):
+    """The float64 I(q) made in runs of lines, each copied to the (resident)
+    host array as soon as it is made, is the one-launch result bit for bit,
+    heavy lines (a block each) split between runs included."""
+    xyz = slab("C", 37, (12.0, 11.0, 13.0))
+    fv = np.full(len(xyz), 6.0 + 0.2j)
+    phis = np.arange(0.0, 180.0, 0.5)  # about 180 entries on the axis line
+    plan = F.VoxelPlan(F.VoxelGeometry(*GEOM), [(xyz, fv, None)], phis=phis,
+                       fill_bkg=True, smooth=1.0, binning="gather")
+    outs = {}
+    try:
+        plan.set_atoms()
+        for k in ("1", "3", "8", "16"):
+            monkeypatch.setenv("GW_IQ_CHUNKS", k)
+            plan.execute()
+            out = np.full((plan.Qc,) * 3, -1.0)  # every page resident
+            plan.iq(out=out)
+            outs[k] = out
+        info = plan.info()
+        counts = plan.counts()
+    finally:
+        plan.close()
+    assert info["gather"] == 1 and info["real"] == 1
+    assert info["heavy_lines"] > 0
+    for k in ("3", "8", "16"):
+        assert np.array_equal(outs[k].view(np.uint64), outs["1"].view(np.uint64)), k
+    assert not outs["1"][counts == 0].any()
+    assert (outs["1"] >= 0).all()
