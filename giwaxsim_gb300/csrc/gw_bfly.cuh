@@ -18,6 +18,18 @@ __host__ __device__ __forceinline__ float2 mul_mi(float2 a) {
   return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
+// a + mul_mi(e) and a - mul_mi(e) in scalar form: the rotation by -+i is
+// folded into the operands (a paired add would need the swapped halves
+// made first)
+template <bool INV>
+__host__ __device__ __forceinline__ float2 add_mi(float2 a, float2 e) {
+  return INV ? make_float2(a.x - e.y, a.y + e.x) : make_float2(a.x + e.y, a.y - e.x);
+}
+template <bool INV>
+__host__ __device__ __forceinline__ float2 sub_mi(float2 a, float2 e) {
+  return INV ? make_float2(a.x + e.y, a.y - e.x) : make_float2(a.x - e.y, a.y + e.x);
+}
+
 template <bool INV>
 __host__ __device__ __forceinline__ void dft2(float2 &a0, float2 &a1) {
   const float2 s = cadd(a0, a1), d = csub(a0, a1);
@@ -29,11 +41,11 @@ template <bool INV>
 __host__ __device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2,
                                      float2 &a3) {
   const float2 s0 = cadd(a0, a2), d0 = csub(a0, a2);
-  const float2 s1 = cadd(a1, a3), d1 = mul_mi<INV>(csub(a1, a3));
+  const float2 s1 = cadd(a1, a3), e = csub(a1, a3);
   a0 = cadd(s0, s1);
   a2 = csub(s0, s1);
-  a1 = cadd(d0, d1);
-  a3 = csub(d0, d1);
+  a1 = add_mi<INV>(d0, e);
+  a3 = sub_mi<INV>(d0, e);
 }
 
 // W_16^m (forward sign); m in 0..15
@@ -74,10 +86,10 @@ __host__ __device__ __forceinline__ void dft3(float2 *v) {
   const float2 t1 = cadd(v[1], v[2]);
   const float2 t2 = make_float2(v[0].x - 0.5f * t1.x, v[0].y - 0.5f * t1.y);
   const float2 d = csub(v[1], v[2]);
-  const float2 m = INV ? make_float2(-s * d.y, s * d.x) : make_float2(s * d.y, -s * d.x);
+  const float2 sd = make_float2(s * d.x, s * d.y);
   v[0] = cadd(v[0], t1);
-  v[1] = cadd(t2, m);
-  v[2] = csub(t2, m);
+  v[1] = add_mi<INV>(t2, sd);
+  v[2] = sub_mi<INV>(t2, sd);
 }
 
 // 5-point DFT with c_k = cos(2 pi k/5), s_k = sin(2 pi k/5):
@@ -94,14 +106,12 @@ __host__ __device__ __forceinline__ void dft5(float2 *v) {
   const float2 b2 = make_float2(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
   const float2 d1 = make_float2(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
   const float2 d2 = make_float2(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
-  // -i d = (d.y, -d.x); +i d = (-d.y, d.x)
-  const float2 m1 = INV ? make_float2(-d1.y, d1.x) : make_float2(d1.y, -d1.x);
-  const float2 m2 = INV ? make_float2(-d2.y, d2.x) : make_float2(d2.y, -d2.x);
+  // y1 = b1 - i d1 (forward), y4 = b1 + i d1; likewise y2, y3 from b2, d2
   v[0] = cadd(v[0], cadd(t1, t2));
-  v[1] = cadd(b1, m1);
-  v[4] = csub(b1, m1);
-  v[2] = cadd(b2, m2);
-  v[3] = csub(b2, m2);
+  v[1] = add_mi<INV>(b1, d1);
+  v[4] = sub_mi<INV>(b1, d1);
+  v[2] = add_mi<INV>(b2, d2);
+  v[3] = sub_mi<INV>(b2, d2);
 }
 
 template <int R, bool INV>

@@ -305,11 +305,30 @@ __device__ __forceinline__ void dev_error(int *err, int code) {
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+// Complex sums and differences as one paired float32 instruction (add /
+// sub .f32x2, round to nearest: each half rounds exactly as a scalar add);
+// the host build keeps the scalar form.
 __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  return __fadd2_rn(a, b);
+#else
   return make_float2(a.x + b.x, a.y + b.y);
+#endif
 }
 __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  float2 d;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "sub.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+#else
   return make_float2(a.x - b.x, a.y - b.y);
+#endif
 }
 __host__ __device__ __forceinline__ float2 cscale(float2 a, float s) {
   return make_float2(a.x * s, a.y * s);

@@ -168,8 +168,12 @@ __device__ __forceinline__ void fft_pass(float2 *buf, const float2 *tw,
       else dft<R, INV>(v[e]);
     }
   }
-  // a first pass may read inputs that alias its shared destination
-  if (DST == 0) __syncthreads();
+  // The writes wait for every thread's reads (passes are in place; a first
+  // pass may read inputs that alias its shared destination), except in a
+  // last pass (NS R = M): there Q = NS, so base = j and a butterfly writes
+  // exactly the slots j + r Q it read, which no other thread touches.
+  constexpr bool kOwnSlots = NS * R == M && SRC == 0;
+  if (DST == 0 && !kOwnSlots) __syncthreads();
 #pragma unroll
   for (int e = 0; e < PER; ++e) {
     const int b = threadIdx.x + e * NT;

@@ -85,8 +85,20 @@ class VoxelGeometry:
                             "simulation. Please lower delta_q value")
 
     def phi_table(self, phis):
-        """Per-slice scalars as numpy computes them in the reference."""
+        """Per-slice scalars as numpy computes them in the reference (the
+        last table made is kept for a call with the same phis; read-only)."""
         phis = np.asarray(phis, dtype=np.float64)
+        global _PHI_TABLE_LAST
+        key = (self.h_max, phis.tobytes())
+        last = _PHI_TABLE_LAST  # one (key, table) tuple: threads see either whole
+        if last is not None and last[0] == key:
+            return last[1]
+        t = self._phi_table(phis)
+        t.flags.writeable = False
+        _PHI_TABLE_LAST = (key, t)
+        return t
+
+    def _phi_table(self, phis):
         t = np.zeros(len(phis), dtype=_dtype_of(N.Phi))
         pr = np.radians(phis)
         t["cos_phi"] = np.cos(pr)
@@ -105,6 +117,7 @@ class VoxelGeometry:
 
 
 _DTYPES = {}
+_PHI_TABLE_LAST = None  # ((h_max, phis bytes), table) of the last phi_table
 
 
 def _dtype_of(ctype):
@@ -122,10 +135,8 @@ def element_kinds(elements):
     are of one element."""
     a = np.asarray(elements)
     if a.ndim == 1 and len(a) and a.dtype.kind == "U" and a.dtype.itemsize <= 8:
-        cp = np.ascontiguousarray(a).view(np.uint32).reshape(len(a), -1)
-        key = cp[:, 0].astype(np.uint64)
-        if cp.shape[1] == 2:
-            key |= cp[:, 1].astype(np.uint64) << np.uint64(32)
+        c = np.ascontiguousarray(a)
+        key = c.view(np.uint64 if c.dtype.itemsize == 8 else np.uint32)
         if (key == key[0]).all():
             return [str(a[0])], np.zeros(len(a), np.intp)
         _, first, inv = np.unique(key, return_index=True, return_inverse=True)
@@ -141,6 +152,8 @@ def element_f_values(elements, energy, f1f2=None):
     d = f1f2 if f1f2 is not None else get_element_f1_f2_dict(energy, uniq)
     vals = np.array([complex(d[e]) for e in uniq], dtype=complex)
     vals += np.array([ptable[e] for e in uniq])
+    if len(vals) == 1:
+        return np.full(len(inv), vals[0])
     return vals[inv]
 
 
@@ -329,8 +342,10 @@ class VoxelPlan:
             xyz.append(coords)
             fs.append(fv.astype(np.complex64))
         self.structs = st
+        # the plan's own copy of the coordinates; the f values are already
+        # a fresh array for one structure
         self.xyz = np.ascontiguousarray(np.concatenate(xyz))
-        self.f = np.ascontiguousarray(np.concatenate(fs)).view(np.float32)
+        self.f = (fs[0] if len(fs) == 1 else np.concatenate(fs)).view(np.float32)
         self.phi_tab = geom.phi_table(self.phis)
         p = N.VoxelParams()
         p.grid_size = geom.grid_size
