@@ -305,18 +305,10 @@ __device__ __forceinline__ void dev_error(int *err, int code) {
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-// Complex sums and differences as one paired float32 instruction (add /
-// sub .f32x2, round to nearest: each half rounds exactly as a scalar add);
-// the host build keeps the scalar form.
-__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
-#ifdef __CUDA_ARCH__
-  return __fadd2_rn(a, b);
-#else
-  return make_float2(a.x + b.x, a.y + b.y);
-#endif
-}
-__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
-#ifdef __CUDA_ARCH__
+// a - b on both halves in one paired float32 instruction (sub.rn.f32x2:
+// each half rounds exactly as the scalar subtraction).  The paired add,
+// multiply and fma are CUDA's __fadd2_rn / __fmul2_rn / __ffma2_rn.
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
   float2 d;
   asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
       "mov.b64 pa, {%2, %3};\n\t"
@@ -326,6 +318,20 @@ __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
       : "=f"(d.x), "=f"(d.y)
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
   return d;
+}
+
+// Complex sums and differences as one paired float32 instruction each; the
+// host build keeps the scalar form.
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  return f2_sub(a, b);
 #else
   return make_float2(a.x - b.x, a.y - b.y);
 #endif

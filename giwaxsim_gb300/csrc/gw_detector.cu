@@ -285,9 +285,15 @@ struct PlaneArgs {
 };
 // The two free rows of an orientation's affine map, packed for three
 // 16-byte shared loads: (A_u, b_u), (A_v, b_v), (d_u, d_v, w, -).
-struct PlaneOrient {
-  float4 u, v, e;
+// One orientation of the plane gather.  Each member pairs the u axis's
+// value with the v axis's (x, y and z coefficients, constant, certainty
+// bound), so that both axes' indices are made with paired float32
+// instructions; w is the orientation's weight.  Three 16-byte words.
+struct __align__(16) PlaneOrient {
+  float2 x, y, z, c, d;
+  float w, pad;
 };
+static_assert(sizeof(PlaneOrient) == 48, "three 16-byte words per orientation");
 constexpr int kPlTW = 32, kPlTH = 32, kPlThreads = 512;
 // A compile-time bool as a value (selects a lambda's instantiation).
 template <bool B>
@@ -308,33 +314,31 @@ __global__ void k_plane_extract(DetArgs a, PlaneArgs pa, float *P) {
   }
 }
 
-// fast_axis with the floor taken by one addition rounded toward minus
-// infinity: r = 1.5 * 2^23 + floor(c) exactly for c in [0, 2^22), so k and
-// the certainty test are those of fast_axis, in fewer operations.  nm1 is
-// n - 1 as a float.
-__device__ __forceinline__ bool plane_axis(float t, float d, float nm1, int &k) {
-  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
-  const float c = fminf(fmaxf(t + d, 0.f), nm1);
-  const float r = __fadd_rd(c, kMagic);
-  k = __float_as_int(r) - 0x4B400000;
-  return fmaxf(t - d, 0.f) >= __fsub_rn(r, kMagic);
-}
-
-// Same operation order as fast_index on those rows.  ZX: the pixels' x is
-// +-0 for every pixel, so the x products (exact zeros added to the rest of
-// the chain) are left out: fmaf(a, +-0, c) == c for c != 0, and a signed
+// Both axes of fast_index on those rows, u in the first half of each pair
+// and v in the second: t = (y c_y + (z c_z + c)) (same operation order), and
+// for each axis fast_axis with the floor taken by one addition rounded
+// toward minus infinity: r = 1.5 * 2^23 + floor(t + d) exactly for clamped
+// values in [0, 2^22), so the index and the certainty test are those of
+// fast_axis, in fewer operations.  The paired instructions round each half
+// as the scalar ones.  n1 = (nu - 1, nv - 1) as floats.  ZX: the pixels' x
+// is +-0 for every pixel, so the x products (exact zeros added to the rest
+// of the chain) are left out: fmaf(a, +-0, c) == c for c != 0, and a signed
 // zero does not change a floor.
 template <bool ZX>
-__device__ __forceinline__ bool plane_index(const PlaneOrient &T, float nu1,
-                                            float nv1, float x, float y,
-                                            float z, int &iu, int &iv) {
-  float tu = fmaf(T.u.y, y, fmaf(T.u.z, z, T.u.w));
-  float tv = fmaf(T.v.y, y, fmaf(T.v.z, z, T.v.w));
-  if (!ZX) {
-    tu = fmaf(T.u.x, x, tu);
-    tv = fmaf(T.v.x, x, tv);
-  }
-  return plane_axis(tu, T.e.x, nu1, iu) & plane_axis(tv, T.e.y, nv1, iv);
+__device__ __forceinline__ bool plane_index(const PlaneOrient &T, float2 n1,
+                                            float2 xx, float2 yy, float2 zz,
+                                            int &iu, int &iv) {
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  const float2 mg = make_float2(kMagic, kMagic);
+  float2 t = __ffma2_rn(T.y, yy, __ffma2_rn(T.z, zz, T.c));
+  if (!ZX) t = __ffma2_rn(T.x, xx, t);
+  const float2 hi = __fadd2_rn(t, T.d), lo = f2_sub(t, T.d);
+  const float2 c = make_float2(fminf(fmaxf(hi.x, 0.f), n1.x), fminf(fmaxf(hi.y, 0.f), n1.y));
+  const float2 r = __fadd2_rd(c, mg);
+  iu = __float_as_int(r.x) - 0x4B400000;
+  iv = __float_as_int(r.y) - 0x4B400000;
+  const float2 fl = f2_sub(r, mg);
+  return (fmaxf(lo.x, 0.f) >= fl.x) & (fmaxf(lo.y, 0.f) >= fl.y);
 }
 
 template <bool SMEM, bool ZX>
@@ -344,7 +348,7 @@ k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
   extern __shared__ float s_plane[];
   __shared__ PlaneOrient s_ot[kDetChunk];
   constexpr int KP = kPlTH * kPlTW / kPlThreads;  // pixels per thread
-  const float nu1 = (float)(pa.nu - 1), nv1 = (float)(pa.nv - 1);
+  const float2 n1 = make_float2((float)(pa.nu - 1), (float)(pa.nv - 1));
   const int tiles_x = (a.nh + kPlTW - 1) / kPlTW;
   const int j = (blockIdx.x % tiles_x) * kPlTW + (threadIdx.x % kPlTW);
   const int ib = (blockIdx.x / tiles_x) * kPlTH + threadIdx.x / kPlTW;
@@ -389,13 +393,24 @@ k_detector_plane(DetArgs a, const PlaneOrient *ot, PlaneArgs pa,
         unsigned need_bits = 0;
   #pragma unroll 2
         for (int oo = g0; oo < ge; ++oo) {
-          const PlaneOrient T = s_ot[oo];
+          // three 16-byte loads; each holds two (u, v) pairs
+          const float4 *q = reinterpret_cast<const float4 *>(s_ot + oo);
+          const float4 q0 = q[0], q1 = q[1], q2 = q[2];
+          PlaneOrient T;
+          T.x = make_float2(q0.x, q0.y);
+          T.y = make_float2(q0.z, q0.w);
+          T.z = make_float2(q1.x, q1.y);
+          T.c = make_float2(q1.z, q1.w);
+          T.d = make_float2(q2.x, q2.y);
+          T.w = q2.z;
   #pragma unroll
           for (int k = 0; k < KP; ++k) {
             int iu, iv;
-            const bool ok = plane_index<ZX>(T, nu1, nv1, xf[k], yf[k], zf[k], iu, iv);
+            const bool ok = plane_index<ZX>(T, n1, make_float2(xf[k], xf[k]),
+                                            make_float2(yf[k], yf[k]),
+                                            make_float2(zf[k], zf[k]), iu, iv);
             if ((AV || valid[k]) && ok)
-              part[k] = fmaf(SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv), T.e.z,
+              part[k] = fmaf(SMEM ? src[iu * pa.nv + iv] : __ldg(src + iu * pa.nv + iv), T.w,
                              part[k]);
             need_bits |= (unsigned)((AV || valid[k]) && !ok) << ((oo - g0) * KP + k);
           }
@@ -749,9 +764,13 @@ extern "C" int gw_detector_plan_create(gw_ctx *ctx, const gw_detector_params *p,
         std::vector<PlaneOrient> po(n_orient);
         for (int o = 0; o < n_orient; ++o) {
           const OrientFast &T = ot[o];
-          po[o].u = make_float4(T.A[3 * pa.ua], T.A[3 * pa.ua + 1], T.A[3 * pa.ua + 2], T.b[pa.ua]);
-          po[o].v = make_float4(T.A[3 * pa.va], T.A[3 * pa.va + 1], T.A[3 * pa.va + 2], T.b[pa.va]);
-          po[o].e = make_float4(T.d[pa.ua], T.d[pa.va], T.w, 0.f);
+          po[o].x = make_float2(T.A[3 * pa.ua], T.A[3 * pa.va]);
+          po[o].y = make_float2(T.A[3 * pa.ua + 1], T.A[3 * pa.va + 1]);
+          po[o].z = make_float2(T.A[3 * pa.ua + 2], T.A[3 * pa.va + 2]);
+          po[o].c = make_float2(T.b[pa.ua], T.b[pa.va]);
+          po[o].d = make_float2(T.d[pa.ua], T.d[pa.va]);
+          po[o].w = T.w;
+          po[o].pad = 0.f;
         }
         if ((st = up(&P->d_po, po.data(), po.size()))) {
           gw_detector_plan_destroy(P);
