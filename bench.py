@@ -38,8 +38,8 @@ L2_BYTES = 129 * 1024 * 1024
 # traffic is this times its slices (both kernels move per-slice data only).
 NCU_TRAFFIC = {("si-100A", "row_czt", 1280, 1024, 0): (1.48 + 38.03) * 1e6 / 51,
                ("si-100A", "col_czt_bin", 1280, 1024, 0): (148.42 + 28.70) * 1e6 / 51,
-               ("si-100A", "row_czt", 1280, 1024, 1): (1.76 + 39.42) * 1e6 / 102,
-               ("si-100A", "col_czt_bin", 1280, 1024, 1): (83.23 + 15.74) * 1e6 / 102}
+               ("si-100A", "row_czt", 1280, 1024, 1): (1.76 + 42.04) * 1e6 / 102,
+               ("si-100A", "col_czt_bin", 1280, 1024, 1): (83.23 + 15.57) * 1e6 / 102}
 
 
 def parse():
