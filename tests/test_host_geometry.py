@@ -65,6 +65,23 @@ def test_phi_table_matches_reference_scalars():
         assert t["cl_swap"][i] == (phi > 90)
 
 
+def test_phi_table_reuse():
+    """A call with the phis and geometry of the last one gets the same
+    (read-only) table; other phis or another geometry a fresh one, equal to
+    a table made from scratch."""
+    g = F.VoxelGeometry(0.3, 0.03, 3.0)
+    phis = np.linspace(0.0, 179.0, 180)
+    t1 = g.phi_table(phis)
+    t2 = g.phi_table(phis.copy())
+    assert t2 is t1 and not t1.flags.writeable
+    assert t1.tobytes() == g._phi_table(phis).tobytes()
+    t3 = g.phi_table(phis[:-1])
+    assert t3 is not t1 and t3.tobytes() == g._phi_table(phis[:-1]).tobytes()
+    g2 = F.VoxelGeometry(0.25, 0.02, 4.0)  # another h_max
+    t4 = g2.phi_table(phis[:-1])
+    assert t4 is not t3 and t4.tobytes() == g2._phi_table(phis[:-1]).tobytes()
+
+
 def test_structure_constants_match_oracle():
     for name in ("graphite-50A", "si-100A"):
         xyz, el, _ = W.structures(name)[0]
@@ -80,6 +97,7 @@ def test_structure_constants_match_oracle():
     np.array(["C", "H", "O", "C", "N", "H", "C"] * 9),
     ["S", "O", "O", "Si", "C"] * 4,
     np.array(["C", "Si", "Cl"], dtype="<U3"),
+    np.array(["Si", "Sn", "S", "Si", "Sn", "C", "S", "Sn"])[::2],  # strided
     np.array(["H"])])
 def test_element_kinds_match_numpy_unique(elements):
     uniq, inv = F.element_kinds(elements)
