@@ -82,8 +82,9 @@ k_row_czt(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
 // window rows A and B share one transform: x = R_A + i R_B gives
 // Z = Y_A + i Y_B, and Y_A[k] = (Z[k] + conj(Z[-k])) / 2,
 // Y_B[k] = (Z[k] - conj(Z[-k])) / (2 i).  The block deposits its 2 NB rows
-// into the halves of its NB transform buffers (row 2f at f LDM, row 2f+1 at
-// f LDM + LDM/2; the window fits: L <= LDM/2), transforms the NB packed
+// as float arrays into the halves of its NB transform buffers (row r at
+// float offset r LDM: row 2f in the first half of buffer f, row 2f+1 in the
+// second; the window fits: L <= LDM), transforms the NB packed
 // rows, leaves the inverse transform in shared memory, and writes F1 for
 // the columns ky >= 0 only (the column stage needs no others):
 // F1[row][j] = u_row Y_row[m_zero + j], j < nf.
@@ -92,18 +93,18 @@ struct RowLoadPair {
   RowValueArgs va;
   const float2 *A;        // forward chirp
   int L;                  // window length
-  const float2 *rows;     // block row r at rows + r * (LDM / 2)
+  const float *rows;      // block row r: floats rows[r * LDM + n]
   const RowConst *rc;     // per block row (shared memory)
   int row0, n_rows;       // row0: the block's first window row
   __device__ float2 operator()(int f, int n) const {
     if (n >= L) return make_float2(0.f, 0.f);
-    constexpr int HL = FftPlan<M>::LDM / 2;
+    constexpr int LD = FftPlan<M>::LDM;
     float re = 0.f, im = 0.f;
     const int ra = 2 * f, rb = 2 * f + 1;
     // the deposit holds the real row's atom sum r (deposit_rows<.., REAL>):
     // the grid value there is d_value_row of r u, projected back on u
-    if (row0 + ra < n_rows) re = d_value_row_real(va, rc[ra], n, rows[ra * HL + n].x);
-    if (row0 + rb < n_rows) im = d_value_row_real(va, rc[rb], n, rows[rb * HL + n].x);
+    if (row0 + ra < n_rows) re = d_value_row_real(va, rc[ra], n, rows[ra * LD + n]);
+    if (row0 + rb < n_rows) im = d_value_row_real(va, rc[rb], n, rows[rb * LD + n]);
     return cmul(make_float2(re, im), __ldg(A + n));
   }
 };
@@ -124,8 +125,9 @@ k_row_czt_real(SliceArgs a, CztArgs cz, int slice0, int n_sl, int n_rows,
   for (int t = threadIdx.x; t < TWL; t += NT) tw[t] = cz.tw[t];
   const int row0 = blockIdx.x * 2 * NB;
   deposit_rows<2 * NB, NT, false, true>(a, cz.L, slice0, n_sl, n_rows, row0, buf,
-                                        LDM / 2, rs);
-  RowLoadPair<M> ld{row_value_args(a), cz.A, cz.L, buf, rs.k, row0, n_rows};
+                                        LDM, rs);
+  RowLoadPair<M> ld{row_value_args(a), cz.A, cz.L, reinterpret_cast<const float *>(buf),
+                    rs.k, row0, n_rows};
   fft_run<M, NB, NT, false, 1, false, 0, false, HALF, false>(buf, tw, nullptr, ld,
                                                             NoStore());
   // the inverse transform stays in shared memory (natural order; with HALF

@@ -434,9 +434,14 @@ __device__ __forceinline__ void deposit_rows(const SliceArgs &a, int L,
                                              int slice0, int n_sl, int n_rows,
                                              int row0, float2 *buf, int ldm,
                                              RowShared<NB> &rs) {
-  // only the window columns [0, L) are deposited into and read back
+  // only the window columns [0, L) are deposited into and read back; a
+  // real row (REAL) is a float array, row f at float offset f ldm
+  float *rbuf = reinterpret_cast<float *>(buf);
   for (int f = 0; f < NB; ++f)
-    for (int n = threadIdx.x; n < L; n += NT) buf[f * ldm + n] = make_float2(0.f, 0.f);
+    for (int n = threadIdx.x; n < L; n += NT) {
+      if constexpr (REAL) rbuf[f * ldm + n] = 0.f;
+      else buf[f * ldm + n] = make_float2(0.f, 0.f);
+    }
   // the block's rows: slot, window row and atom range, one thread per row
   // (independent loads), then a scan of the atom counts
   static_assert(NB <= 32, "one warp sets the rows up");
@@ -477,7 +482,7 @@ __device__ __forceinline__ void deposit_rows(const SliceArgs &a, int L,
         if (yy < a.Ly) {
           if constexpr (REAL) {
             const float2 u = rs.k[f].u;
-            atomicAdd(&buf[f * ldm + yy].x, fmaf(q.z, u.x, q.w * u.y));
+            atomicAdd(rbuf + f * ldm + yy, fmaf(q.z, u.x, q.w * u.y));
           } else {
             atomicAdd(&buf[f * ldm + yy].x, q.z);
             atomicAdd(&buf[f * ldm + yy].y, q.w);
