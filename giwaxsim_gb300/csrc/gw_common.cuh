@@ -17,6 +17,7 @@
 #include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "giwaxs_gb300.h"
@@ -292,6 +293,33 @@ struct KTimer {
     int _s = (expr);                                                     \
     if (_s != GW_OK) return _s;                                          \
   } while (0)
+
+namespace gw {
+// The largest dynamic shared memory a kernel has been allowed, per device
+// (cudaFuncSetAttribute acts on the current device only): a launch site
+// keeps one record per kernel and calls smem_limit before its launches.
+// Threads may race to set the same limit, which is harmless; the record
+// only grows.
+constexpr int kSmemDevices = 64;
+struct SmemRecord {
+  std::atomic<size_t> bytes[kSmemDevices] = {};
+};
+template <class K>
+int smem_limit(SmemRecord &r, K *kernel, size_t bytes) {
+  int dev = 0;
+  GW_CUDA(cudaGetDevice(&dev));
+  const bool kept = dev >= 0 && dev < kSmemDevices;
+  if (kept && r.bytes[dev].load(std::memory_order_acquire) >= bytes) return GW_OK;
+  GW_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)bytes));
+  if (kept) {
+    size_t cur = r.bytes[dev].load(std::memory_order_relaxed);
+    while (cur < bytes && !r.bytes[dev].compare_exchange_weak(cur, bytes)) {
+    }
+  }
+  return GW_OK;
+}
+}  // namespace gw
 
 // device error codes written to ctx->d_err
 enum { GW_DEVERR_NONE = 0, GW_DEVERR_BOX = 1, GW_DEVERR_MASK_WRAP = 2,

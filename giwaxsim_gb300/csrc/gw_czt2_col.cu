@@ -12,12 +12,8 @@ int launch_col_fused(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                      const BinArgs &bn, int s0, int n_sl) {
   constexpr int NT = NB * Fused<M>::R1;
   const size_t smem = ((size_t)ColLayout<M, NB>::AREA) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_col_fused<M, NB, MINB, HALF, TMA>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  static gw::SmemRecord attr;
+  GW_TRY(gw::smem_limit(attr, k_col_fused<M, NB, MINB, HALF, TMA>, smem));
   if (TMA && P->f1_box_cols != NB)
     return gw::fail(GW_ERR_STATE, "fused column kernel: tensor-map box of " +
                                       std::to_string(P->f1_box_cols) +

@@ -14,12 +14,8 @@ int launch_row_fused(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                      int s0, int n_sl) {
   constexpr int NT = NB * Fused<M>::R1;
   const size_t smem = (size_t)NB * FusedLayout<M>::SEQ * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_row_fused<M, NB, MINB, HALF, BIL>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  static gw::SmemRecord attr;
+  GW_TRY(gw::smem_limit(attr, k_row_fused<M, NB, MINB, HALF, BIL>, smem));
   const int n_rows = batch_rows(P, s0, n_sl);
   gw::KTimer tm(P->ctx, GW_K_ROW);
   k_row_fused<M, NB, MINB, HALF, BIL><<<(n_rows + NB - 1) / NB, NT, smem, P->ctx->stream>>>(

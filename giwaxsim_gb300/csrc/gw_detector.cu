@@ -855,16 +855,9 @@ extern "C" int gw_detector_execute(gw_detector_plan *P) {
       const int tiles = ((P->p.n_h + kPlTW - 1) / kPlTW) * ((P->p.n_v + kPlTH - 1) / kPlTH);
       gw::KTimer tm(P->ctx, GW_K_DETECTOR);
       if (smem <= kPlaneSmemMax) {
-        static bool attr = false;
-        if (!attr) {
-          GW_CUDA(cudaFuncSetAttribute(k_detector_plane<true, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kPlaneSmemMax));
-          GW_CUDA(cudaFuncSetAttribute(k_detector_plane<true, false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kPlaneSmemMax));
-          attr = true;
-        }
+        static gw::SmemRecord attr_zx, attr_gen;
+        GW_TRY(gw::smem_limit(attr_zx, k_detector_plane<true, true>, kPlaneSmemMax));
+        GW_TRY(gw::smem_limit(attr_gen, k_detector_plane<true, false>, kPlaneSmemMax));
         if (P->zero_x)
           k_detector_plane<true, true><<<tiles, kPlThreads, smem, P->ctx->stream>>>(
               a, P->d_po, pa, P->d_acc, P->d_wl, P->d_wl_count, P->wl_cap);

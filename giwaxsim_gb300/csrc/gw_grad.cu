@@ -441,12 +441,8 @@ int launch_col_bwd(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                    const BinArgs &bn, const GradCol &gc, int s0, int n) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = fft_smem<M>();
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_col_bwd<M>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  static gw::SmemRecord attr;
+  GW_TRY(gw::smem_limit(attr, k_col_bwd<M>, smem));
   dim3 grid((P->Nc + NB - 1) / NB, n);
   gw::KTimer tm(P->ctx, GW_K_COLBIN);
   k_col_bwd<M><<<grid, NT, smem, P->ctx->stream>>>(a, cz, bn, gc, s0, P->Nc, P->d_F1);
@@ -460,12 +456,8 @@ int launch_row_bwd_t(gw_voxel_plan *P, const SliceArgs &a, const GradRow &gr,
   const int n_rows = batch_rows(P, s0, n_sl);
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = fft_smem<M>();
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_row_bwd<M, BIL>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  static gw::SmemRecord attr;
+  GW_TRY(gw::smem_limit(attr, k_row_bwd<M, BIL>, smem));
   gw::KTimer tm(P->ctx, GW_K_ROW);
   k_row_bwd<M, BIL><<<(n_rows + NB - 1) / NB, NT, smem, P->ctx->stream>>>(a, gr, s0, n_sl,
                                                                           n_rows);

@@ -165,17 +165,10 @@ int launch_col_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
                  const BinArgs &bn, int slice0, int n_sl) {
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, false, HALF>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    if constexpr (col_tma_ok<M>())
-      GW_CUDA(cudaFuncSetAttribute(k_col_czt_bin<M, true, HALF>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-    attr = true;
-  }
+  static gw::SmemRecord attr, attr_tma;
+  GW_TRY(gw::smem_limit(attr, k_col_czt_bin<M, false, HALF>, smem));
+  if constexpr (col_tma_ok<M>())
+    GW_TRY(gw::smem_limit(attr_tma, k_col_czt_bin<M, true, HALF>, smem));
   dim3 grid((P->Nf + NB - 1) / NB, n_sl);
   gw::KTimer tm(P->ctx, GW_K_COLBIN);
   if constexpr (col_tma_ok<M>()) {

@@ -161,13 +161,8 @@ int launch_row_t(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   const int n_rows = batch_rows(P, slice0, n_sl);
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_row_czt<M, BIL, HALF>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
+  static gw::SmemRecord attr;
+  GW_TRY(gw::smem_limit(attr, k_row_czt<M, BIL, HALF>, smem));
   const int blocks = (n_rows + NB - 1) / NB;
   gw::KTimer tm(P->ctx, GW_K_ROW);
   k_row_czt<M, BIL, HALF><<<blocks, NT, smem, P->ctx->stream>>>(a, cz, slice0, n_sl,
@@ -182,13 +177,8 @@ int launch_row_real(gw_voxel_plan *P, const SliceArgs &a, const CztArgs &cz,
   const int n_rows = batch_rows(P, slice0, n_sl);
   constexpr int NB = FftShape<M>::NB, NT = FftShape<M>::NT;
   const size_t smem = (size_t)(NB * FftPlan<M>::LDM + FftPlan<M>::tw_len()) * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    GW_CUDA(cudaFuncSetAttribute(k_row_czt_real<M, HALF>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
+  static gw::SmemRecord attr;
+  GW_TRY(gw::smem_limit(attr, k_row_czt_real<M, HALF>, smem));
   const int blocks = (n_rows + 2 * NB - 1) / (2 * NB);
   gw::KTimer tm(P->ctx, GW_K_ROW);
   k_row_czt_real<M, HALF><<<blocks, NT, smem, P->ctx->stream>>>(

@@ -1280,18 +1280,17 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t, int line_lo, int line_hi) 
     n_heavy = (int)(std::lower_bound(b, e, wline(line_hi)) - b) - h0;
   }
   const size_t smem = gather_smem(Q, use_f0, heavy);
-  static size_t smem_set[3] = {0, 0, 0};
-  if (smem > (48u << 10) && smem > smem_set[mode]) {
-    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = mode == 0 ? cudaFuncSetAttribute(k_gather<0, 13>, at, (int)smem)
-                  : mode == 1 ? cudaFuncSetAttribute(k_gather<1, 13>, at, (int)smem)
-                              : cudaFuncSetAttribute(k_gather<2, 13>, at, (int)smem);
-    if (e == cudaSuccess)
-      e = mode == 0 ? cudaFuncSetAttribute(k_gather<0, 7>, at, (int)smem)
-        : mode == 1 ? cudaFuncSetAttribute(k_gather<1, 7>, at, (int)smem)
-                    : cudaFuncSetAttribute(k_gather<2, 7>, at, (int)smem);
-    GW_CUDA(e);
-    smem_set[mode] = smem;
+  // above the default 48 KB: the launch's own kernel (mode, span length)
+  static gw::SmemRecord attr[3][2];
+  const bool u7 = Q <= 7 * 32;
+  if (smem > (48u << 10)) {
+    auto &r = attr[mode][u7];
+    if (mode == 0) GW_TRY(u7 ? gw::smem_limit(r, k_gather<0, 7>, smem)
+                             : gw::smem_limit(r, k_gather<0, 13>, smem));
+    else if (mode == 1) GW_TRY(u7 ? gw::smem_limit(r, k_gather<1, 7>, smem)
+                                  : gw::smem_limit(r, k_gather<1, 13>, smem));
+    else GW_TRY(u7 ? gw::smem_limit(r, k_gather<2, 7>, smem)
+                   : gw::smem_limit(r, k_gather<2, 13>, smem));
   }
   const int n_lines = line_hi - line_lo;
   const int blocks = n_heavy + std::max(1, std::min((n_lines + 7) / 8, 16 * ctx->sm_count));
@@ -1305,7 +1304,6 @@ int enqueue_gather(gw_voxel_plan *P, int mode, int t, int line_lo, int line_hi) 
       P->d_C2, P->d_C1, P->W, off, Q, inv_ns, P->d_f0, P->d_zf0, use_f0, f0c, f0iz, \
       o64, o32
   // spans covering a whole line: 7 voxels a lane up to 224 a line, else 13
-  const bool u7 = Q <= 7 * 32;
   if (mode == 0) {
     if (u7) k_gather<0, 7><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
     else k_gather<0, 13><<<blocks, 256, smem, ctx->stream>>>(GW_GATHER_ARGS);
@@ -1356,15 +1354,10 @@ int enqueue_finalize(gw_voxel_plan *P, bool f64) {
       const bool use_f0 = P->p.f0_z > 0;
       const size_t smem = finalize_smem(P->Qc, use_f0);
       // above the default 48 KB (crops beyond about 2400 voxels a side)
-      static size_t smem_set[2] = {0, 0};
-      if (smem > (48u << 10) && smem > smem_set[f64]) {
-        if (f64)
-          GW_CUDA(cudaFuncSetAttribute(k_finalize<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        else
-          GW_CUDA(cudaFuncSetAttribute(k_finalize<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set[f64] = smem;
+      static gw::SmemRecord attr64, attr32;
+      if (smem > (48u << 10)) {
+        if (f64) GW_TRY(gw::smem_limit(attr64, k_finalize<true>, smem));
+        else GW_TRY(gw::smem_limit(attr32, k_finalize<false>, smem));
       }
       const int blocks = std::min((P->Qc * P->Qc + 7) / 8, 16 * ctx->sm_count);
       if (f64)
