@@ -169,6 +169,30 @@ def test_plan_inputs_equal_with_ranges_given():
     assert a.key()[1:] == b.key()[1:]
 
 
+def test_plan_keeps_its_own_atoms():
+    """A plan's coordinates and f values are its own copies (one structure
+    or several): the caller changing its arrays afterwards changes neither
+    what set_atoms() uploads nor the plan's key."""
+    xyz, el, _ = W.structures("graphite-50A")[0]
+    g = F.VoxelGeometry(0.3, 0.03, 3.0)
+
+    class NoContext:
+        handle = None
+    kw = dict(phis=np.arange(5.0), ctx=NoContext(), create=False)
+    for n_struct in (1, 2):
+        coords = [np.array(xyz[:200 + 50 * i]) for i in range(n_struct)]
+        fvs = [F.element_f_values(el[:200 + 50 * i], 10000.0) for i in range(n_struct)]
+        plan = F.VoxelPlan(g, [(c, f, None) for c, f in zip(coords, fvs)], **kw)
+        x0, f0, k0 = plan.xyz.copy(), plan.f.copy(), plan.key()
+        for c, f in zip(coords, fvs):
+            c += 1.0
+            f *= 2.0
+        assert np.array_equal(plan.xyz, x0) and np.array_equal(plan.f, f0)
+        assert plan.key() == k0
+        assert plan.xyz.flags.c_contiguous and plan.f.dtype == np.float32
+        assert len(plan.f) == 2 * len(plan.xyz)
+
+
 def test_missing_xraydb_refuses_without_opt_in(monkeypatch):
     """Without xraydb the f', f'' lookup (utilities.py:342-366) raises, as
     the reference's module-level `import xraydb` (utilities.py:3) does,
